@@ -1,0 +1,198 @@
+/*
+ * qstem_gpu.h -- C ABI of the GB300 multislice library (libqstem_gpu.so).
+ *
+ * This is the drop-in boundary for QSTEM's multislice hot path in
+ * stem3/stemlib.cpp.  Each entry point replaces one reference function of the
+ * call surface declared in stem3/stemlib.h:
+ *
+ *   qs_lut_build        getAtomPotential3D / getAtomPotentialOffset3D
+ *                       (stem3/stemlib.h:51-52; stem3/stemlib.cpp:1342, :1548)
+ *   qs_slices_build     make3DSlices + initSTEMSlices
+ *                       (stem3/stemlib.h:45, :39; stem3/stemlib.cpp:383, :2199)
+ *   qs_probe            probe (stem3/stemlib.h:36; stem3/stemlib.cpp:1952)
+ *   qs_multislice_run   the position loop of doSTEM/doCBED around runMulsSTEM,
+ *                       which fuses transmit, the 2-D FFT pair, propagate_slow,
+ *                       fft_normalize and collectIntensity
+ *                       (stem3/stem3.cpp:2820-2946; stem3/stemlib.h:64, :41,
+ *                        :48-49, :66; stem3/stemlib.cpp:2375, :2576, :2760,
+ *                        :2867, :2890)
+ *   qs_collect          collectIntensity for one k-space wave
+ *                       (stem3/stemlib.h:41; stem3/stemlib.cpp:2576)
+ *
+ * Conventions
+ *   - Plain C types only; complex numbers are interleaved float pairs
+ *     [re, im] ("c64"), matching fftwf_complex.
+ *   - Arrays are row-major [x][y] with y fastest, as the reference's
+ *     complex2Df/complex3Df allocators lay them out
+ *     (libs/memory_fftw3.cpp:446, :523): wave[ix][iy], trans[z][ix][iy].
+ *   - Every function returns an int status: QS_OK (0) or a negative
+ *     QS_ERR_* code; qs_last_error() returns the message of the calling
+ *     thread's last failure.  Nothing calls exit(): the reference's
+ *     printf+exit(0) error paths become error codes.
+ *   - All buffers are owned by the caller.  Pointer arguments are device
+ *     pointers unless the `flags` argument carries QS_HOST_IO, in which case
+ *     they are host pointers and the library copies through its own device
+ *     staging buffers.
+ *   - A context owns one CUDA stream on one device; calls on one context are
+ *     serialised on that stream, different contexts may be used from
+ *     different threads.
+ */
+#ifndef QSTEM_GPU_H
+#define QSTEM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QS_ABI_VERSION 1
+
+/* status codes */
+#define QS_OK 0
+#define QS_ERR_ARG (-1)         /* invalid argument or inconsistent parameters */
+#define QS_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define QS_ERR_NOMEM (-3)       /* device allocation refused (admission control) */
+#define QS_ERR_UNSUPPORTED (-4) /* a size or option this build does not implement */
+#define QS_ERR_TIMEOUT (-5)     /* a bounded device wait gave up */
+
+/* flags */
+#define QS_HOST_IO 1u           /* buffer pointers are host memory */
+#define QS_OUT_POTENTIAL 2u     /* qs_slices_build: stop after make3DSlices (V in .re) */
+#define QS_SYNC 4u              /* synchronise the stream before returning */
+
+/* run modes, same numbering as libs/stemtypes_fftw3.h:35-42 */
+#define QS_MODE_STEM 1
+#define QS_MODE_CBED 2
+#define QS_MODE_TEM 3
+
+#define QS_MAX_DETECTORS 16
+
+/* One atom; identical layout to the reference's `atom`
+ * (libs/stemtypes_fftw3.h:70-77), z first. 28 bytes. */
+typedef struct qs_atom {
+    float z, y, x;
+    float dw;   /* Debye-Waller factor B (A^2) */
+    float occ;  /* occupancy */
+    float q;    /* charge */
+    int Znum;   /* atomic number, 0 = vacancy */
+} qs_atom;
+
+/* One annular detector; the fields the reference's Detector carries for
+ * collectIntensity (libs/data_containers.h:77-97).  k2Inside/k2Outside are
+ * (sin(r*1e-3)/lambda)^2 rounded to float as stem3/stem3.cpp:1343-1350 does;
+ * qs_params_finalize fills them from rInside/rOutside. */
+typedef struct qs_detector {
+    float rInside, rOutside; /* mrad */
+    float k2Inside, k2Outside;
+    float shiftX, shiftY;    /* pixels */
+} qs_detector;
+
+/* The MULS fields the hot path reads (libs/data_containers.h:103-308), with
+ * the reference's own types (float where MULS has float_tt) so that the
+ * arithmetic can reproduce it. */
+typedef struct qs_params {
+    int mode;               /* QS_MODE_* */
+    int nx, ny;             /* wave grid */
+    int potNx, potNy;       /* potential/transmission grid */
+    int slices;             /* slices per stack */
+    int cellDiv;            /* slab count (only 1 supported) */
+    int outputInterval;     /* "slices between outputs" */
+    int centerSlices, nonPeriod, nonPeriodZ, potential3D, fftpotential;
+    int bandlimittrans, tds;
+    float resolutionX, resolutionY; /* A/pixel */
+    float sliceThickness;   /* A */
+    float czOffset;         /* zOffset: A */
+    float potOffsetX, potOffsetY;
+    float potSizeX, potSizeY;
+    float ax, by, c;        /* super-cell size, A */
+    float atomRadius;       /* A */
+    float v0;               /* kV */
+    /* probe optics (stem3/stem3.cpp:1120-1275); lengths in A, angles rad */
+    float alpha;            /* mrad */
+    float Cs, C5, df0, astigMag, astigAngle, Cc, dE_E;
+    float a33, a31, a44, a42, a55, a53, a51, a66, a64, a62;
+    float phi33, phi31, phi44, phi42, phi55, phi53, phi51, phi66, phi64, phi62;
+    int ismoth, gaussFlag;
+    float gaussScale;
+    float aAIS;
+    /* scan (stem3/stem3.cpp:1054-1068, adjusted as :1436-1446) */
+    float scanXStart, scanXStop, scanYStart, scanYStop;
+    int scanXN, scanYN;
+    float electronScale;    /* beam current * dwell time * MILLISEC_PICOAMP */
+    int detectorNum;
+    qs_detector detectors[QS_MAX_DETECTORS];
+} qs_params;
+
+/* A batch of probe positions for qs_multislice_run.  Position p uses the
+ * transmission window at integer offset (iPosX[p], iPosY[p]) of the
+ * potNx x potNy stack and writes detector pixel (detPosX[p], detPosY[p])
+ * (the WAVEFUNC fields of the same names, libs/data_containers.h:35-37).
+ * All four arrays are HOST arrays of length npos.  A NULL iPosX/iPosY
+ * computes the offsets of a full scan_x/scan_y raster the way doSTEM does
+ * (stem3/stem3.cpp:2860-2871) with p = ix*scanYN + iy. */
+typedef struct qs_batch {
+    int npos;
+    const int *iPosX, *iPosY;
+    const int *detPosX, *detPosY;
+} qs_batch;
+
+typedef struct qs_ctx qs_ctx;
+
+/* ---------------------------------------------------------------- context */
+int qs_ctx_create(int device, qs_ctx **out);
+int qs_ctx_destroy(qs_ctx *ctx);
+const char *qs_last_error(void);
+int qs_abi_version(void);
+/* The stream the context launches on (a cudaStream_t, as an opaque pointer). */
+void *qs_ctx_stream(qs_ctx *ctx);
+/* Fill derived fields (detector k2 bounds) exactly as readFile does. */
+int qs_params_finalize(qs_params *p);
+/* Number of thickness outputs tCount+1 (stem3/stemlib.cpp:2589). */
+int qs_thickness_count(const qs_params *p);
+
+/* ------------------------------------------------------------ potentials */
+/* Projected-potential lookup table of one element: Nz_lut x Nr floats
+ * (the real parts of the reference's complex LUT).  `charged` selects the
+ * charge-derivative table of getAtomPotentialOffset3D.  B is the
+ * Debye-Waller factor.  out may be NULL to query the dimensions. */
+int qs_lut_build(qs_ctx *ctx, const qs_params *p, int Znum, double B, int charged,
+                 float *out, int *Nz_lut, int *Nr, int *nzSub, unsigned flags);
+
+/* Build trans[slices][potNx][potNy] (c64) from `natom` atoms: the
+ * scatter-sum of make3DSlices followed by initSTEMSlices' exp(i*lambda*gamma*V)
+ * and optional band limit.  With QS_OUT_POTENTIAL the result stops after the
+ * scatter-sum (V in .re, 0 in .im).  atoms is a host array. */
+int qs_slices_build(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom,
+                    float *trans, unsigned flags);
+
+/* ----------------------------------------------------------------- probe */
+/* nx x ny c64 real-space probe centred at (dx, dy) A. */
+int qs_probe(qs_ctx *ctx, const qs_params *p, double dx, double dy, float *wave,
+             unsigned flags);
+
+/* ------------------------------------------------------------ multislice */
+/* Run every position of `batch` through all slices of `trans` (device,
+ * slices x potNx x potNy c64), starting from `probe` (device nx x ny c64,
+ * NULL = build the centred probe).  Outputs (each may be NULL):
+ *   det_images  [tCount+1][detectorNum][scanXN][scanYN] float, the
+ *               detector images after the last slice of each thickness
+ *               group (collectIntensity's overwrite semantics)
+ *   diffpats    [npos][nx][ny] float, fftshifted |psi(k)|^2/sqrt(nx*ny) of
+ *               the final slice (wave->diffpat)
+ *   exit_waves  [npos][nx][ny] c64 real-space exit waves
+ * Buffers are device pointers, or host pointers with QS_HOST_IO. */
+int qs_multislice_run(qs_ctx *ctx, const qs_params *p, const float *trans, const float *probe,
+                      const qs_batch *batch, float *det_images, float *diffpats,
+                      float *exit_waves, unsigned flags);
+
+/* collectIntensity for one wave already in k-space (after propagate):
+ * returns the per-detector sums and optionally the diffraction pattern. */
+int qs_collect(qs_ctx *ctx, const qs_params *p, const float *wave_k, double *det_sums,
+               float *diffpat, unsigned flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,277 @@
+"""Host front end: stem3 .qsc parameters and .cfg atoms -> qs_params / atoms.
+
+The derived quantities follow stem3's readFile (stem3/stem3.cpp:612-1559)
+with the reference's float (MULS float_tt) arithmetic reproduced through
+numpy float32, and the atom list follows readUnitCell/replicateUnitCell
+(libs/fileio_fftw3.cpp:1313-1657, :1188-1306) for orthogonal unit cells
+without tilt, thermal displacement or partial occupancy.  `write_qsc` /
+`write_cfg` produce input files the reference's own stem3 reads, so that the
+same run can be driven through both.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+
+F32 = np.float32
+ELECTRON_CHARGE = 1.6021773e-19
+MILLISEC_PICOAMP = 1e-3 * (1e-12 / ELECTRON_CHARGE)  # libs/stemtypes_fftw3.h:47-49
+RAD2DEG = 57.2958                                   # stem3/stem3.cpp:73
+
+ELEMENTS = {"H": 1, "He": 2, "Li": 3, "Be": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9, "Ne": 10,
+            "Na": 11, "Mg": 12, "Al": 13, "Si": 14, "P": 15, "S": 16, "Cl": 17, "Ar": 18,
+            "K": 19, "Ca": 20, "Sc": 21, "Ti": 22, "V": 23, "Cr": 24, "Mn": 25, "Fe": 26,
+            "Co": 27, "Ni": 28, "Cu": 29, "Zn": 30, "Ga": 31, "Ge": 32, "As": 33, "Se": 34,
+            "Br": 35, "Kr": 36, "Rb": 37, "Sr": 38, "Y": 39, "Zr": 40, "Nb": 41, "Mo": 42,
+            "Tc": 43, "Ru": 44, "Rh": 45, "Pd": 46, "Ag": 47, "Cd": 48, "In": 49, "Sn": 50,
+            "Sb": 51, "Te": 52, "I": 53, "Xe": 54, "Cs": 55, "Ba": 56, "La": 57, "Ce": 58,
+            "Pr": 59, "Nd": 60, "Pm": 61, "Sm": 62, "Eu": 63, "Gd": 64, "Tb": 65, "Dy": 66,
+            "Ho": 67, "Er": 68, "Tm": 69, "Yb": 70, "Lu": 71, "Hf": 72, "Ta": 73, "W": 74,
+            "Re": 75, "Os": 76, "Ir": 77, "Pt": 78, "Au": 79, "Hg": 80, "Tl": 81, "Pb": 82,
+            "Bi": 83, "Po": 84, "At": 85, "Rn": 86, "Fr": 87, "Ra": 88, "Ac": 89, "Th": 90,
+            "Pa": 91, "U": 92}
+SYMBOL = {v: k for k, v in ELEMENTS.items()}
+MASS = {8: 16.0, 14: 28.0855, 22: 47.867, 38: 87.62, 79: 196.97}
+
+
+def wavelength(kev):
+    """Electron wavelength in A (stem3/stemutil.cpp:714-725)."""
+    return 12.3984244 / math.sqrt(kev * (2 * 510.99906 + kev))
+
+
+# --------------------------------------------------------------- unit cells
+class UnitCell:
+    """Orthogonal unit cell: a, b, c (A) and fractional atoms
+    (Z, fx, fy, fz, dw, occ, q)."""
+
+    def __init__(self, a, b, c, atoms):
+        self.a, self.b, self.c = float(a), float(b), float(c)
+        self.atoms = [tuple(t) for t in atoms]
+
+
+def srtio3_cell(dw=0.0):
+    a = 3.905
+    return UnitCell(a, a, a, [(38, 0, 0, 0, dw, 1, 0), (22, .5, .5, .5, dw, 1, 0),
+                              (8, 0, .5, .5, dw, 1, 0), (8, .5, 0, .5, dw, 1, 0),
+                              (8, .5, .5, 0, dw, 1, 0)])
+
+
+def fcc_cell(Z, a, dw=0.0):
+    return UnitCell(a, a, a, [(Z, 0, 0, 0, dw, 1, 0), (Z, .5, .5, 0, dw, 1, 0),
+                              (Z, .5, 0, .5, dw, 1, 0), (Z, 0, .5, .5, dw, 1, 0)])
+
+
+def si110_cell(dw=0.0):
+    """Si diamond (a = 5.431 A) viewed along [110]: orthorhombic cell
+    a/sqrt2 x a x a/sqrt2 with 4 atoms."""
+    a = 5.431
+    ax, by = a / math.sqrt(2), a
+    frac = [(0.0, 0.0, 0.0), (0.5, 0.5, 0.5), (0.0, 0.25, 0.5), (0.5, 0.75, 0.0)]
+    return UnitCell(ax, by, ax, [(14, fx, fy, fz, dw, 1, 0) for fx, fy, fz in frac])
+
+
+def write_cfg(cell, path):
+    """AtomEye .cfg with dw, occupancy and charge columns (the format
+    readCFGCellParams/readNextCFGAtom read, libs/fileio_fftw3.cpp:721-989)."""
+    lines = ["Number of particles = %d" % len(cell.atoms), "A = 1.0 Angstrom (basic length-scale)"]
+    H = [[cell.a, 0, 0], [0, cell.b, 0], [0, 0, cell.c]]
+    for i in range(3):
+        for j in range(3):
+            lines.append("H0(%d,%d) = %r A" % (i + 1, j + 1, float(H[i][j])))
+    lines += [".NO_VELOCITY.", "entry_count = 6"]
+    last = None
+    for Z, fx, fy, fz, dw, occ, q in cell.atoms:
+        if Z != last:
+            lines += ["%g" % MASS.get(Z, 2.0 * Z), SYMBOL[Z]]
+            last = Z
+        lines.append("%r %r %r %r %r %r" % (float(fx), float(fy), float(fz), float(dw), float(occ), float(q)))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def _cmp_zyx_key(row):
+    return (row[3], row[2], row[1])
+
+
+def replicate(cell, ncx, ncy, ncz):
+    """Cartesian atoms of an ncx x ncy x ncz super-cell, in the order and
+    float32 arithmetic of readUnitCell (libs/fileio_fftw3.cpp:1436-1612):
+    unit-cell atoms sorted by (z, y, x) of their fractional coordinates, then
+    replicated with index ((icz + icy*ncz + icx*ncy*ncz)*ncoord + i), then
+    scaled by the cell vectors in double and stored as float.
+    Returns (atoms[ATOM_DTYPE], ax, by, c) with the super-cell size as float32."""
+    n = len(cell.atoms)
+    frac = np.zeros(n, dtype=abi.ATOM_DTYPE)
+    for i, (Z, fx, fy, fz, dw, occ, q) in enumerate(cell.atoms):
+        frac[i] = (fz, fy, fx, dw, occ, q, Z)
+    order = sorted(range(n), key=lambda i: (frac["z"][i], frac["y"][i], frac["x"][i]))
+    frac = frac[order]
+    out = np.zeros(n * ncx * ncy * ncz, dtype=abi.ATOM_DTYPE)
+    for icx in range(ncx):
+        for icy in range(ncy):
+            for icz in range(ncz):
+                j0 = (icz + icy * ncz + icx * ncy * ncz) * n
+                blk = out[j0:j0 + n]
+                blk[:] = frac
+                blk["x"] = (frac["x"].astype(np.float64) + icx).astype(F32)
+                blk["y"] = (frac["y"].astype(np.float64) + icy).astype(F32)
+                blk["z"] = (frac["z"].astype(np.float64) + icz).astype(F32)
+    out["x"] = (cell.a * out["x"].astype(np.float64)).astype(F32)
+    out["y"] = (cell.b * out["y"].astype(np.float64)).astype(F32)
+    out["z"] = (cell.c * out["z"].astype(np.float64)).astype(F32)
+    ax = F32(cell.a * ncx / 2.0 + cell.a * ncx / 2.0)
+    by = F32(cell.b * ncy / 2.0 + cell.b * ncy / 2.0)
+    cc = F32(cell.c * ncz / 2.0 + cell.c * ncz / 2.0)
+    return out, ax, by, cc
+
+
+# ------------------------------------------------------------------ params
+def make_params(*, mode=abi.QS_MODE_STEM, nx, ny=None, resolutionX, resolutionY=None, v0,
+                slices, sliceThickness, ax, by, c, scan=None, detectors=(), alpha=20.0,
+                Cs_mm=0.0, C5_mm=0.0, defocus_nm=0.0, Cc_mm=0.0, dE_E=0.0,
+                astig_nm=0.0, astig_deg=0.0, outputInterval=None, czOffset=0.0,
+                centerSlices=False, periodicXY=False, periodicZ=False, bandlimit=False,
+                atomRadius=5.0, smooth=True, gaussian=None, aAIS=0.0, beamCurrent=1.0,
+                dwellTime=1.6021773e-4, tds=False):
+    """qs_params as stem3's readFile would fill them from the corresponding
+    .qsc keys (units as in the .qsc: mm, nm, mrad, deg).
+    scan = (x_start, x_stop, x_pixels, y_start, y_stop, y_pixels) in A."""
+    ny = nx if ny is None else ny
+    resolutionY = resolutionX if resolutionY is None else resolutionY
+    p = abi.QsParams()
+    p.mode = mode
+    p.nx, p.ny = nx, ny
+    p.resolutionX, p.resolutionY = F32(resolutionX), F32(resolutionY)
+    p.v0 = F32(v0)
+    p.slices = slices + (1 if centerSlices else 0)
+    p.sliceThickness = F32(sliceThickness)
+    p.centerSlices = int(bool(centerSlices))
+    p.cellDiv = 1
+    p.outputInterval = p.slices if (outputInterval is None or outputInterval < 1) else outputInterval
+    p.czOffset = F32(czOffset)
+    p.ax, p.by, p.c = F32(ax), F32(by), F32(c)
+    p.nonPeriod = 0 if periodicXY else 1
+    p.nonPeriodZ = 0 if periodicZ else 1
+    p.bandlimittrans = int(bool(bandlimit))
+    p.fftpotential = 1
+    p.potential3D = 1
+    p.tds = int(bool(tds))
+    p.atomRadius = F32(atomRadius)
+    # scan window and potential array (stem3/stem3.cpp:1054-1068, :1436-1455)
+    if mode == abi.QS_MODE_STEM:
+        x0, x1, xn, y0, y1, yn = scan
+        p.scanXStart, p.scanXStop, p.scanXN = F32(x0), F32(x1), max(1, int(xn))
+        p.scanYStart, p.scanYStop, p.scanYN = F32(y0), F32(y1), max(1, int(yn))
+    else:
+        if scan is None:
+            x0, y0 = float(F32(ax)) / 2.0, float(F32(by)) / 2.0
+        else:
+            x0, y0 = scan[0], scan[3] if len(scan) > 3 else scan[1]
+        p.scanXStart = p.scanXStop = F32(x0)
+        p.scanYStart = p.scanYStop = F32(y0)
+        p.scanXN = p.scanYN = 1
+    if mode in (abi.QS_MODE_STEM, abi.QS_MODE_CBED):
+        p.potOffsetX = F32(float(p.scanXStart) - 0.5 * nx * float(p.resolutionX))
+        p.potOffsetY = F32(float(p.scanYStart) - 0.5 * ny * float(p.resolutionY))
+        pnx = int(F32(F32(p.scanXStop) - F32(p.scanXStart)) / F32(p.resolutionX))
+        pny = int(F32(F32(p.scanYStop) - F32(p.scanYStart)) / F32(p.resolutionY))
+        p.scanXStop = F32(F32(p.scanXStart) + F32(p.resolutionX) * F32(pnx))
+        p.scanYStop = F32(F32(p.scanYStart) + F32(p.resolutionY) * F32(pny))
+        p.potNx, p.potNy = pnx + nx, pny + ny
+        p.potSizeX = F32(F32(p.potNx) * F32(p.resolutionX))
+        p.potSizeY = F32(F32(p.potNy) * F32(p.resolutionY))
+    else:
+        p.potNx, p.potNy = nx, ny
+        p.potSizeX = F32(F32(nx) * F32(p.resolutionX))
+        p.potSizeY = F32(F32(ny) * F32(p.resolutionY))
+        p.potOffsetX = F32(float(p.scanXStart) - 0.5 * float(p.potSizeX))
+        p.potOffsetY = F32(float(p.scanYStart) - 0.5 * float(p.potSizeY))
+    # optics (stem3/stem3.cpp:1128-1275)
+    p.Cc = F32(1e7 * Cc_mm)
+    p.dE_E = F32(dE_E)
+    p.Cs = F32(F32(Cs_mm) * 1.0e7)
+    p.C5 = F32(F32(C5_mm) * 1.0e7)
+    if defocus_nm is None or (isinstance(defocus_nm, str) and defocus_nm.lower().startswith("s")):
+        p.df0 = F32(-math.sqrt(1.5 * float(p.Cs) * wavelength(float(p.v0))))
+    else:
+        p.df0 = F32(10.0 * float(F32(defocus_nm)))
+    p.astigMag = F32(10.0 * float(F32(astig_nm)))
+    p.astigAngle = F32(float(F32(astig_deg)) * 3.1415926535897 / 180.0)
+    p.alpha = F32(alpha)
+    p.aAIS = F32(aAIS)
+    p.electronScale = F32(float(F32(F32(beamCurrent) * F32(dwellTime))) * MILLISEC_PICOAMP)
+    p.ismoth = int(bool(smooth))
+    p.gaussFlag = 0 if gaussian is None else 1
+    p.gaussScale = F32(0.05 if gaussian is None else gaussian)
+    # detectors (stem3/stem3.cpp:1316-1355)
+    dets = list(detectors)
+    if len(dets) > abi.QS_MAX_DETECTORS:
+        raise ValueError("at most %d detectors" % abi.QS_MAX_DETECTORS)
+    p.detectorNum = len(dets) if mode == abi.QS_MODE_STEM else 0
+    wl = wavelength(float(p.v0))
+    for i, d in enumerate(dets[:p.detectorNum]):
+        rin, rout = d[0], d[1]
+        sx = d[3] if len(d) > 3 else 0.0
+        sy = d[4] if len(d) > 4 else 0.0
+        det = p.detectors[i]
+        det.rInside, det.rOutside = F32(rin), F32(rout)
+        ki = F32(math.sin(float(F32(rin)) * 0.001) / wl)
+        ko = F32(math.sin(float(F32(rout)) * 0.001) / wl)
+        det.k2Inside, det.k2Outside = F32(ki * ki), F32(ko * ko)
+        det.shiftX, det.shiftY = F32(sx), F32(sy)
+    return p
+
+
+def scan_offsets(p):
+    """(iPosX, iPosY) of every raster position p = ix*scanYN + iy
+    (stem3/stem3.cpp:2860-2871)."""
+    ix = np.arange(p.scanXN, dtype=np.int64)
+    iy = np.arange(p.scanYN, dtype=np.int64)
+    fx = (ix.astype(F32) * F32(F32(p.scanXStop) - F32(p.scanXStart))) / (F32(p.scanXN) * F32(p.resolutionX))
+    fy = (iy.astype(F32) * F32(F32(p.scanYStop) - F32(p.scanYStart))) / (F32(p.scanYN) * F32(p.resolutionY))
+    px = np.minimum(fx.astype(F32).astype(np.int64), p.potNx - p.nx)
+    py = np.minimum(fy.astype(F32).astype(np.int64), p.potNy - p.ny)
+    PX = np.repeat(px, p.scanYN)
+    PY = np.tile(py, p.scanXN)
+    DX = np.repeat(ix, p.scanYN)
+    DY = np.tile(iy, p.scanXN)
+    return (PX.astype(np.int32), PY.astype(np.int32), DX.astype(np.int32), DY.astype(np.int32))
+
+
+def write_qsc(path, *, cfg_file, ncell, nx, resolutionX, v0, slices, sliceThickness, scan=None,
+              detectors=(), alpha=20.0, Cs_mm=0.0, C5_mm=0.0, defocus_nm=0.0, outputInterval=None,
+              mode="STEM", bandlimit=False, periodicXY=False, periodicZ=False, folder="out",
+              saveLevel=0, smooth=True, czOffset=0.0, atomRadius=5.0, centerSlices=False):
+    """A stem3 input file for the same run make_params describes."""
+    yn = lambda b: "yes" if b else "no"
+    L = ["mode: %s" % mode, "print level: 1", "save level: %d" % saveLevel,
+         "filename: %s" % cfg_file, "resolutionX: %r" % float(resolutionX),
+         "resolutionY: %r" % float(resolutionX), "NCELLX: %d" % ncell[0], "NCELLY: %d" % ncell[1],
+         "NCELLZ: %d" % ncell[2], "v0: %r" % float(v0), "tds: no",
+         "slice-thickness: %r" % float(sliceThickness), "slices: %d" % slices,
+         "center slices: %s" % yn(centerSlices)]
+    if outputInterval:
+        L.append("slices between outputs: %d" % outputInterval)
+    L += ["zOffset: %r" % float(czOffset), "periodicXY: %s" % yn(periodicXY),
+          "periodicZ: %s" % yn(periodicZ)]
+    if scan is not None:
+        if mode == "STEM":
+            L += ["scan_x_start: %r" % float(scan[0]), "scan_x_stop: %r" % float(scan[1]),
+                  "scan_x_pixels: %d" % scan[2], "scan_y_start: %r" % float(scan[3]),
+                  "scan_y_stop: %r" % float(scan[4]), "scan_y_pixels: %d" % scan[5]]
+        else:
+            L += ["scan_x_start: %r" % float(scan[0]), "scan_y_start: %r" % float(scan[3])]
+    for d in detectors:
+        sx = d[3] if len(d) > 3 else 0.0
+        sy = d[4] if len(d) > 4 else 0.0
+        L.append("detector: %r %r %s %r %r" % (float(d[0]), float(d[1]), d[2], float(sx), float(sy)))
+    L += ["nx: %d" % nx, "ny: %d" % nx, "Cs: %r" % float(Cs_mm), "C5: %r" % float(C5_mm),
+          "Cc: 0", "alpha: %r" % float(alpha), "defocus: %r" % float(defocus_nm),
+          "beam current: 1", "dwell time: 1.6021773e-4", "smooth: %s" % yn(smooth),
+          "gaussian: no", "potential3D: yes", "atom radius: %r" % float(atomRadius),
+          "bandlimit f_trans: %s" % yn(bandlimit), "one time integration: yes",
+          'Folder: "%s"' % folder, "Runs for averaging: 1", "Structure Factors: WK",
+          "sequence: 1 1"]
+    with open(path, "w") as f:
+        f.write("\n".join(L) + "\n")
