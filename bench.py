@@ -1,0 +1,305 @@
+"""Benchmark: batched STEM multislice, SrTiO3 [001] 10x10x20 unit cells,
+512x512 complex64 waves, 40 slices of 1.9525 A, 64x64 probe positions,
+4 annular detectors (0-10, 10-25, 25-70, 70-200 mrad), 200 kV, 20 mrad,
+frozen-phonon configurations with seeded Gaussian displacements
+(u_rms 0.08 A for Sr/Ti, 0.09 A for O per axis).
+
+One step = one frozen-phonon configuration: build the 40-slice
+transmission stack from the displaced atoms (LUT, scatter-sum, phase
+grating) and run all 4096 positions through it, detector images out.
+Metric: probe-positions/s (positions x configurations per second).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the reference's CPU algorithm (the C restatement
+in oracle/, bit-exact with the reference on this path, with OpenMP over
+positions on every host core) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from qstem_gb300 import abi, config  # noqa: E402
+
+WORKLOAD = "stem-batched-512: SrTiO3 10x10x20, 512^2, 40 slices, 64x64 positions, 4 detectors, frozen phonons"
+SEED = 20261203 + 100
+
+
+def workload_params(npix=64):
+    atoms, ax, by, c = config.replicate(config.srtio3_cell(), 10, 10, 20)
+    p = config.make_params(nx=512, resolutionX=39.05 / 512, v0=200, slices=40, sliceThickness=1.9525, ax=ax,
+                           by=by, c=c, scan=(19.525, 23.43, npix, 19.525, 23.43, npix),
+                           detectors=[(0, 10, "BF"), (10, 25, "LAADF"), (25, 70, "MAADF"), (70, 200, "HAADF")],
+                           alpha=20, tds=False)
+    return p, atoms
+
+
+def phonon_atoms(atoms, j):
+    """Configuration j: Gaussian displacements per Cartesian axis from
+    numpy.random.default_rng(SEED + j)."""
+    rng = np.random.default_rng(SEED + j)
+    a = atoms.copy()
+    sig = np.where(a["Znum"] == 8, 0.09, 0.08).astype(np.float64)
+    for k in ("x", "y", "z"):
+        a[k] = (a[k].astype(np.float64) + rng.standard_normal(len(a)) * sig).astype(np.float32)
+    return a
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def cpu_sample(p, atoms, npos_sample, threads):
+    """Reference CPU algorithm on a bounded sample: one slice-stack build plus
+    `npos_sample` positions; returns the extrapolated positions/s of a whole
+    configuration (build + 4096 positions) and the timings."""
+    from oracle import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    V = oracle.potential(p, atoms)
+    T = oracle.transmission(p, V)
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    oracle.stem(p, T, p0=0, p1=npos_sample, nthreads=threads)
+    t_pos = (time.perf_counter() - t0) / npos_sample
+    npos = p.scanXN * p.scanYN
+    return npos / (t_build + npos * t_pos), t_build, t_pos
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    p, atoms = workload_params()
+    threads = os.cpu_count() or 1
+    sample = max(threads, 8)
+    rates = []
+    t_build = None
+    for step in range(args.warmup + args.steps):
+        a = phonon_atoms(atoms, step)
+        r, tb, tp = cpu_sample(p, a, sample, threads)
+        if step >= args.warmup:
+            rates.append((r, tb, tp))
+        t_build = tb
+    value = float(np.median([r[0] for r in rates]))
+    tp = float(np.median([r[2] for r in rates]))
+    line = {"impl": "reference", "metric": "probe-positions/s", "value": value, "unit": "positions/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * (p.scanXN * p.scanYN) / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded frozen-phonon SrTiO3)",
+            "config": {"workload": WORKLOAD, "positions_per_step": p.scanXN * p.scanYN, "slices": p.slices,
+                       "grid": [p.nx, p.ny], "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": "positions/s", "cores": threads, "kind": "port",
+                             "sample": "per step: one full 40-slice stack build (%.1f s) + %d of 4096 positions "
+                                       "(%.3f s each per core-parallel batch), extrapolated to a whole "
+                                       "configuration; C restatement of the reference (bit-exact with it), "
+                                       "project FFT, OpenMP over positions" % (t_build, sample, tp)},
+            "e2e": {"value": value, "unit": "positions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world):
+    import torch
+    from qstem_gb300 import lib
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    p, atoms = workload_params()
+    npos = p.scanXN * p.scanYN
+    nt = p.thickness_count()
+    ctx = lib.Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle, device=torch.device("cuda", dev))
+    trans = torch.empty((p.slices, p.potNx, p.potNy, 2), dtype=torch.float32, device="cuda")
+    det = torch.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), dtype=torch.float32, device="cuda")
+    cfgs = [phonon_atoms(atoms, rank * (args.steps + args.warmup) + j) for j in range(args.warmup + args.steps)]
+
+    def step(j):
+        ctx.slices(p, cfgs[j], out=trans, sync=False)
+        ctx.multislice(p, trans, det=det, sync=False)
+
+    for j in range(args.warmup):
+        step(j)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    ctx.profile(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for j in range(args.warmup, args.warmup + args.steps):
+        step(j)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    st = ctx.stats()
+    ctx.profile(False)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * npos * args.steps / (ms / 1000.0)
+    result = det.cpu().numpy()
+    assert np.isfinite(result).all() and result[-1].sum() > 0
+
+    # end to end through the C ABI: host atoms in, host detector images out
+    host_det = np.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), np.float32)
+    for j in range(min(2, args.warmup)):
+        ctx.stem_run(p, cfgs[j], det=host_det)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for j in range(args.warmup, args.warmup + args.steps):
+        ctx.stem_run(p, cfgs[j], det=host_det)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * npos * args.steps / e2e_s
+
+    if rank != 0:
+        return 0
+    # dominant kernel: the row pass (IFFT_y, 1/N, transmit, FFT_y): 24 B/px algorithmic
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    kern = "row" if st["row_ms"] >= st["col_ms"] else "col"
+    k_ms = st[kern + "_ms"] / max(1, st[kern + "_launches"])
+    k_bytes = st[kern + "_bytes"] / max(1, st[kern + "_launches"])
+    achieved = k_bytes / (k_ms / 1000.0) / 1e9
+    both = (st["row_bytes"] + st["col_bytes"]) / ((st["row_ms"] + st["col_ms"]) / 1000.0) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        traffic = json.load(open(tf)).get(kern)
+
+    # CPU baseline on this host (bounded sample) and the plain GPU path
+    cpu = None
+    if not args.skip_cpu:
+        threads = os.cpu_count() or 1
+        r, tb, tp = cpu_sample(p, cfgs[0], max(threads, 8), threads)
+        cpu = {"value": r, "unit": "positions/s", "cores": threads, "kind": "port",
+               "sample": "one 40-slice stack build (%.1f s) + %d positions (%.3f s/position, core-parallel), "
+                         "extrapolated to 4096 positions; C restatement of the reference (bit-exact), project FFT"
+                         % (tb, max(threads, 8), tp)}
+    plain = None
+    if not args.skip_plain:
+        from qstem_gb300 import plain as plainmod
+        tr = torch.view_as_complex(trans)
+        probe = torch.view_as_complex(torch.from_numpy(ctx.probe(p)).cuda())
+        px, py, _, _ = config.scan_offsets(p)
+        pos = [(int(px[i]), int(py[i])) for i in range(16)]
+        plainmod.run_positions(p, tr, probe, pos[:2])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plainmod.run_positions(p, tr, probe, pos)
+        torch.cuda.synchronize()
+        tpl = (time.perf_counter() - t0) / len(pos)
+        plain = {"value": 1.0 / tpl, "unit": "positions/s",
+                 "sample": "16 positions, one probe at a time, torch ops + cuFFT per slice step",
+                 "batched_over_plain": value / (1.0 / tpl)}
+    line = {"metric": "probe-positions/s", "value": value, "unit": "positions/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded frozen-phonon SrTiO3)",
+            "config": {"workload": WORKLOAD, "positions_per_step": npos, "slices": p.slices, "grid": [p.nx, p.ny],
+                       "slice_steps_per_s": value * p.slices,
+                       "l2": "inputs larger than L2: 8 GiB wave batch and a fresh 101 MB slice stack per step"},
+            "roofline": {"bound": "hbm", "kernel": "ms_rows" if kern == "row" else "ms_cols", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+                         "both_passes_achieved": both, "both_passes_frac": both / peak,
+                         "bytes_model": "40 B per pixel per slice-step (row pass 24, column pass 16)"},
+            "gpu_launches": st["launches"], "clocks": clk,
+            "e2e": {"value": e2e, "unit": "positions/s", "h2d_bytes_per_step": int(cfgs[0].nbytes),
+                    "d2h_bytes_per_step": int(host_det.nbytes)},
+            "cpu_baseline": cpu, "plain_gpu": plain}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-plain", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if (args.impl == "ours" and torch.cuda.is_available()) else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend)
+    rc = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

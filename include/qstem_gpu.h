@@ -187,8 +187,32 @@ int qs_multislice_run(qs_ctx *ctx, const qs_params *p, const float *trans, const
                       const qs_batch *batch, float *det_images, float *diffpats,
                       float *exit_waves, unsigned flags);
 
+/* One frozen-phonon configuration of doSTEM end to end
+ * (stem3/stem3.cpp:2795-2948): make3DSlices + initSTEMSlices from host
+ * atoms into a context-owned device stack, then every position of `batch`
+ * through qs_multislice_run.  Outputs are HOST buffers (as for QS_HOST_IO);
+ * the transmission stack stays on the device. */
+int qs_stem_run(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom,
+                const qs_batch *batch, float *det_images, float *diffpats);
+
+/* ------------------------------------------------------------ profiling */
+/* Per-context counters for measurement: kernel launches of this library and,
+ * while profiling is enabled, CUDA-event times of the row and column passes
+ * of the slice loop (recorded on the context's stream around each launch). */
+typedef struct qs_stats {
+    long long launches;        /* kernels launched by this context */
+    long long row_launches, col_launches;
+    double row_ms, col_ms;     /* summed event time of the passes */
+    double row_bytes, col_bytes; /* algorithmic bytes of those passes */
+} qs_stats;
+int qs_ctx_profile(qs_ctx *ctx, int enable); /* resets the counters */
+int qs_ctx_stats(qs_ctx *ctx, qs_stats *out); /* synchronises the stream */
+
 /* collectIntensity for one wave already in k-space (after propagate):
- * returns the per-detector sums and optionally the diffraction pattern. */
+ * det_sums[d] = sum of |psi(k)|^2 over detector d's annulus (double, not yet
+ * multiplied by electronScale/(nx*ny)^2, the factor the reference applies,
+ * stem3/stemlib.cpp:2587), shifted detectors included; diffpat (may be NULL)
+ * receives the fftshifted |psi(k)|^2/sqrt(nx*ny). */
 int qs_collect(qs_ctx *ctx, const qs_params *p, const float *wave_k, double *det_sums,
                float *diffpat, unsigned flags);
 

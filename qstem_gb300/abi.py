@@ -90,6 +90,12 @@ class QsBatch(ctypes.Structure):
                 ("detPosY", ctypes.POINTER(ctypes.c_int))]
 
 
+class QsStats(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_longlong), ("row_launches", ctypes.c_longlong),
+                ("col_launches", ctypes.c_longlong), ("row_ms", ctypes.c_double), ("col_ms", ctypes.c_double),
+                ("row_bytes", ctypes.c_double), ("col_bytes", ctypes.c_double)]
+
+
 def atoms_to_numpy(atoms):
     a = np.ascontiguousarray(atoms)
     if a.dtype != ATOM_DTYPE:

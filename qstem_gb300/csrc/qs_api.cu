@@ -1,0 +1,764 @@
+// qs_api.cu -- the C ABI (include/qstem_gpu.h): contexts, argument checks,
+// host-side planning and the launch sequences of the multislice path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "qs_fft.cuh"
+#include "qs_internal.h"
+
+struct qs_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // reusable device buffers, grown on demand
+    void* buf[16] = {};
+    size_t cap[16] = {};
+    // profiling
+    bool profile = false;
+    long long launch_base = 0;
+    std::vector<cudaEvent_t> pool;       // event pool
+    size_t pool_used = 0;
+    std::vector<std::pair<size_t, size_t>> row_ev, col_ev;  // indices into pool
+    double row_bytes = 0, col_bytes = 0;
+};
+
+namespace qs {
+
+static thread_local std::string g_err;
+void set_error(const std::string& m) { g_err = m; }
+std::atomic<long long> g_launches{0};
+void count_launch(int n) { g_launches += n; }
+
+static int ev_record(qs_ctx* c, size_t* idx) {
+    if (c->pool_used == c->pool.size()) {
+        cudaEvent_t e;
+        QS_CUDA_TRY(cudaEventCreate(&e));
+        c->pool.push_back(e);
+    }
+    *idx = c->pool_used++;
+    QS_CUDA_TRY(cudaEventRecord(c->pool[*idx], c->stream));
+    return QS_OK;
+}
+
+enum Buf {
+    B_WAVES, B_PROBE, B_PARTIAL, B_POS, B_TABLES, B_TILES, B_TRANS, B_OUT1, B_OUT2, B_OUT3, B_JOBS, B_LUTS,
+    B_LUTPTR, B_SUM, B_DIFF_IN
+};
+
+static int ensure(qs_ctx* c, int which, size_t bytes, void** out) {
+    if (bytes == 0) bytes = 16;
+    if (c->cap[which] < bytes) {
+        if (c->buf[which]) {
+            cudaStreamSynchronize(c->stream);
+            cudaFree(c->buf[which]);
+            c->buf[which] = nullptr;
+            c->cap[which] = 0;
+        }
+        cudaError_t e = cudaMalloc(&c->buf[which], bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error("device allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? QS_ERR_NOMEM : QS_ERR_CUDA;
+        }
+        c->cap[which] = bytes;
+    }
+    *out = c->buf[which];
+    return QS_OK;
+}
+
+static int check_params(const qs_params* p) {
+    if (!p) { set_error("params is NULL"); return QS_ERR_ARG; }
+    if (p->nx < 1 || p->ny < 1 || p->slices < 1 || p->potNx < p->nx || p->potNy < p->ny) {
+        set_error("inconsistent grid sizes (nx, ny, potNx, potNy, slices)");
+        return QS_ERR_ARG;
+    }
+    if (!(p->resolutionX > 0) || !(p->resolutionY > 0) || !(p->sliceThickness > 0) || !(p->v0 > 0)) {
+        set_error("resolution, slice thickness and v0 must be positive");
+        return QS_ERR_ARG;
+    }
+    if (p->cellDiv != 1) { set_error("cellDiv > 1 (slab decomposition) is not supported"); return QS_ERR_UNSUPPORTED; }
+    if (p->outputInterval < 1) { set_error("outputInterval must be >= 1"); return QS_ERR_ARG; }
+    if (p->detectorNum < 0 || p->detectorNum > QS_MAX_DETECTORS) { set_error("detectorNum out of range"); return QS_ERR_ARG; }
+    return QS_OK;
+}
+
+static double wavelength(double kev) { return 12.3984244 / std::sqrt(kev * (2 * 510.99906 + kev)); }
+
+// propagate_slow's tables (stem3/stemlib.cpp:2783-2824), float arithmetic
+struct PropTables {
+    std::vector<float> kx2, ky2;
+    std::vector<float2> px, py;
+    float k2max;
+};
+static PropTables prop_tables(const qs_params& p) {
+    PropTables t;
+    const int nx = p.nx, ny = p.ny;
+    const float ax = p.resolutionX * nx, by = p.resolutionY * ny;
+    const float scale = (float)(p.sliceThickness * 3.14159265358979);
+    const float wavlen = (float)wavelength(p.v0);
+    t.kx2.resize(nx); t.px.resize(nx); t.ky2.resize(ny); t.py.resize(ny);
+    for (int i = 0; i < nx; i++) {
+        float k = (i > nx / 2) ? (float)(i - nx) / ax : (float)i / ax;
+        t.kx2[i] = k * k;
+        float a = scale * (t.kx2[i] * wavlen);
+        t.px[i] = make_float2(cosf(a), -sinf(a));
+    }
+    for (int i = 0; i < ny; i++) {
+        float k = (i > ny / 2) ? (float)(i - ny) / by : (float)i / by;
+        t.ky2[i] = k * k;
+        float a = scale * (t.ky2[i] * wavlen);
+        t.py[i] = make_float2(cosf(a), -sinf(a));
+    }
+    float k2max = nx / (2.0f * ax);
+    if (ny / (2.0f * by) < k2max) k2max = ny / (2.0f * by);
+    k2max = (float)(2.0 / 3.0 * k2max);
+    t.k2max = k2max * k2max;
+    return t;
+}
+
+static int thickness_count(const qs_params& p) { return (p.slices * p.cellDiv) / p.outputInterval + 1; }
+
+}  // namespace qs
+
+using namespace qs;
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* qs_last_error(void) { return g_err.c_str(); }
+int qs_abi_version(void) { return QS_ABI_VERSION; }
+
+int qs_ctx_create(int device, qs_ctx** out) {
+    if (!out) { set_error("out is NULL"); return QS_ERR_ARG; }
+    *out = nullptr;
+    int n = 0;
+    QS_CUDA_TRY(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) { set_error("no such CUDA device"); return QS_ERR_ARG; }
+    QS_CUDA_TRY(cudaSetDevice(device));
+    qs_ctx* c = new qs_ctx();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+        return QS_ERR_CUDA;
+    }
+    *out = c;
+    return QS_OK;
+}
+
+int qs_ctx_destroy(qs_ctx* c) {
+    if (!c) return QS_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
+    for (int i = 0; i < 16; i++)
+        if (c->buf[i]) cudaFree(c->buf[i]);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return QS_OK;
+}
+
+void* qs_ctx_stream(qs_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int qs_ctx_profile(qs_ctx* c, int enable) {
+    if (!c) { set_error("ctx is NULL"); return QS_ERR_ARG; }
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->profile = enable != 0;
+    c->launch_base = g_launches.load();
+    c->pool_used = 0;
+    c->row_ev.clear();
+    c->col_ev.clear();
+    c->row_bytes = c->col_bytes = 0;
+    return QS_OK;
+}
+
+int qs_ctx_stats(qs_ctx* c, qs_stats* out) {
+    if (!c || !out) { set_error("null argument"); return QS_ERR_ARG; }
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    std::memset(out, 0, sizeof(*out));
+    out->launches = g_launches.load() - c->launch_base;
+    out->row_launches = (long long)c->row_ev.size();
+    out->col_launches = (long long)c->col_ev.size();
+    for (auto& pr : c->row_ev) {
+        float ms = 0;
+        QS_CUDA_TRY(cudaEventElapsedTime(&ms, c->pool[pr.first], c->pool[pr.second]));
+        out->row_ms += ms;
+    }
+    for (auto& pr : c->col_ev) {
+        float ms = 0;
+        QS_CUDA_TRY(cudaEventElapsedTime(&ms, c->pool[pr.first], c->pool[pr.second]));
+        out->col_ms += ms;
+    }
+    out->row_bytes = c->row_bytes;
+    out->col_bytes = c->col_bytes;
+    return QS_OK;
+}
+
+int qs_params_finalize(qs_params* p) {
+    if (!p) { set_error("params is NULL"); return QS_ERR_ARG; }
+    const double wl = wavelength(p->v0);
+    for (int i = 0; i < p->detectorNum && i < QS_MAX_DETECTORS; i++) {
+        qs_detector* d = &p->detectors[i];
+        d->k2Inside = (float)(std::sin(d->rInside * 0.001) / wl);
+        d->k2Outside = (float)(std::sin(d->rOutside * 0.001) / wl);
+        d->k2Inside *= d->k2Inside;
+        d->k2Outside *= d->k2Outside;
+    }
+    return QS_OK;
+}
+
+int qs_thickness_count(const qs_params* p) {
+    if (!p || p->outputInterval < 1) return 0;
+    return thickness_count(*p);
+}
+
+int qs_lut_build(qs_ctx* c, const qs_params* p, int Z, double B, int charged, float* out, int* Nz, int* Nr,
+                 int* nzSub, unsigned flags) {
+    if (!c) { set_error("ctx is NULL"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    int nz = 0, nr = 0, ns = 0;
+    QS_TRY(build_lut(*p, Z, B, charged, nullptr, &nz, &nr, &ns, c->stream));
+    if (Nz) *Nz = nz;
+    if (Nr) *Nr = nr;
+    if (nzSub) *nzSub = ns;
+    if (!out) return QS_OK;
+    float* dst = out;
+    if (flags & QS_HOST_IO) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_OUT1, sizeof(float) * (size_t)nz * nr, &d));
+        dst = (float*)d;
+    }
+    QS_TRY(build_lut(*p, Z, B, charged, dst, nullptr, nullptr, nullptr, c->stream));
+    if (flags & QS_HOST_IO) {
+        QS_CUDA_TRY(cudaMemcpyAsync(out, dst, sizeof(float) * (size_t)nz * nr, cudaMemcpyDeviceToHost, c->stream));
+        QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    } else if (flags & QS_SYNC) {
+        QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    return QS_OK;
+}
+
+int qs_slices_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, float* trans_out,
+                    unsigned flags) {
+    if (!c || !trans_out || (natom > 0 && !atoms)) { set_error("null argument"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    if (!p->fftpotential || !p->potential3D) {
+        set_error("only the 3-D FFT-integrated potential (one time integration, potential3D) is supported");
+        return QS_ERR_UNSUPPORTED;
+    }
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    const qs_params& P = *p;
+    const size_t nTrans = (size_t)P.slices * P.potNx * P.potNy;
+    float2* trans = (float2*)trans_out;
+    if (flags & QS_HOST_IO) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_TRANS, sizeof(float2) * nTrans, &d));
+        trans = (float2*)d;
+    }
+    QS_CUDA_TRY(cudaMemsetAsync(trans, 0, sizeof(float2) * nTrans, c->stream));
+
+    // ---- host plan: the control flow of make3DSlices' atom loop
+    // (stem3/stemlib.cpp:678-1213) reduced to one job per contributing atom
+    std::vector<qs_atom> at(atoms, atoms + natom);
+    std::stable_sort(at.begin(), at.end(), [](const qs_atom& a, const qs_atom& b) { return a.z < b.z; });
+    const float cz = P.sliceThickness * (float)P.slices;
+    const float dx = P.resolutionX, dy = P.resolutionY, dzs = P.sliceThickness;
+    const int iRadX = (int)ceilf(P.atomRadius / dx), iRadY = (int)ceilf(P.atomRadius / dy);
+    const int iRadZ = (int)ceilf(P.atomRadius / dzs);
+    std::vector<AtomJob> jobs;
+    std::map<int, int> lutIndex;          // key Z*2+charged -> index
+    std::vector<std::pair<int, double>> lutKeys;  // (key, B)
+    auto atomz = [&](int i) {
+        float z = (float)((double)(at[i].z - cz * 0.0f + P.czOffset) - 0.5 * P.sliceThickness * (1 - P.centerSlices));
+        z -= P.sliceThickness;
+        return z;
+    };
+    for (int ia = 0; ia < natom; ia++) {
+        while (ia < natom && at[ia].Znum == 0) ia++;
+        if (ia >= natom) break;
+        float atomZ = atomz(ia);
+        if (P.nonPeriodZ) {
+            if (atomZ - P.atomRadius > cz) break;
+            do {
+                if (atomZ + P.atomRadius + P.sliceThickness >= 0) break;
+                ++ia;
+                atomZ = atomz(ia);
+            } while (ia < natom - 1);
+        }
+        const float atomX = at[ia].x - P.potOffsetX, atomY = at[ia].y - P.potOffsetY;
+        const int iAtomX = (int)floorf(atomX / dx), iAtomY = (int)floorf(atomY / dy);
+        atomZ += P.sliceThickness;
+        const int iAtomZ = (int)floor(atomZ / dzs + 0.5);
+        AtomJob J;
+        if (P.nonPeriod) {
+            J.iax0 = std::max(iAtomX - iRadX, 0);
+            J.iax1 = std::min(iAtomX + iRadX, P.potNx - 1);
+            J.iay0 = std::max(iAtomY - iRadY, 0);
+            J.iay1 = std::min(iAtomY + iRadY, P.potNy - 1);
+            if (!((J.iax0 < P.potNx) && (J.iax1 >= 0) && (J.iay0 < P.potNy) && (J.iay1 >= 0))) continue;
+        } else {
+            J.iax0 = iAtomX - iRadX;
+            J.iax1 = iAtomX + iRadX - 1;
+            J.iay0 = iAtomY - iRadY;
+            J.iay1 = iAtomY + iRadY - 1;
+        }
+        J.iaz0 = iAtomZ - iRadZ < 0 ? -iAtomZ : -iRadZ;
+        J.iaz1 = iAtomZ + iRadZ >= P.slices ? P.slices - iAtomZ - 1 : iRadZ;
+        if (!((iAtomZ + J.iaz0 < P.slices) && (iAtomZ + J.iaz1 >= 0))) continue;
+        const int Z = at[ia].Znum;
+        if (Z < 1 || Z >= 93) continue;
+        if (J.iax1 < J.iax0 || J.iay1 < J.iay0 || J.iaz1 < J.iaz0) continue;
+        const double B = P.tds ? 0.0 : at[ia].dw;
+        for (int charged = 0; charged < 2; charged++) {
+            if (charged && at[ia].q == 0) break;
+            const int key = Z * 2 + charged;
+            if (!lutIndex.count(key)) {
+                lutIndex[key] = (int)lutKeys.size();
+                lutKeys.push_back({key, B});
+            }
+        }
+        J.atomX = atomX;
+        J.atomY = atomY;
+        J.atomZ = atomZ;
+        J.q = at[ia].q;
+        J.iAtomZ = iAtomZ;
+        J.lut = lutIndex[Z * 2];
+        J.lutq = at[ia].q != 0 ? lutIndex[Z * 2 + 1] : -1;
+        jobs.push_back(J);
+    }
+
+    if (!jobs.empty()) {
+        int Nz = 0, Nr = 0, ns = 0;
+        QS_TRY(build_lut(P, 1, 0.0, 0, nullptr, &Nz, &Nr, &ns, c->stream));
+        const size_t lutElems = (size_t)Nz * Nr;
+        void *dl = nullptr, *dp = nullptr, *dj = nullptr;
+        QS_TRY(ensure(c, B_LUTS, sizeof(float) * lutElems * lutKeys.size(), &dl));
+        QS_TRY(ensure(c, B_LUTPTR, sizeof(float*) * lutKeys.size(), &dp));
+        QS_TRY(ensure(c, B_JOBS, sizeof(AtomJob) * jobs.size(), &dj));
+        std::vector<const float*> ptrs(lutKeys.size());
+        for (size_t k = 0; k < lutKeys.size(); k++) {
+            float* d = (float*)dl + k * lutElems;
+            ptrs[k] = d;
+            QS_TRY(build_lut(P, lutKeys[k].first / 2, lutKeys[k].second, lutKeys[k].first % 2, d, nullptr, nullptr,
+                             nullptr, c->stream));
+        }
+        QS_CUDA_TRY(cudaMemcpyAsync(dp, ptrs.data(), sizeof(float*) * ptrs.size(), cudaMemcpyHostToDevice, c->stream));
+        QS_CUDA_TRY(cudaMemcpyAsync(dj, jobs.data(), sizeof(AtomJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream));
+        // the host vectors must outlive the async copies
+        QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), (const float* const*)dp, Nz, Nr, ns, P, trans,
+                              c->stream));
+    }
+
+    if (!(flags & QS_OUT_POTENTIAL)) {
+        // initSTEMSlices (stem3/stemlib.cpp:2280-2336)
+        const double mm0 = (double)(1.0f + P.v0 / 511.0f);
+        QS_TRY(launch_phase_grating(trans, nTrans, mm0 * wavelength(P.v0), c->stream));
+        if (P.bandlimittrans) {
+            if (!line_supported(P.potNx) || !line_supported(P.potNy)) {
+                set_error("band-limiting the transmission function needs potNx, potNy in {64,128,256,384,512,768,1024}");
+                return QS_ERR_UNSUPPORTED;
+            }
+            const int nx = P.potNx, ny = P.potNy;
+            std::vector<float> kx2(nx), ky2(ny);
+            for (int ix = 0; ix < nx; ix++) {
+                float kx = (ix > nx / 2) ? (float)(ix - nx) / P.potSizeX : (float)ix / P.potSizeX;
+                kx2[ix] = kx * kx;
+            }
+            for (int iy = 0; iy < ny; iy++) {
+                float ky = (iy > ny / 2) ? (float)(iy - ny) / P.by : (float)iy / P.potSizeY;
+                ky2[iy] = ky * ky;
+            }
+            float k2max = nx / (2.0f * P.potSizeX), tt = ny / (2.0f * P.potSizeY);
+            if (tt < k2max) k2max = tt;
+            k2max = (float)((2.0f / 3.0f) * k2max);
+            k2max = k2max * k2max;
+            void* dt = nullptr;
+            QS_TRY(ensure(c, B_TABLES, sizeof(float) * (nx + ny), &dt));
+            std::vector<float> both(kx2);
+            both.insert(both.end(), ky2.begin(), ky2.end());
+            QS_CUDA_TRY(cudaMemcpyAsync(dt, both.data(), sizeof(float) * both.size(), cudaMemcpyHostToDevice, c->stream));
+            QS_TRY(fft2d(trans, nx, ny, P.slices, false, c->stream));
+            QS_TRY(launch_bandlimit_mask(trans, P.slices, nx, ny, (float*)dt, (float*)dt + nx, k2max,
+                                         1.0 / (nx * ny), c->stream));
+            QS_TRY(fft2d(trans, nx, ny, P.slices, true, c->stream));
+            QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        }
+    }
+    if (flags & QS_HOST_IO) {
+        QS_CUDA_TRY(cudaMemcpyAsync(trans_out, trans, sizeof(float2) * nTrans, cudaMemcpyDeviceToHost, c->stream));
+        QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    } else if (flags & QS_SYNC) {
+        QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    return QS_OK;
+}
+
+static int probe_into(qs_ctx* c, const qs_params& P, double dx, double dy, float2* w) {
+    if (!line_supported(P.nx) || !line_supported(P.ny)) {
+        set_error("probe: nx, ny must be in {64,128,256,384,512,768,1024}");
+        return QS_ERR_UNSUPPORTED;
+    }
+    void* ds = nullptr;
+    QS_TRY(ensure(c, B_SUM, sizeof(double) * 2, &ds));
+    QS_TRY(launch_probe_kspace(P, dx, dy, w, c->stream));
+    QS_TRY(fft2d(w, P.nx, P.ny, 1, true, c->stream));
+    QS_TRY(launch_probe_realspace(P, dx, dy, w, (double*)ds, c->stream));
+    QS_TRY(launch_scale_by_sum(w, (size_t)P.nx * P.ny, (double*)ds, (double)P.nx * (double)P.ny, c->stream));
+    return QS_OK;
+}
+
+int qs_probe(qs_ctx* c, const qs_params* p, double dx, double dy, float* wave, unsigned flags) {
+    if (!c || !wave) { set_error("null argument"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    const size_t n = (size_t)p->nx * p->ny;
+    float2* w = (float2*)wave;
+    if (flags & QS_HOST_IO) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_PROBE, sizeof(float2) * n, &d));
+        w = (float2*)d;
+    }
+    QS_TRY(probe_into(c, *p, dx, dy, w));
+    if (flags & QS_HOST_IO) {
+        QS_CUDA_TRY(cudaMemcpyAsync(wave, w, sizeof(float2) * n, cudaMemcpyDeviceToHost, c->stream));
+        QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    } else if (flags & QS_SYNC) {
+        QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    return QS_OK;
+}
+
+int qs_multislice_run(qs_ctx* c, const qs_params* p, const float* trans_in, const float* probe_in,
+                      const qs_batch* batch, float* det_images, float* diffpats, float* exit_waves, unsigned flags) {
+    if (!c || !trans_in || !batch) { set_error("null argument"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    const qs_params& P = *p;
+    if (!line_supported(P.nx) || !line_supported(P.ny)) {
+        set_error("multislice: nx, ny must be in {64,128,256,384,512,768,1024}");
+        return QS_ERR_UNSUPPORTED;
+    }
+    for (int d = 0; d < P.detectorNum; d++)
+        if (P.detectors[d].shiftX != 0 || P.detectors[d].shiftY != 0) {
+            set_error("multislice: shifted detectors are supported by qs_collect only");
+            return QS_ERR_UNSUPPORTED;
+        }
+    const int npos = batch->npos;
+    if (npos < 1) { set_error("batch has no positions"); return QS_ERR_ARG; }
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const int nx = P.nx, ny = P.ny, S = P.slices;
+    const size_t N = (size_t)nx * ny;
+    const bool host = (flags & QS_HOST_IO) != 0;
+    const int nT = thickness_count(P);
+    const int ndet = P.detectorNum;
+    const int npix = P.scanXN * P.scanYN;
+
+    // positions (host side)
+    std::vector<int> px(npos), py(npos), dxp(npos), dyp(npos);
+    for (int i = 0; i < npos; i++) {
+        if (batch->iPosX && batch->iPosY) {
+            px[i] = batch->iPosX[i];
+            py[i] = batch->iPosY[i];
+        } else {
+            const int ix = i / P.scanYN, iy = i % P.scanYN;
+            int x = (int)((float)ix * (P.scanXStop - P.scanXStart) / ((float)P.scanXN * P.resolutionX));
+            int y = (int)((float)iy * (P.scanYStop - P.scanYStart) / ((float)P.scanYN * P.resolutionY));
+            px[i] = std::min(x, P.potNx - nx);
+            py[i] = std::min(y, P.potNy - ny);
+        }
+        dxp[i] = batch->detPosX ? batch->detPosX[i] : i / P.scanYN;
+        dyp[i] = batch->detPosY ? batch->detPosY[i] : i % P.scanYN;
+        if (px[i] < 0 || py[i] < 0 || px[i] > P.potNx - nx || py[i] > P.potNy - ny) {
+            set_error("position " + std::to_string(i) + " puts the window outside the potential array");
+            return QS_ERR_ARG;
+        }
+        if (ndet > 0 && det_images && (dxp[i] < 0 || dxp[i] >= P.scanXN || dyp[i] < 0 || dyp[i] >= P.scanYN)) {
+            set_error("detector pixel of position " + std::to_string(i) + " outside the scan raster");
+            return QS_ERR_ARG;
+        }
+    }
+
+    // propagator tables, band, column tiles
+    PropTables tb = prop_tables(P);
+    int yA = -1, yB = ny;
+    for (int iy = 0; iy <= ny / 2; iy++) if (tb.ky2[iy] < tb.k2max) yA = iy;
+    for (int iy = ny - 1; iy > ny / 2; iy--) if (tb.ky2[iy] < tb.k2max) yB = iy;
+    bool contiguous = true;
+    for (int iy = 0; iy < ny; iy++) {
+        const bool in = tb.ky2[iy] < tb.k2max;
+        if (in != (iy <= yA || iy >= yB)) contiguous = false;
+    }
+    if (!contiguous) { yA = ny; yB = ny; }
+    const int C = col_tile_width(nx);
+    std::vector<int> tiles;
+    for (int c0 = 0; c0 < ny; c0 += C) {
+        bool any = false;
+        for (int k = c0; k < c0 + C && k < ny; k++) any |= (k <= yA || k >= yB);
+        if (any) tiles.push_back(c0);
+    }
+    const int ntiles = (int)tiles.size();
+
+    // output slices: slice s writes thickness slot tOf[s] (collectIntensity's
+    // t, stem3/stemlib.cpp:2597-2610); a slot keeps its last writer only
+    std::vector<int> lastWriter(nT, -1), slotOf(S, -1);
+    for (int sl = 0; sl < S; sl++) {
+        const int t = (sl < S * P.cellDiv - 1) ? sl / P.outputInterval : nT - 1;
+        lastWriter[t] = sl;
+    }
+    for (int t = 0; t < nT; t++) if (lastWriter[t] >= 0) slotOf[lastWriter[t]] = t;
+    const bool wantDet = ndet > 0 && det_images != nullptr;
+
+    // device buffers: tables | tiles | positions
+    void* dtab = nullptr;
+    const size_t tabBytes = sizeof(float) * (nx + ny) + sizeof(float2) * (nx + ny);
+    QS_TRY(ensure(c, B_TABLES, tabBytes, &dtab));
+    float* d_kx2 = (float*)dtab;
+    float* d_ky2 = d_kx2 + nx;
+    float2* d_px = (float2*)(d_ky2 + ny);
+    float2* d_py = d_px + nx;
+    QS_CUDA_TRY(cudaMemcpyAsync(d_kx2, tb.kx2.data(), sizeof(float) * nx, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_ky2, tb.ky2.data(), sizeof(float) * ny, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_px, tb.px.data(), sizeof(float2) * nx, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_py, tb.py.data(), sizeof(float2) * ny, cudaMemcpyHostToDevice, s));
+    void* dtiles = nullptr;
+    QS_TRY(ensure(c, B_TILES, sizeof(int) * std::max(ntiles, 1), &dtiles));
+    if (ntiles) QS_CUDA_TRY(cudaMemcpyAsync(dtiles, tiles.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, s));
+    void* dpos = nullptr;
+    QS_TRY(ensure(c, B_POS, sizeof(int) * 4 * (size_t)npos, &dpos));
+    int* d_px_pos = (int*)dpos;
+    int* d_py_pos = d_px_pos + npos;
+    int* d_dx_pos = d_py_pos + npos;
+    int* d_dy_pos = d_dx_pos + npos;
+    QS_CUDA_TRY(cudaMemcpyAsync(d_px_pos, px.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_py_pos, py.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_dx_pos, dxp.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_dy_pos, dyp.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
+
+    // transmission and probe
+    const size_t nTrans = (size_t)S * P.potNx * P.potNy;
+    const float2* trans = (const float2*)trans_in;
+    if (host) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_TRANS, sizeof(float2) * nTrans, &d));
+        QS_CUDA_TRY(cudaMemcpyAsync(d, trans_in, sizeof(float2) * nTrans, cudaMemcpyHostToDevice, s));
+        trans = (const float2*)d;
+    }
+    void* dprobe = nullptr;
+    QS_TRY(ensure(c, B_PROBE, sizeof(float2) * N, &dprobe));
+    if (probe_in) {
+        QS_CUDA_TRY(cudaMemcpyAsync(dprobe, probe_in, sizeof(float2) * N,
+                                    host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    } else {
+        QS_TRY(probe_into(c, P, (double)(nx / 2 * P.resolutionX), (double)(ny / 2 * P.resolutionY),
+                          (float2*)dprobe));
+    }
+
+    // outputs
+    float* det_dev = det_images;
+    const size_t detElems = (size_t)nT * ndet * npix;
+    if (wantDet && host) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_OUT1, sizeof(float) * detElems, &d));
+        det_dev = (float*)d;
+    }
+    if (wantDet) QS_CUDA_TRY(cudaMemsetAsync(det_dev, 0, sizeof(float) * detElems, s));
+
+    // batch chunking by free device memory (admission control)
+    size_t freeB = 0, totalB = 0;
+    QS_CUDA_TRY(cudaMemGetInfo(&freeB, &totalB));
+    const size_t perWave = sizeof(float2) * N + (size_t)nT * ntiles * std::max(ndet, 1) * sizeof(double) +
+                           (host && diffpats ? sizeof(float) * N : 0) + (host && exit_waves ? sizeof(float2) * N : 0);
+    const size_t have = c->cap[B_WAVES] / (sizeof(float2) * N);
+    const size_t budget = freeB > ((size_t)1 << 30) ? freeB - ((size_t)1 << 30) : freeB / 2;
+    size_t chunk = std::min<size_t>((size_t)npos, std::max<size_t>(have, budget / perWave));
+    if (chunk < 1) { set_error("not enough device memory for one wave"); return QS_ERR_NOMEM; }
+    if (chunk < (size_t)npos) chunk = std::max<size_t>(1, chunk & ~(size_t)7);  // keep 8-row multiples
+
+    void* dw = nullptr;
+    QS_TRY(ensure(c, B_WAVES, sizeof(float2) * N * chunk, &dw));
+    float2* waves = (float2*)dw;
+    void* dpart = nullptr;
+    const size_t partPerT = chunk * ntiles * std::max(ndet, 1);
+    QS_TRY(ensure(c, B_PARTIAL, sizeof(double) * partPerT * nT, &dpart));
+    float* dp_dev = nullptr;
+    if (diffpats && host) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_OUT2, sizeof(float) * N * chunk, &d));
+        dp_dev = (float*)d;
+    }
+    float2* ew_dev = nullptr;
+    if (exit_waves && host) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_OUT3, sizeof(float2) * N * chunk, &d));
+        ew_dev = (float2*)d;
+    }
+    const float2* tw_y = twiddles(ny);
+    const float2* tw_x = twiddles(nx);
+    if (!tw_y || !tw_x) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
+    const double scaleDet = (double)P.electronScale / ((double)(nx * ny) * (double)(nx * ny));
+
+    for (size_t p0 = 0; p0 < (size_t)npos; p0 += chunk) {
+        const int nb = (int)std::min(chunk, (size_t)npos - p0);
+        float* dpOut = diffpats ? (host ? dp_dev : diffpats + p0 * N) : nullptr;
+        float2* ewOut = exit_waves ? (host ? ew_dev : (float2*)exit_waves + p0 * N) : nullptr;
+        if (dpOut) QS_CUDA_TRY(cudaMemsetAsync(dpOut, 0, sizeof(float) * N * nb, s));
+
+        RowArgs ra{};
+        ra.nx = nx; ra.ny = ny; ra.potNx = P.potNx; ra.potNy = P.potNy;
+        ra.nwaves = nb; ra.probe = (const float2*)dprobe; ra.waves = waves; ra.exit_waves = ewOut;
+        ra.posX = d_px_pos + p0; ra.posY = d_py_pos + p0; ra.tw = tw_y; ra.yA = yA; ra.yB = yB;
+        ra.norm = (float)(1.0 / (double)(nx * ny));
+        ColArgs ca{};
+        ca.nx = nx; ca.ny = ny; ca.nwaves = nb; ca.waves = waves; ca.tw = tw_x;
+        ca.kx2 = d_kx2; ca.ky2 = d_ky2; ca.px = d_px; ca.py = d_py; ca.k2max = tb.k2max;
+        ca.tiles = (const int*)dtiles; ca.ntiles = ntiles;
+        for (int d = 0; d < ndet; d++) {
+            ca.k2in[d] = P.detectors[d].k2Inside;
+            ca.k2out[d] = P.detectors[d].k2Outside;
+        }
+        ca.scaleDiff = 1.0 / std::sqrt((double)(nx * ny));
+
+        const double rowBytes = 24.0 * (double)N * nb, colBytes = 16.0 * (double)N * nb;
+        auto rows = [&](RowMode m) -> int {
+            size_t e0 = 0, e1 = 0;
+            if (c->profile) QS_TRY(ev_record(c, &e0));
+            QS_TRY(launch_rows(ra, m, s));
+            if (c->profile) {
+                QS_TRY(ev_record(c, &e1));
+                c->row_ev.push_back({e0, e1});
+                c->row_bytes += rowBytes;
+            }
+            return QS_OK;
+        };
+        auto cols = [&]() -> int {
+            size_t e0 = 0, e1 = 0;
+            if (c->profile) QS_TRY(ev_record(c, &e0));
+            QS_TRY(launch_cols(ca, s));
+            if (c->profile) {
+                QS_TRY(ev_record(c, &e1));
+                c->col_ev.push_back({e0, e1});
+                c->col_bytes += colBytes;
+            }
+            return QS_OK;
+        };
+        ra.trans_slice = trans;
+        QS_TRY(rows(ROW_FIRST));
+        for (int sl = 0; sl < S; sl++) {
+            const int slot = slotOf[sl];
+            ca.ndet = (wantDet && slot >= 0) ? ndet : 0;
+            ca.partial = (double*)dpart + (slot >= 0 ? (size_t)slot * partPerT : 0);
+            ca.diffpat = (sl == S - 1) ? dpOut : nullptr;
+            ca.inverse = (sl < S - 1 || ewOut) ? 1 : 0;
+            QS_TRY(cols());
+            if (sl < S - 1) {
+                ra.trans_slice = trans + (size_t)(sl + 1) * P.potNx * P.potNy;
+                QS_TRY(rows(ROW_MID));
+            }
+        }
+        if (ewOut) QS_TRY(launch_rows(ra, ROW_LAST, s));
+        if (wantDet)
+            for (int t = 0; t < nT; t++) {
+                if (lastWriter[t] < 0) continue;
+                QS_TRY(launch_det_finalize((double*)dpart + (size_t)t * partPerT, nb, ntiles, ndet, scaleDet,
+                                           d_dx_pos + p0, d_dy_pos + p0, P.scanYN, npix,
+                                           det_dev + (size_t)t * ndet * npix, s));
+            }
+        if (host && diffpats)
+            QS_CUDA_TRY(cudaMemcpyAsync(diffpats + p0 * N, dpOut, sizeof(float) * N * nb, cudaMemcpyDeviceToHost, s));
+        if (host && exit_waves)
+            QS_CUDA_TRY(cudaMemcpyAsync(exit_waves + 2 * p0 * N, ewOut, sizeof(float2) * N * nb,
+                                        cudaMemcpyDeviceToHost, s));
+    }
+    if (wantDet && host)
+        QS_CUDA_TRY(cudaMemcpyAsync(det_images, det_dev, sizeof(float) * detElems, cudaMemcpyDeviceToHost, s));
+    if (host || (flags & QS_SYNC)) QS_CUDA_TRY(cudaStreamSynchronize(s));
+    return QS_OK;
+}
+
+int qs_stem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, const qs_batch* batch,
+                float* det_images, float* diffpats) {
+    if (!c || !batch) { set_error("null argument"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    const size_t nTrans = (size_t)p->slices * p->potNx * p->potNy;
+    void* dstack = nullptr;
+    // B_DIFF_IN doubles as the configuration's transmission stack here
+    QS_TRY(ensure(c, B_DIFF_IN, sizeof(float2) * nTrans, &dstack));
+    QS_TRY(qs_slices_build(c, p, atoms, natom, (float*)dstack, 0));
+    const qs_params& P = *p;
+    const int nT = thickness_count(P);
+    const int npix = P.scanXN * P.scanYN;
+    const size_t N = (size_t)P.nx * P.ny;
+    float* ddet = nullptr;
+    float* ddp = nullptr;
+    if (det_images && P.detectorNum > 0) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_OUT1, sizeof(float) * (size_t)nT * P.detectorNum * npix, &d));
+        ddet = (float*)d;
+    }
+    if (diffpats) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_OUT2, sizeof(float) * N * batch->npos, &d));
+        ddp = (float*)d;
+    }
+    QS_TRY(qs_multislice_run(c, p, (const float*)dstack, nullptr, batch, ddet, ddp, nullptr, 0));
+    if (ddet)
+        QS_CUDA_TRY(cudaMemcpyAsync(det_images, ddet, sizeof(float) * (size_t)nT * P.detectorNum * npix,
+                                    cudaMemcpyDeviceToHost, c->stream));
+    if (ddp)
+        QS_CUDA_TRY(cudaMemcpyAsync(diffpats, ddp, sizeof(float) * N * batch->npos, cudaMemcpyDeviceToHost,
+                                    c->stream));
+    QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return QS_OK;
+}
+
+int qs_collect(qs_ctx* c, const qs_params* p, const float* wave_k, double* det_sums, float* diffpat,
+               unsigned flags) {
+    if (!c || !wave_k) { set_error("null argument"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    const qs_params& P = *p;
+    cudaStream_t s = c->stream;
+    const size_t N = (size_t)P.nx * P.ny;
+    const bool host = (flags & QS_HOST_IO) != 0;
+    PropTables tb = prop_tables(P);
+    void* dtab = nullptr;
+    QS_TRY(ensure(c, B_TABLES, sizeof(float) * (P.nx + P.ny), &dtab));
+    QS_CUDA_TRY(cudaMemcpyAsync(dtab, tb.kx2.data(), sizeof(float) * P.nx, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync((float*)dtab + P.nx, tb.ky2.data(), sizeof(float) * P.ny, cudaMemcpyHostToDevice, s));
+    const float2* w = (const float2*)wave_k;
+    if (host) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_DIFF_IN, sizeof(float2) * N, &d));
+        QS_CUDA_TRY(cudaMemcpyAsync(d, wave_k, sizeof(float2) * N, cudaMemcpyHostToDevice, s));
+        w = (const float2*)d;
+    }
+    void* dsum = nullptr;
+    QS_TRY(ensure(c, B_SUM, sizeof(double) * QS_MAX_DETECTORS, &dsum));
+    float* dp = diffpat;
+    if (diffpat && host) {
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_OUT2, sizeof(float) * N, &d));
+        dp = (float*)d;
+    }
+    QS_TRY(launch_collect(P, w, (float*)dtab, (float*)dtab + P.nx, (double*)dsum, dp, s));
+    if (det_sums && P.detectorNum > 0)
+        QS_CUDA_TRY(cudaMemcpyAsync(det_sums, dsum, sizeof(double) * P.detectorNum,
+                                    host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+    if (diffpat && host) QS_CUDA_TRY(cudaMemcpyAsync(diffpat, dp, sizeof(float) * N, cudaMemcpyDeviceToHost, s));
+    if (host || (flags & QS_SYNC)) QS_CUDA_TRY(cudaStreamSynchronize(s));
+    return QS_OK;
+}
+
+}  // extern "C"

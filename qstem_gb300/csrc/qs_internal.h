@@ -1,0 +1,115 @@
+// qs_internal.h -- declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/qstem_gpu.h"
+
+namespace qs {
+
+// ------------------------------------------------------------- errors
+void set_error(const std::string& msg);
+// process-wide count of kernels this library launched (for measurement)
+void count_launch(int n);
+#define QS_CUDA_TRY(expr)                                                               \
+    do {                                                                                \
+        cudaError_t _e = (expr);                                                        \
+        if (_e != cudaSuccess) {                                                        \
+            ::qs::set_error(std::string(#expr " failed: ") + cudaGetErrorString(_e));   \
+            return QS_ERR_CUDA;                                                         \
+        }                                                                               \
+    } while (0)
+#define QS_TRY(expr)              \
+    do {                          \
+        int _rc = (expr);         \
+        if (_rc != QS_OK) return _rc; \
+    } while (0)
+
+// ------------------------------------------------------ multislice step
+// Arguments of one row pass (transforms along y, the contiguous index).
+enum RowMode { ROW_FIRST = 0, ROW_MID = 1, ROW_LAST = 2 };
+
+struct RowArgs {
+    int nx, ny, potNx, potNy;
+    int nwaves;
+    const float2* trans_slice;   // potNx x potNy c64 of the slice applied here
+    const float2* probe;         // nx x ny (ROW_FIRST)
+    float2* waves;               // nwaves x nx x ny
+    float2* exit_waves;          // ROW_LAST destination (may alias waves)
+    const int* posX;             // nwaves window offsets
+    const int* posY;
+    const float2* tw;            // exp(-2 pi i k/ny), k < ny
+    int yA, yB;                  // ky index in band iff iy <= yA || iy >= yB
+    float norm;                  // 1/(nx*ny)
+};
+
+// Arguments of one column pass (transforms along x).
+struct ColArgs {
+    int nx, ny, nwaves;
+    float2* waves;
+    const float2* tw;            // exp(-2 pi i k/nx), k < nx
+    const float* kx2;            // nx, float as propagate_slow computes
+    const float* ky2;            // ny
+    const float2* px;            // nx propagator factors (cos t, -sin t)
+    const float2* py;            // ny
+    float k2max;
+    const int* tiles;            // column tile starts (ky0) of the in-band tiles
+    int ntiles;
+    int inverse;                 // 1: inverse x-transform and store; 0: k-space only
+    // detectors (active when ndet > 0)
+    int ndet;
+    float k2in[QS_MAX_DETECTORS], k2out[QS_MAX_DETECTORS];
+    double* partial;             // [nwaves][ntiles][ndet]
+    float* diffpat;              // [nwaves][nx][ny] or null
+    double scaleDiff;
+};
+
+int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s);
+int launch_cols(const ColArgs& a, cudaStream_t s);
+int col_tile_width(int nx);
+int launch_det_finalize(const double* partial, int nwaves, int ntiles, int ndet, double scale,
+                        const int* detPosX, const int* detPosY, int scanYN, int npix, float* det_out,
+                        cudaStream_t s);
+
+// generic in-place 2-D transform of `howmany` n0 x n1 arrays
+int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t s);
+// twiddle table exp(-2 pi i k/n), k < n, device-resident, cached per n
+const float2* twiddles(int n);
+
+// ---------------------------------------------------------- potentials
+struct LutTable {
+    float* d_lut = nullptr;  // Nz x Nr
+    int Nz = 0, Nr = 0, nzSub = 0;
+};
+int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, int* Nz, int* Nr,
+              int* nzSub, cudaStream_t s);
+
+struct AtomJob {
+    float atomX, atomY, atomZ;   // atomZ after the reference's offsets
+    float q;
+    int iax0, iax1, iay0, iay1;  // inclusive pixel box (unwrapped coordinates)
+    int iaz0, iaz1;              // slice range relative to iAtomZ
+    int iAtomZ;
+    int lut, lutq;               // LUT indices (-1: none)
+};
+int launch_scatter(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
+                   const qs_params& p, float2* trans, cudaStream_t s);
+int launch_phase_grating(float2* trans, size_t n, double scale, cudaStream_t s);
+int launch_bandlimit_mask(float2* trans, int slices, int potNx, int potNy, const float* kx2,
+                          const float* ky2, float k2max, double fftScale, cudaStream_t s);
+
+// ---------------------------------------------------------------- probe
+int launch_probe_kspace(const qs_params& p, double dx, double dy, float2* wave, cudaStream_t s);
+int launch_probe_realspace(const qs_params& p, double dx, double dy, float2* wave, double* d_sum,
+                           cudaStream_t s);
+int launch_scale_by_sum(float2* wave, size_t n, const double* d_sum, double nxy, cudaStream_t s);
+
+// collectIntensity for one k-space wave (compat entry point)
+int launch_collect(const qs_params& p, const float2* wave_k, const float* kx2, const float* ky2,
+                   double* d_sums, float* diffpat, cudaStream_t s);
+
+}  // namespace qs

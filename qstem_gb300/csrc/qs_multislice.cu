@@ -1,0 +1,434 @@
+// qs_multislice.cu -- the fused per-slice passes of the multislice loop.
+//
+// The reference's slice step (runMulsSTEM, stem3/stemlib.cpp:2403-2486) is
+//   transmit -> FFT2 -> propagate_slow -> collectIntensity -> IFFT2 -> /N.
+// Here the 2-D transforms are split into their row (y, contiguous) and
+// column (x, strided) halves and the pointwise work is fused into them, so
+// that a wave crosses HBM twice per slice:
+//   row pass    IFFT_y of the previous slice, 1/N, transmit with slice s,
+//               FFT_y                              (ms_rows)
+//   column pass FFT_x, propagator and band limit, detector sums and the
+//               diffraction pattern on output slices, IFFT_x   (ms_cols)
+// The 2/3 band limit zeroes every column ky with ky^2 >= k2max, so those
+// columns are neither stored by the row pass nor touched by the column pass,
+// and the next row pass reads them as zeros.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "qs_fft.cuh"
+#include "qs_internal.h"
+
+namespace qs {
+
+constexpr int ROW_LINES = 8;
+
+template <int N, int MODE>
+__global__ void __launch_bounds__(line_threads(N) * ROW_LINES)
+    ms_rows(RowArgs a) {
+    using Cfg = typename Line<N>::cfg;
+    constexpr int T = Cfg::T, E = Cfg::E;
+    extern __shared__ float2 dsm[];
+    float2* s_tw = dsm;
+    float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
+    const int tid = threadIdx.x + T * threadIdx.y;
+    for (int i = tid; i < N; i += T * ROW_LINES) s_tw[i] = a.tw[i];
+    __syncthreads();
+
+    const int t = threadIdx.x;
+    const long line = (long)blockIdx.x * ROW_LINES + threadIdx.y;
+    const int b = (int)(line / a.nx);
+    const int x = (int)(line - (long)b * a.nx);
+    const SmemRow sm{s_line};
+    float2 reg[E];
+    if constexpr (MODE == ROW_FIRST) {
+        const float2* src = a.probe + (size_t)x * N;
+#pragma unroll
+        for (int e = 0; e < E; ++e) reg[e] = __ldg(src + t + T * e);
+    } else {
+        const float2* src = a.waves + ((size_t)b * a.nx + x) * N;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int y = t + T * e;
+            reg[e] = (y <= a.yA || y >= a.yB) ? src[y] : make_float2(0.f, 0.f);
+        }
+        line_fft<Cfg, true>(reg, sm, s_tw, t);
+#pragma unroll
+        for (int e = 0; e < E; ++e) reg[e] = cscale(reg[e], a.norm);
+    }
+    if constexpr (MODE == ROW_LAST) {
+        float2* dst = a.exit_waves + ((size_t)b * a.nx + x) * N;
+#pragma unroll
+        for (int e = 0; e < E; ++e) dst[t + T * e] = reg[e];
+    } else {
+        // transmit (stem3/stemlib.cpp:2867-2888): window at (posX, posY)
+        const float2* tr = a.trans_slice + (size_t)(x + __ldg(a.posX + b)) * a.potNy + __ldg(a.posY + b);
+#pragma unroll
+        for (int e = 0; e < E; ++e) reg[e] = cmul(reg[e], __ldg(tr + t + T * e));
+        line_fft<Cfg, false>(reg, sm, s_tw, t);
+        float2* dst = a.waves + ((size_t)b * a.nx + x) * N;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int y = t + T * e;
+            if (y <= a.yA || y >= a.yB) dst[y] = reg[e];
+        }
+    }
+}
+
+template <int N>
+constexpr int col_tile() {
+    return N >= 768 ? 8 : 16;
+}
+
+template <int N, bool DET, bool INVERSE>
+__global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
+    ms_cols(ColArgs a) {
+    using Cfg = typename Line<N>::cfg;
+    constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();
+    constexpr int NT = C * T;
+    constexpr int NWARPS = (NT + 31) / 32;
+    extern __shared__ float2 dsm[];
+    float2* s_tw = dsm;
+    float2* s_tile = dsm + N;
+    __shared__ double s_det[QS_MAX_DETECTORS][NWARPS];
+    const int tid = threadIdx.x + C * threadIdx.y;
+    for (int i = tid; i < N; i += NT) s_tw[i] = a.tw[i];
+    __syncthreads();
+
+    const int c = threadIdx.x, t = threadIdx.y;
+    const int tile = blockIdx.x % a.ntiles;
+    const int b = blockIdx.x / a.ntiles;
+    const int ky = __ldg(a.tiles + tile) + c;
+    float2* col = a.waves + (size_t)b * a.nx * a.ny + ky;
+    float2 reg[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) reg[e] = col[(size_t)(t + T * e) * a.ny];
+    const SmemCol<C> sm{s_tile, c};
+    line_fft<Cfg, false, true>(reg, sm, s_tw, t);
+
+    // propagate_slow (stem3/stemlib.cpp:2831-2849)
+    const float ky2 = __ldg(a.ky2 + ky);
+    const float2 pyv = __ldg(a.py + ky);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int kx = t + T * e;
+        const float kx2 = __ldg(a.kx2 + kx);
+        if (kx2 < a.k2max && (kx2 + ky2) < a.k2max)
+            reg[e] = cmul(cmul(reg[e], pyv), __ldg(a.px + kx));
+        else
+            reg[e] = make_float2(0.f, 0.f);
+    }
+
+    if constexpr (DET) {
+        // collectIntensity (stem3/stemlib.cpp:2615-2657): |psi(k)|^2 in float,
+        // summed per annulus in double
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int d = 0; d < a.ndet; ++d) {
+            double acc = 0.0;
+            const float lo = a.k2in[d], hi = a.k2out[d];
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const float k2 = __ldg(a.kx2 + t + T * e) + ky2;
+                const float I = reg[e].x * reg[e].x + reg[e].y * reg[e].y;
+                if (k2 >= lo && k2 <= hi) acc += (double)I;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) s_det[d][warp] = acc;
+        }
+        if (a.diffpat) {
+            float* dp = a.diffpat + (size_t)b * a.nx * a.ny + (ky + a.ny / 2) % a.ny;
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int kx = t + T * e;
+                const float I = reg[e].x * reg[e].x + reg[e].y * reg[e].y;
+                dp[(size_t)((kx + a.nx / 2) % a.nx) * a.ny] = (float)((double)I * a.scaleDiff);
+            }
+        }
+        __syncthreads();
+        if (tid < a.ndet) {
+            double s = 0.0;
+            for (int w = 0; w < NWARPS; ++w) s += s_det[tid][w];
+            a.partial[((size_t)b * a.ntiles + tile) * a.ndet + tid] = s;
+        }
+    }
+    if constexpr (INVERSE) {
+        line_fft<Cfg, true, true>(reg, sm, s_tw, t);
+#pragma unroll
+        for (int e = 0; e < E; ++e) col[(size_t)(t + T * e) * a.ny] = reg[e];
+    }
+}
+
+__global__ void det_finalize(const double* __restrict__ partial, int nwaves, int ntiles, int ndet, double scale,
+                             const int* __restrict__ detPosX, const int* __restrict__ detPosY, int scanYN,
+                             int npix, float* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nwaves * ndet) return;
+    const int b = i / ndet, d = i - b * ndet;
+    double s = 0.0;
+    for (int k = 0; k < ntiles; ++k) s += partial[((size_t)b * ntiles + k) * ndet + d];
+    out[(size_t)d * npix + (size_t)detPosX[b] * scanYN + detPosY[b]] = (float)(s * scale);
+}
+
+// ------------------------------------------------------------- launchers
+template <int N>
+static size_t row_smem() {
+    return sizeof(float2) * (N + ROW_LINES * Line<N>::cfg::SMEM);
+}
+template <int N>
+static size_t col_smem() {
+    return sizeof(float2) * (N + (size_t)N * col_tile<N>());
+}
+
+template <int N, int MODE>
+static int rows_n(const RowArgs& a, cudaStream_t s) {
+    using Cfg = typename Line<N>::cfg;
+    static bool attr = false;  // per-process; the attribute is per function
+    const size_t sm = row_smem<N>();
+    if (!attr) {
+        QS_CUDA_TRY(cudaFuncSetAttribute(ms_rows<N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr = true;
+    }
+    const long lines = (long)a.nwaves * a.nx;
+    if (lines % ROW_LINES) {
+        set_error("row pass: nwaves*nx must be a multiple of 8");
+        return QS_ERR_ARG;
+    }
+    dim3 block(Cfg::T, ROW_LINES);
+    ms_rows<N, MODE><<<(unsigned)(lines / ROW_LINES), block, sm, s>>>(a);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+template <int MODE>
+static int rows_mode(const RowArgs& a, cudaStream_t s) {
+    switch (a.ny) {
+        case 64: return rows_n<64, MODE>(a, s);
+        case 128: return rows_n<128, MODE>(a, s);
+        case 256: return rows_n<256, MODE>(a, s);
+        case 384: return rows_n<384, MODE>(a, s);
+        case 512: return rows_n<512, MODE>(a, s);
+        case 768: return rows_n<768, MODE>(a, s);
+        case 1024: return rows_n<1024, MODE>(a, s);
+    }
+    set_error("row pass: unsupported ny");
+    return QS_ERR_UNSUPPORTED;
+}
+
+int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s) {
+    if (mode == ROW_FIRST) return rows_mode<ROW_FIRST>(a, s);
+    if (mode == ROW_MID) return rows_mode<ROW_MID>(a, s);
+    return rows_mode<ROW_LAST>(a, s);
+}
+
+template <int N, bool DET, bool INV>
+static int cols_n3(const ColArgs& a, cudaStream_t s) {
+    using Cfg = typename Line<N>::cfg;
+    static bool attr = false;
+    const size_t sm = col_smem<N>();
+    if (!attr) {
+        QS_CUDA_TRY(cudaFuncSetAttribute(ms_cols<N, DET, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr = true;
+    }
+    dim3 block(col_tile<N>(), Cfg::T);
+    const long nblk = (long)a.nwaves * a.ntiles;
+    if (nblk <= 0) return QS_OK;
+    ms_cols<N, DET, INV><<<(unsigned)nblk, block, sm, s>>>(a);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+template <int N>
+static int cols_n(const ColArgs& a, cudaStream_t s) {
+    const bool det = a.ndet > 0 || a.diffpat != nullptr;
+    if (det) return a.inverse ? cols_n3<N, true, true>(a, s) : cols_n3<N, true, false>(a, s);
+    return a.inverse ? cols_n3<N, false, true>(a, s) : cols_n3<N, false, false>(a, s);
+}
+
+int launch_cols(const ColArgs& a, cudaStream_t s) {
+    switch (a.nx) {
+        case 64: return cols_n<64>(a, s);
+        case 128: return cols_n<128>(a, s);
+        case 256: return cols_n<256>(a, s);
+        case 384: return cols_n<384>(a, s);
+        case 512: return cols_n<512>(a, s);
+        case 768: return cols_n<768>(a, s);
+        case 1024: return cols_n<1024>(a, s);
+    }
+    set_error("column pass: unsupported nx");
+    return QS_ERR_UNSUPPORTED;
+}
+
+int col_tile_width(int nx) { return nx >= 768 ? 8 : 16; }
+
+int launch_det_finalize(const double* partial, int nwaves, int ntiles, int ndet, double scale,
+                        const int* detPosX, const int* detPosY, int scanYN, int npix, float* det_out,
+                        cudaStream_t s) {
+    const int n = nwaves * ndet;
+    if (n <= 0) return QS_OK;
+    det_finalize<<<(n + 255) / 256, 256, 0, s>>>(partial, nwaves, ntiles, ndet, scale, detPosX, detPosY, scanYN,
+                                                 npix, det_out);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+// ------------------------------------------------ generic 2-D transforms
+template <int N, bool INV>
+__global__ void __launch_bounds__(line_threads(N) * ROW_LINES) fft_rows(float2* data, long nlines, const float2* tw) {
+    using Cfg = typename Line<N>::cfg;
+    constexpr int T = Cfg::T, E = Cfg::E;
+    extern __shared__ float2 dsm[];
+    float2* s_tw = dsm;
+    float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
+    const int tid = threadIdx.x + T * threadIdx.y;
+    for (int i = tid; i < N; i += T * ROW_LINES) s_tw[i] = tw[i];
+    __syncthreads();
+    const long line = (long)blockIdx.x * ROW_LINES + threadIdx.y;
+    const bool ok = line < nlines;
+    float2* p = data + (ok ? line : 0) * N;
+    const int t = threadIdx.x;
+    float2 reg[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) reg[e] = ok ? p[t + T * e] : make_float2(0.f, 0.f);
+    line_fft<Cfg, INV>(reg, SmemRow{s_line}, s_tw, t);
+    if (ok) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) p[t + T * e] = reg[e];
+    }
+}
+
+template <int N, bool INV>
+__global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
+    fft_cols(float2* data, int ncols, const float2* tw) {
+    // columns of length N, row stride ncols; blockIdx.y = array index
+    using Cfg = typename Line<N>::cfg;
+    constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();
+    extern __shared__ float2 dsm[];
+    float2* s_tw = dsm;
+    float2* s_tile = dsm + N;
+    const int tid = threadIdx.x + C * threadIdx.y;
+    for (int i = tid; i < N; i += C * T) s_tw[i] = tw[i];
+    __syncthreads();
+    const int c = threadIdx.x, t = threadIdx.y;
+    const int col = blockIdx.x * C + c;
+    const bool ok = col < ncols;
+    float2* p = data + (size_t)blockIdx.y * N * ncols + (ok ? col : 0);
+    float2 reg[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) reg[e] = ok ? p[(size_t)(t + T * e) * ncols] : make_float2(0.f, 0.f);
+    line_fft<Cfg, INV, true>(reg, SmemCol<C>{s_tile, c}, s_tw, t);
+    if (ok) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) p[(size_t)(t + T * e) * ncols] = reg[e];
+    }
+}
+
+template <int N, bool INV>
+static int fft_rows_n(float2* data, long nlines, cudaStream_t s) {
+    static bool attr = false;
+    const size_t sm = row_smem<N>();
+    if (!attr) {
+        QS_CUDA_TRY(cudaFuncSetAttribute(fft_rows<N, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr = true;
+    }
+    dim3 block(Line<N>::cfg::T, ROW_LINES);
+    fft_rows<N, INV><<<(unsigned)((nlines + ROW_LINES - 1) / ROW_LINES), block, sm, s>>>(data, nlines, twiddles(N));
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+template <int N, bool INV>
+static int fft_cols_n(float2* data, int ncols, int howmany, cudaStream_t s) {
+    static bool attr = false;
+    const size_t sm = col_smem<N>();
+    if (!attr) {
+        QS_CUDA_TRY(cudaFuncSetAttribute(fft_cols<N, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr = true;
+    }
+    constexpr int C = col_tile<N>();
+    dim3 block(C, Line<N>::cfg::T);
+    dim3 grid((ncols + C - 1) / C, howmany);
+    fft_cols<N, INV><<<grid, block, sm, s>>>(data, ncols, twiddles(N));
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+template <bool INV>
+static int fft_rows_any(float2* data, int n, long nlines, cudaStream_t s) {
+    switch (n) {
+        case 64: return fft_rows_n<64, INV>(data, nlines, s);
+        case 128: return fft_rows_n<128, INV>(data, nlines, s);
+        case 256: return fft_rows_n<256, INV>(data, nlines, s);
+        case 384: return fft_rows_n<384, INV>(data, nlines, s);
+        case 512: return fft_rows_n<512, INV>(data, nlines, s);
+        case 768: return fft_rows_n<768, INV>(data, nlines, s);
+        case 1024: return fft_rows_n<1024, INV>(data, nlines, s);
+    }
+    set_error("fft2d: unsupported row length " + std::to_string(n));
+    return QS_ERR_UNSUPPORTED;
+}
+
+template <bool INV>
+static int fft_cols_any(float2* data, int n, int ncols, int howmany, cudaStream_t s) {
+    switch (n) {
+        case 64: return fft_cols_n<64, INV>(data, ncols, howmany, s);
+        case 128: return fft_cols_n<128, INV>(data, ncols, howmany, s);
+        case 256: return fft_cols_n<256, INV>(data, ncols, howmany, s);
+        case 384: return fft_cols_n<384, INV>(data, ncols, howmany, s);
+        case 512: return fft_cols_n<512, INV>(data, ncols, howmany, s);
+        case 768: return fft_cols_n<768, INV>(data, ncols, howmany, s);
+        case 1024: return fft_cols_n<1024, INV>(data, ncols, howmany, s);
+    }
+    set_error("fft2d: unsupported column length " + std::to_string(n));
+    return QS_ERR_UNSUPPORTED;
+}
+
+int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t s) {
+    if (!line_supported(n0) || !line_supported(n1)) {
+        set_error("fft2d: size " + std::to_string(n0) + "x" + std::to_string(n1) + " not supported");
+        return QS_ERR_UNSUPPORTED;
+    }
+    const long lines = (long)n0 * howmany;
+    if (inverse) {
+        QS_TRY(fft_rows_any<true>(data, n1, lines, s));
+        QS_TRY(fft_cols_any<true>(data, n0, n1, howmany, s));
+    } else {
+        QS_TRY(fft_rows_any<false>(data, n1, lines, s));
+        QS_TRY(fft_cols_any<false>(data, n0, n1, howmany, s));
+    }
+    return QS_OK;
+}
+
+const float2* twiddles(int n) {
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, float2*> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_pair(dev, n);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    std::vector<float2> h(n);
+    for (int k = 0; k < n; ++k) {
+        // exp(-2 pi i k/n) with the angle reduced exactly in turns
+        double turns = (double)k / (double)n;
+        if (turns > 0.5) turns -= 1.0;
+        const double ang = -2.0 * kPi * turns;
+        h[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+    }
+    float2* d = nullptr;
+    if (cudaMalloc(&d, sizeof(float2) * n) != cudaSuccess) return nullptr;
+    cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+    cache[key] = d;
+    return d;
+}
+
+}  // namespace qs

@@ -1,0 +1,361 @@
+// qs_potential.cu -- projected-potential lookup tables, the atom scatter-sum
+// into the slice stack, and the phase grating.
+//
+//   LUT          getAtomPotential3D / getAtomPotentialOffset3D
+//                (stem3/stemlib.cpp:1342-1541, :1548-1741), in FP64
+//   scatter-sum  make3DSlices, default 3-D branch (stem3/stemlib.cpp:894-1036,
+//                :1090-1213)
+//   grating      initSTEMSlices (stem3/stemlib.cpp:2280-2336)
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "qs_internal.h"
+#include "qs_rez_table.h"
+
+namespace qs {
+
+constexpr int NSF = QS_REZ_NSF;
+constexpr int OVERSAMP = 2;
+
+// --------------------------------------------------------------- spline
+static void akima(const double* x, const double* y, double* b, double* c, double* d, int n) {
+    // Akima local cubic with linearly extrapolated end secants
+    // (same construction as stem3/stemutil.cpp:975-1041)
+    const double tiny = 1.0e-25;
+    double m5 = (y[3] - y[2]) / (x[3] - x[2]);
+    double m4 = (y[2] - y[1]) / (x[2] - x[1]);
+    double m3 = (y[1] - y[0]) / (x[1] - x[0]);
+    double m2 = m3 + m3 - m4;
+    double m1 = m2 + m2 - m3;
+    double m54 = std::fabs(m5 - m4), m43 = std::fabs(m4 - m3), m32 = std::fabs(m3 - m2), m21 = std::fabs(m2 - m1);
+    double t1 = ((m43 + m21) > tiny) ? (m43 * m2 + m21 * m3) / (m43 + m21) : 0.5 * (m2 + m3);
+    for (int i = 0; i < n - 1; i++) {
+        double t2 = ((m54 + m32) > tiny) ? (m54 * m3 + m32 * m4) / (m54 + m32) : 0.5 * (m3 + m4);
+        double h = x[i + 1] - x[i];
+        b[i] = t1;
+        c[i] = (3.0 * m3 - t1 - t1 - t2) / h;
+        d[i] = (t1 + t2 - m3 - m3) / (h * h);
+        m1 = m2; m2 = m3; m3 = m4; m4 = m5;
+        m5 = (i < n - 4) ? (y[i + 4] - y[i + 3]) / (x[i + 4] - x[i + 3]) : m4 + m4 - m3;
+        m21 = m32; m32 = m43; m43 = m54; m54 = std::fabs(m5 - m4);
+        t1 = t2;
+    }
+    (void)m1;
+}
+
+__device__ __forceinline__ double spline_eval(const double* __restrict__ x, const double* __restrict__ y,
+                                              const double* __restrict__ b, const double* __restrict__ c,
+                                              const double* __restrict__ d, double x0) {
+    int i;
+    if (x0 <= x[0]) i = 0;
+    else if (x0 >= x[NSF - 2]) i = NSF - 2;
+    else {
+        int lo = 0, hi = NSF;
+        do {
+            int k = (lo + hi) >> 1;
+            if (x0 < x[k]) hi = k;
+            else lo = k;
+        } while (hi - lo > 1);
+        i = lo;
+    }
+    const double z = x0 - x[i];
+    return y[i] + (b[i] + (c[i] + d[i] * z) * z) * z;
+}
+
+// tail truncation of the s-grid at the LUT's k_max (stem3/stemlib.cpp:1390-1413)
+static void truncate_tail(double* grid, double* row, double kmax) {
+    grid[NSF - 1] = 1.2 * kmax;
+    grid[NSF - 2] = 1.1 * kmax;
+    grid[NSF - 3] = kmax;
+    if (grid[NSF - 4] > grid[NSF - 3]) {
+        for (int ix = 0; ix < NSF - 10; ix++) {
+            if (grid[NSF - 4 - ix] < grid[NSF - 3] - 0.001 * (ix + 1)) break;
+            grid[NSF - 4 - ix] = grid[NSF - 3] - 0.001 * (ix + 1);
+            row[NSF - 4 - ix] = 0;
+        }
+    }
+}
+
+struct LutGeom {
+    int nx, nz, nzPer, izOffset;
+    double dkx, dky, dkz, smax2, zPos;
+};
+
+static LutGeom lut_geom(const qs_params& p) {
+    LutGeom g;
+    const float rx = p.resolutionX, ry = p.resolutionY, dzs = p.sliceThickness, R = p.atomRadius;
+    g.nx = 2 * OVERSAMP * (int)ceilf(R / rx);
+    const int ny = 2 * OVERSAMP * (int)ceilf(R / ry);
+    int nzPer = (int)floorf((float)OVERSAMP * dzs / rx);
+    if (2.0 * (nzPer >> 1) == nzPer) nzPer += 1;
+    g.nzPer = nzPer;
+    g.nz = (2 * (int)ceilf(R / dzs)) * nzPer;
+    g.dkx = 0.5 * OVERSAMP / (double)((float)g.nx * rx);
+    g.dky = 0.5 * OVERSAMP / (double)((float)ny * ry);
+    g.dkz = nzPer / (double)((float)g.nz * dzs);
+    const double kmax = 0.5 * g.nx * g.dkx / (double)OVERSAMP;
+    g.smax2 = kmax * kmax;
+    g.izOffset = (nzPer - 1) / 2;
+    // the reference's PI (stem3/stemlib.cpp:75) in zPos (:1438)
+    g.zPos = -2.0 * 3.14159265358979 * (double)(dzs / (float)nzPer * (float)g.izOffset);
+    return g;
+}
+
+// f(kx, kz) with the analytic qy sum (stem3/stemlib.cpp:1446-1480)
+__global__ void lut_fgrid(const double* __restrict__ tab, int nx, int nz, double dkx, double dqy, double dkz,
+                          double smax2, double B, double zPos, float2* __restrict__ temp) {
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iz = blockIdx.y;
+    if (ix >= nx) return;
+    const double* g1 = tab;
+    const double* r1 = tab + NSF;
+    const double* sb = tab + 2 * NSF;
+    const double* sc = tab + 3 * NSF;
+    const double* sd = tab + 4 * NSF;
+    const double* g2 = tab + 5 * NSF;
+    const double* r2 = tab + 6 * NSF;
+    const double kz = dkz * (iz < nz / 2 ? iz : iz - nz);
+    const double kx = dkx * (ix < nx / 2 ? ix : ix - nx);
+    const double s2 = kx * kx + kz * kz;
+    float2 out = make_float2(0.f, 0.f);
+    if (s2 < smax2) {
+        double f = spline_eval(g1, r1, sb, sc, sd, sqrt(s2)) * exp(-s2 * B * 0.25);
+        for (int iy = 1; iy < nx; iy++) {
+            double s3 = dqy * iy;
+            s3 = s3 * s3 + s2;
+            if (s3 < smax2) f += 2 * spline_eval(g2, r2, sb, sc, sd, sqrt(s3)) * exp(-s3 * B * 0.25);
+            else break;
+        }
+        f *= dkx;
+        const double phase = kz * zPos;  // the kx*xPos term is zero (:1437)
+        double sn, cs;
+        sincos(phase, &sn, &cs);
+        out = make_float2((float)(f * cs), (float)(f * sn));
+    }
+    temp[(size_t)iz * nx + ix] = out;
+}
+
+// backward DFT along x, keeping outputs ix' < nx/2 (FP64)
+__global__ void lut_dft_x(const float2* __restrict__ temp, int nx, int nz, double2* __restrict__ G) {
+    const int kx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iz = blockIdx.y;
+    if (kx >= nx / 2) return;
+    double re = 0, im = 0;
+    for (int ix = 0; ix < nx; ix++) {
+        const float2 v = temp[(size_t)iz * nx + ix];
+        const int k = (int)(((long)ix * kx) % nx);
+        double sn, cs;
+        sincospi(2.0 * k / nx, &sn, &cs);
+        re += v.x * cs - v.y * sn;
+        im += v.x * sn + v.y * cs;
+    }
+    G[(size_t)iz * (nx / 2) + kx] = make_double2(re, im);
+}
+
+// backward DFT along z, real part of outputs iz' < nz/2, rounded to float as
+// the reference's single-precision transform stores it
+__global__ void lut_dft_z(const double2* __restrict__ G, int nxh, int nz, float* __restrict__ H) {
+    const int kx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int kz = blockIdx.y;
+    if (kx >= nxh) return;
+    double re = 0;
+    for (int iz = 0; iz < nz; iz++) {
+        const double2 v = G[(size_t)iz * nxh + kx];
+        const int k = (int)(((long)iz * kz) % nz);
+        double sn, cs;
+        sincospi(2.0 * k / nz, &sn, &cs);
+        re += v.x * cs - v.y * sn;
+    }
+    H[(size_t)kz * nxh + kx] = (float)re;
+}
+
+// sum over nzPerSlice sub-samples, clamp at 0, scale (:1503-1522)
+__global__ void lut_zsum(const float* __restrict__ H, int nxh, int nzh, int izOffset, double scale,
+                         float* __restrict__ out) {
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iz = blockIdx.y;
+    if (ix >= nxh) return;
+    double z = 0;
+    for (int iiz = -izOffset; iiz <= izOffset; iiz++)
+        if (iz + izOffset + iiz < nzh) z += H[(size_t)(iz + izOffset + iiz) * nxh + ix];
+    if (z < 0) z = 0;
+    out[(size_t)iz * nxh + ix] = (float)(scale * z);
+}
+
+int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, int* Nz, int* Nr, int* nzSub,
+              cudaStream_t s) {
+    if (Z < 1 || Z >= QS_REZ_NELEM) {
+        set_error("qs_lut_build: atomic number out of range");
+        return QS_ERR_ARG;
+    }
+    const LutGeom g = lut_geom(p);
+    if (Nz) *Nz = g.nz / 2;
+    if (Nr) *Nr = g.nx / 2;
+    if (nzSub) *nzSub = g.nzPer;
+    if (!d_out) return QS_OK;
+    const double kmax = std::sqrt(g.smax2);
+    std::vector<double> tab(7 * NSF);
+    double *g1 = tab.data(), *r1 = g1 + NSF, *sb = g1 + 2 * NSF, *sc = g1 + 3 * NSF, *sd = g1 + 4 * NSF,
+           *g2 = g1 + 5 * NSF, *r2 = g1 + 6 * NSF;
+    // neutral table, truncated (always applied first, as the reference does)
+    std::memcpy(g2, QS_REZ_F[0], sizeof(double) * NSF);
+    std::memcpy(r2, QS_REZ_F[Z], sizeof(double) * NSF);
+    truncate_tail(g2, r2, kmax);
+    if (charged) {
+        std::memcpy(g1, QS_REZ_Q[0], sizeof(double) * NSF);
+        std::memcpy(r1, QS_REZ_Q[Z], sizeof(double) * NSF);
+        truncate_tail(g1, r1, kmax);
+    } else {
+        std::memcpy(g1, g2, sizeof(double) * NSF);
+        std::memcpy(r1, r2, sizeof(double) * NSF);
+    }
+    akima(g1, r1, sb, sc, sd, NSF);
+    // the charged table's qy sum evaluates the neutral table with the charged
+    // spline coefficients and the y step dky (stem3/stemlib.cpp:1668-1675)
+    const double dqy = charged ? g.dky : g.dkx;
+
+    double* d_tab = nullptr;
+    float2* d_temp = nullptr;
+    double2* d_G = nullptr;
+    float* d_H = nullptr;
+    const int nxh = g.nx / 2, nzh = g.nz / 2;
+    int rc = QS_OK;
+    auto fail = [&](cudaError_t e, const char* what) {
+        set_error(std::string("qs_lut_build: ") + what + ": " + cudaGetErrorString(e));
+        rc = QS_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaMallocAsync(&d_tab, sizeof(double) * 7 * NSF, s)) != cudaSuccess) { fail(e, "alloc"); return rc; }
+    if ((e = cudaMallocAsync(&d_temp, sizeof(float2) * (size_t)g.nx * g.nz, s)) != cudaSuccess) fail(e, "alloc");
+    if (!rc && (e = cudaMallocAsync(&d_G, sizeof(double2) * (size_t)nxh * g.nz, s)) != cudaSuccess) fail(e, "alloc");
+    if (!rc && (e = cudaMallocAsync(&d_H, sizeof(float) * (size_t)nxh * nzh, s)) != cudaSuccess) fail(e, "alloc");
+    if (!rc) {
+        cudaMemcpyAsync(d_tab, tab.data(), sizeof(double) * 7 * NSF, cudaMemcpyHostToDevice, s);
+        lut_fgrid<<<dim3((g.nx + 127) / 128, g.nz), 128, 0, s>>>(d_tab, g.nx, g.nz, g.dkx, dqy, g.dkz, g.smax2, B,
+                                                              g.zPos, d_temp);
+        lut_dft_x<<<dim3((nxh + 127) / 128, g.nz), 128, 0, s>>>(d_temp, g.nx, g.nz, d_G);
+        lut_dft_z<<<dim3((nxh + 127) / 128, nzh), 128, 0, s>>>(d_G, nxh, g.nz, d_H);
+        const double scale = 47.8658 * g.dkx * g.dkz / (g.nz);
+        lut_zsum<<<dim3((nxh + 127) / 128, nzh), 128, 0, s>>>(d_H, nxh, nzh, g.izOffset, scale, d_out);
+        if ((e = cudaGetLastError()) != cudaSuccess) fail(e, "launch");
+        else count_launch(4);
+    }
+    cudaFreeAsync(d_H, s);
+    cudaFreeAsync(d_G, s);
+    cudaFreeAsync(d_temp, s);
+    cudaFreeAsync(d_tab, s);
+    return rc;
+}
+
+// --------------------------------------------------------- scatter-sum
+// One block per atom job; threads stride over the atom's pixel box.  The
+// interpolation follows stem3/stemlib.cpp:935-1028 (radial linear
+// interpolation at dr = dx/2, nearest sub-slice in z).
+__global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts, int Nz,
+                              int Nr, int nzSub, float dx, float dy, double dr, float dzs, int potNx, int potNy,
+                              int periodic, float2* __restrict__ trans) {
+    const AtomJob J = jobs[blockIdx.x];
+    const float* lut = luts[J.lut];
+    const float* lutq = J.lutq >= 0 ? luts[J.lutq] : nullptr;
+    const int w = J.iay1 - J.iay0 + 1;
+    const int npx = (J.iax1 - J.iax0 + 1) * w;
+    const size_t sliceStep = (size_t)potNx * potNy;
+    const int limHi = Nr * (Nz - 1), limLo = -Nr * (Nz - 1), step = nzSub * Nr;
+    const double dOffsZ = (double)(((float)(J.iAtomZ + J.iaz0) - J.atomZ / dzs) * (float)nzSub);
+    const int iOffsZ0 = ((int)(dOffsZ + 0.5)) * Nr;
+    for (int k = threadIdx.x; k < npx; k += blockDim.x) {
+        const int iax = J.iax0 + k / w;
+        const int iay = J.iay0 + k % w;
+        double x2 = (double)((float)iax * dx - J.atomX);
+        x2 *= x2;
+        double y2 = (double)((float)iay * dy - J.atomY);
+        y2 *= y2;
+        const double r = sqrt(x2 + y2);
+        double ddr = r / dr;
+        const int ir = (int)floor(ddr);
+        if (ir >= Nr - 1) continue;
+        ddr -= (double)ir;
+        const int cx = periodic ? ((iax % potNx) + potNx) % potNx : iax;
+        const int cy = periodic ? ((iay % potNy) + potNy) % potNy : iay;
+        float* dst = &trans[(size_t)(J.iAtomZ + J.iaz0) * sliceStep + (size_t)cx * potNy + cy].x;
+        int iOffsZ = iOffsZ0;
+        for (int iaz = J.iaz0; iaz <= J.iaz1; iaz++) {
+            double v = 0;
+            if (iOffsZ < 0) {
+                if (iOffsZ > limLo) {
+                    v = (1 - ddr) * lut[ir - iOffsZ + Nr] + ddr * lut[ir + 1 - iOffsZ + Nr];
+                    if (lutq) v += J.q * ((1 - ddr) * lutq[ir - iOffsZ + Nr] + ddr * lutq[ir + 1 - iOffsZ + Nr]);
+                }
+            } else if (iOffsZ < limHi) {
+                v = (1 - ddr) * lut[ir + iOffsZ] + ddr * lut[ir + 1 + iOffsZ];
+                if (lutq) v += J.q * ((1 - ddr) * lutq[ir + iOffsZ] + ddr * lutq[ir + 1 + iOffsZ]);
+            }
+            if (v != 0) atomicAdd(dst, (float)v);
+            dst += 2 * sliceStep;
+            iOffsZ += step;
+        }
+    }
+}
+
+int launch_scatter(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
+                   const qs_params& p, float2* trans, cudaStream_t s) {
+    if (njobs <= 0) return QS_OK;
+    const double dr = p.resolutionX / OVERSAMP;
+    scatter_atoms<<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr,
+                                        p.sliceThickness, p.potNx, p.potNy, p.nonPeriod ? 0 : 1, trans);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+// ------------------------------------------------------- phase grating
+__global__ void phase_grating(float2* __restrict__ t, size_t n, double scale) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double vz = t[i].x * scale;
+        double sn, cs;
+        sincos(vz, &sn, &cs);
+        t[i] = make_float2((float)cs, (float)sn);
+    }
+}
+
+int launch_phase_grating(float2* trans, size_t n, double scale, cudaStream_t s) {
+    if (!n) return QS_OK;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    phase_grating<<<sms * 8, 256, 0, s>>>(trans, n, scale);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+__global__ void bandlimit_mask(float2* __restrict__ t, int slices, int potNx, int potNy,
+                               const float* __restrict__ kx2, const float* __restrict__ ky2, float k2max,
+                               double fftScale) {
+    const size_t n = (size_t)slices * potNx * potNy;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int iy = (int)(i % potNy);
+        const int ix = (int)((i / potNy) % potNx);
+        const float k2 = ky2[iy] + kx2[ix];
+        float2 v = t[i];
+        if (k2 < k2max) v = make_float2((float)(v.x * fftScale), (float)(v.y * fftScale));
+        else v = make_float2(0.f, 0.f);
+        t[i] = v;
+    }
+}
+
+int launch_bandlimit_mask(float2* trans, int slices, int potNx, int potNy, const float* kx2, const float* ky2,
+                          float k2max, double fftScale, cudaStream_t s) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    bandlimit_mask<<<sms * 8, 256, 0, s>>>(trans, slices, potNx, potNy, kx2, ky2, k2max, fftScale);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+}  // namespace qs

@@ -1,0 +1,214 @@
+"""ctypes binding of libqstem_gpu.so and a thin Python host API over it.
+
+The functions mirror the reference's call surface (stem3/stemlib.h):
+make3DSlices+initSTEMSlices -> Context.slices, probe -> Context.probe,
+the doSTEM/runMulsSTEM position loop -> Context.multislice,
+collectIntensity -> Context.collect, getAtomPotential3D -> Context.lut.
+Buffers may be numpy arrays (host, copied through the library's staging
+buffers) or CUDA torch tensors (device pointers, no copies).
+There is no CPU fallback: when the library cannot be loaded every call
+raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libqstem_gpu.so")
+
+EXPORTS = ["qs_ctx_create", "qs_ctx_destroy", "qs_last_error", "qs_abi_version", "qs_ctx_stream",
+           "qs_params_finalize", "qs_thickness_count", "qs_lut_build", "qs_slices_build", "qs_probe",
+           "qs_multislice_run", "qs_collect", "qs_stem_run", "qs_ctx_profile", "qs_ctx_stats"]
+
+_lib = None
+
+
+class QsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("qstem_gpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+def load(path=LIB_PATH):
+    """Load the library (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        from . import build as _b
+        _b.build()
+    L = ctypes.CDLL(path)
+    P = ctypes.POINTER(abi.QsParams)
+    vp = ctypes.c_void_p
+    L.qs_last_error.restype = ctypes.c_char_p
+    L.qs_ctx_create.argtypes = [ctypes.c_int, ctypes.POINTER(vp)]
+    L.qs_ctx_destroy.argtypes = [vp]
+    L.qs_ctx_stream.restype = vp
+    L.qs_ctx_stream.argtypes = [vp]
+    L.qs_params_finalize.argtypes = [P]
+    L.qs_thickness_count.argtypes = [P]
+    L.qs_lut_build.argtypes = [vp, P, ctypes.c_int, ctypes.c_double, ctypes.c_int, vp,
+                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                               ctypes.POINTER(ctypes.c_int), ctypes.c_uint]
+    L.qs_slices_build.argtypes = [vp, P, vp, ctypes.c_int, vp, ctypes.c_uint]
+    L.qs_probe.argtypes = [vp, P, ctypes.c_double, ctypes.c_double, vp, ctypes.c_uint]
+    L.qs_multislice_run.argtypes = [vp, P, vp, vp, ctypes.POINTER(abi.QsBatch), vp, vp, vp, ctypes.c_uint]
+    L.qs_collect.argtypes = [vp, P, vp, vp, vp, ctypes.c_uint]
+    L.qs_stem_run.argtypes = [vp, P, vp, ctypes.c_int, ctypes.POINTER(abi.QsBatch), vp, vp]
+    L.qs_ctx_profile.argtypes = [vp, ctypes.c_int]
+    L.qs_ctx_stats.argtypes = [vp, ctypes.POINTER(abi.QsStats)]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise QsError(rc, load().qs_last_error().decode(errors="replace"))
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_torch(a):
+        if not a.is_cuda or not a.is_contiguous():
+            raise ValueError("torch tensors must be contiguous CUDA tensors")
+        return ctypes.c_void_p(a.data_ptr())
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("numpy arrays must be C-contiguous")
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _io_flags(*arrays):
+    kinds = {(_is_torch(a)) for a in arrays if a is not None}
+    if len(kinds) > 1:
+        raise ValueError("mix of host (numpy) and device (torch) buffers")
+    return 0 if kinds == {True} else abi.QS_HOST_IO
+
+
+def _batch(p, positions):
+    if positions is None:
+        return abi.QsBatch(p.scanXN * p.scanYN, None, None, None, None), ()
+    arrs = [np.ascontiguousarray(a, dtype=np.int32) for a in positions]
+    ip = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) for a in arrs]
+    return abi.QsBatch(len(arrs[0]), *ip), arrs
+
+
+class Context:
+    """One device + one CUDA stream (qs_ctx_create)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        _check(self.lib.qs_ctx_create(device, ctypes.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            self.lib.qs_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream_handle(self):
+        return self.lib.qs_ctx_stream(self.h)
+
+    # -------------------------------------------------------------- LUTs
+    def lut(self, p, Z, B=0.0, charged=False):
+        nz, nr, ns = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(self.lib.qs_lut_build(self.h, ctypes.byref(p), Z, B, int(charged), None, ctypes.byref(nz),
+                                     ctypes.byref(nr), ctypes.byref(ns), 0))
+        out = np.zeros((nz.value, nr.value), np.float32)
+        _check(self.lib.qs_lut_build(self.h, ctypes.byref(p), Z, B, int(charged), _ptr(out), None, None, None,
+                                     abi.QS_HOST_IO))
+        return out, ns.value
+
+    # ------------------------------------------------------------ slices
+    def slices(self, p, atoms, out=None, potential_only=False, sync=True):
+        """make3DSlices + initSTEMSlices -> trans[slices][potNx][potNy][2]."""
+        a = abi.atoms_to_numpy(atoms)
+        if out is None:
+            out = np.zeros((p.slices, p.potNx, p.potNy, 2), np.float32)
+        flags = _io_flags(out) | (abi.QS_OUT_POTENTIAL if potential_only else 0) | (abi.QS_SYNC if sync else 0)
+        _check(self.lib.qs_slices_build(self.h, ctypes.byref(p), a.ctypes.data_as(ctypes.c_void_p), len(a),
+                                        _ptr(out), flags))
+        return out
+
+    # ------------------------------------------------------------- probe
+    def probe(self, p, dx=None, dy=None, out=None, sync=True):
+        if dx is None:
+            dx = float(np.float32(p.nx // 2 * np.float32(p.resolutionX)))
+        if dy is None:
+            dy = float(np.float32(p.ny // 2 * np.float32(p.resolutionY)))
+        if out is None:
+            out = np.zeros((p.nx, p.ny, 2), np.float32)
+        flags = _io_flags(out) | (abi.QS_SYNC if sync else 0)
+        _check(self.lib.qs_probe(self.h, ctypes.byref(p), dx, dy, _ptr(out), flags))
+        return out
+
+    # -------------------------------------------------------- multislice
+    def multislice(self, p, trans, probe=None, positions=None, det=None, diffpats=None, exit_waves=None,
+                   want_det=True, want_diffpats=False, want_exit_waves=False, sync=True):
+        """Run probe positions through the slice stack.
+
+        positions: None (the full scan raster) or (iPosX, iPosY, detPosX, detPosY) int arrays.
+        Output buffers are allocated (numpy, host) when not given and requested."""
+        bx, keep = _batch(p, positions)
+        npos = bx.npos
+        host = not _is_torch(trans)
+        nt = p.thickness_count()
+        if det is None and want_det and p.detectorNum > 0:
+            det = np.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), np.float32) if host else None
+        if diffpats is None and want_diffpats:
+            diffpats = np.zeros((npos, p.nx, p.ny), np.float32) if host else None
+        if exit_waves is None and want_exit_waves:
+            exit_waves = np.zeros((npos, p.nx, p.ny, 2), np.float32) if host else None
+        flags = _io_flags(trans, probe, det, diffpats, exit_waves) | (abi.QS_SYNC if sync else 0)
+        _check(self.lib.qs_multislice_run(self.h, ctypes.byref(p), _ptr(trans), _ptr(probe), ctypes.byref(bx),
+                                          _ptr(det), _ptr(diffpats), _ptr(exit_waves), flags))
+        del keep
+        return det, diffpats, exit_waves
+
+    def stem_run(self, p, atoms, positions=None, det=None, diffpats=None):
+        """One frozen-phonon configuration end to end (host atoms in, host
+        detector images out): qs_stem_run."""
+        a = abi.atoms_to_numpy(atoms)
+        bx, keep = _batch(p, positions)
+        if det is None and p.detectorNum > 0:
+            det = np.zeros((p.thickness_count(), p.detectorNum, p.scanXN, p.scanYN), np.float32)
+        _check(self.lib.qs_stem_run(self.h, ctypes.byref(p), a.ctypes.data_as(ctypes.c_void_p), len(a),
+                                    ctypes.byref(bx), _ptr(det), _ptr(diffpats)))
+        del keep
+        return det
+
+    def profile(self, enable=True):
+        _check(self.lib.qs_ctx_profile(self.h, int(enable)))
+
+    def stats(self):
+        st = abi.QsStats()
+        _check(self.lib.qs_ctx_stats(self.h, ctypes.byref(st)))
+        return {n: getattr(st, n) for n, _ in abi.QsStats._fields_}
+
+    # ----------------------------------------------------------- collect
+    def collect(self, p, wave_k, diffpat=False):
+        w = np.ascontiguousarray(wave_k, dtype=np.float32)
+        sums = np.zeros(max(p.detectorNum, 1), np.float64)
+        dp = np.zeros((p.nx, p.ny), np.float32) if diffpat else None
+        _check(self.lib.qs_collect(self.h, ctypes.byref(p), _ptr(w), _ptr(sums), _ptr(dp), abi.QS_HOST_IO))
+        return sums[:p.detectorNum], dp
+
+
+def thickness_count(p):
+    return load().qs_thickness_count(ctypes.byref(p))

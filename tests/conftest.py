@@ -1,0 +1,81 @@
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from qstem_gb300 import abi  # noqa: E402
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+REFERENCE = os.environ.get("QS_REFERENCE_DIR", "/root/reference")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the GB300 library)")
+
+
+def params_from_dict(d):
+    p = abi.QsParams()
+    for name, _ in abi.QsParams._fields_:
+        if name == "detectors":
+            continue
+        setattr(p, name, d[name])
+    for i, (rin, rout, sx, sy) in enumerate(d["detectors"]):
+        p.detectors[i].rInside, p.detectors[i].rOutside = rin, rout
+        p.detectors[i].shiftX, p.detectors[i].shiftY = sx, sy
+    from qstem_gb300 import config
+    wl = config.wavelength(float(p.v0))
+    import math
+    for i in range(p.detectorNum):
+        det = p.detectors[i]
+        ki = np.float32(math.sin(float(det.rInside) * 0.001) / wl)
+        ko = np.float32(math.sin(float(det.rOutside) * 0.001) / wl)
+        det.k2Inside, det.k2Outside = np.float32(ki * ki), np.float32(ko * ko)
+    return p
+
+
+class Golden:
+    def __init__(self, name):
+        self.name = name
+        z = np.load(os.path.join(GOLDEN, name + ".npz"))
+        self.z = z
+        self.params = params_from_dict(json.loads(str(z["params_json"])))
+        self.meta = json.loads(str(z["meta_json"]))
+        self.case = json.loads(str(z["case_json"]))
+
+    def __getitem__(self, k):
+        return self.z[k]
+
+    def __contains__(self, k):
+        return k in self.z.files
+
+    def keys(self):
+        return self.z.files
+
+
+GOLDEN_CASES = ["sto64", "sto64q", "si64cbed"]
+
+
+@pytest.fixture(params=GOLDEN_CASES)
+def golden(request):
+    return Golden(request.param)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.linalg.norm(b.ravel())
+    return float(np.linalg.norm((a - b).ravel()) / (den if den > 0 else 1.0))
+
+
+def has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False

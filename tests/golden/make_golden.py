@@ -1,0 +1,147 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs the reference's own CPU path (compiled from its sources by
+`make -C oracle ref`, FFTW supplied by the project's FFT shim) through
+oracle/ref_harness on small seeded cases, and stores its inputs and outputs
+as compressed .npz files:
+
+  params    the qs_params the case describes (as a dict)
+  meta      the MULS fields readFile derived (to pin qstem_gb300.config)
+  atoms     readFile's atoms (struct atom records)
+  lut_*     getAtomPotential3D / getAtomPotentialOffset3D tables
+  V, T      trans after make3DSlices and after initSTEMSlices
+  probe     probe() at the window centre
+  det       detector images after doSTEM (STEM cases that run)
+  diffpat_* / wave_*   diffAvg_ix_iy.img / mulswav_ix_iy.img the reference
+            wrote for the first positions (saveLevel 2)
+
+Usage: python tests/golden/make_golden.py   (needs the reference tree; the
+fixtures are committed so the tests do not)
+"""
+import json
+import os
+import shutil
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle  # noqa: E402
+from qstem_gb300 import abi, config, imageio  # noqa: E402
+
+CASES = {
+    # configuration-1-like: non-periodic, neutral atoms, one output group
+    "sto64": dict(cell="sto", ncell=(3, 3, 4), nx=64, resolutionX=0.0915, v0=200.0, slices=8,
+                  sliceThickness=1.9525, scan=(3.905, 7.81, 4, 3.905, 7.81, 4),
+                  detectors=[(0.0, 20.0, "BF"), (20.0, 40.0, "ADF"), (40.0, 90.0, "HAADF")],
+                  alpha=20.0, outputInterval=4, mode="STEM", run=True),
+    # periodic in x-y, charged atoms with Debye-Waller factors, centred slices,
+    # z offset, uneven output groups, aberrated probe
+    "sto64q": dict(cell="stoq", ncell=(3, 3, 3), nx=64, resolutionX=0.0915, v0=300.0, slices=6,
+                   sliceThickness=1.9525, scan=(2.0, 5.905, 3, 2.5, 6.405, 3),
+                   detectors=[(10.0, 40.0, "A"), (40.0, 80.0, "B")], alpha=15.0, outputInterval=4,
+                   Cs_mm=0.5, defocus_nm=-5.0, czOffset=0.3, centerSlices=True, periodicXY=True,
+                   mode="STEM", run=True),
+    # CBED geometry (potential grid = wave grid) with the transmission band limit
+    "si64cbed": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=5, sliceThickness=2.0,
+                     scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
+                     mode="CBED", run=False),
+}
+
+
+def cell_of(name):
+    if name == "sto":
+        return config.srtio3_cell()
+    if name == "stoq":
+        a = 3.905
+        return config.UnitCell(a, a, a, [(38, 0, 0, 0, 0.6214, 1, 2.0), (22, .5, .5, .5, 0.4390, 1, 4.0),
+                                         (8, 0, .5, .5, 0.7323, 1, -2.0), (8, .5, 0, .5, 0.7323, 1, -2.0),
+                                         (8, .5, .5, 0, 0.7323, 1, -2.0)])
+    if name == "si":
+        return config.si110_cell()
+    raise KeyError(name)
+
+
+def params_for(case):
+    cell = cell_of(case["cell"])
+    atoms, ax, by, c = config.replicate(cell, *case["ncell"])
+    mode = {"STEM": abi.QS_MODE_STEM, "CBED": abi.QS_MODE_CBED, "TEM": abi.QS_MODE_TEM}[case["mode"]]
+    p = config.make_params(mode=mode, nx=case["nx"], resolutionX=case["resolutionX"], v0=case["v0"],
+                           slices=case["slices"], sliceThickness=case["sliceThickness"], ax=ax, by=by, c=c,
+                           scan=case["scan"], detectors=case["detectors"], alpha=case["alpha"],
+                           Cs_mm=case.get("Cs_mm", 0.0), defocus_nm=case.get("defocus_nm", 0.0),
+                           outputInterval=case.get("outputInterval"), czOffset=case.get("czOffset", 0.0),
+                           centerSlices=case.get("centerSlices", False),
+                           periodicXY=case.get("periodicXY", False), bandlimit=case.get("bandlimit", False))
+    return cell, atoms, p
+
+
+def run_case(name, case, workdir):
+    cell, atoms, p = params_for(case)
+    cfg = os.path.join(workdir, "cell.cfg")
+    config.write_cfg(cell, cfg)
+    qsc = os.path.join(workdir, "run.qsc")
+    config.write_qsc(qsc, cfg_file="cell.cfg", ncell=case["ncell"], nx=case["nx"],
+                     resolutionX=case["resolutionX"], v0=case["v0"], slices=case["slices"],
+                     sliceThickness=case["sliceThickness"], scan=case["scan"], detectors=case["detectors"],
+                     alpha=case["alpha"], Cs_mm=case.get("Cs_mm", 0.0), defocus_nm=case.get("defocus_nm", 0.0),
+                     outputInterval=case.get("outputInterval"), mode=case["mode"],
+                     bandlimit=case.get("bandlimit", False), periodicXY=case.get("periodicXY", False),
+                     folder="out", saveLevel=2 if case["run"] else 0, czOffset=case.get("czOffset", 0.0),
+                     centerSlices=case.get("centerSlices", False))
+    dump = os.path.join(workdir, "dump")
+    oracle.run_reference(qsc, dump, run=case["run"])
+    meta = dict(l.split(" = ", 1) for l in open(os.path.join(dump, "meta.txt")).read().strip().split("\n"))
+    out = {}
+    out["atoms"] = np.fromfile(os.path.join(dump, "atoms.bin"), dtype=abi.ATOM_DTYPE)
+    shp = (p.slices, p.potNx, p.potNy, 2)
+    assert int(meta["potNx"]) == p.potNx and int(meta["potNy"]) == p.potNy, (meta, p.potNx)
+    out["V"] = np.fromfile(os.path.join(dump, "potential.bin"), np.float32).reshape(shp)
+    out["T"] = np.fromfile(os.path.join(dump, "trans.bin"), np.float32).reshape(shp)
+    out["probe"] = np.fromfile(os.path.join(dump, "probe.bin"), np.float32).reshape(p.nx, p.ny, 2)
+    for line in open(os.path.join(dump, "lut_dims.txt")):
+        Z, Nz, Nr, ns = map(int, line.split())
+        out["lut_%d" % Z] = np.fromfile(os.path.join(dump, "lut_%d.bin" % Z), np.float32).reshape(Nz, Nr, 2)[..., 0]
+        qf = os.path.join(dump, "lutq_%d.bin" % Z)
+        if os.path.exists(qf):
+            out["lutq_%d" % Z] = np.fromfile(qf, np.float32).reshape(Nz, Nr, 2)[..., 0]
+        out["nzsub"] = np.int32(ns)
+    if case["run"] and case["mode"] == "STEM":
+        nt = p.thickness_count()
+        det = np.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), np.float32)
+        for t in range(nt):
+            for i in range(p.detectorNum):
+                det[t, i] = np.fromfile(os.path.join(dump, "det_%d_%d.bin" % (t, i)), np.float32).reshape(
+                    p.scanXN, p.scanYN)
+        out["det"] = det
+        folder = os.path.join(workdir, "out")
+        for ix, iy in [(0, 0), (0, 1), (1, 0), (p.scanXN - 1, p.scanYN - 1)]:
+            dp = imageio.read_img(os.path.join(folder, "diffAvg_%d_%d.img" % (ix, iy)))
+            out["diffpat_%d_%d" % (ix, iy)] = dp.data.astype(np.float32)
+            ww = imageio.read_img(os.path.join(folder, "mulswav_%d_%d.img" % (ix, iy)))
+            out["wave_%d_%d" % (ix, iy)] = np.stack([ww.data.real, ww.data.imag], -1).astype(np.float32)
+    out["params_json"] = np.array(json.dumps(p.as_dict()))
+    out["meta_json"] = np.array(json.dumps(meta))
+    out["case_json"] = np.array(json.dumps({k: v for k, v in case.items()}))
+    return out
+
+
+def main():
+    oracle.build(quiet=False)
+    for name, case in CASES.items():
+        work = tempfile.mkdtemp(prefix="qs_golden_")
+        try:
+            out = run_case(name, case, work)
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **out)
+        print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,65 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point
+include/qstem_gpu.h declares (no GPU needed: nothing is launched)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from qstem_gb300 import abi, lib
+
+HEADER = os.path.join(ROOT, "include", "qstem_gpu.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(qs_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    from qstem_gb300 import build
+    build.build()
+    return lib.load()
+
+
+def test_exports_every_declared_symbol(L):
+    names = declared_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(lib.EXPORTS)
+
+
+def test_abi_version(L):
+    assert L.qs_abi_version() == 1
+
+
+def test_struct_layouts():
+    assert ctypes.sizeof(abi.QsAtom) == 28
+    assert abi.ATOM_DTYPE.itemsize == 28
+    assert ctypes.sizeof(abi.QsDetector) == 24
+    # field order of qs_params as declared in the header
+    text = open(HEADER).read()
+    body = text[text.index("typedef struct qs_params"):text.index("} qs_params;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = []
+    for decl in re.findall(r"(?:int|float|qs_detector)\s+([^;]+);", body):
+        for n in decl.split(","):
+            names.append(n.strip().split("[")[0])
+    assert names == [f[0] for f in abi.QsParams._fields_]
+
+
+def test_params_finalize_and_thickness(L):
+    from qstem_gb300 import config
+    p = config.make_params(nx=64, resolutionX=0.1, v0=200, slices=20, sliceThickness=2, ax=20, by=20, c=40,
+                           scan=(5, 9, 4, 5, 9, 4), detectors=[(70, 200, "HAADF")], outputInterval=7)
+    k_in, k_out = p.detectors[0].k2Inside, p.detectors[0].k2Outside
+    p.detectors[0].k2Inside = 0
+    assert L.qs_params_finalize(ctypes.byref(p)) == 0
+    assert np.float32(p.detectors[0].k2Inside) == np.float32(k_in)
+    assert np.float32(p.detectors[0].k2Outside) == np.float32(k_out)
+    assert L.qs_thickness_count(ctypes.byref(p)) == 20 // 7 + 1

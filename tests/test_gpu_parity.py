@@ -1,0 +1,173 @@
+"""GPU library (through the C ABI) against the oracle and against the
+reference's own outputs (golden fixtures).
+
+Tolerances (relative L2 unless noted):
+  LUT, potential, transmission  1e-5   (FP64 table build; float atomics)
+  probe                         1e-5
+  detectors / diffraction patterns / exit waves after the slice loop
+                                1e-4   (the contract's bound for the
+                                        complex-FP32 multislice)
+"""
+import numpy as np
+import pytest
+
+from conftest import Golden, rel_l2
+from oracle import oracle
+from qstem_gb300 import config, lib
+
+pytestmark = pytest.mark.gpu
+
+TOL_BUILD = 1e-5
+TOL_MS = 1e-4
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    oracle.build()
+    c = lib.Context(0)
+    yield c
+    c.close()
+
+
+def _B(g, Z, charged):
+    a = g["atoms"]
+    sel = a[(a["Znum"] == Z) & ((a["q"] != 0) if charged else True)]
+    return 0.0 if (g.params.tds or len(sel) == 0) else float(sel["dw"][0])
+
+
+def test_lut_vs_oracle_and_reference(ctx, golden):
+    p = golden.params
+    for k in golden.keys():
+        if not (k.startswith("lut_") or k.startswith("lutq_")):
+            continue
+        Z = int(k.split("_")[1])
+        charged = k.startswith("lutq_")
+        B = _B(golden, Z, charged)
+        gpu, ns = ctx.lut(p, Z, B, charged)
+        cpu, _ = oracle.lut(p, Z, B, charged)
+        assert ns == int(golden["nzsub"])
+        assert rel_l2(gpu, cpu) <= TOL_BUILD, k
+        assert rel_l2(gpu, golden[k]) <= TOL_BUILD, k
+
+
+def test_potential_and_transmission(ctx, golden):
+    p = golden.params
+    V = ctx.slices(p, golden["atoms"], potential_only=True)
+    assert rel_l2(V, golden["V"]) <= TOL_BUILD
+    T = ctx.slices(p, golden["atoms"])
+    assert rel_l2(T, golden["T"]) <= TOL_BUILD
+    # |t| = 1 without band limit
+    if not p.bandlimittrans:
+        assert np.abs(np.hypot(T[..., 0], T[..., 1]) - 1).max() < 1e-5
+
+
+def test_probe(ctx, golden):
+    p = golden.params
+    pr = ctx.probe(p)
+    assert rel_l2(pr, golden["probe"]) <= TOL_BUILD
+    assert rel_l2(pr, oracle.probe(p)) <= TOL_BUILD
+    assert abs(np.sum(pr.astype(np.float64) ** 2) / (p.nx * p.ny) - 1) < 1e-5
+
+
+def test_multislice_vs_reference(ctx, golden):
+    if "det" not in golden:
+        pytest.skip("case does not run the scan")
+    p = golden.params
+    det, dps, ews = ctx.multislice(p, golden["T"], golden["probe"], want_diffpats=True, want_exit_waves=True)
+    assert rel_l2(det, golden["det"]) <= TOL_MS
+    ocd, ocp, ocw = oracle.stem(p, golden["T"], golden["probe"], diffpats=True, exit_waves=True)
+    assert rel_l2(det, ocd) <= TOL_MS
+    assert rel_l2(dps, ocp) <= TOL_MS
+    assert rel_l2(ews, ocw) <= TOL_MS
+    for k in golden.keys():
+        if k.startswith("diffpat_") or k.startswith("wave_"):
+            ix, iy = map(int, k.split("_")[1:])
+            pos = ix * p.scanYN + iy
+            mine = dps[pos] if k.startswith("diffpat_") else ews[pos]
+            assert rel_l2(mine, golden[k]) <= TOL_MS, k
+
+
+def test_end_to_end_from_atoms(ctx):
+    """atoms -> slices -> probe -> scan entirely on the GPU vs the oracle chain."""
+    g = Golden("sto64")
+    p = g.params
+    T = ctx.slices(p, g["atoms"])
+    det, _, _ = ctx.multislice(p, T)
+    To = oracle.transmission(p, oracle.potential(p, g["atoms"]))
+    dco, _, _ = oracle.stem(p, To)
+    assert rel_l2(det, dco) <= TOL_MS
+    assert rel_l2(det, g["det"]) <= TOL_MS
+
+
+def sto_case(nx, res, slices, ncell, scan_px, dets, v0=200.0, alpha=20.0, out_every=None, periodic=False):
+    cell = config.srtio3_cell()
+    atoms, ax, by, c = config.replicate(cell, *ncell)
+    a = 3.905
+    x0 = a * (ncell[0] // 2)
+    y0 = a * (ncell[1] // 2)
+    p = config.make_params(nx=nx, resolutionX=res, v0=v0, slices=slices, sliceThickness=1.9525, ax=ax, by=by,
+                           c=c, scan=(x0, x0 + a, scan_px, y0, y0 + a, scan_px), detectors=dets, alpha=alpha,
+                           outputInterval=out_every, periodicXY=periodic)
+    return p, atoms
+
+
+@pytest.mark.parametrize("nx,res,ncell", [(256, 0.0763, (5, 5, 4)), (128, 0.0915, (4, 4, 4)),
+                                          (384, 0.0763, (7, 7, 3)), (512, 0.07627, (10, 10, 2))])
+def test_larger_grids_vs_oracle(ctx, nx, res, ncell):
+    dets = [(0, 10, "BF"), (10, 25, "LA"), (25, 70, "MA"), (70, 200, "HAADF")]
+    p, atoms = sto_case(nx, res, 2 * ncell[2], ncell, 2, dets, out_every=3)
+    T = ctx.slices(p, atoms)
+    To = oracle.transmission(p, oracle.potential(p, atoms))
+    assert rel_l2(T, To) <= TOL_BUILD
+    det, dps, ews = ctx.multislice(p, To, want_diffpats=True, want_exit_waves=True)
+    dco, dpo, ewo = oracle.stem(p, To, diffpats=True, exit_waves=True)
+    assert rel_l2(det, dco) <= TOL_MS
+    assert rel_l2(dps, dpo) <= TOL_MS
+    assert rel_l2(ews, ewo) <= TOL_MS
+
+
+def test_bandlimited_cbed(ctx):
+    g = Golden("si64cbed")
+    p = g.params
+    T = ctx.slices(p, g["atoms"])
+    assert rel_l2(T, g["T"]) <= TOL_BUILD
+    # one CBED position at the window origin, diffraction pattern out
+    pos = (np.zeros(1), np.zeros(1), np.zeros(1), np.zeros(1))
+    _, dp, ew = ctx.multislice(p, g["T"], g["probe"], positions=pos, want_det=False, want_diffpats=True,
+                               want_exit_waves=True)
+    w, _, dpo = oracle.run_position(p, g["T"], 0, 0, g["probe"])
+    assert rel_l2(dp[0], dpo) <= TOL_MS
+    assert rel_l2(ew[0], w) <= TOL_MS
+
+
+def test_collect_matches_oracle_semantics(ctx):
+    g = Golden("sto64")
+    p = g.params
+    rng = np.random.default_rng(3)
+    w = rng.standard_normal((p.nx, p.ny, 2)).astype(np.float32)
+    sums, dp = ctx.collect(p, w, diffpat=True)
+    I = (w[..., 0] * w[..., 0] + w[..., 1] * w[..., 1]).astype(np.float64)
+    t = config  # noqa
+    ax = np.float32(np.float32(p.resolutionX) * p.nx)
+    k = np.arange(p.nx)
+    kx = np.where(k > p.nx // 2, (k - p.nx).astype(np.float32) / ax, k.astype(np.float32) / ax).astype(np.float32)
+    k2 = (kx[:, None] * kx[:, None] + (kx * kx)[None, :]).astype(np.float32)
+    for d in range(p.detectorNum):
+        m = (k2 >= np.float32(p.detectors[d].k2Inside)) & (k2 <= np.float32(p.detectors[d].k2Outside))
+        assert abs(sums[d] - I[m].sum()) <= 1e-9 * I.sum()
+    ref_dp = np.fft.fftshift(I) / np.sqrt(p.nx * p.ny)
+    assert rel_l2(dp, ref_dp) <= 1e-6
+
+
+def test_errors_are_codes_not_exits(ctx):
+    g = Golden("sto64")
+    p = g.params.copy()
+    p.nx = p.ny = 100  # no FFT kernel for 100
+    with pytest.raises(lib.QsError) as e:
+        ctx.probe(p)
+    assert e.value.code == -4
+    p2 = g.params.copy()
+    p2.slices = 0
+    with pytest.raises(lib.QsError) as e:
+        ctx.slices(p2, g["atoms"])
+    assert e.value.code == -1

@@ -1,0 +1,108 @@
+"""The C restatement (oracle/) against fixtures produced by the reference
+itself (tests/golden/make_golden.py).  On the build machine the agreement is
+bit-exact; the tolerances below only absorb last-bit differences of another
+machine's libm (cos/sin/exp of the host the tests run on)."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from oracle import oracle
+from qstem_gb300 import abi
+
+TOL = 1e-5  # relative; bit-exact where the C library is the one the fixtures were made with
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build():
+    oracle.build()
+
+
+def lut_B(golden, Z, charged):
+    """Debye-Waller factor the reference's LUT was built with: that of the
+    element's first contributing atom (its static LUT cache is per element,
+    stem3/stemlib.cpp:1417); the harness builds tables of elements without
+    such atoms itself with B = 0."""
+    a = golden["atoms"]
+    sel = a[(a["Znum"] == Z) & ((a["q"] != 0) if charged else True)]
+    if golden.params.tds or len(sel) == 0:
+        return 0.0
+    return float(sel["dw"][0])
+
+
+def test_lut(golden):
+    p = golden.params
+    for k in golden.keys():
+        if not (k.startswith("lut_") or k.startswith("lutq_")):
+            continue
+        Z = int(k.split("_")[1])
+        charged = k.startswith("lutq_")
+        mine, nzsub = oracle.lut(p, Z, lut_B(golden, Z, charged), charged=charged)
+        ref = golden[k]
+        assert mine.shape == ref.shape
+        assert nzsub == int(golden["nzsub"])
+        assert np.abs(mine - ref).max() <= TOL * np.abs(ref).max(), k
+
+
+def test_potential(golden):
+    V = oracle.potential(golden.params, golden["atoms"])
+    ref = golden["V"]
+    assert np.abs(V - ref).max() <= TOL * np.abs(ref).max()
+    assert np.all(V[..., 1] == 0)
+
+
+def test_transmission(golden):
+    T = oracle.transmission(golden.params, golden["V"])
+    ref = golden["T"]
+    assert np.abs(T - ref).max() <= TOL * max(1.0, np.abs(ref).max())
+
+
+def test_probe(golden):
+    pr = oracle.probe(golden.params)
+    ref = golden["probe"]
+    assert np.abs(pr - ref).max() <= TOL * np.abs(ref).max()
+
+
+def test_stem_detectors_diffpats_waves(golden):
+    if "det" not in golden:
+        pytest.skip("case does not run the scan")
+    p = golden.params
+    det, dps, ews = oracle.stem(p, golden["T"], golden["probe"], diffpats=True, exit_waves=True)
+    ref = golden["det"]
+    assert det.shape == ref.shape
+    assert rel_l2(det, ref) <= TOL
+    for k in golden.keys():
+        if k.startswith("diffpat_") or k.startswith("wave_"):
+            ix, iy = map(int, k.split("_")[1:])
+            pos = ix * p.scanYN + iy
+            mine = dps[pos] if k.startswith("diffpat_") else ews[pos]
+            assert rel_l2(mine, golden[k]) <= TOL, k
+
+
+def test_params_match_readfile(golden):
+    """qstem_gb300.config.make_params reproduces readFile's derived fields."""
+    p, m = golden.params, golden.meta
+    for key in ("nx", "ny", "potNx", "potNy", "slices", "scanXN", "scanYN", "outputInterval",
+                "nonPeriod", "nonPeriodZ", "centerSlices", "bandlimittrans"):
+        assert getattr(p, key) == int(m[key]), key
+    for key in ("resolutionX", "sliceThickness", "potOffsetX", "potOffsetY", "potSizeX", "potSizeY",
+                "scanXStart", "scanXStop", "scanYStop", "v0", "alpha", "Cs", "df0", "electronScale", "ax", "by",
+                "czOffset"):
+        assert np.float32(getattr(p, key)) == np.float32(float(m[key])), key
+    for i in range(p.detectorNum):
+        vals = [float(v) for v in m["det%d" % i].split()]
+        assert np.float32(p.detectors[i].k2Inside) == np.float32(vals[2])
+        assert np.float32(p.detectors[i].k2Outside) == np.float32(vals[3])
+
+
+def test_atoms_match_readunitcell(golden):
+    """qstem_gb300.config.replicate reproduces readUnitCell's atom list bit for bit."""
+    import sys, os
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_golden
+    cell, atoms, _ = make_golden.params_for(golden.case)
+    assert np.array_equal(atoms.view(np.uint8), golden["atoms"].view(np.uint8))
+
+
+def test_thickness_slots(golden):
+    p = golden.params
+    assert p.thickness_count() == (p.slices // p.outputInterval) + 1
