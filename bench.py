@@ -35,6 +35,7 @@ SEED = 20261203 + 100
 
 
 def workload_params(npix=64):
+    """npix: scan raster edge (64 for the workload; smaller only for profiling captures)."""
     atoms, ax, by, c = config.replicate(config.srtio3_cell(), 10, 10, 20)
     p = config.make_params(nx=512, resolutionX=39.05 / 512, v0=200, slices=40, sliceThickness=1.9525, ax=ax,
                            by=by, c=c, scan=(19.525, 23.43, npix, 19.525, 23.43, npix),
@@ -156,7 +157,7 @@ def run_ours(args, rank, world):
     from qstem_gb300 import lib
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    p, atoms = workload_params()
+    p, atoms = workload_params(args.npix)
     npos = p.scanXN * p.scanYN
     nt = p.thickness_count()
     ctx = lib.Context(dev)
@@ -284,6 +285,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--npix", type=int, default=64, help="scan raster edge; 64 is the workload")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
