@@ -224,7 +224,6 @@ struct LineCfg {
     using rad = RAD;
     static_assert(RAD::prefix(RAD::count) == N, "radices must multiply to N");
     static_assert(T <= 32 && (32 % T) == 0, "row lines must live inside one warp");
-    static_assert(T == line_threads(N_), "line_threads() must match the configuration");
 };
 
 __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
@@ -304,6 +303,7 @@ __device__ __forceinline__ void line_fft(float2 (&reg)[Cfg::E], const SM& sm, co
 // One configuration per supported line length.
 template <int N>
 struct Line;
+// (the product kernels size __launch_bounds__ with line_threads(N))
 template <> struct Line<64> { using cfg = LineCfg<64, 8, radices<8, 8>>; };
 template <> struct Line<128> { using cfg = LineCfg<128, 8, radices<16, 8>>; };
 template <> struct Line<256> { using cfg = LineCfg<256, 16, radices<16, 16>>; };
@@ -311,6 +311,15 @@ template <> struct Line<384> { using cfg = LineCfg<384, 16, radices<8, 6, 8>>; }
 template <> struct Line<512> { using cfg = LineCfg<512, 16, radices<32, 16>>; };
 template <> struct Line<768> { using cfg = LineCfg<768, 32, radices<8, 12, 8>>; };
 template <> struct Line<1024> { using cfg = LineCfg<1024, 32, radices<32, 32>>; };
+
+template <int N>
+constexpr bool line_threads_match() {
+    return Line<N>::cfg::T == line_threads(N);
+}
+static_assert(line_threads_match<64>() && line_threads_match<128>() && line_threads_match<256>() &&
+                  line_threads_match<384>() && line_threads_match<512>() && line_threads_match<768>() &&
+                  line_threads_match<1024>(),
+              "line_threads() must match the Line<N> configurations");
 
 inline bool line_supported(int n) {
     return n == 64 || n == 128 || n == 256 || n == 384 || n == 512 || n == 768 || n == 1024;
