@@ -208,6 +208,31 @@ typedef struct qs_stats {
 int qs_ctx_profile(qs_ctx *ctx, int enable); /* resets the counters */
 int qs_ctx_stats(qs_ctx *ctx, qs_stats *out); /* synchronises the stream */
 
+/* ------------------------------------------------- without allocation */
+/* No counterpart in the reference.  qs_multislice_run for callers that must
+ * not allocate device memory while they run: cudaFree waits for the whole
+ * device (stalling every other stream in the process), a framework's caching
+ * allocator may own all device memory, or a deployment may have reserved its
+ * whole budget up front.  This variant allocates nothing: besides the
+ * caller's buffers it uses only a fixed scratch area of
+ * QS_NOALLOC_SCRATCH_BYTES compiled into the library (held on every GPU that
+ * loads the library until the process exits).
+ *   - stream is a cudaStream_t (NULL: the default stream); all pointers are
+ *     device pointers; probe is required (make it with qs_probe first).
+ *   - Limit: the scratch holds the whole batch -- about nx*ny*8 bytes per
+ *     position plus small tables -- so a 512x512 batch takes at most ~30
+ *     positions, 256x256 ~120; larger batches are rejected with QS_ERR_ARG and
+ *     a message giving the bytes needed.  Split the scan into such batches.
+ *   - The first call on each device looks up the scratch address with
+ *     cudaGetSymbolAddress; make that first call before any stream capture.
+ *   - All calls share the one scratch area, which keeps the previous call's
+ *     contents (the call clears what must start at zero): calls whose GPU work
+ *     overlaps race on it and must be serialised by the caller. */
+#define QS_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int qs_multislice_run_noalloc(void *stream, const qs_params *p, const float *trans, const float *probe,
+                              const qs_batch *batch, float *det_images, float *diffpats,
+                              float *exit_waves);
+
 /* collectIntensity for one wave already in k-space (after propagate):
  * det_sums[d] = sum of |psi(k)|^2 over detector d's annulus (double, not yet
  * multiplied by electronScale/(nx*ny)^2, the factor the reference applies,

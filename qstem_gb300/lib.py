@@ -21,7 +21,8 @@ LIB_PATH = os.path.join(HERE, "_lib", "libqstem_gpu.so")
 
 EXPORTS = ["qs_ctx_create", "qs_ctx_destroy", "qs_last_error", "qs_abi_version", "qs_ctx_stream",
            "qs_params_finalize", "qs_thickness_count", "qs_lut_build", "qs_slices_build", "qs_probe",
-           "qs_multislice_run", "qs_collect", "qs_stem_run", "qs_ctx_profile", "qs_ctx_stats"]
+           "qs_multislice_run", "qs_collect", "qs_stem_run", "qs_ctx_profile", "qs_ctx_stats",
+           "qs_multislice_run_noalloc"]
 
 _lib = None
 
@@ -60,6 +61,7 @@ def load(path=LIB_PATH):
     L.qs_stem_run.argtypes = [vp, P, vp, ctypes.c_int, ctypes.POINTER(abi.QsBatch), vp, vp]
     L.qs_ctx_profile.argtypes = [vp, ctypes.c_int]
     L.qs_ctx_stats.argtypes = [vp, ctypes.POINTER(abi.QsStats)]
+    L.qs_multislice_run_noalloc.argtypes = [vp, P, vp, vp, ctypes.POINTER(abi.QsBatch), vp, vp, vp]
     _lib = L
     return L
 
