@@ -11,14 +11,14 @@
 // j + r*N/R -- which are exactly the thread's own registers q + r*E/R -- so
 // no data moves before a butterfly.  Outputs go to (j/Ns)*Ns*R + j%Ns + r*Ns;
 // for every pass but the last they are exchanged through a padded shared
-// memory line (one float2 of padding per 16, so that the stride-R writes of
-// the first pass hit distinct banks).  The last pass writes its outputs
+// memory line (one float2 of padding per first-pass radix, so that the
+// stride-R writes of the first pass hit distinct banks).  The last pass writes its outputs
 // straight back to the thread's registers in natural order.  A line's
 // threads are one warp or half-warp, so the exchanges need only __syncwarp.
 //
-// Inter-pass twiddles exp(-+2 pi i r (j%Ns)/(Ns R)) come from a table of
-// exp(-2 pi i k/N) (rounded from double) staged in shared memory; the
-// in-register DFTs use compile-time constants.
+// Inter-pass twiddles exp(-+2 pi i r (j%Ns)/(Ns R)) come from a per-pass
+// table (rounded from double) staged in shared memory; the in-register DFTs
+// use compile-time constants.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -214,25 +214,41 @@ constexpr int line_threads(int n) {
 }
 
 // Line configuration: N points, T threads per line.
+//
+// Shared-memory exchange scratch of a row line: element i lives at
+// i + i / R0 (R0 = first radix), so the stride-R0 writes of the first pass
+// land on an odd float2 stride and a half-warp hits 16 distinct 8-byte bank
+// pairs.  Inter-pass twiddles: pass p >= 1 (radix R, Ns = product of the
+// earlier radices) multiplies input r of butterfly j by
+// exp(-+2 pi i r (j mod Ns)/(Ns R)); the table stores them per pass as
+// [r-1][j mod Ns] so that consecutive lanes read consecutive words.
 template <int N_, int T_, class RAD>
 struct LineCfg {
     static constexpr int N = N_;
     static constexpr int T = T_;
     static constexpr int E = N / T;
     static constexpr int PASSES = RAD::count;
-    static constexpr int SMEM = N + N / 16;  // padded float2 per line
+    static constexpr int R0 = RAD::at(0);
+    static constexpr int SMEM = N + N / R0 + 1;  // padded float2 per row line
     using rad = RAD;
+    // offset of pass p's twiddles in the table (pass 0 has none)
+    static constexpr int tw_offset(int p) {
+        int o = 0;
+        for (int k = 1; k < p; ++k) o += (RAD::at(k) - 1) * RAD::prefix(k);
+        return o;
+    }
+    static constexpr int TW = tw_offset(RAD::count);  // table length
     static_assert(RAD::prefix(RAD::count) == N, "radices must multiply to N");
     static_assert(T <= 32 && (32 % T) == 0, "row lines must live inside one warp");
+    static_assert(TW <= N, "twiddle table must fit in N entries");
 };
-
-__device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
 
 // Shared-memory views of a line's exchange scratch.
 // Row lines: one padded line of Cfg::SMEM float2 per line.
+template <int R0>
 struct SmemRow {
     float2* p;
-    __device__ __forceinline__ float2& operator()(int i) const { return p[pad16(i)]; }
+    __device__ __forceinline__ float2& operator()(int i) const { return p[i + i / R0]; }
 };
 // Column tiles: element i of column c at p[i*C + c] (columns interleaved, so a
 // half-warp of consecutive columns touches consecutive words).
@@ -250,7 +266,7 @@ __device__ __forceinline__ void line_sync() {
 }
 
 // Transform the E registers of thread t (elements t + T*e) in place.
-// sm: this line's shared scratch view; tw: table of exp(-2 pi i k/N), k < N.
+// sm: this line's shared scratch view; tw: the per-pass twiddle table of Cfg.
 // BLOCK selects __syncthreads (a line spread over several warps) instead of
 // __syncwarp; with BLOCK every thread of the block must call.
 template <class Cfg, bool INV, bool BLOCK = false, class SM>
@@ -273,10 +289,10 @@ __device__ __forceinline__ void line_fft(float2 (&reg)[Cfg::E], const SM& sm, co
 #pragma unroll
             for (int r = 0; r < R; ++r) v[r] = reg[q + r * Q];
             if constexpr (Ns > 1) {
-                constexpr int step = N / (Ns * R);
+                constexpr int off = Cfg::tw_offset(p);
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
-                    const float2 w = tw[r * jm * step];
+                    const float2 w = tw[off + (r - 1) * Ns + jm];
                     v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
                 }
             }

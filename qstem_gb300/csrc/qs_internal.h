@@ -6,6 +6,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/qstem_gpu.h"
 
@@ -42,7 +43,7 @@ struct RowArgs {
     float2* exit_waves;          // ROW_LAST destination (may alias waves)
     const int* posX;             // nwaves window offsets
     const int* posY;
-    const float2* tw;            // exp(-2 pi i k/ny), k < ny
+    const float2* tw;            // twiddle table of the length-ny line transform
     int yA, yB;                  // ky index in band iff iy <= yA || iy >= yB
     float norm;                  // 1/(nx*ny)
 };
@@ -51,7 +52,7 @@ struct RowArgs {
 struct ColArgs {
     int nx, ny, nwaves;
     float2* waves;
-    const float2* tw;            // exp(-2 pi i k/nx), k < nx
+    const float2* tw;            // twiddle table of the length-nx line transform
     const float* kx2;            // nx, float as propagate_slow computes
     const float* ky2;            // ny
     const float2* px;            // nx propagator factors (cos t, -sin t)
@@ -77,8 +78,11 @@ int launch_det_finalize(const double* partial, int nwaves, int ntiles, int ndet,
 
 // generic in-place 2-D transform of `howmany` n0 x n1 arrays
 int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t s);
-// twiddle table exp(-2 pi i k/n), k < n, device-resident, cached per n
+// inter-pass twiddle table of the length-n line transform (per-pass layout of
+// LineCfg), device-resident and cached per device and n; twiddle_host fills
+// the same table on the host
 const float2* twiddles(int n);
+int twiddle_host(int n, std::vector<float2>& h);
 
 // ---------------------------------------------------------- potentials
 struct LutTable {

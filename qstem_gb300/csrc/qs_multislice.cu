@@ -14,6 +14,7 @@
 // and the next row pass reads them as zeros.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -26,8 +27,12 @@ namespace qs {
 
 constexpr int ROW_LINES = 8;
 
+// CTAs per SM the row pass is compiled for (register budget); 512^2 runs
+// fastest with three 128-thread CTAs (168 registers) rather than two.
+constexpr int row_min_blocks(int n) { return n == 512 ? 3 : 1; }
+
 template <int N, int MODE>
-__global__ void __launch_bounds__(line_threads(N) * ROW_LINES)
+__global__ void __launch_bounds__(line_threads(N) * ROW_LINES, row_min_blocks(N))
     ms_rows(RowArgs a) {
     using Cfg = typename Line<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E;
@@ -35,14 +40,14 @@ __global__ void __launch_bounds__(line_threads(N) * ROW_LINES)
     float2* s_tw = dsm;
     float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
     const int tid = threadIdx.x + T * threadIdx.y;
-    for (int i = tid; i < N; i += T * ROW_LINES) s_tw[i] = a.tw[i];
+    for (int i = tid; i < Cfg::TW; i += T * ROW_LINES) s_tw[i] = a.tw[i];
     __syncthreads();
 
     const int t = threadIdx.x;
     const long line = (long)blockIdx.x * ROW_LINES + threadIdx.y;
     const int b = (int)(line / a.nx);
     const int x = (int)(line - (long)b * a.nx);
-    const SmemRow sm{s_line};
+    const SmemRow<Cfg::R0> sm{s_line};
     float2 reg[E];
     if constexpr (MODE == ROW_FIRST) {
         const float2* src = a.probe + (size_t)x * N;
@@ -83,83 +88,123 @@ constexpr int col_tile() {
     return N >= 768 ? 8 : 16;
 }
 
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+
+// Column pass, persistent: each CTA walks the (wave, column tile) work items
+// blockIdx.x, blockIdx.x + gridDim.x, ...  While one tile is transformed, the
+// next one is copied into the other shared-memory stage with cp.async; once a
+// thread has read its elements of the current stage into registers, that
+// stage serves as the FFT exchange scratch.
 template <int N, bool DET, bool INVERSE>
 __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
-    ms_cols(ColArgs a) {
+    ms_cols(ColArgs a, long nitems) {
     using Cfg = typename Line<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();
     constexpr int NT = C * T;
     constexpr int NWARPS = (NT + 31) / 32;
     extern __shared__ float2 dsm[];
     float2* s_tw = dsm;
-    float2* s_tile = dsm + N;
+    float2* s_stage = dsm + N;  // two stages of N*C
     __shared__ double s_det[QS_MAX_DETECTORS][NWARPS];
     const int tid = threadIdx.x + C * threadIdx.y;
-    for (int i = tid; i < N; i += NT) s_tw[i] = a.tw[i];
-    __syncthreads();
-
     const int c = threadIdx.x, t = threadIdx.y;
-    const int tile = blockIdx.x % a.ntiles;
-    const int b = blockIdx.x / a.ntiles;
-    const int ky = __ldg(a.tiles + tile) + c;
-    float2* col = a.waves + (size_t)b * a.nx * a.ny + ky;
-    float2 reg[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) reg[e] = col[(size_t)(t + T * e) * a.ny];
-    const SmemCol<C> sm{s_tile, c};
-    line_fft<Cfg, false, true>(reg, sm, s_tw, t);
+    for (int i = tid; i < Cfg::TW; i += NT) s_tw[i] = a.tw[i];
 
-    // propagate_slow (stem3/stemlib.cpp:2831-2849)
-    const float ky2 = __ldg(a.ky2 + ky);
-    const float2 pyv = __ldg(a.py + ky);
+    auto column = [&](long item) {
+        const int tile = (int)(item % a.ntiles);
+        const int b = (int)(item / a.ntiles);
+        return a.waves + (size_t)b * a.nx * a.ny + __ldg(a.tiles + tile) + c;
+    };
+    auto prefetch = [&](long item, int stage) {
+        if (item < nitems) {
+            const float2* col = column(item);
+            float2* dst = s_stage + stage * N * C;
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-        const int kx = t + T * e;
-        const float kx2 = __ldg(a.kx2 + kx);
-        if (kx2 < a.k2max && (kx2 + ky2) < a.k2max)
-            reg[e] = cmul(cmul(reg[e], pyv), __ldg(a.px + kx));
-        else
-            reg[e] = make_float2(0.f, 0.f);
-    }
+            for (int e = 0; e < E; ++e) cp_async8(dst + (t + T * e) * C + c, col + (size_t)(t + T * e) * a.ny);
+        }
+        cp_async_commit();
+    };
 
-    if constexpr (DET) {
-        // collectIntensity (stem3/stemlib.cpp:2615-2657): |psi(k)|^2 in float,
-        // summed per annulus in double
-        const int lane = tid & 31, warp = tid >> 5;
-        for (int d = 0; d < a.ndet; ++d) {
-            double acc = 0.0;
-            const float lo = a.k2in[d], hi = a.k2out[d];
+    long item = blockIdx.x;
+    prefetch(item, 0);
+    __syncthreads();
+    for (int it = 0; item < nitems; ++it, item += gridDim.x) {
+        prefetch(item + gridDim.x, (it + 1) & 1);
+        cp_async_wait<1>();
+        float2* stage = s_stage + (it & 1) * N * C;
+        float2 reg[E];
 #pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const float k2 = __ldg(a.kx2 + t + T * e) + ky2;
-                const float I = reg[e].x * reg[e].x + reg[e].y * reg[e].y;
-                if (k2 >= lo && k2 <= hi) acc += (double)I;
+        for (int e = 0; e < E; ++e) reg[e] = stage[(t + T * e) * C + c];
+        __syncthreads();  // all elements read before the stage becomes exchange scratch
+        const SmemCol<C> sm{stage, c};
+        line_fft<Cfg, false, true>(reg, sm, s_tw, t);
+
+        const int tile = (int)(item % a.ntiles);
+        const int b = (int)(item / a.ntiles);
+        const int ky = __ldg(a.tiles + tile) + c;
+        // propagate_slow (stem3/stemlib.cpp:2831-2849)
+        const float ky2 = __ldg(a.ky2 + ky);
+        const float2 pyv = __ldg(a.py + ky);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int kx = t + T * e;
+            const float kx2 = __ldg(a.kx2 + kx);
+            if (kx2 < a.k2max && (kx2 + ky2) < a.k2max)
+                reg[e] = cmul(cmul(reg[e], pyv), __ldg(a.px + kx));
+            else
+                reg[e] = make_float2(0.f, 0.f);
+        }
+
+        if constexpr (DET) {
+            // collectIntensity (stem3/stemlib.cpp:2615-2657): |psi(k)|^2 in
+            // float, summed per annulus in double
+            const int lane = tid & 31, warp = tid >> 5;
+            for (int d = 0; d < a.ndet; ++d) {
+                double acc = 0.0;
+                const float lo = a.k2in[d], hi = a.k2out[d];
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const float k2 = __ldg(a.kx2 + t + T * e) + ky2;
+                    const float I = reg[e].x * reg[e].x + reg[e].y * reg[e].y;
+                    if (k2 >= lo && k2 <= hi) acc += (double)I;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) s_det[d][warp] = acc;
             }
+            if (a.diffpat) {
+                float* dp = a.diffpat + (size_t)b * a.nx * a.ny + (ky + a.ny / 2) % a.ny;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) s_det[d][warp] = acc;
-        }
-        if (a.diffpat) {
-            float* dp = a.diffpat + (size_t)b * a.nx * a.ny + (ky + a.ny / 2) % a.ny;
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const int kx = t + T * e;
-                const float I = reg[e].x * reg[e].x + reg[e].y * reg[e].y;
-                dp[(size_t)((kx + a.nx / 2) % a.nx) * a.ny] = (float)((double)I * a.scaleDiff);
+                for (int e = 0; e < E; ++e) {
+                    const int kx = t + T * e;
+                    const float I = reg[e].x * reg[e].x + reg[e].y * reg[e].y;
+                    dp[(size_t)((kx + a.nx / 2) % a.nx) * a.ny] = (float)((double)I * a.scaleDiff);
+                }
+            }
+            __syncthreads();
+            if (tid < a.ndet) {
+                double sum = 0.0;
+                for (int w = 0; w < NWARPS; ++w) sum += s_det[tid][w];
+                a.partial[((size_t)b * a.ntiles + tile) * a.ndet + tid] = sum;
             }
         }
-        __syncthreads();
-        if (tid < a.ndet) {
-            double s = 0.0;
-            for (int w = 0; w < NWARPS; ++w) s += s_det[tid][w];
-            a.partial[((size_t)b * a.ntiles + tile) * a.ndet + tid] = s;
-        }
-    }
-    if constexpr (INVERSE) {
-        line_fft<Cfg, true, true>(reg, sm, s_tw, t);
+        if constexpr (INVERSE) {
+            line_fft<Cfg, true, true>(reg, sm, s_tw, t);
+            float2* col = a.waves + (size_t)b * a.nx * a.ny + ky;
 #pragma unroll
-        for (int e = 0; e < E; ++e) col[(size_t)(t + T * e) * a.ny] = reg[e];
+            for (int e = 0; e < E; ++e) col[(size_t)(t + T * e) * a.ny] = reg[e];
+        }
+        __syncthreads();  // scratch and s_det reads done before the stage is refilled
     }
+    cp_async_wait<0>();
 }
 
 __global__ void det_finalize(const double* __restrict__ partial, int nwaves, int ntiles, int ndet, double scale,
@@ -180,6 +225,10 @@ static size_t row_smem() {
 }
 template <int N>
 static size_t col_smem() {
+    return sizeof(float2) * (N + 2 * (size_t)N * col_tile<N>());
+}
+template <int N>
+static size_t col_smem_plain() {
     return sizeof(float2) * (N + (size_t)N * col_tile<N>());
 }
 
@@ -228,16 +277,26 @@ int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s) {
 template <int N, bool DET, bool INV>
 static int cols_n3(const ColArgs& a, cudaStream_t s) {
     using Cfg = typename Line<N>::cfg;
-    static bool attr = false;
+    static int resident = 0;  // CTAs per SM, from the occupancy calculator
+    static int sms = 0;
     const size_t sm = col_smem<N>();
-    if (!attr) {
+    if (!resident) {
         QS_CUDA_TRY(cudaFuncSetAttribute(ms_cols<N, DET, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        attr = true;
+        int dev = 0;
+        QS_CUDA_TRY(cudaGetDevice(&dev));
+        QS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        QS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, ms_cols<N, DET, INV>,
+                                                                  col_tile<N>() * Cfg::T, sm));
+        if (resident < 1) {
+            set_error("column pass does not fit on an SM");
+            return QS_ERR_UNSUPPORTED;
+        }
     }
     dim3 block(col_tile<N>(), Cfg::T);
-    const long nblk = (long)a.nwaves * a.ntiles;
-    if (nblk <= 0) return QS_OK;
-    ms_cols<N, DET, INV><<<(unsigned)nblk, block, sm, s>>>(a);
+    const long nitems = (long)a.nwaves * a.ntiles;
+    if (nitems <= 0) return QS_OK;
+    const long grid = std::min<long>(nitems, (long)sms * resident);
+    ms_cols<N, DET, INV><<<(unsigned)grid, block, sm, s>>>(a, nitems);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;
@@ -287,7 +346,7 @@ __global__ void __launch_bounds__(line_threads(N) * ROW_LINES) fft_rows(float2* 
     float2* s_tw = dsm;
     float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
     const int tid = threadIdx.x + T * threadIdx.y;
-    for (int i = tid; i < N; i += T * ROW_LINES) s_tw[i] = tw[i];
+    for (int i = tid; i < Cfg::TW; i += T * ROW_LINES) s_tw[i] = tw[i];
     __syncthreads();
     const long line = (long)blockIdx.x * ROW_LINES + threadIdx.y;
     const bool ok = line < nlines;
@@ -296,7 +355,7 @@ __global__ void __launch_bounds__(line_threads(N) * ROW_LINES) fft_rows(float2* 
     float2 reg[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) reg[e] = ok ? p[t + T * e] : make_float2(0.f, 0.f);
-    line_fft<Cfg, INV>(reg, SmemRow{s_line}, s_tw, t);
+    line_fft<Cfg, INV>(reg, SmemRow<Cfg::R0>{s_line}, s_tw, t);
     if (ok) {
 #pragma unroll
         for (int e = 0; e < E; ++e) p[t + T * e] = reg[e];
@@ -313,7 +372,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
     float2* s_tw = dsm;
     float2* s_tile = dsm + N;
     const int tid = threadIdx.x + C * threadIdx.y;
-    for (int i = tid; i < N; i += C * T) s_tw[i] = tw[i];
+    for (int i = tid; i < Cfg::TW; i += C * T) s_tw[i] = tw[i];
     __syncthreads();
     const int c = threadIdx.x, t = threadIdx.y;
     const int col = blockIdx.x * C + c;
@@ -347,7 +406,7 @@ static int fft_rows_n(float2* data, long nlines, cudaStream_t s) {
 template <int N, bool INV>
 static int fft_cols_n(float2* data, int ncols, int howmany, cudaStream_t s) {
     static bool attr = false;
-    const size_t sm = col_smem<N>();
+    const size_t sm = col_smem_plain<N>();
     if (!attr) {
         QS_CUDA_TRY(cudaFuncSetAttribute(fft_cols<N, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         attr = true;
@@ -407,6 +466,38 @@ int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t 
     return QS_OK;
 }
 
+template <int N>
+static void fill_twiddles(std::vector<float2>& h) {
+    using Cfg = typename Line<N>::cfg;
+    using RAD = typename Cfg::rad;
+    h.assign(N, make_float2(0.f, 0.f));
+    for (int p = 1; p < Cfg::PASSES; ++p) {
+        const int R = RAD::at(p), Ns = RAD::prefix(p), off = Cfg::tw_offset(p);
+        for (int r = 1; r < R; ++r)
+            for (int jm = 0; jm < Ns; ++jm) {
+                // exp(-2 pi i r jm/(Ns R)), angle reduced exactly in turns
+                double turns = (double)(r * jm) / (double)(Ns * R);
+                turns -= std::floor(turns + 0.5);
+                const double ang = -2.0 * kPi * turns;
+                h[off + (r - 1) * Ns + jm] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+            }
+    }
+}
+
+int twiddle_host(int n, std::vector<float2>& h) {
+    switch (n) {
+        case 64: fill_twiddles<64>(h); return QS_OK;
+        case 128: fill_twiddles<128>(h); return QS_OK;
+        case 256: fill_twiddles<256>(h); return QS_OK;
+        case 384: fill_twiddles<384>(h); return QS_OK;
+        case 512: fill_twiddles<512>(h); return QS_OK;
+        case 768: fill_twiddles<768>(h); return QS_OK;
+        case 1024: fill_twiddles<1024>(h); return QS_OK;
+    }
+    set_error("no line transform of length " + std::to_string(n));
+    return QS_ERR_UNSUPPORTED;
+}
+
 const float2* twiddles(int n) {
     static std::mutex mu;
     static std::map<std::pair<int, int>, float2*> cache;
@@ -416,14 +507,8 @@ const float2* twiddles(int n) {
     auto key = std::make_pair(dev, n);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
-    std::vector<float2> h(n);
-    for (int k = 0; k < n; ++k) {
-        // exp(-2 pi i k/n) with the angle reduced exactly in turns
-        double turns = (double)k / (double)n;
-        if (turns > 0.5) turns -= 1.0;
-        const double ang = -2.0 * kPi * turns;
-        h[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
-    }
+    std::vector<float2> h;
+    if (twiddle_host(n, h) != QS_OK) return nullptr;
     float2* d = nullptr;
     if (cudaMalloc(&d, sizeof(float2) * n) != cudaSuccess) return nullptr;
     cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);

@@ -97,16 +97,6 @@ void prop_tables(const qs_params& p, std::vector<float>& kx2, std::vector<float>
     k2max = km * km;
 }
 
-void twiddle_table(int n, std::vector<float2>& h) {
-    h.resize(n);
-    for (int k = 0; k < n; ++k) {
-        double turns = (double)k / (double)n;
-        if (turns > 0.5) turns -= 1.0;
-        const double ang = -2.0 * qs::kPi * turns;
-        h[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
-    }
-}
-
 }  // namespace
 
 using namespace qs;
@@ -222,8 +212,8 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
     float2* waves = (float2*)cv.take(sizeof(float2) * N * npos);
 
     std::vector<float2> twy, twx;
-    twiddle_table(ny, twy);
-    twiddle_table(nx, twx);
+    QS_TRY(twiddle_host(ny, twy));
+    QS_TRY(twiddle_host(nx, twx));
     // the host vectors are consumed by the copies before these pageable-memory
     // cudaMemcpyAsync calls return
     QS_CUDA_TRY(cudaMemcpyAsync(d_tw_y, twy.data(), sizeof(float2) * ny, cudaMemcpyHostToDevice, s));
