@@ -195,6 +195,34 @@ int qs_multislice_run(qs_ctx *ctx, const qs_params *p, const float *trans, const
 int qs_stem_run(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom,
                 const qs_batch *batch, float *det_images, float *diffpats);
 
+/* ------------------------------------------------------------ gradients */
+/* initSTEMSlices' phase grating for a given potential stack V
+ * (stem3/stemlib.cpp:2280-2299): trans = exp(i*lambda*gamma*V), V a device
+ * slices x potNx x potNy float array, trans a device c64 array (no band limit). */
+int qs_phase_grating(qs_ctx *ctx, const qs_params *p, const float *V, float *trans, unsigned flags);
+
+/* Differentiable 4D-STEM.  The reference has no adjoint; the forward model is
+ * its runMulsSTEM (stem3/stemlib.cpp:2375-2534) for the positions of `batch`.
+ * Loss L = sum_p sum_k (I_p(k) - target_p(k))^2, I_p the diffraction pattern
+ * after the last slice (fftshifted |psi(k)|^2/sqrt(nx*ny), the layout of
+ * qs_multislice_run's diffpats).  Writes L (host double, may be NULL),
+ * dL/dV for every slice of the potential (device float,
+ * slices x potNx x potNy, through t = exp(i*lambda*gamma*V)) and optionally
+ * the forward patterns (device, [npos][nx][ny]).  Forward waves are kept every
+ * `ckpt` slices and recomputed in between (1 = keep all).  All arrays are
+ * device pointers; trans must not be band-limited. */
+int qs_adjoint_run(qs_ctx *ctx, const qs_params *p, const float *trans, const float *probe,
+                   const qs_batch *batch, const float *target, int ckpt, double *loss, float *dL_dV,
+                   float *diffpats, unsigned flags);
+
+/* dL/dx and dL/dy of every atom (grad_xy: host, natom x 2 doubles) from
+ * dL/dV (device): the adjoint of make3DSlices' scatter-sum
+ * (stem3/stemlib.cpp:894-1213) through its radial linear interpolation.
+ * Atoms that contribute to no slice get zero; z gradients are not returned
+ * (the LUT is nearest-neighbour in z, stem3/stemlib.cpp:76). */
+int qs_atoms_grad(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom, const float *dL_dV,
+                  double *grad_xy, unsigned flags);
+
 /* ------------------------------------------------------------ profiling */
 /* Per-context counters for measurement: kernel launches of this library and,
  * while profiling is enabled, CUDA-event times of the row and column passes

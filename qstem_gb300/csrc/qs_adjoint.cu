@@ -1,0 +1,340 @@
+// qs_adjoint.cu -- the adjoint of the multislice scan (differentiable 4D-STEM)
+// and of the slice builder's scatter-sum.
+//
+// Loss  L = sum_p sum_k (I_p(k) - T_p(k))^2 with I_p the diffraction pattern
+// of position p after the last slice (|psi(k)|^2/sqrt(nx*ny), the reference's
+// wave->diffpat, stem3/stemlib.cpp:2630) and T_p a target pattern.
+//
+// Gradients use the conjugate convention g_z = dL/d(conj z), so that
+// dL = 2 Re sum conj(g_z) dz.  Per slice the forward step
+//   psi = IFFT_y(h)/N;  phi = psi * t;  A = FFT_y(phi)      (row pass)
+//   B' = P * FFT_x(A);  h' = IFFT_x(B')                      (column pass)
+// has the adjoint
+//   g_A = IFFT_x(conj(P) * FFT_x(g_h'))                      (column pass, conj P)
+//   g_phi = IFFT_y(g_A);  g_t = conj(psi) g_phi;  g_psi = conj(t) g_phi;
+//   g_h = FFT_y(g_psi)/N                                      (row adjoint)
+//   dL/dV = -2 sigma Im(conj(sum_p g_t,p) t)                  (window gather)
+// with t = exp(i sigma V), sigma = lambda*gamma (initSTEMSlices,
+// stem3/stemlib.cpp:2290-2299).  The last slice seeds g_B' = 2(I - T) c B'.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "qs_fft.cuh"
+#include "qs_internal.h"
+
+namespace qs {
+
+constexpr int ADJ_ROW_LINES = 8;
+
+// ---------------------------------------------- last slice: loss and seed
+// One block per (wave, column tile), all tiles of the grid: forward FFT_x
+// and propagator of the last slice, loss terms, g_B' = 2 (I - T) c B',
+// g_A = IFFT_x(conj(P) g_B').
+template <int N>
+__global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
+    adj_last_cols(AdjLastArgs a) {
+    using Cfg = typename Line<N>::cfg;
+    constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();
+    constexpr int NT = C * T;
+    constexpr int NWARPS = (NT + 31) / 32;
+    extern __shared__ float2 dsm[];
+    float2* s_tw = dsm;
+    float2* s_tile = dsm + N;
+    __shared__ double s_loss[NWARPS];
+    const int tid = threadIdx.x + C * threadIdx.y;
+    for (int i = tid; i < Cfg::TW; i += NT) s_tw[i] = a.tw[i];
+    __syncthreads();
+    const int c = threadIdx.x, t = threadIdx.y;
+    const int ntiles = a.ny / C;
+    const int tile = blockIdx.x % ntiles;
+    const int b = blockIdx.x / ntiles;
+    const int ky = tile * C + c;
+    float2* col = a.waves + (size_t)b * a.nx * a.ny + ky;
+    const bool inband = (ky <= a.yA || ky >= a.yB);
+    float2 reg[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) reg[e] = inband ? col[(size_t)(t + T * e) * a.ny] : make_float2(0.f, 0.f);
+    const SmemCol<C> sm{s_tile, c};
+    line_fft<Cfg, false, true>(reg, sm, s_tw, t);
+    const float ky2 = a.ky2[ky];
+    const float2 pyv = a.py[ky];
+    const float* tgt = a.target + (size_t)b * a.nx * a.ny + (ky + a.ny / 2) % a.ny;
+    float* dp = a.diffpat ? a.diffpat + (size_t)b * a.nx * a.ny + (ky + a.ny / 2) % a.ny : nullptr;
+    double loss = 0.0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int kx = t + T * e;
+        const float kx2 = a.kx2[kx];
+        const float2 pxv = a.px[kx];
+        const bool pass = inband && kx2 < a.k2max && (kx2 + ky2) < a.k2max;
+        const float2 Bp = pass ? cmul(cmul(reg[e], pyv), pxv) : make_float2(0.f, 0.f);
+        const double I = (double)(Bp.x * Bp.x + Bp.y * Bp.y) * a.scaleDiff;
+        const size_t ik = (size_t)((kx + a.nx / 2) % a.nx) * a.ny;
+        const double dI = I - (double)tgt[ik];
+        loss += dI * dI;
+        if (dp) dp[ik] = (float)I;
+        // g_B' = 2 dI c B', then g_B = conj(P) g_B'
+        const float g = (float)(2.0 * dI * a.scaleDiff);
+        const float2 gBp = make_float2(g * Bp.x, g * Bp.y);
+        reg[e] = pass ? cmulc(cmulc(gBp, pyv), pxv) : make_float2(0.f, 0.f);
+    }
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+    if (lane == 0) s_loss[warp] = loss;
+    line_fft<Cfg, true, true>(reg, sm, s_tw, t);
+#pragma unroll
+    for (int e = 0; e < E; ++e) col[(size_t)(t + T * e) * a.ny] = reg[e];
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0.0;
+        for (int w = 0; w < NWARPS; ++w) s += s_loss[w];
+        a.loss_partial[blockIdx.x] = s;
+    }
+}
+
+// ------------------------------------------------------------ row adjoint
+template <int N, bool FIRST>
+__global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES)
+    adj_rows(AdjRowArgs a) {
+    using Cfg = typename Line<N>::cfg;
+    constexpr int T = Cfg::T, E = Cfg::E;
+    extern __shared__ float2 dsm[];
+    float2* s_tw = dsm;
+    float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
+    const int tid = threadIdx.x + T * threadIdx.y;
+    for (int i = tid; i < Cfg::TW; i += T * ADJ_ROW_LINES) s_tw[i] = a.tw[i];
+    __syncthreads();
+    const int t = threadIdx.x;
+    const long line = (long)blockIdx.x * ADJ_ROW_LINES + threadIdx.y;
+    const int b = (int)(line / a.nx);
+    const int x = (int)(line - (long)b * a.nx);
+    const SmemRow<Cfg::R0> sm{s_line};
+    // g_phi = IFFT_y(g_A)
+    float2* grow = a.grad + ((size_t)b * a.nx + x) * N;
+    float2 g[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int y = t + T * e;
+        g[e] = (y <= a.yA || y >= a.yB) ? grow[y] : make_float2(0.f, 0.f);
+    }
+    line_fft<Cfg, true>(g, sm, s_tw, t);
+    // psi of this slice: the probe, or IFFT_y(h)/N of the stored state
+    float2 psi[E];
+    if constexpr (FIRST) {
+        const float2* src = a.probe + (size_t)x * N;
+#pragma unroll
+        for (int e = 0; e < E; ++e) psi[e] = __ldg(src + t + T * e);
+    } else {
+        const float2* src = a.state + ((size_t)b * a.nx + x) * N;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int y = t + T * e;
+            psi[e] = (y <= a.yA || y >= a.yB) ? src[y] : make_float2(0.f, 0.f);
+        }
+        line_fft<Cfg, true>(psi, sm, s_tw, t);
+#pragma unroll
+        for (int e = 0; e < E; ++e) psi[e] = cscale(psi[e], a.norm);
+    }
+    const float2* tr = a.trans_slice + (size_t)(x + __ldg(a.posX + b)) * a.potNy + __ldg(a.posY + b);
+    float2* gt = a.grad_t + ((size_t)b * a.nx + x) * N;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const float2 tv = __ldg(tr + t + T * e);
+        gt[t + T * e] = cmulc(g[e], psi[e]);  // conj(psi) g_phi
+        g[e] = cmulc(g[e], tv);               // conj(t) g_phi
+    }
+    if constexpr (!FIRST) {
+        line_fft<Cfg, false>(g, sm, s_tw, t);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int y = t + T * e;
+            if (y <= a.yA || y >= a.yB) grow[y] = cscale(g[e], a.norm);
+        }
+    }
+}
+
+// dL/dV of one slice: sum the windows of all positions, then
+// -2 sigma Im(conj(G) t).  One thread per potential pixel; positions loop.
+__global__ void adj_dv_gather(const float2* __restrict__ grad_t, int npos, int nx, int ny, int potNx, int potNy,
+                              const int* __restrict__ posX, const int* __restrict__ posY,
+                              const float2* __restrict__ trans_slice, double sigma, float* __restrict__ dV) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int X = blockIdx.y;
+    if (i >= potNy) return;
+    const int Y = i;
+    double gr = 0.0, gi = 0.0;
+    for (int p = 0; p < npos; ++p) {
+        const int lx = X - __ldg(posX + p), ly = Y - __ldg(posY + p);
+        if (lx >= 0 && lx < nx && ly >= 0 && ly < ny) {
+            const float2 v = grad_t[((size_t)p * nx + lx) * ny + ly];
+            gr += v.x;
+            gi += v.y;
+        }
+    }
+    const float2 tv = trans_slice[(size_t)X * potNy + Y];
+    // Im(conj(G) t) = gr*t.y - gi*t.x
+    dV[(size_t)X * potNy + Y] = (float)(-2.0 * sigma * (gr * tv.y - gi * tv.x));
+}
+
+// ---------------------------------------------- scatter-sum adjoint (atoms)
+// dL/d(atomX, atomY) = sum over the atom's pixels and slices of
+// dL/dV * dV/dr * dr/d(atom), dV/dr the slope of the radial linear
+// interpolation (stem3/stemlib.cpp:957-1019), dr/datomX = -(x_pixel - atomX)/r.
+__global__ void atoms_grad(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts, int Nz, int Nr,
+                           int nzSub, float dx, float dy, double dr, float dzs, int potNx, int potNy, int periodic,
+                           const float* __restrict__ dV, double* __restrict__ grad) {
+    const AtomJob J = jobs[blockIdx.x];
+    const float* lut = luts[J.lut];
+    const float* lutq = J.lutq >= 0 ? luts[J.lutq] : nullptr;
+    const int w = J.iay1 - J.iay0 + 1;
+    const int npx = (J.iax1 - J.iax0 + 1) * w;
+    const size_t sliceStep = (size_t)potNx * potNy;
+    const int limHi = Nr * (Nz - 1), limLo = -Nr * (Nz - 1), step = nzSub * Nr;
+    const double dOffsZ = (double)(((float)(J.iAtomZ + J.iaz0) - J.atomZ / dzs) * (float)nzSub);
+    const int iOffsZ0 = ((int)(dOffsZ + 0.5)) * Nr;
+    double gx = 0.0, gy = 0.0;
+    for (int k = threadIdx.x; k < npx; k += blockDim.x) {
+        const int iax = J.iax0 + k / w;
+        const int iay = J.iay0 + k % w;
+        // the reference's float offsets, rounded step by step (no FMA
+        // contraction: an atom on a pixel must give r == 0 exactly)
+        const double ddx = (double)__fsub_rn(__fmul_rn((float)iax, dx), J.atomX);
+        const double ddy = (double)__fsub_rn(__fmul_rn((float)iay, dy), J.atomY);
+        const double r = sqrt(ddx * ddx + ddy * ddy);
+        const double rr = r / dr;
+        const int ir = (int)floor(rr);
+        if (ir >= Nr - 1 || r <= 0.0) continue;
+        const int cx = periodic ? ((iax % potNx) + potNx) % potNx : iax;
+        const int cy = periodic ? ((iay % potNy) + potNy) % potNy : iay;
+        const float* g = dV + (size_t)(J.iAtomZ + J.iaz0) * sliceStep + (size_t)cx * potNy + cy;
+        int iOffsZ = iOffsZ0;
+        double dLdr = 0.0;
+        for (int iaz = J.iaz0; iaz <= J.iaz1; iaz++) {
+            int row = -1;
+            if (iOffsZ < 0) {
+                if (iOffsZ > limLo) row = -iOffsZ + Nr;
+            } else if (iOffsZ < limHi) {
+                row = iOffsZ;
+            }
+            if (row >= 0) {
+                double slope = (double)lut[row + ir + 1] - (double)lut[row + ir];
+                if (lutq) slope += J.q * ((double)lutq[row + ir + 1] - (double)lutq[row + ir]);
+                dLdr += (double)*g * slope / dr;
+            }
+            g += sliceStep;
+            iOffsZ += step;
+        }
+        gx += dLdr * (-ddx / r);
+        gy += dLdr * (-ddy / r);
+    }
+    __shared__ double sx[256], sy[256];
+    sx[threadIdx.x] = gx;
+    sy[threadIdx.x] = gy;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sx[threadIdx.x] += sx[threadIdx.x + o];
+            sy[threadIdx.x] += sy[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        grad[2 * (size_t)J.index] = sx[0];
+        grad[2 * (size_t)J.index + 1] = sy[0];
+    }
+}
+
+// --------------------------------------------------------------- launchers
+template <int N>
+static int last_n(const AdjLastArgs& a, cudaStream_t s) {
+    using Cfg = typename Line<N>::cfg;
+    constexpr int C = col_tile<N>();
+    static bool attr = false;
+    const size_t sm = sizeof(float2) * (N + (size_t)N * C);
+    if (!attr) {
+        QS_CUDA_TRY(cudaFuncSetAttribute(adj_last_cols<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr = true;
+    }
+    const long nblk = (long)a.nwaves * (a.ny / C);
+    adj_last_cols<N><<<(unsigned)nblk, dim3(C, Cfg::T), sm, s>>>(a);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+int launch_adj_last(const AdjLastArgs& a, cudaStream_t s) {
+    switch (a.nx) {
+        case 64: return last_n<64>(a, s);
+        case 128: return last_n<128>(a, s);
+        case 256: return last_n<256>(a, s);
+        case 384: return last_n<384>(a, s);
+        case 512: return last_n<512>(a, s);
+        case 768: return last_n<768>(a, s);
+        case 1024: return last_n<1024>(a, s);
+    }
+    set_error("adjoint: unsupported nx");
+    return QS_ERR_UNSUPPORTED;
+}
+
+template <int N, bool FIRST>
+static int adj_rows_n(const AdjRowArgs& a, cudaStream_t s) {
+    using Cfg = typename Line<N>::cfg;
+    static bool attr = false;
+    const size_t sm = sizeof(float2) * (N + ADJ_ROW_LINES * Cfg::SMEM);
+    if (!attr) {
+        QS_CUDA_TRY(cudaFuncSetAttribute(adj_rows<N, FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr = true;
+    }
+    const long lines = (long)a.nwaves * a.nx;
+    adj_rows<N, FIRST><<<(unsigned)(lines / ADJ_ROW_LINES), dim3(Cfg::T, ADJ_ROW_LINES), sm, s>>>(a);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+template <bool FIRST>
+static int adj_rows_any(const AdjRowArgs& a, cudaStream_t s) {
+    switch (a.ny) {
+        case 64: return adj_rows_n<64, FIRST>(a, s);
+        case 128: return adj_rows_n<128, FIRST>(a, s);
+        case 256: return adj_rows_n<256, FIRST>(a, s);
+        case 384: return adj_rows_n<384, FIRST>(a, s);
+        case 512: return adj_rows_n<512, FIRST>(a, s);
+        case 768: return adj_rows_n<768, FIRST>(a, s);
+        case 1024: return adj_rows_n<1024, FIRST>(a, s);
+    }
+    set_error("adjoint: unsupported ny");
+    return QS_ERR_UNSUPPORTED;
+}
+
+int launch_adj_rows(const AdjRowArgs& a, bool first, cudaStream_t s) {
+    return first ? adj_rows_any<true>(a, s) : adj_rows_any<false>(a, s);
+}
+
+int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, int potNy, const int* posX,
+                     const int* posY, const float2* trans_slice, double sigma, float* dV, cudaStream_t s) {
+    dim3 block(256);
+    dim3 grid((potNy + 255) / 256, potNx);
+    adj_dv_gather<<<grid, block, 0, s>>>(grad_t, npos, nx, ny, potNx, potNy, posX, posY, trans_slice, sigma, dV);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+int launch_atoms_grad(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
+                      const qs_params& p, const float* dV, double* grad, cudaStream_t s) {
+    if (njobs <= 0) return QS_OK;
+    const double dr = p.resolutionX / 2;
+    atoms_grad<<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr,
+                                     p.sliceThickness, p.potNx, p.potNy, p.nonPeriod ? 0 : 1, dV, grad);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+}  // namespace qs

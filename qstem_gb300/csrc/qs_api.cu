@@ -8,6 +8,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "qs_fft.cuh"
@@ -17,8 +18,8 @@ struct qs_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     // reusable device buffers, grown on demand
-    void* buf[16] = {};
-    size_t cap[16] = {};
+    void* buf[17] = {};
+    size_t cap[17] = {};
     // profiling
     bool profile = false;
     long long launch_base = 0;
@@ -26,6 +27,16 @@ struct qs_ctx {
     size_t pool_used = 0;
     std::vector<std::pair<size_t, size_t>> row_ev, col_ev;  // indices into pool
     double row_bytes = 0, col_bytes = 0;
+    // projected-potential tables built so far, keyed by everything they depend on
+    struct LutKey {
+        int Z, charged;
+        double B;
+        float rx, ry, dz, R;
+        bool operator<(const LutKey& o) const {
+            return std::tie(Z, charged, B, rx, ry, dz, R) < std::tie(o.Z, o.charged, o.B, o.rx, o.ry, o.dz, o.R);
+        }
+    };
+    std::map<LutKey, float*> luts;
 };
 
 namespace qs {
@@ -48,7 +59,7 @@ static int ev_record(qs_ctx* c, size_t* idx) {
 
 enum Buf {
     B_WAVES, B_PROBE, B_PARTIAL, B_POS, B_TABLES, B_TILES, B_TRANS, B_OUT1, B_OUT2, B_OUT3, B_JOBS, B_LUTS,
-    B_LUTPTR, B_SUM, B_DIFF_IN
+    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, NBUF
 };
 
 static int ensure(qs_ctx* c, int which, size_t bytes, void** out) {
@@ -124,6 +135,127 @@ static PropTables prop_tables(const qs_params& p) {
 
 static int thickness_count(const qs_params& p) { return (p.slices * p.cellDiv) / p.outputInterval + 1; }
 
+// The control flow of make3DSlices' atom loop (stem3/stemlib.cpp:678-1213)
+// reduced to one job per contributing atom: atoms sorted by z (stable), the
+// vacancy skip, the non-periodic z cut-offs, the pixel box and the slice
+// range.  lutKeys lists (Z*2 + charged, B) in first-use order; B is the
+// Debye-Waller factor of the element's first contributing atom, as the
+// reference's per-element LUT cache keeps it (:1417).
+static void plan_atoms(const qs_params& P, const qs_atom* atoms, int natom, std::vector<AtomJob>& jobs,
+                       std::vector<std::pair<int, double>>& lutKeys) {
+    std::vector<int> order(natom);
+    for (int i = 0; i < natom; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return atoms[a].z < atoms[b].z; });
+    std::vector<qs_atom> at(natom);
+    for (int i = 0; i < natom; i++) at[i] = atoms[order[i]];
+    const float cz = P.sliceThickness * (float)P.slices;
+    const float dx = P.resolutionX, dy = P.resolutionY, dzs = P.sliceThickness;
+    const int iRadX = (int)ceilf(P.atomRadius / dx), iRadY = (int)ceilf(P.atomRadius / dy);
+    const int iRadZ = (int)ceilf(P.atomRadius / dzs);
+    jobs.clear();
+    lutKeys.clear();
+    std::map<int, int> lutIndex;          // key Z*2+charged -> index
+    auto atomz = [&](int i) {
+        float z = (float)((double)(at[i].z - cz * 0.0f + P.czOffset) - 0.5 * P.sliceThickness * (1 - P.centerSlices));
+        z -= P.sliceThickness;
+        return z;
+    };
+    for (int ia = 0; ia < natom; ia++) {
+        while (ia < natom && at[ia].Znum == 0) ia++;
+        if (ia >= natom) break;
+        float atomZ = atomz(ia);
+        if (P.nonPeriodZ) {
+            if (atomZ - P.atomRadius > cz) break;
+            do {
+                if (atomZ + P.atomRadius + P.sliceThickness >= 0) break;
+                ++ia;
+                atomZ = atomz(ia);
+            } while (ia < natom - 1);
+        }
+        const float atomX = at[ia].x - P.potOffsetX, atomY = at[ia].y - P.potOffsetY;
+        const int iAtomX = (int)floorf(atomX / dx), iAtomY = (int)floorf(atomY / dy);
+        atomZ += P.sliceThickness;
+        const int iAtomZ = (int)floor(atomZ / dzs + 0.5);
+        AtomJob J;
+        if (P.nonPeriod) {
+            J.iax0 = std::max(iAtomX - iRadX, 0);
+            J.iax1 = std::min(iAtomX + iRadX, P.potNx - 1);
+            J.iay0 = std::max(iAtomY - iRadY, 0);
+            J.iay1 = std::min(iAtomY + iRadY, P.potNy - 1);
+            if (!((J.iax0 < P.potNx) && (J.iax1 >= 0) && (J.iay0 < P.potNy) && (J.iay1 >= 0))) continue;
+        } else {
+            J.iax0 = iAtomX - iRadX;
+            J.iax1 = iAtomX + iRadX - 1;
+            J.iay0 = iAtomY - iRadY;
+            J.iay1 = iAtomY + iRadY - 1;
+        }
+        J.iaz0 = iAtomZ - iRadZ < 0 ? -iAtomZ : -iRadZ;
+        J.iaz1 = iAtomZ + iRadZ >= P.slices ? P.slices - iAtomZ - 1 : iRadZ;
+        if (!((iAtomZ + J.iaz0 < P.slices) && (iAtomZ + J.iaz1 >= 0))) continue;
+        const int Z = at[ia].Znum;
+        if (Z < 1 || Z >= 93) continue;
+        if (J.iax1 < J.iax0 || J.iay1 < J.iay0 || J.iaz1 < J.iaz0) continue;
+        const double B = P.tds ? 0.0 : at[ia].dw;
+        for (int charged = 0; charged < 2; charged++) {
+            if (charged && at[ia].q == 0) break;
+            const int key = Z * 2 + charged;
+            if (!lutIndex.count(key)) {
+                lutIndex[key] = (int)lutKeys.size();
+                lutKeys.push_back({key, B});
+            }
+        }
+        J.index = order[ia];
+        J.atomX = atomX;
+        J.atomY = atomY;
+        J.atomZ = atomZ;
+        J.q = at[ia].q;
+        J.iAtomZ = iAtomZ;
+        J.lut = lutIndex[Z * 2];
+        J.lutq = at[ia].q != 0 ? lutIndex[Z * 2 + 1] : -1;
+        jobs.push_back(J);
+    }
+
+}
+
+// Device LUT pointers for lutKeys, built on first use and kept by the context.
+static int prepare_luts(qs_ctx* c, const qs_params& P, const std::vector<std::pair<int, double>>& lutKeys,
+                        const float* const** d_ptrs, int* Nz, int* Nr, int* nzSub) {
+    QS_TRY(build_lut(P, 1, 0.0, 0, nullptr, Nz, Nr, nzSub, c->stream));
+    const size_t lutElems = (size_t)(*Nz) * (*Nr);
+    void* dp = nullptr;
+    QS_TRY(ensure(c, B_LUTPTR, sizeof(float*) * std::max<size_t>(lutKeys.size(), 1), &dp));
+    std::vector<const float*> ptrs(lutKeys.size());
+    for (size_t k = 0; k < lutKeys.size(); k++) {
+        // tables depend only on the element, charge flag, B and the sampling;
+        // the context keeps them across calls (frozen-phonon runs reuse them)
+        const qs_ctx::LutKey key{lutKeys[k].first / 2, lutKeys[k].first % 2, lutKeys[k].second,
+                                 P.resolutionX, P.resolutionY, P.sliceThickness, P.atomRadius};
+        auto it = c->luts.find(key);
+        if (it == c->luts.end()) {
+            float* d = nullptr;
+            cudaError_t e = cudaMalloc(&d, sizeof(float) * lutElems);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                set_error(std::string("LUT allocation failed: ") + cudaGetErrorString(e));
+                return QS_ERR_NOMEM;
+            }
+            const int rc = build_lut(P, key.Z, key.B, key.charged, d, nullptr, nullptr, nullptr, c->stream);
+            if (rc != QS_OK) {
+                cudaStreamSynchronize(c->stream);
+                cudaFree(d);
+                return rc;
+            }
+            it = c->luts.emplace(key, d).first;
+        }
+        ptrs[k] = it->second;
+    }
+    if (!ptrs.empty())
+        QS_CUDA_TRY(cudaMemcpyAsync(dp, ptrs.data(), sizeof(float*) * ptrs.size(), cudaMemcpyHostToDevice, c->stream));
+    QS_CUDA_TRY(cudaStreamSynchronize(c->stream));  // the host vector must outlive the copy
+    *d_ptrs = (const float* const*)dp;
+    return QS_OK;
+}
+
 }  // namespace qs
 
 using namespace qs;
@@ -158,7 +290,8 @@ int qs_ctx_destroy(qs_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
-    for (int i = 0; i < 16; i++)
+    for (auto& kv : c->luts) cudaFree(kv.second);
+    for (int i = 0; i < 17; i++)
         if (c->buf[i]) cudaFree(c->buf[i]);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -267,97 +400,20 @@ int qs_slices_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int nat
     }
     QS_CUDA_TRY(cudaMemsetAsync(trans, 0, sizeof(float2) * nTrans, c->stream));
 
-    // ---- host plan: the control flow of make3DSlices' atom loop
-    // (stem3/stemlib.cpp:678-1213) reduced to one job per contributing atom
-    std::vector<qs_atom> at(atoms, atoms + natom);
-    std::stable_sort(at.begin(), at.end(), [](const qs_atom& a, const qs_atom& b) { return a.z < b.z; });
-    const float cz = P.sliceThickness * (float)P.slices;
-    const float dx = P.resolutionX, dy = P.resolutionY, dzs = P.sliceThickness;
-    const int iRadX = (int)ceilf(P.atomRadius / dx), iRadY = (int)ceilf(P.atomRadius / dy);
-    const int iRadZ = (int)ceilf(P.atomRadius / dzs);
     std::vector<AtomJob> jobs;
-    std::map<int, int> lutIndex;          // key Z*2+charged -> index
-    std::vector<std::pair<int, double>> lutKeys;  // (key, B)
-    auto atomz = [&](int i) {
-        float z = (float)((double)(at[i].z - cz * 0.0f + P.czOffset) - 0.5 * P.sliceThickness * (1 - P.centerSlices));
-        z -= P.sliceThickness;
-        return z;
-    };
-    for (int ia = 0; ia < natom; ia++) {
-        while (ia < natom && at[ia].Znum == 0) ia++;
-        if (ia >= natom) break;
-        float atomZ = atomz(ia);
-        if (P.nonPeriodZ) {
-            if (atomZ - P.atomRadius > cz) break;
-            do {
-                if (atomZ + P.atomRadius + P.sliceThickness >= 0) break;
-                ++ia;
-                atomZ = atomz(ia);
-            } while (ia < natom - 1);
-        }
-        const float atomX = at[ia].x - P.potOffsetX, atomY = at[ia].y - P.potOffsetY;
-        const int iAtomX = (int)floorf(atomX / dx), iAtomY = (int)floorf(atomY / dy);
-        atomZ += P.sliceThickness;
-        const int iAtomZ = (int)floor(atomZ / dzs + 0.5);
-        AtomJob J;
-        if (P.nonPeriod) {
-            J.iax0 = std::max(iAtomX - iRadX, 0);
-            J.iax1 = std::min(iAtomX + iRadX, P.potNx - 1);
-            J.iay0 = std::max(iAtomY - iRadY, 0);
-            J.iay1 = std::min(iAtomY + iRadY, P.potNy - 1);
-            if (!((J.iax0 < P.potNx) && (J.iax1 >= 0) && (J.iay0 < P.potNy) && (J.iay1 >= 0))) continue;
-        } else {
-            J.iax0 = iAtomX - iRadX;
-            J.iax1 = iAtomX + iRadX - 1;
-            J.iay0 = iAtomY - iRadY;
-            J.iay1 = iAtomY + iRadY - 1;
-        }
-        J.iaz0 = iAtomZ - iRadZ < 0 ? -iAtomZ : -iRadZ;
-        J.iaz1 = iAtomZ + iRadZ >= P.slices ? P.slices - iAtomZ - 1 : iRadZ;
-        if (!((iAtomZ + J.iaz0 < P.slices) && (iAtomZ + J.iaz1 >= 0))) continue;
-        const int Z = at[ia].Znum;
-        if (Z < 1 || Z >= 93) continue;
-        if (J.iax1 < J.iax0 || J.iay1 < J.iay0 || J.iaz1 < J.iaz0) continue;
-        const double B = P.tds ? 0.0 : at[ia].dw;
-        for (int charged = 0; charged < 2; charged++) {
-            if (charged && at[ia].q == 0) break;
-            const int key = Z * 2 + charged;
-            if (!lutIndex.count(key)) {
-                lutIndex[key] = (int)lutKeys.size();
-                lutKeys.push_back({key, B});
-            }
-        }
-        J.atomX = atomX;
-        J.atomY = atomY;
-        J.atomZ = atomZ;
-        J.q = at[ia].q;
-        J.iAtomZ = iAtomZ;
-        J.lut = lutIndex[Z * 2];
-        J.lutq = at[ia].q != 0 ? lutIndex[Z * 2 + 1] : -1;
-        jobs.push_back(J);
-    }
+    std::vector<std::pair<int, double>> lutKeys;
+    plan_atoms(P, atoms, natom, jobs, lutKeys);
 
     if (!jobs.empty()) {
         int Nz = 0, Nr = 0, ns = 0;
-        QS_TRY(build_lut(P, 1, 0.0, 0, nullptr, &Nz, &Nr, &ns, c->stream));
-        const size_t lutElems = (size_t)Nz * Nr;
-        void *dl = nullptr, *dp = nullptr, *dj = nullptr;
-        QS_TRY(ensure(c, B_LUTS, sizeof(float) * lutElems * lutKeys.size(), &dl));
-        QS_TRY(ensure(c, B_LUTPTR, sizeof(float*) * lutKeys.size(), &dp));
+        const float* const* d_luts = nullptr;
+        QS_TRY(prepare_luts(c, P, lutKeys, &d_luts, &Nz, &Nr, &ns));
+        void* dj = nullptr;
         QS_TRY(ensure(c, B_JOBS, sizeof(AtomJob) * jobs.size(), &dj));
-        std::vector<const float*> ptrs(lutKeys.size());
-        for (size_t k = 0; k < lutKeys.size(); k++) {
-            float* d = (float*)dl + k * lutElems;
-            ptrs[k] = d;
-            QS_TRY(build_lut(P, lutKeys[k].first / 2, lutKeys[k].second, lutKeys[k].first % 2, d, nullptr, nullptr,
-                             nullptr, c->stream));
-        }
-        QS_CUDA_TRY(cudaMemcpyAsync(dp, ptrs.data(), sizeof(float*) * ptrs.size(), cudaMemcpyHostToDevice, c->stream));
         QS_CUDA_TRY(cudaMemcpyAsync(dj, jobs.data(), sizeof(AtomJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream));
-        // the host vectors must outlive the async copies
+        // the host vector must outlive the async copy
         QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
-        QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), (const float* const*)dp, Nz, Nr, ns, P, trans,
-                              c->stream));
+        QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), d_luts, Nz, Nr, ns, P, trans, c->stream));
     }
 
     if (!(flags & QS_OUT_POTENTIAL)) {
@@ -719,6 +775,235 @@ int qs_stem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, 
     if (ddp)
         QS_CUDA_TRY(cudaMemcpyAsync(diffpats, ddp, sizeof(float) * N * batch->npos, cudaMemcpyDeviceToHost,
                                     c->stream));
+    QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return QS_OK;
+}
+
+int qs_phase_grating(qs_ctx* c, const qs_params* p, const float* V, float* trans, unsigned flags) {
+    if (!c || !V || !trans) { set_error("null argument"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    if (p->bandlimittrans) {
+        set_error("qs_phase_grating: use qs_slices_build for band-limited transmission functions");
+        return QS_ERR_UNSUPPORTED;
+    }
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    const size_t n = (size_t)p->slices * p->potNx * p->potNy;
+    const double mm0 = (double)(1.0f + p->v0 / 511.0f);
+    QS_TRY(launch_grating_from_real(V, (float2*)trans, n, mm0 * wavelength(p->v0), c->stream));
+    if (flags & QS_SYNC) QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return QS_OK;
+}
+
+int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const float* probe_in,
+                   const qs_batch* batch, const float* target, int ckpt, double* loss, float* dL_dV, float* diffpats,
+                   unsigned flags) {
+    if (!c || !trans_in || !probe_in || !batch || !target || !dL_dV) { set_error("null argument"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    const qs_params& P = *p;
+    if (!line_supported(P.nx) || !line_supported(P.ny)) {
+        set_error("adjoint: nx, ny must be in {64,128,256,384,512,768,1024}");
+        return QS_ERR_UNSUPPORTED;
+    }
+    if (P.bandlimittrans) {
+        set_error("adjoint: band-limited transmission functions are not supported");
+        return QS_ERR_UNSUPPORTED;
+    }
+    const int npos = batch->npos, S = P.slices, nx = P.nx, ny = P.ny;
+    if (npos < 1) { set_error("batch has no positions"); return QS_ERR_ARG; }
+    if (ckpt < 1) ckpt = 1;
+    if (ckpt > S) ckpt = S;
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const size_t N = (size_t)nx * ny;
+
+    std::vector<int> px(npos), py(npos);
+    for (int i = 0; i < npos; i++) {
+        if (batch->iPosX && batch->iPosY) {
+            px[i] = batch->iPosX[i];
+            py[i] = batch->iPosY[i];
+        } else {
+            const int ix = i / P.scanYN, iy = i % P.scanYN;
+            int x = (int)((float)ix * (P.scanXStop - P.scanXStart) / ((float)P.scanXN * P.resolutionX));
+            int y = (int)((float)iy * (P.scanYStop - P.scanYStart) / ((float)P.scanYN * P.resolutionY));
+            px[i] = std::min(x, P.potNx - nx);
+            py[i] = std::min(y, P.potNy - ny);
+        }
+        if (px[i] < 0 || py[i] < 0 || px[i] > P.potNx - nx || py[i] > P.potNy - ny) {
+            set_error("position " + std::to_string(i) + " puts the window outside the potential array");
+            return QS_ERR_ARG;
+        }
+    }
+    PropTables tb = prop_tables(P);
+    int yA = -1, yB = ny;
+    for (int iy = 0; iy <= ny / 2; iy++) if (tb.ky2[iy] < tb.k2max) yA = iy;
+    for (int iy = ny - 1; iy > ny / 2; iy--) if (tb.ky2[iy] < tb.k2max) yB = iy;
+    for (int iy = 0; iy < ny; iy++)
+        if ((tb.ky2[iy] < tb.k2max) != (iy <= yA || iy >= yB)) { yA = ny; yB = ny; break; }
+    const int C = col_tile_width(nx);
+    std::vector<int> tiles;
+    for (int c0 = 0; c0 < ny; c0 += C) {
+        bool any = false;
+        for (int k = c0; k < c0 + C; k++) any |= (k <= yA || k >= yB);
+        if (any) tiles.push_back(c0);
+    }
+    const int ntiles = (int)tiles.size();
+    std::vector<float2> pxc(tb.px), pyc(tb.py);
+    for (auto& v : pxc) v.y = -v.y;
+    for (auto& v : pyc) v.y = -v.y;
+
+    // device memory: tables | tiles | positions | loss partials | buffers
+    const int nseg = (S + ckpt - 1) / ckpt;
+    const size_t waveBytes = sizeof(float2) * N * npos;
+    const size_t nLoss = (size_t)npos * (ny / C);
+    auto rup = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t small = rup(sizeof(float) * (nx + ny)) + 2 * rup(sizeof(float2) * (nx + ny)) +
+                         rup(sizeof(int) * std::max(ntiles, 1)) + rup(sizeof(int) * 2 * npos) + rup(sizeof(double) * nLoss);
+    // work, grad, grad_t, checkpoints 1..nseg-1, segment states 1..ckpt-1
+    const size_t nbuf = 3 + (size_t)(nseg - 1) + (size_t)(ckpt - 1);
+    void* base = nullptr;
+    QS_TRY(ensure(c, B_ADJ, small + nbuf * rup(waveBytes), &base));
+    unsigned char* cur = (unsigned char*)base;
+    auto take = [&](size_t b) { void* q = cur; cur += rup(b); return q; };
+    float* d_kx2 = (float*)take(sizeof(float) * (nx + ny));
+    float* d_ky2 = d_kx2 + nx;
+    float2* d_px = (float2*)take(sizeof(float2) * (nx + ny));
+    float2* d_py = d_px + nx;
+    float2* d_pxc = (float2*)take(sizeof(float2) * (nx + ny));
+    float2* d_pyc = d_pxc + nx;
+    int* d_tiles = (int*)take(sizeof(int) * std::max(ntiles, 1));
+    int* d_pos = (int*)take(sizeof(int) * 2 * npos);
+    double* d_loss = (double*)take(sizeof(double) * nLoss);
+    float2* work = (float2*)take(waveBytes);
+    float2* grad = (float2*)take(waveBytes);
+    float2* grad_t = (float2*)take(waveBytes);
+    std::vector<float2*> ck(nseg, nullptr), seg(ckpt, nullptr);
+    for (int k = 1; k < nseg; k++) ck[k] = (float2*)take(waveBytes);
+    for (int k = 1; k < ckpt; k++) seg[k] = (float2*)take(waveBytes);
+
+    QS_CUDA_TRY(cudaMemcpyAsync(d_kx2, tb.kx2.data(), sizeof(float) * nx, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_ky2, tb.ky2.data(), sizeof(float) * ny, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_px, tb.px.data(), sizeof(float2) * nx, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_py, tb.py.data(), sizeof(float2) * ny, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_pxc, pxc.data(), sizeof(float2) * nx, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_pyc, pyc.data(), sizeof(float2) * ny, cudaMemcpyHostToDevice, s));
+    if (ntiles) QS_CUDA_TRY(cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_pos, px.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemcpyAsync(d_pos + npos, py.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
+    QS_CUDA_TRY(cudaMemsetAsync(work, 0, waveBytes, s));
+    QS_CUDA_TRY(cudaMemsetAsync(grad, 0, waveBytes, s));
+    const float2* tw_y = twiddles(ny);
+    const float2* tw_x = twiddles(nx);
+    if (!tw_y || !tw_x) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
+    const float2* trans = (const float2*)trans_in;
+    const float2* probe = (const float2*)probe_in;
+    const size_t sliceElems = (size_t)P.potNx * P.potNy;
+
+    RowArgs ra{};
+    ra.nx = nx; ra.ny = ny; ra.potNx = P.potNx; ra.potNy = P.potNy; ra.nwaves = npos; ra.probe = probe;
+    ra.posX = d_pos; ra.posY = d_pos + npos; ra.tw = tw_y; ra.yA = yA; ra.yB = yB;
+    ra.norm = (float)(1.0 / (double)N);
+    ColArgs ca{};
+    ca.nx = nx; ca.ny = ny; ca.nwaves = npos; ca.tw = tw_x; ca.kx2 = d_kx2; ca.ky2 = d_ky2;
+    ca.k2max = tb.k2max; ca.tiles = d_tiles; ca.ntiles = ntiles; ca.inverse = 1; ca.ndet = 0;
+    // Forward through slices [s0, upto) starting from h_{s0} in `buf`.  The
+    // full run (keepStates false) starts at slice 0, copies the checkpoint
+    // states h_{k*ckpt} and ends after the last row pass (the last column
+    // pass is the loss kernel).  A segment recompute (keepStates true) only
+    // needs the states h_s, s0 < s < upto, and stores them in `seg`.
+    auto forward = [&](float2* buf, int s0, int upto, bool keepStates) -> int {
+        ra.waves = buf;
+        ca.waves = buf;
+        ca.px = d_px;
+        ca.py = d_py;
+        const int last = keepStates ? upto - 1 : upto;
+        for (int sl = s0; sl < last; sl++) {
+            ra.trans_slice = trans + (size_t)sl * sliceElems;
+            QS_TRY(launch_rows(ra, sl == 0 ? ROW_FIRST : ROW_MID, s));
+            if (sl == S - 1) break;
+            QS_TRY(launch_cols(ca, s));
+            const int nxt = sl + 1;
+            if (keepStates)
+                QS_CUDA_TRY(cudaMemcpyAsync(seg[nxt - s0], buf, waveBytes, cudaMemcpyDeviceToDevice, s));
+            else if (nxt % ckpt == 0 && nxt < S)
+                QS_CUDA_TRY(cudaMemcpyAsync(ck[nxt / ckpt], buf, waveBytes, cudaMemcpyDeviceToDevice, s));
+        }
+        return QS_OK;
+    };
+    // 1. forward with checkpoints, ending with the state after the last row pass
+    QS_TRY(forward(work, 0, S, false));
+    // 2. loss and its gradient at the last slice: g_A of slice S-1 in `grad`
+    QS_CUDA_TRY(cudaMemcpyAsync(grad, work, waveBytes, cudaMemcpyDeviceToDevice, s));
+    AdjLastArgs la{};
+    la.nx = nx; la.ny = ny; la.nwaves = npos; la.yA = yA; la.yB = yB; la.waves = grad; la.tw = tw_x;
+    la.kx2 = d_kx2; la.ky2 = d_ky2; la.px = d_px; la.py = d_py; la.k2max = tb.k2max; la.target = target;
+    la.diffpat = diffpats; la.scaleDiff = 1.0 / std::sqrt((double)N); la.loss_partial = d_loss;
+    QS_TRY(launch_adj_last(la, s));
+    // 3. backward, segment by segment
+    const double sigma = (double)(1.0f + P.v0 / 511.0f) * wavelength(P.v0);
+    AdjRowArgs ar{};
+    ar.nx = nx; ar.ny = ny; ar.potNx = P.potNx; ar.potNy = P.potNy; ar.nwaves = npos; ar.yA = yA; ar.yB = yB;
+    ar.grad = grad; ar.probe = probe; ar.grad_t = grad_t; ar.posX = d_pos; ar.posY = d_pos + npos; ar.tw = tw_y;
+    ar.norm = (float)(1.0 / (double)N);
+    for (int sg = nseg - 1; sg >= 0; sg--) {
+        const int s0 = sg * ckpt, s1 = std::min(S, s0 + ckpt);
+        // recompute the segment's states h_s, s0 < s < s1
+        if (s1 - s0 > 1) {
+            if (s0 > 0) QS_CUDA_TRY(cudaMemcpyAsync(work, ck[sg], waveBytes, cudaMemcpyDeviceToDevice, s));
+            QS_TRY(forward(work, s0, s1, true));
+        }
+        for (int sl = s1 - 1; sl >= s0; sl--) {
+            if (sl < S - 1) {
+                // column pass with conj(P): g_h(sl+1) -> g_A(sl)
+                ca.waves = grad; ca.px = d_pxc; ca.py = d_pyc;
+                QS_TRY(launch_cols(ca, s));
+            }
+            ar.state = sl == s0 ? (s0 > 0 ? ck[sg] : nullptr) : seg[sl - s0];
+            ar.trans_slice = trans + (size_t)sl * sliceElems;
+            QS_TRY(launch_adj_rows(ar, sl == 0, s));
+            QS_TRY(launch_dv_gather(grad_t, npos, nx, ny, P.potNx, P.potNy, d_pos, d_pos + npos,
+                                    trans + (size_t)sl * sliceElems, sigma, dL_dV + (size_t)sl * sliceElems, s));
+        }
+    }
+    if (loss) {
+        std::vector<double> h(nLoss);
+        QS_CUDA_TRY(cudaMemcpyAsync(h.data(), d_loss, sizeof(double) * nLoss, cudaMemcpyDeviceToHost, s));
+        QS_CUDA_TRY(cudaStreamSynchronize(s));
+        double t = 0;
+        for (double v : h) t += v;
+        *loss = t;
+    } else if (flags & QS_SYNC) {
+        QS_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    return QS_OK;
+}
+
+int qs_atoms_grad(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, const float* dL_dV,
+                  double* grad_xy, unsigned flags) {
+    if (!c || !dL_dV || !grad_xy || (natom > 0 && !atoms)) { set_error("null argument"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    if (!p->fftpotential || !p->potential3D) {
+        set_error("only the 3-D FFT-integrated potential is supported");
+        return QS_ERR_UNSUPPORTED;
+    }
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    (void)flags;
+    std::vector<AtomJob> jobs;
+    std::vector<std::pair<int, double>> lutKeys;
+    plan_atoms(*p, atoms, natom, jobs, lutKeys);
+    void* dg = nullptr;
+    QS_TRY(ensure(c, B_OUT3, sizeof(double) * 2 * std::max(natom, 1), &dg));
+    QS_CUDA_TRY(cudaMemsetAsync(dg, 0, sizeof(double) * 2 * std::max(natom, 1), c->stream));
+    if (!jobs.empty()) {
+        int Nz = 0, Nr = 0, ns = 0;
+        const float* const* d_luts = nullptr;
+        QS_TRY(prepare_luts(c, *p, lutKeys, &d_luts, &Nz, &Nr, &ns));
+        void* dj = nullptr;
+        QS_TRY(ensure(c, B_JOBS, sizeof(AtomJob) * jobs.size(), &dj));
+        QS_CUDA_TRY(cudaMemcpyAsync(dj, jobs.data(), sizeof(AtomJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream));
+        QS_TRY(launch_atoms_grad((const AtomJob*)dj, (int)jobs.size(), d_luts, Nz, Nr, ns, *p, dL_dV, (double*)dg,
+                                 c->stream));
+    }
+    QS_CUDA_TRY(cudaMemcpyAsync(grad_xy, dg, sizeof(double) * 2 * natom, cudaMemcpyDeviceToHost, c->stream));
     QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return QS_OK;
 }

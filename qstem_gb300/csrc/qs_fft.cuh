@@ -328,6 +328,12 @@ template <> struct Line<512> { using cfg = LineCfg<512, 16, radices<32, 16>>; };
 template <> struct Line<768> { using cfg = LineCfg<768, 32, radices<8, 12, 8>>; };
 template <> struct Line<1024> { using cfg = LineCfg<1024, 32, radices<32, 32>>; };
 
+// columns per column-pass tile (128-byte row segments; 64 bytes from 768 up)
+template <int N>
+constexpr int col_tile() {
+    return N >= 768 ? 8 : 16;
+}
+
 template <int N>
 constexpr bool line_threads_match() {
     return Line<N>::cfg::T == line_threads(N);

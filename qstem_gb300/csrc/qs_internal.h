@@ -93,6 +93,7 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
               int* nzSub, cudaStream_t s);
 
 struct AtomJob {
+    int index;                   // the atom's position in the caller's array
     float atomX, atomY, atomZ;   // atomZ after the reference's offsets
     float q;
     int iax0, iax1, iay0, iay1;  // inclusive pixel box (unwrapped coordinates)
@@ -111,6 +112,38 @@ int launch_probe_kspace(const qs_params& p, double dx, double dy, float2* wave, 
 int launch_probe_realspace(const qs_params& p, double dx, double dy, float2* wave, double* d_sum,
                            cudaStream_t s);
 int launch_scale_by_sum(float2* wave, size_t n, const double* d_sum, double nxy, cudaStream_t s);
+
+// ----------------------------------------------------------------- adjoint
+struct AdjLastArgs {
+    int nx, ny, nwaves, yA, yB;
+    float2* waves;               // in: state after the last row pass; out: g_A
+    const float2* tw;            // twiddles of the length-nx transform
+    const float *kx2, *ky2;
+    const float2 *px, *py;       // forward propagator factors
+    float k2max;
+    const float* target;         // [nwaves][nx][ny], fftshifted like diffpat
+    float* diffpat;              // optional forward patterns
+    double scaleDiff;            // 1/sqrt(nx*ny)
+    double* loss_partial;        // [nwaves * ny/C]
+};
+struct AdjRowArgs {
+    int nx, ny, potNx, potNy, nwaves, yA, yB;
+    float2* grad;                // in: g_A, out: g_h (band-limited columns)
+    const float2* state;         // h of this slice (not read for the first slice)
+    const float2* probe;         // first slice
+    const float2* trans_slice;
+    float2* grad_t;              // out: conj(psi) g_phi, [nwaves][nx][ny]
+    const int *posX, *posY;
+    const float2* tw;            // twiddles of the length-ny transform
+    float norm;
+};
+int launch_adj_last(const AdjLastArgs& a, cudaStream_t s);
+int launch_adj_rows(const AdjRowArgs& a, bool first, cudaStream_t s);
+int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, int potNy, const int* posX,
+                     const int* posY, const float2* trans_slice, double sigma, float* dV, cudaStream_t s);
+int launch_atoms_grad(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
+                      const qs_params& p, const float* dV, double* grad, cudaStream_t s);
+int launch_grating_from_real(const float* V, float2* trans, size_t n, double scale, cudaStream_t s);
 
 // collectIntensity for one k-space wave (compat entry point)
 int launch_collect(const qs_params& p, const float2* wave_k, const float* kx2, const float* ky2,

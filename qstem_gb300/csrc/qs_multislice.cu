@@ -83,11 +83,6 @@ __global__ void __launch_bounds__(line_threads(N) * ROW_LINES, row_min_blocks(N)
     }
 }
 
-template <int N>
-constexpr int col_tile() {
-    return N >= 768 ? 8 : 16;
-}
-
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");

@@ -269,9 +269,11 @@ __global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* con
     for (int k = threadIdx.x; k < npx; k += blockDim.x) {
         const int iax = J.iax0 + k / w;
         const int iay = J.iay0 + k % w;
-        double x2 = (double)((float)iax * dx - J.atomX);
+        // x2 = iax*dx - atomX in float as the reference forms it
+        // (stem3/stemlib.cpp:931-938), rounded step by step (no FMA)
+        double x2 = (double)__fsub_rn(__fmul_rn((float)iax, dx), J.atomX);
         x2 *= x2;
-        double y2 = (double)((float)iay * dy - J.atomY);
+        double y2 = (double)__fsub_rn(__fmul_rn((float)iay, dy), J.atomY);
         y2 *= y2;
         const double r = sqrt(x2 + y2);
         double ddr = r / dr;
@@ -327,6 +329,25 @@ int launch_phase_grating(float2* trans, size_t n, double scale, cudaStream_t s) 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     phase_grating<<<sms * 8, 256, 0, s>>>(trans, n, scale);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+__global__ void grating_from_real(const float* __restrict__ V, float2* __restrict__ t, size_t n, double scale) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double sn, cs;
+        sincos((double)V[i] * scale, &sn, &cs);
+        t[i] = make_float2((float)cs, (float)sn);
+    }
+}
+
+int launch_grating_from_real(const float* V, float2* trans, size_t n, double scale, cudaStream_t s) {
+    if (!n) return QS_OK;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    grating_from_real<<<sms * 8, 256, 0, s>>>(V, trans, n, scale);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libqstem_gpu.so")
 EXPORTS = ["qs_ctx_create", "qs_ctx_destroy", "qs_last_error", "qs_abi_version", "qs_ctx_stream",
            "qs_params_finalize", "qs_thickness_count", "qs_lut_build", "qs_slices_build", "qs_probe",
            "qs_multislice_run", "qs_collect", "qs_stem_run", "qs_ctx_profile", "qs_ctx_stats",
-           "qs_multislice_run_noalloc"]
+           "qs_multislice_run_noalloc", "qs_phase_grating", "qs_adjoint_run", "qs_atoms_grad"]
 
 _lib = None
 
@@ -62,6 +62,10 @@ def load(path=LIB_PATH):
     L.qs_ctx_profile.argtypes = [vp, ctypes.c_int]
     L.qs_ctx_stats.argtypes = [vp, ctypes.POINTER(abi.QsStats)]
     L.qs_multislice_run_noalloc.argtypes = [vp, P, vp, vp, ctypes.POINTER(abi.QsBatch), vp, vp, vp]
+    L.qs_phase_grating.argtypes = [vp, P, vp, vp, ctypes.c_uint]
+    L.qs_adjoint_run.argtypes = [vp, P, vp, vp, ctypes.POINTER(abi.QsBatch), vp, ctypes.c_int,
+                                 ctypes.POINTER(ctypes.c_double), vp, vp, ctypes.c_uint]
+    L.qs_atoms_grad.argtypes = [vp, P, vp, ctypes.c_int, vp, vp, ctypes.c_uint]
     _lib = L
     return L
 
@@ -194,6 +198,34 @@ class Context:
                                     ctypes.byref(bx), _ptr(det), _ptr(diffpats)))
         del keep
         return det
+
+    def phase_grating(self, p, V, out=None):
+        """t = exp(i lambda gamma V) for a device potential stack V (torch)."""
+        import torch
+        if out is None:
+            out = torch.empty((p.slices, p.potNx, p.potNy, 2), dtype=torch.float32, device=V.device)
+        _check(self.lib.qs_phase_grating(self.h, ctypes.byref(p), _ptr(V), _ptr(out), abi.QS_SYNC))
+        return out
+
+    def adjoint(self, p, trans, probe, target, positions=None, ckpt=6, want_diffpats=False):
+        """Loss sum (I - target)^2 and dL/dV (device torch tensors in and out)."""
+        import torch
+        bx, keep = _batch(p, positions)
+        dV = torch.empty((p.slices, p.potNx, p.potNy), dtype=torch.float32, device=trans.device)
+        dps = torch.empty((bx.npos, p.nx, p.ny), dtype=torch.float32, device=trans.device) if want_diffpats else None
+        loss = ctypes.c_double()
+        _check(self.lib.qs_adjoint_run(self.h, ctypes.byref(p), _ptr(trans), _ptr(probe), ctypes.byref(bx),
+                                       _ptr(target), int(ckpt), ctypes.byref(loss), _ptr(dV), _ptr(dps),
+                                       abi.QS_SYNC))
+        del keep
+        return loss.value, dV, dps
+
+    def atoms_grad(self, p, atoms, dV):
+        a = abi.atoms_to_numpy(atoms)
+        g = np.zeros((len(a), 2), np.float64)
+        _check(self.lib.qs_atoms_grad(self.h, ctypes.byref(p), a.ctypes.data_as(ctypes.c_void_p), len(a), _ptr(dV),
+                                      g.ctypes.data_as(ctypes.c_void_p), 0))
+        return g
 
     def profile(self, enable=True):
         _check(self.lib.qs_ctx_profile(self.h, int(enable)))
