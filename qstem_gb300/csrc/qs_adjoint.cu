@@ -53,7 +53,8 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
     const int tile = blockIdx.x % ntiles;
     const int b = blockIdx.x / ntiles;
     const int ky = tile * C + c;
-    float2* col = a.waves + (size_t)b * a.nx * a.ny + ky;
+    const float2* col = a.waves + (size_t)b * a.nx * a.ny + ky;
+    float2* out = a.waves_out + (size_t)b * a.nx * a.ny + ky;
     const bool inband = (ky <= a.yA || ky >= a.yB);
     float2 reg[E];
 #pragma unroll
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
     if (lane == 0) s_loss[warp] = loss;
     line_fft<Cfg, true, true>(reg, sm, s_tw, t);
 #pragma unroll
-    for (int e = 0; e < E; ++e) col[(size_t)(t + T * e) * a.ny] = reg[e];
+    for (int e = 0; e < E; ++e) out[(size_t)(t + T * e) * a.ny] = reg[e];
     __syncthreads();
     if (tid == 0) {
         double s = 0.0;
@@ -159,26 +160,44 @@ __global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES)
 }
 
 // dL/dV of one slice: sum the windows of all positions, then
-// -2 sigma Im(conj(G) t).  One thread per potential pixel; positions loop.
-__global__ void adj_dv_gather(const float2* __restrict__ grad_t, int npos, int nx, int ny, int potNx, int potNy,
-                              const int* __restrict__ posX, const int* __restrict__ posY,
-                              const float2* __restrict__ trans_slice, double sigma, float* __restrict__ dV) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// -2 sigma Im(conj(G) t).  Stage 1: blockIdx.z picks a chunk of DV_CHUNK
+// positions, one thread per potential pixel sums that chunk (coalesced along
+// Y); stage 2 adds the chunks in a fixed order (deterministic).
+constexpr int DV_CHUNK = 32;
+
+__global__ void adj_dv_partial(const float2* __restrict__ grad_t, int npos, int nx, int ny, int potNx, int potNy,
+                               const int* __restrict__ posX, const int* __restrict__ posY,
+                               double2* __restrict__ partial) {
+    const int Y = blockIdx.x * blockDim.x + threadIdx.x;
     const int X = blockIdx.y;
-    if (i >= potNy) return;
-    const int Y = i;
+    if (Y >= potNy) return;
+    const int p0 = blockIdx.z * DV_CHUNK, p1 = min(npos, p0 + DV_CHUNK);
     double gr = 0.0, gi = 0.0;
-    for (int p = 0; p < npos; ++p) {
+    for (int p = p0; p < p1; ++p) {
         const int lx = X - __ldg(posX + p), ly = Y - __ldg(posY + p);
         if (lx >= 0 && lx < nx && ly >= 0 && ly < ny) {
-            const float2 v = grad_t[((size_t)p * nx + lx) * ny + ly];
+            const float2 v = __ldg(grad_t + ((size_t)p * nx + lx) * ny + ly);
             gr += v.x;
             gi += v.y;
         }
     }
-    const float2 tv = trans_slice[(size_t)X * potNy + Y];
-    // Im(conj(G) t) = gr*t.y - gi*t.x
-    dV[(size_t)X * potNy + Y] = (float)(-2.0 * sigma * (gr * tv.y - gi * tv.x));
+    partial[((size_t)blockIdx.z * potNx + X) * potNy + Y] = make_double2(gr, gi);
+}
+
+__global__ void adj_dv_finish(const double2* __restrict__ partial, int nchunks, int potNx, int potNy,
+                              const float2* __restrict__ trans_slice, double sigma, float* __restrict__ dV) {
+    const size_t n = (size_t)potNx * potNy;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double gr = 0.0, gi = 0.0;
+        for (int c = 0; c < nchunks; ++c) {
+            const double2 v = partial[(size_t)c * n + i];
+            gr += v.x;
+            gi += v.y;
+        }
+        const float2 tv = trans_slice[i];
+        // Im(conj(G) t) = gr*t.y - gi*t.x
+        dV[i] = (float)(-2.0 * sigma * (gr * tv.y - gi * tv.x));
+    }
 }
 
 // ---------------------------------------------- scatter-sum adjoint (atoms)
@@ -268,6 +287,10 @@ static int last_n(const AdjLastArgs& a, cudaStream_t s) {
 }
 
 int launch_adj_last(const AdjLastArgs& a, cudaStream_t s) {
+    if (!a.waves || !a.waves_out || !a.target || !a.loss_partial) {
+        set_error("adjoint: last-slice pass given a null buffer");
+        return QS_ERR_ARG;
+    }
     switch (a.nx) {
         case 64: return last_n<64>(a, s);
         case 128: return last_n<128>(a, s);
@@ -313,16 +336,30 @@ static int adj_rows_any(const AdjRowArgs& a, cudaStream_t s) {
 }
 
 int launch_adj_rows(const AdjRowArgs& a, bool first, cudaStream_t s) {
+    if (!a.grad || !a.grad_t || (first ? !a.probe : !a.state)) {
+        set_error("adjoint: row pass given a null buffer");
+        return QS_ERR_ARG;
+    }
     return first ? adj_rows_any<true>(a, s) : adj_rows_any<false>(a, s);
 }
 
+size_t dv_partial_elems(int npos, int potNx, int potNy) {
+    return 2 * (size_t)((npos + DV_CHUNK - 1) / DV_CHUNK) * potNx * potNy;
+}
+
 int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, int potNy, const int* posX,
-                     const int* posY, const float2* trans_slice, double sigma, float* dV, cudaStream_t s) {
-    dim3 block(256);
-    dim3 grid((potNy + 255) / 256, potNx);
-    adj_dv_gather<<<grid, block, 0, s>>>(grad_t, npos, nx, ny, potNx, potNy, posX, posY, trans_slice, sigma, dV);
+                     const int* posY, const float2* trans_slice, double sigma, double* partial, float* dV,
+                     cudaStream_t s) {
+    const int nchunks = (npos + DV_CHUNK - 1) / DV_CHUNK;
+    adj_dv_partial<<<dim3((potNy + 127) / 128, potNx, nchunks), 128, 0, s>>>(grad_t, npos, nx, ny, potNx, potNy,
+                                                                            posX, posY, (double2*)partial);
     QS_CUDA_TRY(cudaGetLastError());
-    count_launch(1);
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    adj_dv_finish<<<sms * 4, 256, 0, s>>>((const double2*)partial, nchunks, potNx, potNy, trans_slice, sigma, dV);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(2);
     return QS_OK;
 }
 

@@ -858,10 +858,11 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     auto rup = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t small = rup(sizeof(float) * (nx + ny)) + 2 * rup(sizeof(float2) * (nx + ny)) +
                          rup(sizeof(int) * std::max(ntiles, 1)) + rup(sizeof(int) * 2 * npos) + rup(sizeof(double) * nLoss);
-    // work, grad, grad_t, checkpoints 1..nseg-1, segment states 1..ckpt-1
-    const size_t nbuf = 3 + (size_t)(nseg - 1) + (size_t)(ckpt - 1);
+    // work, scratch state, grad, grad_t, checkpoints 1..nseg-1, segment states 1..ckpt-1
+    const size_t nbuf = 4 + (size_t)(nseg - 1) + (size_t)(ckpt - 1);
+    const size_t partElems = dv_partial_elems(npos, P.potNx, P.potNy);
     void* base = nullptr;
-    QS_TRY(ensure(c, B_ADJ, small + nbuf * rup(waveBytes), &base));
+    QS_TRY(ensure(c, B_ADJ, small + rup(sizeof(double) * partElems) + nbuf * rup(waveBytes), &base));
     unsigned char* cur = (unsigned char*)base;
     auto take = [&](size_t b) { void* q = cur; cur += rup(b); return q; };
     float* d_kx2 = (float*)take(sizeof(float) * (nx + ny));
@@ -873,7 +874,9 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     int* d_tiles = (int*)take(sizeof(int) * std::max(ntiles, 1));
     int* d_pos = (int*)take(sizeof(int) * 2 * npos);
     double* d_loss = (double*)take(sizeof(double) * nLoss);
+    double* d_part = (double*)take(sizeof(double) * partElems);
     float2* work = (float2*)take(waveBytes);
+    float2* hscr = (float2*)take(waveBytes);
     float2* grad = (float2*)take(waveBytes);
     float2* grad_t = (float2*)take(waveBytes);
     std::vector<float2*> ck(nseg, nullptr), seg(ckpt, nullptr);
@@ -890,6 +893,7 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     QS_CUDA_TRY(cudaMemcpyAsync(d_pos, px.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
     QS_CUDA_TRY(cudaMemcpyAsync(d_pos + npos, py.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
     QS_CUDA_TRY(cudaMemsetAsync(work, 0, waveBytes, s));
+    QS_CUDA_TRY(cudaMemsetAsync(hscr, 0, waveBytes, s));
     QS_CUDA_TRY(cudaMemsetAsync(grad, 0, waveBytes, s));
     const float2* tw_y = twiddles(ny);
     const float2* tw_x = twiddles(nx);
@@ -905,36 +909,48 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     ColArgs ca{};
     ca.nx = nx; ca.ny = ny; ca.nwaves = npos; ca.tw = tw_x; ca.kx2 = d_kx2; ca.ky2 = d_ky2;
     ca.k2max = tb.k2max; ca.tiles = d_tiles; ca.ntiles = ntiles; ca.inverse = 1; ca.ndet = 0;
-    // Forward through slices [s0, upto) starting from h_{s0} in `buf`.  The
-    // full run (keepStates false) starts at slice 0, copies the checkpoint
-    // states h_{k*ckpt} and ends after the last row pass (the last column
-    // pass is the loss kernel).  A segment recompute (keepStates true) only
-    // needs the states h_s, s0 < s < upto, and stores them in `seg`.
-    auto forward = [&](float2* buf, int s0, int upto, bool keepStates) -> int {
-        ra.waves = buf;
-        ca.waves = buf;
+    // Forward through slices [s0, upto).  The row pass of slice s reads the
+    // state h_s (the probe for s = 0) and writes `work`; the column pass reads
+    // `work` and writes h_{s+1} straight into the buffer that keeps it, so no
+    // state is ever copied.  The full run (full true) keeps the checkpoint
+    // states h_{k*ckpt} in ck[k] and the states of the last segment in seg,
+    // and ends after the last row pass (the last column pass is the loss
+    // kernel).  A segment recompute writes h_s, s0 < s < upto, into seg.
+    const int lastS0 = (nseg - 1) * ckpt;
+    auto state_of = [&](int sl, int s0) -> float2* {
+        if (sl == 0) return nullptr;
+        if (sl > s0) return seg[sl - s0];
+        return ck[sl / ckpt];
+    };
+    auto forward = [&](int s0, int upto, bool full) -> int {
         ca.px = d_px;
         ca.py = d_py;
-        const int last = keepStates ? upto - 1 : upto;
+        const int last = full ? upto : upto - 1;
+        float2* cur = state_of(s0, s0);
         for (int sl = s0; sl < last; sl++) {
+            ra.waves = cur;
+            ra.waves_out = work;
             ra.trans_slice = trans + (size_t)sl * sliceElems;
             QS_TRY(launch_rows(ra, sl == 0 ? ROW_FIRST : ROW_MID, s));
             if (sl == S - 1) break;
-            QS_TRY(launch_cols(ca, s));
             const int nxt = sl + 1;
-            if (keepStates)
-                QS_CUDA_TRY(cudaMemcpyAsync(seg[nxt - s0], buf, waveBytes, cudaMemcpyDeviceToDevice, s));
-            else if (nxt % ckpt == 0 && nxt < S)
-                QS_CUDA_TRY(cudaMemcpyAsync(ck[nxt / ckpt], buf, waveBytes, cudaMemcpyDeviceToDevice, s));
+            float2* dst;
+            if (!full || nxt > lastS0) dst = seg[nxt - (full ? lastS0 : s0)];
+            else if (nxt % ckpt == 0) dst = ck[nxt / ckpt];
+            else dst = hscr;
+            ca.waves = work;
+            ca.waves_out = dst;
+            QS_TRY(launch_cols(ca, s));
+            cur = dst;
         }
         return QS_OK;
     };
-    // 1. forward with checkpoints, ending with the state after the last row pass
-    QS_TRY(forward(work, 0, S, false));
+    // 1. forward through all slices
+    QS_TRY(forward(0, S, true));
     // 2. loss and its gradient at the last slice: g_A of slice S-1 in `grad`
-    QS_CUDA_TRY(cudaMemcpyAsync(grad, work, waveBytes, cudaMemcpyDeviceToDevice, s));
     AdjLastArgs la{};
-    la.nx = nx; la.ny = ny; la.nwaves = npos; la.yA = yA; la.yB = yB; la.waves = grad; la.tw = tw_x;
+    la.nx = nx; la.ny = ny; la.nwaves = npos; la.yA = yA; la.yB = yB; la.waves = work; la.waves_out = grad;
+    la.tw = tw_x;
     la.kx2 = d_kx2; la.ky2 = d_ky2; la.px = d_px; la.py = d_py; la.k2max = tb.k2max; la.target = target;
     la.diffpat = diffpats; la.scaleDiff = 1.0 / std::sqrt((double)N); la.loss_partial = d_loss;
     QS_TRY(launch_adj_last(la, s));
@@ -946,22 +962,24 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     ar.norm = (float)(1.0 / (double)N);
     for (int sg = nseg - 1; sg >= 0; sg--) {
         const int s0 = sg * ckpt, s1 = std::min(S, s0 + ckpt);
-        // recompute the segment's states h_s, s0 < s < s1
-        if (s1 - s0 > 1) {
-            if (s0 > 0) QS_CUDA_TRY(cudaMemcpyAsync(work, ck[sg], waveBytes, cudaMemcpyDeviceToDevice, s));
-            QS_TRY(forward(work, s0, s1, true));
-        }
+        // recompute the segment's states h_s, s0 < s < s1 (the full run kept
+        // those of the last segment)
+        if (sg < nseg - 1 && s1 - s0 > 1) QS_TRY(forward(s0, s1, false));
         for (int sl = s1 - 1; sl >= s0; sl--) {
             if (sl < S - 1) {
                 // column pass with conj(P): g_h(sl+1) -> g_A(sl)
-                ca.waves = grad; ca.px = d_pxc; ca.py = d_pyc;
+                ca.waves = grad;
+                ca.waves_out = nullptr;
+                ca.px = d_pxc;
+                ca.py = d_pyc;
                 QS_TRY(launch_cols(ca, s));
             }
-            ar.state = sl == s0 ? (s0 > 0 ? ck[sg] : nullptr) : seg[sl - s0];
+            ar.state = state_of(sl, s0);
             ar.trans_slice = trans + (size_t)sl * sliceElems;
             QS_TRY(launch_adj_rows(ar, sl == 0, s));
             QS_TRY(launch_dv_gather(grad_t, npos, nx, ny, P.potNx, P.potNy, d_pos, d_pos + npos,
-                                    trans + (size_t)sl * sliceElems, sigma, dL_dV + (size_t)sl * sliceElems, s));
+                                    trans + (size_t)sl * sliceElems, sigma, d_part, dL_dV + (size_t)sl * sliceElems,
+                                    s));
         }
     }
     if (loss) {

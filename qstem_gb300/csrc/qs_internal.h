@@ -40,6 +40,7 @@ struct RowArgs {
     const float2* trans_slice;   // potNx x potNy c64 of the slice applied here
     const float2* probe;         // nx x ny (ROW_FIRST)
     float2* waves;               // nwaves x nx x ny
+    float2* waves_out;           // where ROW_FIRST/ROW_MID write (nullptr: in place)
     float2* exit_waves;          // ROW_LAST destination (may alias waves)
     const int* posX;             // nwaves window offsets
     const int* posY;
@@ -52,6 +53,7 @@ struct RowArgs {
 struct ColArgs {
     int nx, ny, nwaves;
     float2* waves;
+    float2* waves_out;           // where the inverse transform is stored (nullptr: in place)
     const float2* tw;            // twiddle table of the length-nx line transform
     const float* kx2;            // nx, float as propagate_slow computes
     const float* ky2;            // ny
@@ -116,7 +118,8 @@ int launch_scale_by_sum(float2* wave, size_t n, const double* d_sum, double nxy,
 // ----------------------------------------------------------------- adjoint
 struct AdjLastArgs {
     int nx, ny, nwaves, yA, yB;
-    float2* waves;               // in: state after the last row pass; out: g_A
+    const float2* waves;         // state after the last row pass
+    float2* waves_out;           // g_A of the last slice
     const float2* tw;            // twiddles of the length-nx transform
     const float *kx2, *ky2;
     const float2 *px, *py;       // forward propagator factors
@@ -139,8 +142,12 @@ struct AdjRowArgs {
 };
 int launch_adj_last(const AdjLastArgs& a, cudaStream_t s);
 int launch_adj_rows(const AdjRowArgs& a, bool first, cudaStream_t s);
+// dL/dV of one slice from the per-position g_t: positions are summed in
+// chunks into `partial` (dv_partial_elems doubles), then reduced
+size_t dv_partial_elems(int npos, int potNx, int potNy);
 int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, int potNy, const int* posX,
-                     const int* posY, const float2* trans_slice, double sigma, float* dV, cudaStream_t s);
+                     const int* posY, const float2* trans_slice, double sigma, double* partial, float* dV,
+                     cudaStream_t s);
 int launch_atoms_grad(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
                       const qs_params& p, const float* dV, double* grad, cudaStream_t s);
 int launch_grating_from_real(const float* V, float2* trans, size_t n, double scale, cudaStream_t s);

@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(line_threads(N) * ROW_LINES, row_min_blocks(N)
 #pragma unroll
         for (int e = 0; e < E; ++e) reg[e] = cmul(reg[e], __ldg(tr + t + T * e));
         line_fft<Cfg, false>(reg, sm, s_tw, t);
-        float2* dst = a.waves + ((size_t)b * a.nx + x) * N;
+        float2* dst = (a.waves_out ? a.waves_out : a.waves) + ((size_t)b * a.nx + x) * N;
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int y = t + T * e;
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
         }
         if constexpr (INVERSE) {
             line_fft<Cfg, true, true>(reg, sm, s_tw, t);
-            float2* col = a.waves + (size_t)b * a.nx * a.ny + ky;
+            float2* col = (a.waves_out ? a.waves_out : a.waves) + (size_t)b * a.nx * a.ny + ky;
 #pragma unroll
             for (int e = 0; e < E; ++e) col[(size_t)(t + T * e) * a.ny] = reg[e];
         }
@@ -264,6 +264,10 @@ static int rows_mode(const RowArgs& a, cudaStream_t s) {
 }
 
 int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s) {
+    if ((mode == ROW_FIRST ? !a.probe : !a.waves) || (mode == ROW_LAST ? !a.exit_waves : !(a.waves_out || a.waves))) {
+        set_error("row pass given a null buffer");
+        return QS_ERR_ARG;
+    }
     if (mode == ROW_FIRST) return rows_mode<ROW_FIRST>(a, s);
     if (mode == ROW_MID) return rows_mode<ROW_MID>(a, s);
     return rows_mode<ROW_LAST>(a, s);
@@ -305,6 +309,10 @@ static int cols_n(const ColArgs& a, cudaStream_t s) {
 }
 
 int launch_cols(const ColArgs& a, cudaStream_t s) {
+    if (!a.waves) {
+        set_error("column pass given a null buffer");
+        return QS_ERR_ARG;
+    }
     switch (a.nx) {
         case 64: return cols_n<64>(a, s);
         case 128: return cols_n<128>(a, s);
