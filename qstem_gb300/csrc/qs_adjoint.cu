@@ -161,18 +161,21 @@ __global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES)
 
 // dL/dV of one slice: sum the windows of all positions, then
 // -2 sigma Im(conj(G) t).  Stage 1: blockIdx.z picks a chunk of DV_CHUNK
-// positions, one thread per potential pixel sums that chunk (coalesced along
-// Y); stage 2 adds the chunks in a fixed order (deterministic).
+// positions, one thread per potential pixel sums that chunk in float
+// (coalesced along Y; FP64 adds run at a small fraction of the FP32 rate on
+// this part); stage 2 adds the chunks in double in a fixed order, so the
+// result is deterministic.
 constexpr int DV_CHUNK = 32;
 
 __global__ void adj_dv_partial(const float2* __restrict__ grad_t, int npos, int nx, int ny, int potNx, int potNy,
                                const int* __restrict__ posX, const int* __restrict__ posY,
-                               double2* __restrict__ partial) {
+                               float2* __restrict__ partial) {
     const int Y = blockIdx.x * blockDim.x + threadIdx.x;
     const int X = blockIdx.y;
     if (Y >= potNy) return;
     const int p0 = blockIdx.z * DV_CHUNK, p1 = min(npos, p0 + DV_CHUNK);
-    double gr = 0.0, gi = 0.0;
+    float gr = 0.f, gi = 0.f;
+#pragma unroll 8
     for (int p = p0; p < p1; ++p) {
         const int lx = X - __ldg(posX + p), ly = Y - __ldg(posY + p);
         if (lx >= 0 && lx < nx && ly >= 0 && ly < ny) {
@@ -181,16 +184,16 @@ __global__ void adj_dv_partial(const float2* __restrict__ grad_t, int npos, int 
             gi += v.y;
         }
     }
-    partial[((size_t)blockIdx.z * potNx + X) * potNy + Y] = make_double2(gr, gi);
+    partial[((size_t)blockIdx.z * potNx + X) * potNy + Y] = make_float2(gr, gi);
 }
 
-__global__ void adj_dv_finish(const double2* __restrict__ partial, int nchunks, int potNx, int potNy,
+__global__ void adj_dv_finish(const float2* __restrict__ partial, int nchunks, int potNx, int potNy,
                               const float2* __restrict__ trans_slice, double sigma, float* __restrict__ dV) {
     const size_t n = (size_t)potNx * potNy;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         double gr = 0.0, gi = 0.0;
         for (int c = 0; c < nchunks; ++c) {
-            const double2 v = partial[(size_t)c * n + i];
+            const float2 v = partial[(size_t)c * n + i];
             gr += v.x;
             gi += v.y;
         }
@@ -343,21 +346,21 @@ int launch_adj_rows(const AdjRowArgs& a, bool first, cudaStream_t s) {
     return first ? adj_rows_any<true>(a, s) : adj_rows_any<false>(a, s);
 }
 
-size_t dv_partial_elems(int npos, int potNx, int potNy) {
-    return 2 * (size_t)((npos + DV_CHUNK - 1) / DV_CHUNK) * potNx * potNy;
+size_t dv_partial_bytes(int npos, int potNx, int potNy) {
+    return sizeof(float2) * (size_t)((npos + DV_CHUNK - 1) / DV_CHUNK) * potNx * potNy;
 }
 
 int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, int potNy, const int* posX,
-                     const int* posY, const float2* trans_slice, double sigma, double* partial, float* dV,
+                     const int* posY, const float2* trans_slice, double sigma, void* partial, float* dV,
                      cudaStream_t s) {
     const int nchunks = (npos + DV_CHUNK - 1) / DV_CHUNK;
     adj_dv_partial<<<dim3((potNy + 127) / 128, potNx, nchunks), 128, 0, s>>>(grad_t, npos, nx, ny, potNx, potNy,
-                                                                            posX, posY, (double2*)partial);
+                                                                            posX, posY, (float2*)partial);
     QS_CUDA_TRY(cudaGetLastError());
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    adj_dv_finish<<<sms * 4, 256, 0, s>>>((const double2*)partial, nchunks, potNx, potNy, trans_slice, sigma, dV);
+    adj_dv_finish<<<sms * 4, 256, 0, s>>>((const float2*)partial, nchunks, potNx, potNy, trans_slice, sigma, dV);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(2);
     return QS_OK;

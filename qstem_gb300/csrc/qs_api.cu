@@ -860,9 +860,9 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
                          rup(sizeof(int) * std::max(ntiles, 1)) + rup(sizeof(int) * 2 * npos) + rup(sizeof(double) * nLoss);
     // work, scratch state, grad, grad_t, checkpoints 1..nseg-1, segment states 1..ckpt-1
     const size_t nbuf = 4 + (size_t)(nseg - 1) + (size_t)(ckpt - 1);
-    const size_t partElems = dv_partial_elems(npos, P.potNx, P.potNy);
+    const size_t partBytes = dv_partial_bytes(npos, P.potNx, P.potNy);
     void* base = nullptr;
-    QS_TRY(ensure(c, B_ADJ, small + rup(sizeof(double) * partElems) + nbuf * rup(waveBytes), &base));
+    QS_TRY(ensure(c, B_ADJ, small + rup(partBytes) + nbuf * rup(waveBytes), &base));
     unsigned char* cur = (unsigned char*)base;
     auto take = [&](size_t b) { void* q = cur; cur += rup(b); return q; };
     float* d_kx2 = (float*)take(sizeof(float) * (nx + ny));
@@ -874,7 +874,7 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     int* d_tiles = (int*)take(sizeof(int) * std::max(ntiles, 1));
     int* d_pos = (int*)take(sizeof(int) * 2 * npos);
     double* d_loss = (double*)take(sizeof(double) * nLoss);
-    double* d_part = (double*)take(sizeof(double) * partElems);
+    void* d_part = take(partBytes);
     float2* work = (float2*)take(waveBytes);
     float2* hscr = (float2*)take(waveBytes);
     float2* grad = (float2*)take(waveBytes);

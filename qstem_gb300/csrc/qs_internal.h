@@ -143,10 +143,10 @@ struct AdjRowArgs {
 int launch_adj_last(const AdjLastArgs& a, cudaStream_t s);
 int launch_adj_rows(const AdjRowArgs& a, bool first, cudaStream_t s);
 // dL/dV of one slice from the per-position g_t: positions are summed in
-// chunks into `partial` (dv_partial_elems doubles), then reduced
-size_t dv_partial_elems(int npos, int potNx, int potNy);
+// chunks into `partial` (dv_partial_bytes), then reduced
+size_t dv_partial_bytes(int npos, int potNx, int potNy);
 int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, int potNy, const int* posX,
-                     const int* posY, const float2* trans_slice, double sigma, double* partial, float* dV,
+                     const int* posY, const float2* trans_slice, double sigma, void* partial, float* dV,
                      cudaStream_t s);
 int launch_atoms_grad(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
                       const qs_params& p, const float* dV, double* grad, cudaStream_t s);
