@@ -207,9 +207,28 @@ __global__ void adj_dv_finish(const float2* __restrict__ partial, int nchunks, i
 // dL/d(atomX, atomY) = sum over the atom's pixels and slices of
 // dL/dV * dV/dr * dr/d(atom), dV/dr the slope of the radial linear
 // interpolation (stem3/stemlib.cpp:957-1019), dr/datomX = -(x_pixel - atomX)/r.
-__global__ void atoms_grad(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts, int Nz, int Nr,
-                           int nzSub, float dx, float dy, double dr, float dzs, int potNx, int potNy, int periodic,
-                           const float* __restrict__ dV, double* __restrict__ grad) {
+// FP32 arithmetic (FP64 runs at a small fraction of the FP32 rate here): the
+// per-thread sums over pixels are Kahan-compensated, because an atom's
+// gradient is a small difference of large symmetric contributions, and the
+// block reduction runs in double.  The radial interval is the forward's
+// (stem3/stemlib.cpp:944-952: r and r/dr in double): the float radius is
+// within 1e-6 relative of it, so only pixels whose r/dr lies within 2e-4 of
+// a knot recompute it in double.
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ void add(float v) {
+        const float y = __fsub_rn(v, c);
+        const float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+};
+
+__global__ void __launch_bounds__(256) atoms_grad(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts,
+                                                  int Nz, int Nr, int nzSub, float dx, float dy, double dr,
+                                                  float inv_dr, float dzs,
+                                                  int potNx, int potNy, int periodic, const float* __restrict__ dV,
+                                                  double* __restrict__ grad) {
     const AtomJob J = jobs[blockIdx.x];
     const float* lut = luts[J.lut];
     const float* lutq = J.lutq >= 0 ? luts[J.lutq] : nullptr;
@@ -219,23 +238,32 @@ __global__ void atoms_grad(const AtomJob* __restrict__ jobs, const float* const*
     const int limHi = Nr * (Nz - 1), limLo = -Nr * (Nz - 1), step = nzSub * Nr;
     const double dOffsZ = (double)(((float)(J.iAtomZ + J.iaz0) - J.atomZ / dzs) * (float)nzSub);
     const int iOffsZ0 = ((int)(dOffsZ + 0.5)) * Nr;
-    double gx = 0.0, gy = 0.0;
+    const float q = J.q;
+    Kahan gx, gy;
     for (int k = threadIdx.x; k < npx; k += blockDim.x) {
         const int iax = J.iax0 + k / w;
         const int iay = J.iay0 + k % w;
         // the reference's float offsets, rounded step by step (no FMA
         // contraction: an atom on a pixel must give r == 0 exactly)
-        const double ddx = (double)__fsub_rn(__fmul_rn((float)iax, dx), J.atomX);
-        const double ddy = (double)__fsub_rn(__fmul_rn((float)iay, dy), J.atomY);
-        const double r = sqrt(ddx * ddx + ddy * ddy);
-        const double rr = r / dr;
-        const int ir = (int)floor(rr);
-        if (ir >= Nr - 1 || r <= 0.0) continue;
+        const float ddx = __fsub_rn(__fmul_rn((float)iax, dx), J.atomX);
+        const float ddy = __fsub_rn(__fmul_rn((float)iay, dy), J.atomY);
+        const float r2 = ddx * ddx + ddy * ddy;
+        if (r2 <= 0.f) continue;
+        const float rinv = rsqrtf(r2);
+        const float r = r2 * rinv;
+        const float rr = r * inv_dr;
+        int ir = (int)floorf(rr);
+        const float fr = rr - (float)ir;
+        if (fr < 2e-4f || fr > 1.f - 2e-4f) {
+            const double x2 = (double)ddx * ddx, y2 = (double)ddy * ddy;
+            ir = (int)floor(sqrt(x2 + y2) / dr);
+        }
+        if (ir >= Nr - 1) continue;
         const int cx = periodic ? ((iax % potNx) + potNx) % potNx : iax;
         const int cy = periodic ? ((iay % potNy) + potNy) % potNy : iay;
         const float* g = dV + (size_t)(J.iAtomZ + J.iaz0) * sliceStep + (size_t)cx * potNy + cy;
         int iOffsZ = iOffsZ0;
-        double dLdr = 0.0;
+        float dLdr = 0.f;
         for (int iaz = J.iaz0; iaz <= J.iaz1; iaz++) {
             int row = -1;
             if (iOffsZ < 0) {
@@ -244,19 +272,21 @@ __global__ void atoms_grad(const AtomJob* __restrict__ jobs, const float* const*
                 row = iOffsZ;
             }
             if (row >= 0) {
-                double slope = (double)lut[row + ir + 1] - (double)lut[row + ir];
-                if (lutq) slope += J.q * ((double)lutq[row + ir + 1] - (double)lutq[row + ir]);
-                dLdr += (double)*g * slope / dr;
+                float slope = __ldg(lut + row + ir + 1) - __ldg(lut + row + ir);
+                if (lutq) slope += q * (__ldg(lutq + row + ir + 1) - __ldg(lutq + row + ir));
+                dLdr += __ldg(g) * slope;
             }
             g += sliceStep;
             iOffsZ += step;
         }
-        gx += dLdr * (-ddx / r);
-        gy += dLdr * (-ddy / r);
+        // dV/dr = slope / dr
+        dLdr *= inv_dr;
+        gx.add(-dLdr * ddx * rinv);
+        gy.add(-dLdr * ddy * rinv);
     }
     __shared__ double sx[256], sy[256];
-    sx[threadIdx.x] = gx;
-    sy[threadIdx.x] = gy;
+    sx[threadIdx.x] = (double)gx.s - (double)gx.c;
+    sy[threadIdx.x] = (double)gy.s - (double)gy.c;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o) {
@@ -370,7 +400,8 @@ int launch_atoms_grad(const AtomJob* d_jobs, int njobs, const float* const* d_lu
                       const qs_params& p, const float* dV, double* grad, cudaStream_t s) {
     if (njobs <= 0) return QS_OK;
     const double dr = p.resolutionX / 2;
-    atoms_grad<<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr,
+    const float inv_dr = (float)(1.0 / dr);
+    atoms_grad<<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr, inv_dr,
                                      p.sliceThickness, p.potNx, p.potNy, p.nonPeriod ? 0 : 1, dV, grad);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
