@@ -65,7 +65,10 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
     const float2 pyv = a.py[ky];
     const float* tgt = a.target + (size_t)b * a.nx * a.ny + (ky + a.ny / 2) % a.ny;
     float* dp = a.diffpat ? a.diffpat + (size_t)b * a.nx * a.ny + (ky + a.ny / 2) % a.ny : nullptr;
-    double loss = 0.0;
+    // FP32 per pixel (FP64 runs at a small fraction of the FP32 rate here);
+    // a thread's E squared residuals are summed in FP32, the rest in double
+    const float sc = (float)a.scaleDiff;
+    float loss = 0.f;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const int kx = t + T * e;
@@ -73,20 +76,21 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
         const float2 pxv = a.px[kx];
         const bool pass = inband && kx2 < a.k2max && (kx2 + ky2) < a.k2max;
         const float2 Bp = pass ? cmul(cmul(reg[e], pyv), pxv) : make_float2(0.f, 0.f);
-        const double I = (double)(Bp.x * Bp.x + Bp.y * Bp.y) * a.scaleDiff;
+        const float I = (Bp.x * Bp.x + Bp.y * Bp.y) * sc;
         const size_t ik = (size_t)((kx + a.nx / 2) % a.nx) * a.ny;
-        const double dI = I - (double)tgt[ik];
+        const float dI = I - tgt[ik];
         loss += dI * dI;
-        if (dp) dp[ik] = (float)I;
+        if (dp) dp[ik] = I;
         // g_B' = 2 dI c B', then g_B = conj(P) g_B'
-        const float g = (float)(2.0 * dI * a.scaleDiff);
+        const float g = 2.f * dI * sc;
         const float2 gBp = make_float2(g * Bp.x, g * Bp.y);
         reg[e] = pass ? cmulc(cmulc(gBp, pyv), pxv) : make_float2(0.f, 0.f);
     }
     const int lane = tid & 31, warp = tid >> 5;
+    double lsum = (double)loss;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
-    if (lane == 0) s_loss[warp] = loss;
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if (lane == 0) s_loss[warp] = lsum;
     line_fft<Cfg, true, true>(reg, sm, s_tw, t);
 #pragma unroll
     for (int e = 0; e < E; ++e) out[(size_t)(t + T * e) * a.ny] = reg[e];

@@ -160,28 +160,32 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
 
         if constexpr (DET) {
             // collectIntensity (stem3/stemlib.cpp:2615-2657): |psi(k)|^2 in
-            // float, summed per annulus in double
+            // float, summed per annulus.  The sums of a thread's E pixels and
+            // of a warp are FP32 (positive terms: relative error ~1e-6; FP64
+            // adds run at a small fraction of the FP32 rate on this part); the
+            // warps of a CTA and the CTAs are added in double.
             const int lane = tid & 31, warp = tid >> 5;
             for (int d = 0; d < a.ndet; ++d) {
-                double acc = 0.0;
+                float acc = 0.f;
                 const float lo = a.k2in[d], hi = a.k2out[d];
 #pragma unroll
                 for (int e = 0; e < E; ++e) {
                     const float k2 = __ldg(a.kx2 + t + T * e) + ky2;
                     const float I = reg[e].x * reg[e].x + reg[e].y * reg[e].y;
-                    if (k2 >= lo && k2 <= hi) acc += (double)I;
+                    if (k2 >= lo && k2 <= hi) acc += I;
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                if (lane == 0) s_det[d][warp] = acc;
+                if (lane == 0) s_det[d][warp] = (double)acc;
             }
             if (a.diffpat) {
                 float* dp = a.diffpat + (size_t)b * a.nx * a.ny + (ky + a.ny / 2) % a.ny;
+                const float sc = (float)a.scaleDiff;
 #pragma unroll
                 for (int e = 0; e < E; ++e) {
                     const int kx = t + T * e;
                     const float I = reg[e].x * reg[e].x + reg[e].y * reg[e].y;
-                    dp[(size_t)((kx + a.nx / 2) % a.nx) * a.ny] = (float)((double)I * a.scaleDiff);
+                    dp[(size_t)((kx + a.nx / 2) % a.nx) * a.ny] = I * sc;
                 }
             }
             __syncthreads();

@@ -253,13 +253,20 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
 // --------------------------------------------------------- scatter-sum
 // One block per atom job; threads stride over the atom's pixel box.  The
 // interpolation follows stem3/stemlib.cpp:935-1028 (radial linear
-// interpolation at dr = dx/2, nearest sub-slice in z).
+// interpolation at dr = dx/2, nearest sub-slice in z).  FP32 arithmetic
+// (FP64 runs at a small fraction of the FP32 rate on this part): the
+// reference forms r and r/dr in double (stem3/stemlib.cpp:944-952); the
+// float radius is within ~2e-7 relative of that, so the radial interval is
+// taken from the float value except within 2e-4 of a knot, where the double
+// computation decides it.  The interpolation weight and the sum then run in
+// float (~1e-7 relative).
 __global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts, int Nz,
-                              int Nr, int nzSub, float dx, float dy, double dr, float dzs, int potNx, int potNy,
-                              int periodic, float2* __restrict__ trans) {
+                              int Nr, int nzSub, float dx, float dy, double dr, float drf, float dzs, int potNx,
+                              int potNy, int periodic, float2* __restrict__ trans) {
     const AtomJob J = jobs[blockIdx.x];
     const float* lut = luts[J.lut];
     const float* lutq = J.lutq >= 0 ? luts[J.lutq] : nullptr;
+    const float q = J.q;
     const int w = J.iay1 - J.iay0 + 1;
     const int npx = (J.iax1 - J.iax0 + 1) * w;
     const size_t sliceStep = (size_t)potNx * potNy;
@@ -271,31 +278,35 @@ __global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* con
         const int iay = J.iay0 + k % w;
         // x2 = iax*dx - atomX in float as the reference forms it
         // (stem3/stemlib.cpp:931-938), rounded step by step (no FMA)
-        double x2 = (double)__fsub_rn(__fmul_rn((float)iax, dx), J.atomX);
-        x2 *= x2;
-        double y2 = (double)__fsub_rn(__fmul_rn((float)iay, dy), J.atomY);
-        y2 *= y2;
-        const double r = sqrt(x2 + y2);
-        double ddr = r / dr;
-        const int ir = (int)floor(ddr);
+        const float ddx = __fsub_rn(__fmul_rn((float)iax, dx), J.atomX);
+        const float ddy = __fsub_rn(__fmul_rn((float)iay, dy), J.atomY);
+        const float rr = __fsqrt_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy))) / drf;
+        int ir = (int)floorf(rr);
+        float ddr = rr - (float)ir;
+        if (ddr < 2e-4f || ddr > 1.f - 2e-4f) {
+            const double x2 = (double)ddx * ddx, y2 = (double)ddy * ddy;
+            const double dd = sqrt(x2 + y2) / dr;
+            ir = (int)floor(dd);
+            ddr = (float)(dd - (double)ir);
+        }
         if (ir >= Nr - 1) continue;
-        ddr -= (double)ir;
         const int cx = periodic ? ((iax % potNx) + potNx) % potNx : iax;
         const int cy = periodic ? ((iay % potNy) + potNy) % potNy : iay;
         float* dst = &trans[(size_t)(J.iAtomZ + J.iaz0) * sliceStep + (size_t)cx * potNy + cy].x;
+        const float w0 = 1.f - ddr;
         int iOffsZ = iOffsZ0;
         for (int iaz = J.iaz0; iaz <= J.iaz1; iaz++) {
-            double v = 0;
+            int row = -1;
             if (iOffsZ < 0) {
-                if (iOffsZ > limLo) {
-                    v = (1 - ddr) * lut[ir - iOffsZ + Nr] + ddr * lut[ir + 1 - iOffsZ + Nr];
-                    if (lutq) v += J.q * ((1 - ddr) * lutq[ir - iOffsZ + Nr] + ddr * lutq[ir + 1 - iOffsZ + Nr]);
-                }
+                if (iOffsZ > limLo) row = -iOffsZ + Nr;
             } else if (iOffsZ < limHi) {
-                v = (1 - ddr) * lut[ir + iOffsZ] + ddr * lut[ir + 1 + iOffsZ];
-                if (lutq) v += J.q * ((1 - ddr) * lutq[ir + iOffsZ] + ddr * lutq[ir + 1 + iOffsZ]);
+                row = iOffsZ;
             }
-            if (v != 0) atomicAdd(dst, (float)v);
+            if (row >= 0) {
+                float v = w0 * __ldg(lut + row + ir) + ddr * __ldg(lut + row + ir + 1);
+                if (lutq) v += q * (w0 * __ldg(lutq + row + ir) + ddr * __ldg(lutq + row + ir + 1));
+                if (v != 0.f) atomicAdd(dst, v);
+            }
             dst += 2 * sliceStep;
             iOffsZ += step;
         }
@@ -306,7 +317,7 @@ int launch_scatter(const AtomJob* d_jobs, int njobs, const float* const* d_luts,
                    const qs_params& p, float2* trans, cudaStream_t s) {
     if (njobs <= 0) return QS_OK;
     const double dr = p.resolutionX / OVERSAMP;
-    scatter_atoms<<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr,
+    scatter_atoms<<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr, (float)dr,
                                         p.sliceThickness, p.potNx, p.potNy, p.nonPeriod ? 0 : 1, trans);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
