@@ -151,6 +151,46 @@ def adjoint_measure(ctx, torch, reps=3):
             "adjoint_definition": "loss + dL/dV for all slices, forward included; forward = diffraction patterns"}
 
 
+def tem_workload():
+    """TEM Si [110] (3.840 x 5.431 x 3.840 A cell replicated 10 x 7 x 26), 1024^2,
+    dx 0.0375 A, 2 A slices x 50, 300 kV, transmission band limit on, 16
+    frozen-phonon configurations with N(0, 0.075^2) A per Cartesian axis from
+    numpy.random.default_rng(20261203 + j).  Objective lens: Cs 1.2 mm, defocus
+    -60 nm, aperture 20 mrad with a 1 mrad cosine edge."""
+    atoms, ax, by, c = config.replicate(config.si110_cell(), 10, 7, 26)
+    p = config.make_params(mode=abi.QS_MODE_TEM, nx=1024, resolutionX=float(np.float32(ax)) / 1024,
+                           resolutionY=float(np.float32(by)) / 1024, v0=300, slices=50, sliceThickness=2.0, ax=ax,
+                           by=by, c=c, bandlimit=True, alpha=0.0)
+    configs = []
+    for j in range(16):
+        rng = np.random.default_rng(SEED - 100 + j)
+        a = atoms.copy()
+        for k in ("x", "y", "z"):
+            a[k] = (a[k].astype(np.float64) + rng.standard_normal(len(a)) * 0.075).astype(np.float32)
+        configs.append(a)
+    lam = config.wavelength(300.0)
+    ctf = dict(Cs=1.2e7, kmax=0.020 / lam, edge=0.001 / lam)
+    return p, configs, ctf, [-600.0]
+
+
+def tem_measure(ctx, reps=2):
+    """qs_tem_run end to end (host atoms in, host images out): 16 slice-stack
+    builds + one batched 16-wave multislice + mean intensity + CTF image."""
+    p, configs, ctf, defoci = tem_workload()
+    ctx.tem(p, configs[:2], ctf=ctf, defoci=defoci)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        mean, imgs, _ = ctx.tem(p, configs, ctf=ctf, defoci=defoci)
+        t = time.perf_counter() - t0
+        best = t if best is None else min(best, t)
+    ss = len(configs) * p.slices
+    return {"workload": "TEM Si[110] 10x7x26 (%d atoms), 1024^2, 50 slices, 300 kV, band limit, 16 configurations, "
+                        "CTF Cs 1.2 mm df -60 nm aperture 20 mrad" % len(configs[0]),
+            "e2e_ms": best * 1e3, "configurations_per_s": len(configs) / best, "slice_steps_per_s": ss / best,
+            "mean_intensity": float(mean.mean()), "ctf_image_mean": float(imgs[0].mean())}
+
+
 def cpu_sample(p, atoms, npos_sample, threads):
     """Reference CPU algorithm on a bounded sample: one slice-stack build plus
     `npos_sample` positions; returns the extrapolated positions/s of a whole
@@ -308,6 +348,9 @@ def run_ours(args, rank, world):
     adj = None
     if not args.skip_adjoint:
         adj = adjoint_measure(ctx, torch)
+    tem = None
+    if not args.skip_tem:
+        tem = tem_measure(ctx)
     line = {"metric": "probe-positions/s", "value": value, "unit": "positions/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded frozen-phonon SrTiO3)",
@@ -322,7 +365,7 @@ def run_ours(args, rank, world):
             "gpu_launches": st["launches"], "clocks": clk,
             "e2e": {"value": e2e, "unit": "positions/s", "h2d_bytes_per_step": int(cfgs[0].nbytes),
                     "d2h_bytes_per_step": int(host_det.nbytes)},
-            "cpu_baseline": cpu, "plain_gpu": plain, "adjoint": adj}
+            "cpu_baseline": cpu, "plain_gpu": plain, "adjoint": adj, "tem": tem}
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0
@@ -338,6 +381,7 @@ def main():
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--npix", type=int, default=64, help="scan raster edge; 64 is the workload")
     ap.add_argument("--skip-adjoint", action="store_true")
+    ap.add_argument("--skip-tem", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -18,6 +18,11 @@
  *                        :2867, :2890)
  *   qs_collect          collectIntensity for one k-space wave
  *                       (stem3/stemlib.h:41; stem3/stemlib.cpp:2576)
+ *   qs_tem_run          doTEM's configuration loop (stem3/stem3.cpp:2354-2710):
+ *                       plane wave, every frozen-phonon configuration as one
+ *                       batch, exit-wave intensity average, and the
+ *                       through-focus CTF images of
+ *                       GUI_Matlab/simImageFromWave.m:57-73
  *
  * Conventions
  *   - Plain C types only; complex numbers are interleaved float pairs
@@ -194,6 +199,44 @@ int qs_multislice_run(qs_ctx *ctx, const qs_params *p, const float *trans, const
  * the transmission stack stays on the device. */
 int qs_stem_run(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom,
                 const qs_batch *batch, float *det_images, float *diffpats);
+
+/* ------------------------------------------------------------------ TEM */
+/* Objective-lens transfer of GUI_Matlab/simImageFromWave.m:57-73 (lengths in
+ * Angstrom, angles in radians, spatial frequencies in 1/Angstrom):
+ *   H(k) = A(k) exp(-i pi (lambda (df + astig cos 2(phi - astigPhi)) k^2
+ *                          + lambda^3 Cs k^4 / 2))
+ *          exp(-2 (focalSpread lambda k^2)^2)                 temporal envelope
+ *          exp(-(pi alpha df + pi alpha lambda^2 Cs k^2)^2 k^2) spatial envelope
+ * A(k) = 1 for k < kmax - edge/2, 0 for k > kmax + edge/2, and a raised
+ * cosine between (edge = 0: the script's hard aperture k^2 < kmax^2;
+ * kmax <= 0: no aperture).  df is the defocus of each image. */
+typedef struct qs_ctf {
+    double Cs;           /* spherical aberration */
+    double astig;        /* two-fold astigmatism magnitude */
+    double astigPhi;     /* its azimuth */
+    double focalSpread;  /* Cc * dE/E */
+    double alpha;        /* illumination semi-angle */
+    double kmax;         /* objective aperture radius */
+    double edge;         /* width of the aperture's cosine edge */
+} qs_ctf;
+
+/* doTEM for `nconf` frozen-phonon configurations (stem3/stem3.cpp:2354-2710).
+ * atoms holds the configurations back to back, natoms[c] atoms each (host).
+ * Every configuration gets its own slice stack (make3DSlices +
+ * initSTEMSlices), and all of them run as one batch from doTEM's untilted
+ * incident plane wave psi = 1 (:2403-2406) to their exit waves.
+ * Outputs (HOST buffers, each may be NULL):
+ *   mean_intensity  [nx][ny] float, the mean over configurations of
+ *                   |psi_exit|^2 (doTEM's image.img holds (nx*ny)^2 times
+ *                   its running mean: an unnormalised FFT round trip,
+ *                   :2583-2608)
+ *   ctf_images      [ndef][nx][ny] float, the mean over configurations of
+ *                   |IFFT(FFT(psi_exit) H_df)|^2 for df = defoci[i]
+ *   exit_waves      [nconf][nx][ny] c64 (doTEM's wave.img per configuration)
+ * Configurations are batched as device memory allows. */
+int qs_tem_run(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, const int *natoms, int nconf,
+               const qs_ctf *ctf, int ndef, const double *defoci, float *mean_intensity,
+               float *ctf_images, float *exit_waves);
 
 /* ------------------------------------------------------------ gradients */
 /* initSTEMSlices' phase grating for a given potential stack V

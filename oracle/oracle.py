@@ -9,7 +9,7 @@ import subprocess
 
 import numpy as np
 
-from qstem_gb300 import abi
+from qstem_gb300 import abi, config
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
@@ -133,3 +133,54 @@ def run_reference(qsc_path, outdir, run=True):
     if r.returncode != 0:
         raise RuntimeError("reference harness failed: " + r.stdout[-2000:] + r.stderr[-2000:])
     return outdir
+
+
+def ctf_transfer(p, ctf, df):
+    """Objective-lens transfer H(k) of GUI_Matlab/simImageFromWave.m:57-73 in
+    float64, in FFT order on the wave grid (k = (i < n/2 ? i : i - n)/(n dx),
+    the script's fftshifted [-n/2, n/2) grid).  ctf: dict of the qs_ctf
+    fields; the aperture gets an optional raised-cosine edge of width
+    `edge` (the script's hard aperture when edge = 0)."""
+    lam = config.wavelength(float(np.float32(p.v0)))
+    c = dict(Cs=0.0, astig=0.0, astigPhi=0.0, focalSpread=0.0, alpha=0.0, kmax=0.0, edge=0.0)
+    c.update(ctf or {})
+    ix = np.arange(p.nx)
+    iy = np.arange(p.ny)
+    kx = np.where(ix < p.nx // 2, ix, ix - p.nx) / (p.nx * float(np.float32(p.resolutionX)))
+    ky = np.where(iy < p.ny // 2, iy, iy - p.ny) / (p.ny * float(np.float32(p.resolutionY)))
+    KX, KY = np.meshgrid(kx, ky, indexing="ij")
+    k2 = KX ** 2 + KY ** 2
+    k = np.sqrt(k2)
+    if c["kmax"] > 0:
+        if c["edge"] <= 0:
+            A = (k2 < c["kmax"] ** 2).astype(np.float64)
+        else:
+            lo, hi = c["kmax"] - 0.5 * c["edge"], c["kmax"] + 0.5 * c["edge"]
+            A = np.where(k <= lo, 1.0, np.where(k >= hi, 0.0, 0.5 * (1 + np.cos(np.pi * (k - lo) / c["edge"]))))
+    else:
+        A = np.ones_like(k2)
+    phi = np.arctan2(KY, KX)
+    Et = np.exp(-2.0 * (c["focalSpread"] * lam * k2) ** 2)
+    Es = np.exp(-(np.pi * c["alpha"] * df + np.pi * c["alpha"] * lam ** 2 * c["Cs"] * k2) ** 2 * k2)
+    chi = np.pi * (lam * (df + c["astig"] * np.cos(2 * (phi - c["astigPhi"]))) * k2 + 0.5 * lam ** 3 * c["Cs"] * k2 ** 2)
+    return A * Et * Es * np.exp(-1j * chi)
+
+
+def tem(p, stacks, ctf=None, defoci=()):
+    """doTEM over frozen-phonon configurations (stem3/stem3.cpp:2354-2710):
+    the untilted plane wave psi = 1 (:2403-2406) through each configuration's
+    transmission stack (runMulsSTEM), the mean exit intensity, and the mean
+    over configurations of |IFFT(FFT(psi_exit) H_df)|^2 (float64 FFTs)."""
+    plane = np.zeros((p.nx, p.ny, 2), np.float32)
+    plane[..., 0] = 1.0
+    ews = [run_position(p, T, 0, 0, plane)[0] for T in stacks]
+    mean = np.mean([w[..., 0].astype(np.float64) ** 2 + w[..., 1].astype(np.float64) ** 2 for w in ews], axis=0)
+    imgs = []
+    for df in defoci:
+        H = ctf_transfer(p, ctf, df)
+        acc = np.zeros((p.nx, p.ny))
+        for w in ews:
+            z = w[..., 0].astype(np.float64) + 1j * w[..., 1].astype(np.float64)
+            acc += np.abs(np.fft.ifft2(np.fft.fft2(z) * H)) ** 2
+        imgs.append(acc / len(ews))
+    return mean, (np.array(imgs) if len(imgs) else None), np.array(ews)

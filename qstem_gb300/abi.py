@@ -90,6 +90,14 @@ class QsBatch(ctypes.Structure):
                 ("detPosY", ctypes.POINTER(ctypes.c_int))]
 
 
+class QsCtf(ctypes.Structure):
+    """qs_ctf: objective-lens transfer of GUI_Matlab/simImageFromWave.m:57-73
+    (Angstrom, radians, 1/Angstrom)."""
+    _fields_ = [("Cs", ctypes.c_double), ("astig", ctypes.c_double), ("astigPhi", ctypes.c_double),
+                ("focalSpread", ctypes.c_double), ("alpha", ctypes.c_double), ("kmax", ctypes.c_double),
+                ("edge", ctypes.c_double)]
+
+
 class QsStats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_longlong), ("row_launches", ctypes.c_longlong),
                 ("col_launches", ctypes.c_longlong), ("row_ms", ctypes.c_double), ("col_ms", ctypes.c_double),

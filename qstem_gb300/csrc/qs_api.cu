@@ -14,12 +14,14 @@
 #include "qs_fft.cuh"
 #include "qs_internal.h"
 
+constexpr int kMaxBufs = 32;
+
 struct qs_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     // reusable device buffers, grown on demand
-    void* buf[17] = {};
-    size_t cap[17] = {};
+    void* buf[kMaxBufs] = {};
+    size_t cap[kMaxBufs] = {};
     // profiling
     bool profile = false;
     long long launch_base = 0;
@@ -59,8 +61,9 @@ static int ev_record(qs_ctx* c, size_t* idx) {
 
 enum Buf {
     B_WAVES, B_PROBE, B_PARTIAL, B_POS, B_TABLES, B_TILES, B_TRANS, B_OUT1, B_OUT2, B_OUT3, B_JOBS, B_LUTS,
-    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, NBUF
+    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, NBUF
 };
+static_assert(NBUF <= kMaxBufs, "context buffer table too small");
 
 static int ensure(qs_ctx* c, int which, size_t bytes, void** out) {
     if (bytes == 0) bytes = 16;
@@ -291,7 +294,7 @@ int qs_ctx_destroy(qs_ctx* c) {
     cudaStreamSynchronize(c->stream);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     for (auto& kv : c->luts) cudaFree(kv.second);
-    for (int i = 0; i < 17; i++)
+    for (int i = 0; i < kMaxBufs; i++)
         if (c->buf[i]) cudaFree(c->buf[i]);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -495,9 +498,18 @@ int qs_probe(qs_ctx* c, const qs_params* p, double dx, double dy, float* wave, u
     return QS_OK;
 }
 
-int qs_multislice_run(qs_ctx* c, const qs_params* p, const float* trans_in, const float* probe_in,
-                      const qs_batch* batch, float* det_images, float* diffpats, float* exit_waves, unsigned flags) {
+// The scan of qs_multislice_run, generalised to one transmission stack and
+// one incident wave per wave of the batch (device arrays, consecutive waves
+// transStride / probeStride elements apart; 0 = shared by all waves), which
+// the TEM and CBED batch drivers use.
+static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_in, size_t transStride,
+                             const float* probe_in, size_t probeStride, const qs_batch* batch, float* det_images,
+                             float* diffpats, float* exit_waves, unsigned flags) {
     if (!c || !trans_in || !batch) { set_error("null argument"); return QS_ERR_ARG; }
+    if ((transStride || probeStride) && ((flags & QS_HOST_IO) || (probeStride && !probe_in))) {
+        set_error("per-wave stacks and incident waves must be device arrays");
+        return QS_ERR_ARG;
+    }
     QS_TRY(check_params(p));
     const qs_params& P = *p;
     if (!line_supported(P.nx) || !line_supported(P.ny)) {
@@ -611,11 +623,14 @@ int qs_multislice_run(qs_ctx* c, const qs_params* p, const float* trans_in, cons
         trans = (const float2*)d;
     }
     void* dprobe = nullptr;
-    QS_TRY(ensure(c, B_PROBE, sizeof(float2) * N, &dprobe));
-    if (probe_in) {
+    if (probeStride) {
+        dprobe = (void*)probe_in;
+    } else if (probe_in) {
+        QS_TRY(ensure(c, B_PROBE, sizeof(float2) * N, &dprobe));
         QS_CUDA_TRY(cudaMemcpyAsync(dprobe, probe_in, sizeof(float2) * N,
                                     host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
     } else {
+        QS_TRY(ensure(c, B_PROBE, sizeof(float2) * N, &dprobe));
         QS_TRY(probe_into(c, P, (double)(nx / 2 * P.resolutionX), (double)(ny / 2 * P.resolutionY),
                           (float2*)dprobe));
     }
@@ -672,7 +687,11 @@ int qs_multislice_run(qs_ctx* c, const qs_params* p, const float* trans_in, cons
 
         RowArgs ra{};
         ra.nx = nx; ra.ny = ny; ra.potNx = P.potNx; ra.potNy = P.potNy;
-        ra.nwaves = nb; ra.probe = (const float2*)dprobe; ra.waves = waves; ra.exit_waves = ewOut;
+        ra.nwaves = nb; ra.waves = waves; ra.exit_waves = ewOut;
+        ra.probe = (const float2*)dprobe + p0 * probeStride;
+        ra.probe_stride = probeStride;
+        ra.trans_stride = transStride;
+        const float2* transChunk = trans + p0 * transStride;
         ra.posX = d_px_pos + p0; ra.posY = d_py_pos + p0; ra.tw = tw_y; ra.yA = yA; ra.yB = yB;
         ra.norm = (float)(1.0 / (double)(nx * ny));
         ColArgs ca{};
@@ -708,7 +727,7 @@ int qs_multislice_run(qs_ctx* c, const qs_params* p, const float* trans_in, cons
             }
             return QS_OK;
         };
-        ra.trans_slice = trans;
+        ra.trans_slice = transChunk;
         QS_TRY(rows(ROW_FIRST));
         for (int sl = 0; sl < S; sl++) {
             const int slot = slotOf[sl];
@@ -718,7 +737,7 @@ int qs_multislice_run(qs_ctx* c, const qs_params* p, const float* trans_in, cons
             ca.inverse = (sl < S - 1 || ewOut) ? 1 : 0;
             QS_TRY(cols());
             if (sl < S - 1) {
-                ra.trans_slice = trans + (size_t)(sl + 1) * P.potNx * P.potNy;
+                ra.trans_slice = transChunk + (size_t)(sl + 1) * P.potNx * P.potNy;
                 QS_TRY(rows(ROW_MID));
             }
         }
@@ -740,6 +759,11 @@ int qs_multislice_run(qs_ctx* c, const qs_params* p, const float* trans_in, cons
         QS_CUDA_TRY(cudaMemcpyAsync(det_images, det_dev, sizeof(float) * detElems, cudaMemcpyDeviceToHost, s));
     if (host || (flags & QS_SYNC)) QS_CUDA_TRY(cudaStreamSynchronize(s));
     return QS_OK;
+}
+
+int qs_multislice_run(qs_ctx* c, const qs_params* p, const float* trans_in, const float* probe_in,
+                      const qs_batch* batch, float* det_images, float* diffpats, float* exit_waves, unsigned flags) {
+    return multislice_run_ex(c, p, trans_in, 0, probe_in, 0, batch, det_images, diffpats, exit_waves, flags);
 }
 
 int qs_stem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, const qs_batch* batch,
@@ -776,6 +800,93 @@ int qs_stem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, 
         QS_CUDA_TRY(cudaMemcpyAsync(diffpats, ddp, sizeof(float) * N * batch->npos, cudaMemcpyDeviceToHost,
                                     c->stream));
     QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return QS_OK;
+}
+
+int qs_tem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, const int* natoms, int nconf, const qs_ctf* ctf,
+               int ndef, const double* defoci, float* mean_intensity, float* ctf_images, float* exit_waves) {
+    if (!c || !natoms || nconf < 1) { set_error("null argument or no configurations"); return QS_ERR_ARG; }
+    if (ndef > 0 && ctf_images && (!ctf || !defoci)) { set_error("CTF images need ctf and defoci"); return QS_ERR_ARG; }
+    QS_TRY(check_params(p));
+    const qs_params& P = *p;
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const int nx = P.nx, ny = P.ny;
+    const size_t N = (size_t)nx * ny;
+    const size_t stack = (size_t)P.slices * P.potNx * P.potNy;
+    const int nimg = (ctf_images && ndef > 0) ? ndef : 0;
+    size_t natomTotal = 0;
+    for (int k = 0; k < nconf; k++) {
+        if (natoms[k] < 0) { set_error("negative atom count"); return QS_ERR_ARG; }
+        natomTotal += (size_t)natoms[k];
+    }
+    if (natomTotal > 0 && !atoms) { set_error("null atoms"); return QS_ERR_ARG; }
+
+    // configurations per batch: stack + exit wave + k-space copy + scratch +
+    // the scan's own wave buffer, within the free memory less 1 GiB
+    size_t freeB = 0, totalB = 0;
+    QS_CUDA_TRY(cudaMemGetInfo(&freeB, &totalB));
+    const size_t perConf = sizeof(float2) * (stack + (nimg ? 4 : 2) * N);
+    const size_t fixed = sizeof(float2) * N * (1 + nimg) + sizeof(float) * N * (1 + nimg);
+    const size_t budget = freeB > ((size_t)1 << 30) + fixed ? freeB - ((size_t)1 << 30) - fixed : 0;
+    const int chunk = (int)std::min<size_t>((size_t)nconf, budget / perConf);
+    if (chunk < 1) { set_error("not enough device memory for one configuration"); return QS_ERR_NOMEM; }
+
+    // carve: stacks | exit waves | k-space | scratch | plane wave | H | accumulators
+    auto rup = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t waveB = sizeof(float2) * N;
+    const size_t total = rup(sizeof(float2) * stack * chunk) + rup(waveB * chunk) * (nimg ? 3 : 1) + rup(waveB) +
+                         rup(waveB) + rup(sizeof(float) * N * (1 + nimg));
+    void* base = nullptr;
+    QS_TRY(ensure(c, B_TEM, total, &base));
+    unsigned char* cur = (unsigned char*)base;
+    auto take = [&](size_t b) { void* q = cur; cur += rup(b); return q; };
+    float2* stacks = (float2*)take(sizeof(float2) * stack * chunk);
+    float2* ew = (float2*)take(waveB * chunk);
+    float2* kw = nimg ? (float2*)take(waveB * chunk) : nullptr;
+    float2* scr = nimg ? (float2*)take(waveB * chunk) : nullptr;
+    float2* plane = (float2*)take(waveB);
+    float2* H = (float2*)take(waveB);
+    float* acc = (float*)take(sizeof(float) * N * (1 + nimg));
+    QS_CUDA_TRY(cudaMemsetAsync(acc, 0, sizeof(float) * N * (1 + nimg), s));
+    // doTEM's incident wave without beam tilt (stem3/stem3.cpp:2403-2406)
+    QS_TRY(launch_fill(plane, N, 1.f, 0.f, s));
+
+    const double lambda = wavelength(P.v0);
+    const float inv = 1.0f / (float)nconf;
+    const float invImg = (float)(1.0 / ((double)nconf * (double)N * (double)N));
+    std::vector<int> zeros(chunk, 0);
+    size_t atomOff = 0;
+    for (int c0 = 0; c0 < nconf; c0 += chunk) {
+        const int nb = std::min(chunk, nconf - c0);
+        for (int k = 0; k < nb; k++) {
+            QS_TRY(qs_slices_build(c, p, atoms ? atoms + atomOff : nullptr, natoms[c0 + k],
+                                   (float*)(stacks + (size_t)k * stack), 0));
+            atomOff += (size_t)natoms[c0 + k];
+        }
+        qs_batch bt{nb, zeros.data(), zeros.data(), zeros.data(), zeros.data()};
+        QS_TRY(multislice_run_ex(c, p, (const float*)stacks, stack, (const float*)plane, 0, &bt, nullptr, nullptr,
+                                 (float*)ew, 0));
+        QS_TRY(launch_acc_intensity(ew, nb, N, inv, acc, s));
+        if (exit_waves)
+            QS_CUDA_TRY(cudaMemcpyAsync(exit_waves + 2 * (size_t)c0 * N, ew, waveB * nb, cudaMemcpyDeviceToHost, s));
+        if (nimg) {
+            // FFT(psi) once, then per defocus IFFT(FFT(psi) H) and |.|^2
+            QS_CUDA_TRY(cudaMemcpyAsync(kw, ew, waveB * nb, cudaMemcpyDeviceToDevice, s));
+            QS_TRY(fft2d(kw, nx, ny, nb, false, s));
+            for (int d = 0; d < nimg; d++) {
+                QS_TRY(launch_ctf_table(nx, ny, P.resolutionX, P.resolutionY, lambda, *ctf, defoci[d], H, s));
+                QS_TRY(launch_mul_table(kw, H, nb, N, scr, s));
+                QS_TRY(fft2d(scr, nx, ny, nb, true, s));
+                QS_TRY(launch_acc_intensity(scr, nb, N, invImg, acc + (size_t)(1 + d) * N, s));
+            }
+        }
+    }
+    if (mean_intensity)
+        QS_CUDA_TRY(cudaMemcpyAsync(mean_intensity, acc, sizeof(float) * N, cudaMemcpyDeviceToHost, s));
+    if (nimg)
+        QS_CUDA_TRY(cudaMemcpyAsync(ctf_images, acc + N, sizeof(float) * N * nimg, cudaMemcpyDeviceToHost, s));
+    QS_CUDA_TRY(cudaStreamSynchronize(s));
     return QS_OK;
 }
 

@@ -38,7 +38,9 @@ struct RowArgs {
     int nx, ny, potNx, potNy;
     int nwaves;
     const float2* trans_slice;   // potNx x potNy c64 of the slice applied here
+    size_t trans_stride;         // elements between the stacks of consecutive waves (0: one shared stack)
     const float2* probe;         // nx x ny (ROW_FIRST)
+    size_t probe_stride;         // elements between consecutive waves' incident waves (0: shared)
     float2* waves;               // nwaves x nx x ny
     float2* waves_out;           // where ROW_FIRST/ROW_MID write (nullptr: in place)
     float2* exit_waves;          // ROW_LAST destination (may alias waves)
@@ -151,6 +153,16 @@ int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, 
 int launch_atoms_grad(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
                       const qs_params& p, const float* dV, double* grad, cudaStream_t s);
 int launch_grating_from_real(const float* V, float2* trans, size_t n, double scale, cudaStream_t s);
+
+// ------------------------------------------------------------------- TEM
+int launch_fill(float2* w, size_t n, float re, float im, cudaStream_t s);
+// acc[i] += scale * sum over nwaves arrays (n apart) of |w[i]|^2
+int launch_acc_intensity(const float2* w, int nwaves, size_t n, float scale, float* acc, cudaStream_t s);
+// out_b = in_b * H elementwise, b < nwaves
+int launch_mul_table(const float2* in, const float2* H, int nwaves, size_t n, float2* out, cudaStream_t s);
+// objective-lens transfer H(k) of defocus df on an nx x ny grid (FFT order)
+int launch_ctf_table(int nx, int ny, double dx, double dy, double lambda, const qs_ctf& C, double df, float2* H,
+                     cudaStream_t s);
 
 // collectIntensity for one k-space wave (compat entry point)
 int launch_collect(const qs_params& p, const float2* wave_k, const float* kx2, const float* ky2,

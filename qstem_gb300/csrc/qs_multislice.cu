@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(line_threads(N) * ROW_LINES, row_min_blocks(N)
     const SmemRow<Cfg::R0> sm{s_line};
     float2 reg[E];
     if constexpr (MODE == ROW_FIRST) {
-        const float2* src = a.probe + (size_t)x * N;
+        const float2* src = a.probe + b * a.probe_stride + (size_t)x * N;
 #pragma unroll
         for (int e = 0; e < E; ++e) reg[e] = __ldg(src + t + T * e);
     } else {
@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(line_threads(N) * ROW_LINES, row_min_blocks(N)
         for (int e = 0; e < E; ++e) dst[t + T * e] = reg[e];
     } else {
         // transmit (stem3/stemlib.cpp:2867-2888): window at (posX, posY)
-        const float2* tr = a.trans_slice + (size_t)(x + __ldg(a.posX + b)) * a.potNy + __ldg(a.posY + b);
+        const float2* tr = a.trans_slice + b * a.trans_stride + (size_t)(x + __ldg(a.posX + b)) * a.potNy +
+                           __ldg(a.posY + b);
 #pragma unroll
         for (int e = 0; e < E; ++e) reg[e] = cmul(reg[e], __ldg(tr + t + T * e));
         line_fft<Cfg, false>(reg, sm, s_tw, t);

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libqstem_gpu.so")
 EXPORTS = ["qs_ctx_create", "qs_ctx_destroy", "qs_last_error", "qs_abi_version", "qs_ctx_stream",
            "qs_params_finalize", "qs_thickness_count", "qs_lut_build", "qs_slices_build", "qs_probe",
            "qs_multislice_run", "qs_collect", "qs_stem_run", "qs_ctx_profile", "qs_ctx_stats",
-           "qs_multislice_run_noalloc", "qs_phase_grating", "qs_adjoint_run", "qs_atoms_grad"]
+           "qs_multislice_run_noalloc", "qs_phase_grating", "qs_adjoint_run", "qs_atoms_grad", "qs_tem_run"]
 
 _lib = None
 
@@ -59,6 +59,7 @@ def load(path=LIB_PATH):
     L.qs_multislice_run.argtypes = [vp, P, vp, vp, ctypes.POINTER(abi.QsBatch), vp, vp, vp, ctypes.c_uint]
     L.qs_collect.argtypes = [vp, P, vp, vp, vp, ctypes.c_uint]
     L.qs_stem_run.argtypes = [vp, P, vp, ctypes.c_int, ctypes.POINTER(abi.QsBatch), vp, vp]
+    L.qs_tem_run.argtypes = [vp, P, vp, vp, ctypes.c_int, ctypes.POINTER(abi.QsCtf), ctypes.c_int, vp, vp, vp, vp]
     L.qs_ctx_profile.argtypes = [vp, ctypes.c_int]
     L.qs_ctx_stats.argtypes = [vp, ctypes.POINTER(abi.QsStats)]
     L.qs_multislice_run_noalloc.argtypes = [vp, P, vp, vp, ctypes.POINTER(abi.QsBatch), vp, vp, vp]
@@ -198,6 +199,27 @@ class Context:
                                     ctypes.byref(bx), _ptr(det), _ptr(diffpats)))
         del keep
         return det
+
+    def tem(self, p, configs, ctf=None, defoci=(), want_exit_waves=False):
+        """doTEM over frozen-phonon configurations (qs_tem_run).
+
+        configs: list of atom arrays (abi.ATOM_DTYPE), one per configuration.
+        ctf: abi.QsCtf or a dict of its fields; defoci: defocus per CTF image
+        (Angstrom).  Returns (mean |psi_exit|^2, CTF images [ndef][nx][ny] or
+        None, exit waves [nconf][nx][ny][2] or None), host numpy arrays."""
+        arrs = [abi.atoms_to_numpy(a) for a in configs]
+        cat = np.ascontiguousarray(np.concatenate(arrs)) if arrs else np.zeros(0, abi.ATOM_DTYPE)
+        nat = np.array([len(a) for a in arrs], np.int32)
+        mean = np.zeros((p.nx, p.ny), np.float32)
+        defs = np.ascontiguousarray(defoci, dtype=np.float64)
+        imgs = np.zeros((len(defs), p.nx, p.ny), np.float32) if len(defs) else None
+        ew = np.zeros((len(arrs), p.nx, p.ny, 2), np.float32) if want_exit_waves else None
+        c = ctf if isinstance(ctf, abi.QsCtf) else abi.QsCtf(**(ctf or {}))
+        _check(self.lib.qs_tem_run(self.h, ctypes.byref(p), cat.ctypes.data_as(ctypes.c_void_p),
+                                   nat.ctypes.data_as(ctypes.c_void_p), len(arrs), ctypes.byref(c), len(defs),
+                                   defs.ctypes.data_as(ctypes.c_void_p) if len(defs) else None, _ptr(mean),
+                                   _ptr(imgs), _ptr(ew)))
+        return mean, imgs, ew
 
     def phase_grating(self, p, V, out=None):
         """t = exp(i lambda gamma V) for a device potential stack V (torch)."""

@@ -14,9 +14,11 @@ as compressed .npz files:
   det       detector images after doSTEM (STEM cases that run)
   diffpat_* / wave_*   diffAvg_ix_iy.img / mulswav_ix_iy.img the reference
             wrote for the first positions (saveLevel 2)
+  cbed_diffpat  doCBED's diffraction pattern (diffAvg_1.img)
+  exit_wave     doTEM's exit wave (wave.img)
 
-Usage: python tests/golden/make_golden.py   (needs the reference tree; the
-fixtures are committed so the tests do not)
+Usage: python tests/golden/make_golden.py [case ...]   (needs the reference
+tree; the fixtures are committed so the tests do not)
 """
 import json
 import os
@@ -49,7 +51,10 @@ CASES = {
     # CBED geometry (potential grid = wave grid) with the transmission band limit
     "si64cbed": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=5, sliceThickness=2.0,
                      scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
-                     mode="CBED", run=False),
+                     mode="CBED", run=True, saveLevel=1),
+    # TEM: plane wave through a band-limited Si [110] slab (doTEM's exit wave)
+    "si64tem": dict(cell="si", ncell=(4, 3, 4), nx=64, resolutionX=0.06, v0=300.0, slices=7, sliceThickness=2.0,
+                    scan=None, detectors=[], alpha=0.0, bandlimit=True, mode="TEM", run=True),
 }
 
 
@@ -91,7 +96,7 @@ def run_case(name, case, workdir):
                      alpha=case["alpha"], Cs_mm=case.get("Cs_mm", 0.0), defocus_nm=case.get("defocus_nm", 0.0),
                      outputInterval=case.get("outputInterval"), mode=case["mode"],
                      bandlimit=case.get("bandlimit", False), periodicXY=case.get("periodicXY", False),
-                     folder="out", saveLevel=2 if case["run"] else 0, czOffset=case.get("czOffset", 0.0),
+                     folder="out", saveLevel=case.get("saveLevel", 2 if case["run"] else 0), czOffset=case.get("czOffset", 0.0),
                      centerSlices=case.get("centerSlices", False))
     dump = os.path.join(workdir, "dump")
     oracle.run_reference(qsc, dump, run=case["run"])
@@ -124,15 +129,28 @@ def run_case(name, case, workdir):
             out["diffpat_%d_%d" % (ix, iy)] = dp.data.astype(np.float32)
             ww = imageio.read_img(os.path.join(folder, "mulswav_%d_%d.img" % (ix, iy)))
             out["wave_%d_%d" % (ix, iy)] = np.stack([ww.data.real, ww.data.imag], -1).astype(np.float32)
+    folder = os.path.join(workdir, "out")
+    if case["run"] and case["mode"] == "CBED":
+        # doCBED moves the last collectIntensity pattern to diffAvg_1.img (at
+        # save level <= 1; above it runMulsSTEM's extra real-space
+        # collectIntensity, stem3/stemlib.cpp:2475-2482, overwrites it)
+        out["cbed_diffpat"] = imageio.read_img(os.path.join(folder, "diffAvg_1.img")).data.astype(np.float32)
+    if case["run"] and case["mode"] == "TEM":
+        # doTEM writes the exit wave of its first run before it fails on the
+        # diff.img it never wrote (stem3/stem3.cpp:2494-2517, 2545-2547)
+        ww = imageio.read_img(os.path.join(folder, "wave.img"))
+        out["exit_wave"] = np.stack([ww.data.real, ww.data.imag], -1).astype(np.float32)
     out["params_json"] = np.array(json.dumps(p.as_dict()))
     out["meta_json"] = np.array(json.dumps(meta))
     out["case_json"] = np.array(json.dumps({k: v for k, v in case.items()}))
     return out
 
 
-def main():
+def main(names=None):
     oracle.build(quiet=False)
     for name, case in CASES.items():
+        if names and name not in names:
+            continue
         work = tempfile.mkdtemp(prefix="qs_golden_")
         try:
             out = run_case(name, case, work)
@@ -144,4 +162,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

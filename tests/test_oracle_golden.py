@@ -106,3 +106,29 @@ def test_atoms_match_readunitcell(golden):
 def test_thickness_slots(golden):
     p = golden.params
     assert p.thickness_count() == (p.slices // p.outputInterval) + 1
+
+
+def cbed_probe_offset(p):
+    """doCBED's probe position (stem3/stem3.cpp:2096-2100): the scan start
+    minus the potential offset, in the reference's float fields."""
+    return (float(np.float32(p.scanXStart) - np.float32(p.potOffsetX)),
+            float(np.float32(p.scanYStart) - np.float32(p.potOffsetY)))
+
+
+def test_cbed_pattern(golden):
+    if "cbed_diffpat" not in golden:
+        pytest.skip("not a CBED run")
+    p = golden.params
+    pr = oracle.probe(p, *cbed_probe_offset(p))
+    _, _, dp = oracle.run_position(p, golden["T"], 0, 0, pr)
+    assert rel_l2(dp, golden["cbed_diffpat"]) <= TOL
+
+
+def test_tem_exit_wave(golden):
+    if "exit_wave" not in golden:
+        pytest.skip("not a TEM run")
+    p = golden.params
+    plane = np.zeros((p.nx, p.ny, 2), np.float32)
+    plane[..., 0] = 1.0
+    w, _, _ = oracle.run_position(p, golden["T"], 0, 0, plane)
+    assert rel_l2(w, golden["exit_wave"]) <= TOL
