@@ -191,6 +191,52 @@ def tem_measure(ctx, reps=2):
             "mean_intensity": float(mean.mean()), "ctf_image_mean": float(imgs[0].mean())}
 
 
+def cbed_workload():
+    """64 CBED instances from numpy.random.default_rng(20261203 + 200): grid
+    uniform in {256, 384, 512, 768, 1024}^2, material uniform in {fcc Au
+    a = 4.078, Si (cubic diamond, a = 5.431), SrTiO3}, thickness U(5, 50) nm in
+    2 A slices, alpha U(5, 25) mrad, 200 kV, lateral supercell ~40 A
+    (round(40/a) cells), dx = lateral cell / n, transmission band limit on."""
+    rng = np.random.default_rng(SEED + 100)
+    cells = [config.fcc_cell(79, 4.078), config.diamond_cell(), config.srtio3_cell()]
+    jobs = []
+    for _ in range(64):
+        n = int(rng.choice([256, 384, 512, 768, 1024]))
+        cell = cells[int(rng.integers(3))]
+        thick = float(rng.uniform(5.0, 50.0))
+        alpha = float(rng.uniform(5.0, 25.0))
+        slices = max(1, int(round(thick * 10.0 / 2.0)))
+        nl = max(1, int(round(40.0 / cell.a)))
+        nz = int(np.ceil(slices * 2.0 / cell.c))
+        atoms, ax, by, c = config.replicate(cell, nl, nl, nz)
+        p = config.make_params(mode=abi.QS_MODE_CBED, nx=n, resolutionX=float(np.float32(ax)) / n,
+                               resolutionY=float(np.float32(by)) / n, v0=200, slices=slices, sliceThickness=2.0,
+                               ax=ax, by=by, c=c, scan=None, alpha=alpha, bandlimit=True)
+        jobs.append((p, atoms))
+    return jobs
+
+
+def cbed_measure(ctx):
+    """qs_cbed_batch_run end to end (host atoms in, host patterns out) on the
+    64-instance workload, against the same instances run one call each."""
+    jobs = cbed_workload()
+    ctx.cbed_batch(jobs[:2])
+    t0 = time.perf_counter()
+    dps, rep = ctx.cbed_batch(jobs)
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for j in jobs:
+        ctx.cbed_batch([j])
+    t_single = time.perf_counter() - t0
+    ss = sum(p.slices for p, _ in jobs)
+    by = sum(40.0 * p.nx * p.ny * p.slices for p, _ in jobs)
+    return {"workload": "uneven CBED: 64 instances, grids 256-1024, Au/Si/SrTiO3, 5-50 nm, 5-25 mrad, 200 kV",
+            "e2e_ms": t_batch * 1e3, "instances_per_s": len(jobs) / t_batch, "slice_steps": ss,
+            "slice_steps_per_s": ss / t_batch, "multislice_GBps_model": by / t_batch / 1e9,
+            "one_call_per_instance_ms": t_single * 1e3, "batched_over_one_call": t_single / t_batch,
+            "report": rep, "pattern_sum_mean": float(np.mean([d.sum() for d in dps]))}
+
+
 def cpu_sample(p, atoms, npos_sample, threads):
     """Reference CPU algorithm on a bounded sample: one slice-stack build plus
     `npos_sample` positions; returns the extrapolated positions/s of a whole
@@ -351,6 +397,9 @@ def run_ours(args, rank, world):
     tem = None
     if not args.skip_tem:
         tem = tem_measure(ctx)
+    cbed = None
+    if not args.skip_cbed:
+        cbed = cbed_measure(ctx)
     line = {"metric": "probe-positions/s", "value": value, "unit": "positions/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded frozen-phonon SrTiO3)",
@@ -365,7 +414,8 @@ def run_ours(args, rank, world):
             "gpu_launches": st["launches"], "clocks": clk,
             "e2e": {"value": e2e, "unit": "positions/s", "h2d_bytes_per_step": int(cfgs[0].nbytes),
                     "d2h_bytes_per_step": int(host_det.nbytes)},
-            "cpu_baseline": cpu, "plain_gpu": plain, "adjoint": adj, "tem": tem}
+            "cpu_baseline": cpu, "plain_gpu": plain, "adjoint": adj, "tem": tem,
+            "cbed": cbed}
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0
@@ -382,6 +432,7 @@ def main():
     ap.add_argument("--npix", type=int, default=64, help="scan raster edge; 64 is the workload")
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--skip-tem", action="store_true")
+    ap.add_argument("--skip-cbed", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

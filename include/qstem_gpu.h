@@ -18,6 +18,9 @@
  *                        :2867, :2890)
  *   qs_collect          collectIntensity for one k-space wave
  *                       (stem3/stemlib.h:41; stem3/stemlib.cpp:2576)
+ *   qs_cbed_batch_run   doCBED (stem3/stem3.cpp:2048-2344) for many independent
+ *                       instances of mixed grids, thicknesses and optics in
+ *                       one call, admitted by device-memory footprint
  *   qs_tem_run          doTEM's configuration loop (stem3/stem3.cpp:2354-2710):
  *                       plane wave, every frozen-phonon configuration as one
  *                       batch, exit-wave intensity average, and the
@@ -199,6 +202,41 @@ int qs_multislice_run(qs_ctx *ctx, const qs_params *p, const float *trans, const
  * the transmission stack stays on the device. */
 int qs_stem_run(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom,
                 const qs_batch *batch, float *det_images, float *diffpats);
+
+/* ----------------------------------------------------------------- CBED */
+/* One doCBED instance (stem3/stem3.cpp:2048-2344): mode CBED parameters
+ * (potential grid = wave grid, qs_params as readFile fills them), the probe
+ * at (scanXStart - potOffsetX, scanYStart - potOffsetY) (:2096-2100), host
+ * atoms, and the HOST output: the fftshifted |psi(k)|^2/sqrt(nx*ny) after the
+ * last slice (the collectIntensity pattern doCBED writes as diffAvg_1.img at
+ * save level <= 1). */
+typedef struct qs_cbed_job {
+    qs_params params;
+    const qs_atom *atoms;
+    int natom;
+    float *diffpat;          /* [nx][ny] */
+} qs_cbed_job;
+
+/* What the scheduler did. */
+typedef struct qs_cbed_report {
+    int groups;              /* batches of instances sharing grid, sampling, slice thickness and energy */
+    int rounds;              /* admission rounds */
+    int streams;             /* CUDA streams the groups of a round ran on */
+    double admitted_bytes;   /* largest device footprint of a round */
+    double budget_bytes;     /* the admission budget used */
+} qs_cbed_report;
+
+/* Run `njobs` independent CBED instances.  Instances with the same grid,
+ * sampling, slice thickness and energy share propagator tables and run as
+ * one batch (per-instance slice stacks and probes, each wave stopping after
+ * its own slice count); the batches of a round run concurrently on separate
+ * streams.  A round admits whole batches, largest first, while the sum of
+ * their footprints (slice stacks + waves + probes + patterns) fits the budget:
+ * the free device memory less 1 GiB, or max_bytes if that is smaller and not
+ * 0.  An instance that alone does not fit is rejected (QS_ERR_NOMEM).
+ * report may be NULL. */
+int qs_cbed_batch_run(qs_ctx *ctx, const qs_cbed_job *jobs, int njobs, size_t max_bytes,
+                      qs_cbed_report *report);
 
 /* ------------------------------------------------------------------ TEM */
 /* Objective-lens transfer of GUI_Matlab/simImageFromWave.m:57-73 (lengths in

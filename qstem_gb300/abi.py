@@ -98,6 +98,16 @@ class QsCtf(ctypes.Structure):
                 ("edge", ctypes.c_double)]
 
 
+class QsCbedJob(ctypes.Structure):
+    _fields_ = [("params", QsParams), ("atoms", ctypes.c_void_p), ("natom", ctypes.c_int),
+                ("diffpat", ctypes.c_void_p)]
+
+
+class QsCbedReport(ctypes.Structure):
+    _fields_ = [("groups", ctypes.c_int), ("rounds", ctypes.c_int), ("streams", ctypes.c_int),
+                ("admitted_bytes", ctypes.c_double), ("budget_bytes", ctypes.c_double)]
+
+
 class QsStats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_longlong), ("row_launches", ctypes.c_longlong),
                 ("col_launches", ctypes.c_longlong), ("row_ms", ctypes.c_double), ("col_ms", ctypes.c_double),

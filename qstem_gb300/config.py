@@ -62,6 +62,13 @@ def fcc_cell(Z, a, dw=0.0):
                               (Z, .5, 0, .5, dw, 1, 0), (Z, 0, .5, .5, dw, 1, 0)])
 
 
+def diamond_cell(Z=14, a=5.431, dw=0.0):
+    """Cubic diamond (Si by default) along [001]: 8 atoms."""
+    base = [(0, 0, 0), (.5, .5, 0), (.5, 0, .5), (0, .5, .5)]
+    frac = base + [(x + .25, y + .25, z + .25) for x, y, z in base]
+    return UnitCell(a, a, a, [(Z, fx, fy, fz, dw, 1, 0) for fx, fy, fz in frac])
+
+
 def si110_cell(dw=0.0):
     """Si diamond (a = 5.431 A) viewed along [110]: orthorhombic cell
     a/sqrt2 x a x a/sqrt2 with 4 atoms."""

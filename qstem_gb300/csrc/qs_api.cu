@@ -61,7 +61,7 @@ static int ev_record(qs_ctx* c, size_t* idx) {
 
 enum Buf {
     B_WAVES, B_PROBE, B_PARTIAL, B_POS, B_TABLES, B_TILES, B_TRANS, B_OUT1, B_OUT2, B_OUT3, B_JOBS, B_LUTS,
-    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, NBUF
+    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, NBUF
 };
 static_assert(NBUF <= kMaxBufs, "context buffer table too small");
 
@@ -801,6 +801,272 @@ int qs_stem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, 
                                     c->stream));
     QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return QS_OK;
+}
+
+// ------------------------------------------------------------- CBED batch
+namespace {
+
+// Instances that can share one batched scan: the propagator tables, the band
+// and the column tiles depend on exactly these fields.
+struct GridKey {
+    int nx, ny, potNx, potNy;
+    float rx, ry, dz, v0;
+    bool operator<(const GridKey& o) const {
+        return std::tie(nx, ny, potNx, potNy, rx, ry, dz, v0) <
+               std::tie(o.nx, o.ny, o.potNx, o.potNy, o.rx, o.ry, o.dz, o.v0);
+    }
+};
+
+struct CbedUnit {
+    std::vector<int> jobs;   // sorted by slice count, descending
+    int smax = 0;
+    size_t bytes = 0;
+};
+
+size_t rup256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Device bytes of a unit of nb waves of grid N, slice stacks of smax slices.
+size_t cbed_unit_bytes(const qs_params& P, int nb, int smax) {
+    const size_t N = (size_t)P.nx * P.ny, Pp = (size_t)P.potNx * P.potNy;
+    return rup256(sizeof(float2) * Pp * smax * nb) + 2 * rup256(sizeof(float2) * N * nb) +
+           rup256(sizeof(float) * N * nb) + rup256(sizeof(float) * (P.nx + P.ny)) +
+           rup256(sizeof(float2) * (P.nx + P.ny)) + 2 * rup256(sizeof(int) * (P.ny + nb));
+}
+
+}  // namespace
+
+int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_bytes, qs_cbed_report* rep) {
+    if (!c || !jobs || njobs < 1) { set_error("null argument or no jobs"); return QS_ERR_ARG; }
+    for (int i = 0; i < njobs; i++) {
+        const qs_cbed_job& J = jobs[i];
+        QS_TRY(check_params(&J.params));
+        const qs_params& P = J.params;
+        if (!J.diffpat || J.natom < 0 || (J.natom > 0 && !J.atoms)) {
+            set_error("job " + std::to_string(i) + ": null output, atoms or negative atom count");
+            return QS_ERR_ARG;
+        }
+        if (P.potNx != P.nx || P.potNy != P.ny) {
+            set_error("job " + std::to_string(i) + ": CBED needs the potential grid equal to the wave grid");
+            return QS_ERR_ARG;
+        }
+        if (!line_supported(P.nx) || !line_supported(P.ny)) {
+            set_error("job " + std::to_string(i) + ": nx, ny must be in {64,128,256,384,512,768,1024}");
+            return QS_ERR_UNSUPPORTED;
+        }
+    }
+    QS_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+
+    // batches of compatible instances, longest first inside each
+    std::map<GridKey, std::vector<int>> groups;
+    for (int i = 0; i < njobs; i++) {
+        const qs_params& P = jobs[i].params;
+        groups[GridKey{P.nx, P.ny, P.potNx, P.potNy, P.resolutionX, P.resolutionY, P.sliceThickness, P.v0}]
+            .push_back(i);
+    }
+    size_t freeB = 0, totalB = 0;
+    QS_CUDA_TRY(cudaMemGetInfo(&freeB, &totalB));
+    const size_t reserve = (size_t)1 << 30;
+    size_t budget = freeB > reserve ? freeB - reserve : 0;
+    if (max_bytes && max_bytes < budget) budget = max_bytes;
+    // split each batch into units that fit the budget
+    std::vector<CbedUnit> units;
+    for (auto& g : groups) {
+        std::vector<int>& v = g.second;
+        std::stable_sort(v.begin(), v.end(),
+                         [&](int a, int b) { return jobs[a].params.slices > jobs[b].params.slices; });
+        CbedUnit u;
+        for (int i : v) {
+            const qs_params& P = jobs[i].params;
+            const int smax = u.jobs.empty() ? P.slices : u.smax;
+            const size_t b = cbed_unit_bytes(P, (int)u.jobs.size() + 1, smax);
+            if (!u.jobs.empty() && b > budget) {
+                units.push_back(u);
+                u = CbedUnit();
+            }
+            if (u.jobs.empty()) u.smax = P.slices;
+            u.jobs.push_back(i);
+            u.bytes = cbed_unit_bytes(P, (int)u.jobs.size(), u.smax);
+            if (u.bytes > budget) {
+                set_error("job " + std::to_string(i) + " needs " + std::to_string(u.bytes) +
+                          " bytes of device memory, more than the " + std::to_string(budget) + " available");
+                return QS_ERR_NOMEM;
+            }
+        }
+        if (!u.jobs.empty()) units.push_back(u);
+    }
+    // rounds: first fit, largest unit first
+    std::vector<int> order(units.size());
+    for (size_t k = 0; k < order.size(); k++) order[k] = (int)k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return units[a].bytes > units[b].bytes; });
+    std::vector<std::vector<int>> rounds;
+    std::vector<size_t> roundBytes;
+    for (int k : order) {
+        size_t r = 0;
+        while (r < rounds.size() && roundBytes[r] + units[k].bytes > budget) r++;
+        if (r == rounds.size()) { rounds.emplace_back(); roundBytes.push_back(0); }
+        rounds[r].push_back(k);
+        roundBytes[r] += units[k].bytes;
+    }
+    const int nstreams = (int)std::min<size_t>(4, units.size());
+    std::vector<cudaStream_t> streams(nstreams, nullptr);
+    std::vector<cudaEvent_t> evs(nstreams + 1, nullptr);
+    auto cleanup = [&]() {
+        for (auto& e : evs) if (e) cudaEventDestroy(e);
+        for (auto& t : streams) if (t) cudaStreamDestroy(t);
+    };
+    int rc = QS_OK;
+    for (int k = 0; k < nstreams && rc == QS_OK; k++) {
+        if (cudaStreamCreateWithFlags(&streams[k], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming) != cudaSuccess) {
+            set_error("stream or event creation failed");
+            rc = QS_ERR_CUDA;
+        }
+    }
+    if (rc == QS_OK && cudaEventCreateWithFlags(&evs[nstreams], cudaEventDisableTiming) != cudaSuccess) {
+        set_error("event creation failed");
+        rc = QS_ERR_CUDA;
+    }
+    size_t admitted = 0;
+    for (size_t r = 0; r < rounds.size() && rc == QS_OK; r++) {
+        rc = [&]() -> int {
+            void* base = nullptr;
+            QS_TRY(ensure(c, B_CBED, roundBytes[r], &base));
+            admitted = std::max(admitted, roundBytes[r]);
+            unsigned char* cur = (unsigned char*)base;
+            auto take = [&](size_t b) { void* q = cur; cur += rup256(b); return q; };
+            struct Carved {
+                float2 *stacks, *probes, *waves;
+                float* dp;
+                float *kx2, *ky2;
+                float2 *px, *py;
+                int *tiles, *zeros;
+                PropTables tb;
+                std::vector<int> tilesH;
+                int yA, yB;
+            };
+            std::vector<Carved> cv(rounds[r].size());
+            // 1. slice stacks and probes on the context's stream
+            for (size_t k = 0; k < rounds[r].size(); k++) {
+                const CbedUnit& u = units[rounds[r][k]];
+                const qs_params& P0 = jobs[u.jobs[0]].params;
+                const int nb = (int)u.jobs.size();
+                const size_t N = (size_t)P0.nx * P0.ny, Pp = (size_t)P0.potNx * P0.potNy;
+                Carved& C = cv[k];
+                C.stacks = (float2*)take(sizeof(float2) * Pp * u.smax * nb);
+                C.probes = (float2*)take(sizeof(float2) * N * nb);
+                C.waves = (float2*)take(sizeof(float2) * N * nb);
+                C.dp = (float*)take(sizeof(float) * N * nb);
+                C.kx2 = (float*)take(sizeof(float) * (P0.nx + P0.ny));
+                C.ky2 = C.kx2 + P0.nx;
+                C.px = (float2*)take(sizeof(float2) * (P0.nx + P0.ny));
+                C.py = C.px + P0.nx;
+                C.tiles = (int*)take(sizeof(int) * (P0.ny + nb));
+                C.zeros = (int*)take(sizeof(int) * (P0.ny + nb));
+                for (int w = 0; w < nb; w++) {
+                    const qs_cbed_job& J = jobs[u.jobs[w]];
+                    QS_TRY(qs_slices_build(c, &J.params, J.atoms, J.natom, (float*)(C.stacks + (size_t)w * u.smax * Pp),
+                                           0));
+                    // doCBED's probe position (stem3/stem3.cpp:2096-2100)
+                    const double dx = (double)(J.params.scanXStart - J.params.potOffsetX);
+                    const double dy = (double)(J.params.scanYStart - J.params.potOffsetY);
+                    QS_TRY(probe_into(c, J.params, dx, dy, C.probes + (size_t)w * N));
+                }
+                C.tb = prop_tables(P0);
+                const int ny = P0.ny;
+                C.yA = -1;
+                C.yB = ny;
+                for (int iy = 0; iy <= ny / 2; iy++) if (C.tb.ky2[iy] < C.tb.k2max) C.yA = iy;
+                for (int iy = ny - 1; iy > ny / 2; iy--) if (C.tb.ky2[iy] < C.tb.k2max) C.yB = iy;
+                for (int iy = 0; iy < ny; iy++)
+                    if ((C.tb.ky2[iy] < C.tb.k2max) != (iy <= C.yA || iy >= C.yB)) { C.yA = ny; C.yB = ny; break; }
+                const int Cw = col_tile_width(P0.nx);
+                for (int c0 = 0; c0 < ny; c0 += Cw) {
+                    bool any = false;
+                    for (int q = c0; q < c0 + Cw; q++) any |= (q <= C.yA || q >= C.yB);
+                    if (any) C.tilesH.push_back(c0);
+                }
+                QS_CUDA_TRY(cudaMemcpyAsync(C.kx2, C.tb.kx2.data(), sizeof(float) * P0.nx, cudaMemcpyHostToDevice, s));
+                QS_CUDA_TRY(cudaMemcpyAsync(C.ky2, C.tb.ky2.data(), sizeof(float) * ny, cudaMemcpyHostToDevice, s));
+                QS_CUDA_TRY(cudaMemcpyAsync(C.px, C.tb.px.data(), sizeof(float2) * P0.nx, cudaMemcpyHostToDevice, s));
+                QS_CUDA_TRY(cudaMemcpyAsync(C.py, C.tb.py.data(), sizeof(float2) * ny, cudaMemcpyHostToDevice, s));
+                if (!C.tilesH.empty())
+                    QS_CUDA_TRY(cudaMemcpyAsync(C.tiles, C.tilesH.data(), sizeof(int) * C.tilesH.size(),
+                                                cudaMemcpyHostToDevice, s));
+                QS_CUDA_TRY(cudaMemsetAsync(C.zeros, 0, sizeof(int) * (P0.ny + nb), s));
+                QS_CUDA_TRY(cudaMemsetAsync(C.dp, 0, sizeof(float) * N * nb, s));
+                if (!twiddles(P0.nx) || !twiddles(P0.ny)) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
+            }
+            QS_CUDA_TRY(cudaEventRecord(evs[nstreams], s));
+            // 2. the units' scans, concurrently on the side streams
+            for (size_t k = 0; k < rounds[r].size(); k++) {
+                const CbedUnit& u = units[rounds[r][k]];
+                const Carved& C = cv[k];
+                cudaStream_t st = streams[k % nstreams];
+                QS_CUDA_TRY(cudaStreamWaitEvent(st, evs[nstreams], 0));
+                const qs_params& P0 = jobs[u.jobs[0]].params;
+                const int nb = (int)u.jobs.size(), nx = P0.nx, ny = P0.ny;
+                const size_t N = (size_t)nx * ny, Pp = (size_t)P0.potNx * P0.potNy;
+                std::vector<int> S(nb);
+                for (int w = 0; w < nb; w++) S[w] = jobs[u.jobs[w]].params.slices;
+                RowArgs ra{};
+                ra.nx = nx; ra.ny = ny; ra.potNx = P0.potNx; ra.potNy = P0.potNy;
+                ra.probe = C.probes; ra.probe_stride = N; ra.trans_stride = (size_t)u.smax * Pp;
+                ra.waves = C.waves; ra.posX = C.zeros; ra.posY = C.zeros; ra.tw = twiddles(ny);
+                ra.yA = C.yA; ra.yB = C.yB; ra.norm = (float)(1.0 / (double)N);
+                ColArgs ca{};
+                ca.nx = nx; ca.ny = ny; ca.tw = twiddles(nx); ca.kx2 = C.kx2; ca.ky2 = C.ky2; ca.px = C.px;
+                ca.py = C.py; ca.k2max = C.tb.k2max; ca.tiles = C.tiles; ca.ntiles = (int)C.tilesH.size();
+                ca.scaleDiff = 1.0 / std::sqrt((double)N);
+                for (int sl = 0; sl < u.smax; sl++) {
+                    int active = 0, cont = 0;
+                    for (int w = 0; w < nb; w++) {
+                        active += S[w] > sl;
+                        cont += S[w] > sl + 1;
+                    }
+                    ra.nwaves = active;
+                    ra.trans_slice = C.stacks + (size_t)sl * Pp;
+                    QS_TRY(launch_rows(ra, sl == 0 ? ROW_FIRST : ROW_MID, st));
+                    if (cont > 0) {
+                        ca.waves = C.waves; ca.nwaves = cont; ca.inverse = 1; ca.diffpat = nullptr; ca.ndet = 0;
+                        QS_TRY(launch_cols(ca, st));
+                    }
+                    if (active > cont) {
+                        // waves whose last slice this is: the pattern, no inverse
+                        ca.waves = C.waves + (size_t)cont * N; ca.nwaves = active - cont; ca.inverse = 0;
+                        ca.diffpat = C.dp + (size_t)cont * N; ca.ndet = 0;
+                        QS_TRY(launch_cols(ca, st));
+                    }
+                }
+                QS_CUDA_TRY(cudaEventRecord(evs[k % nstreams], st));
+                QS_CUDA_TRY(cudaStreamWaitEvent(s, evs[k % nstreams], 0));
+            }
+            // 3. patterns back to the host
+            for (size_t k = 0; k < rounds[r].size(); k++) {
+                const CbedUnit& u = units[rounds[r][k]];
+                const size_t N = (size_t)jobs[u.jobs[0]].params.nx * jobs[u.jobs[0]].params.ny;
+                for (size_t w = 0; w < u.jobs.size(); w++)
+                    QS_CUDA_TRY(cudaMemcpyAsync(jobs[u.jobs[w]].diffpat, cv[k].dp + w * N, sizeof(float) * N,
+                                                cudaMemcpyDeviceToHost, s));
+            }
+            QS_CUDA_TRY(cudaStreamSynchronize(s));
+            return QS_OK;
+        }();
+    }
+    if (rc != QS_OK) {
+        // leave no side-stream work in flight
+        for (auto& t : streams) if (t) cudaStreamSynchronize(t);
+        cudaStreamSynchronize(s);
+    }
+    cleanup();
+    if (rc == QS_OK && rep) {
+        rep->groups = (int)groups.size();
+        rep->rounds = (int)rounds.size();
+        rep->streams = nstreams;
+        rep->admitted_bytes = (double)admitted;
+        rep->budget_bytes = (double)budget;
+    }
+    return rc;
 }
 
 int qs_tem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, const int* natoms, int nconf, const qs_ctf* ctf,

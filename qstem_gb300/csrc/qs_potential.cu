@@ -325,12 +325,16 @@ int launch_scatter(const AtomJob* d_jobs, int njobs, const float* const* d_luts,
 }
 
 // ------------------------------------------------------- phase grating
-__global__ void phase_grating(float2* __restrict__ t, size_t n, double scale) {
+// t = exp(i scale V).  The reference evaluates cos/sin in double
+// (stem3/stemlib.cpp:2290-2299); here the phase is rounded to float once and
+// sincosf (within 2 ulp) evaluates it: for the phases of real potentials
+// (|scale V| of order 10 rad) the result differs by ~1e-6 absolute, and FP64
+// transcendentals run at a small fraction of the FP32 rate on this part.
+__global__ void phase_grating(float2* __restrict__ t, size_t n, float scale) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const double vz = t[i].x * scale;
-        double sn, cs;
-        sincos(vz, &sn, &cs);
-        t[i] = make_float2((float)cs, (float)sn);
+        float sn, cs;
+        sincosf(t[i].x * scale, &sn, &cs);
+        t[i] = make_float2(cs, sn);
     }
 }
 
@@ -339,17 +343,17 @@ int launch_phase_grating(float2* trans, size_t n, double scale, cudaStream_t s) 
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    phase_grating<<<sms * 8, 256, 0, s>>>(trans, n, scale);
+    phase_grating<<<sms * 8, 256, 0, s>>>(trans, n, (float)scale);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;
 }
 
-__global__ void grating_from_real(const float* __restrict__ V, float2* __restrict__ t, size_t n, double scale) {
+__global__ void grating_from_real(const float* __restrict__ V, float2* __restrict__ t, size_t n, float scale) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        double sn, cs;
-        sincos((double)V[i] * scale, &sn, &cs);
-        t[i] = make_float2((float)cs, (float)sn);
+        float sn, cs;
+        sincosf(V[i] * scale, &sn, &cs);
+        t[i] = make_float2(cs, sn);
     }
 }
 
@@ -358,7 +362,7 @@ int launch_grating_from_real(const float* V, float2* trans, size_t n, double sca
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    grating_from_real<<<sms * 8, 256, 0, s>>>(V, trans, n, scale);
+    grating_from_real<<<sms * 8, 256, 0, s>>>(V, trans, n, (float)scale);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;

@@ -22,7 +22,8 @@ LIB_PATH = os.path.join(HERE, "_lib", "libqstem_gpu.so")
 EXPORTS = ["qs_ctx_create", "qs_ctx_destroy", "qs_last_error", "qs_abi_version", "qs_ctx_stream",
            "qs_params_finalize", "qs_thickness_count", "qs_lut_build", "qs_slices_build", "qs_probe",
            "qs_multislice_run", "qs_collect", "qs_stem_run", "qs_ctx_profile", "qs_ctx_stats",
-           "qs_multislice_run_noalloc", "qs_phase_grating", "qs_adjoint_run", "qs_atoms_grad", "qs_tem_run"]
+           "qs_multislice_run_noalloc", "qs_phase_grating", "qs_adjoint_run", "qs_atoms_grad", "qs_tem_run",
+           "qs_cbed_batch_run"]
 
 _lib = None
 
@@ -60,6 +61,7 @@ def load(path=LIB_PATH):
     L.qs_collect.argtypes = [vp, P, vp, vp, vp, ctypes.c_uint]
     L.qs_stem_run.argtypes = [vp, P, vp, ctypes.c_int, ctypes.POINTER(abi.QsBatch), vp, vp]
     L.qs_tem_run.argtypes = [vp, P, vp, vp, ctypes.c_int, ctypes.POINTER(abi.QsCtf), ctypes.c_int, vp, vp, vp, vp]
+    L.qs_cbed_batch_run.argtypes = [vp, vp, ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(abi.QsCbedReport)]
     L.qs_ctx_profile.argtypes = [vp, ctypes.c_int]
     L.qs_ctx_stats.argtypes = [vp, ctypes.POINTER(abi.QsStats)]
     L.qs_multislice_run_noalloc.argtypes = [vp, P, vp, vp, ctypes.POINTER(abi.QsBatch), vp, vp, vp]
@@ -199,6 +201,28 @@ class Context:
                                     ctypes.byref(bx), _ptr(det), _ptr(diffpats)))
         del keep
         return det
+
+    def cbed_batch(self, jobs, max_bytes=0):
+        """doCBED for many instances (qs_cbed_batch_run).
+
+        jobs: list of (params, atoms).  Returns (list of diffraction patterns
+        [nx][ny] as host numpy arrays, report dict)."""
+        arr = (abi.QsCbedJob * len(jobs))()
+        keep, outs = [], []
+        for k, (p, atoms) in enumerate(jobs):
+            a = abi.atoms_to_numpy(atoms)
+            dp = np.zeros((p.nx, p.ny), np.float32)
+            keep.append(a)
+            outs.append(dp)
+            arr[k].params = p
+            arr[k].atoms = a.ctypes.data_as(ctypes.c_void_p).value if len(a) else None
+            arr[k].natom = len(a)
+            arr[k].diffpat = dp.ctypes.data_as(ctypes.c_void_p).value
+        rep = abi.QsCbedReport()
+        _check(self.lib.qs_cbed_batch_run(self.h, ctypes.cast(arr, ctypes.c_void_p), len(jobs), int(max_bytes),
+                                          ctypes.byref(rep)))
+        del keep
+        return outs, {n: getattr(rep, n) for n, _ in abi.QsCbedReport._fields_}
 
     def tem(self, p, configs, ctf=None, defoci=(), want_exit_waves=False):
         """doTEM over frozen-phonon configurations (qs_tem_run).

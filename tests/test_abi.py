@@ -63,3 +63,31 @@ def test_params_finalize_and_thickness(L):
     assert np.float32(p.detectors[0].k2Inside) == np.float32(k_in)
     assert np.float32(p.detectors[0].k2Outside) == np.float32(k_out)
     assert L.qs_thickness_count(ctypes.byref(p)) == 20 // 7 + 1
+
+
+def test_struct_sizes_and_offsets_match_the_c_compiler(tmp_path):
+    """ctypes mirrors of the header's structs against gcc's own layout."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"qs_atom": abi.QsAtom, "qs_detector": abi.QsDetector, "qs_params": abi.QsParams,
+               "qs_batch": abi.QsBatch, "qs_stats": abi.QsStats, "qs_ctf": abi.QsCtf,
+               "qs_cbed_job": abi.QsCbedJob, "qs_cbed_report": abi.QsCbedReport}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "qstem_gpu.h"', "int main(void) {"]
+    for cname, ct in structs.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f in ct._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f[0], cname, f[0]))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, ct in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(ct), cname
+        for f in ct._fields_:
+            assert got[(cname, f[0])] == getattr(ct, f[0]).offset, (cname, f[0])
