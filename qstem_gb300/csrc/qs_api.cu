@@ -61,7 +61,7 @@ static int ev_record(qs_ctx* c, size_t* idx) {
 
 enum Buf {
     B_WAVES, B_PROBE, B_PARTIAL, B_POS, B_TABLES, B_TILES, B_TRANS, B_OUT1, B_OUT2, B_OUT3, B_JOBS, B_LUTS,
-    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, NBUF
+    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, NBUF
 };
 static_assert(NBUF <= kMaxBufs, "context buffer table too small");
 
@@ -424,11 +424,21 @@ int qs_slices_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int nat
         const double mm0 = (double)(1.0f + P.v0 / 511.0f);
         QS_TRY(launch_phase_grating(trans, nTrans, mm0 * wavelength(P.v0), c->stream));
         if (P.bandlimittrans) {
-            if (!line_supported(P.potNx) || !line_supported(P.potNy)) {
-                set_error("band-limiting the transmission function needs potNx, potNy in {64,128,256,384,512,768,1024}");
-                return QS_ERR_UNSUPPORTED;
-            }
             const int nx = P.potNx, ny = P.potNy;
+            // line FFTs where they exist, DFT matrix products otherwise
+            const bool lines = line_supported(nx) && line_supported(ny);
+            float2* scr = nullptr;
+            int scrSlices = 0;
+            if (!lines) {
+                scrSlices = std::min(P.slices, 16);
+                void* d = nullptr;
+                QS_TRY(ensure(c, B_DFT, sizeof(float2) * (size_t)nx * ny * scrSlices, &d));
+                scr = (float2*)d;
+            }
+            auto xform = [&](bool inverse) -> int {
+                return lines ? fft2d(trans, nx, ny, P.slices, inverse, c->stream)
+                             : dft2d(trans, nx, ny, P.slices, inverse, scr, scrSlices, c->stream);
+            };
             std::vector<float> kx2(nx), ky2(ny);
             for (int ix = 0; ix < nx; ix++) {
                 float kx = (ix > nx / 2) ? (float)(ix - nx) / P.potSizeX : (float)ix / P.potSizeX;
@@ -447,10 +457,10 @@ int qs_slices_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int nat
             std::vector<float> both(kx2);
             both.insert(both.end(), ky2.begin(), ky2.end());
             QS_CUDA_TRY(cudaMemcpyAsync(dt, both.data(), sizeof(float) * both.size(), cudaMemcpyHostToDevice, c->stream));
-            QS_TRY(fft2d(trans, nx, ny, P.slices, false, c->stream));
+            QS_TRY(xform(false));
             QS_TRY(launch_bandlimit_mask(trans, P.slices, nx, ny, (float*)dt, (float*)dt + nx, k2max,
                                          1.0 / (nx * ny), c->stream));
-            QS_TRY(fft2d(trans, nx, ny, P.slices, true, c->stream));
+            QS_TRY(xform(true));
             QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
         }
     }

@@ -82,6 +82,11 @@ int launch_det_finalize(const double* partial, int nwaves, int ntiles, int ndet,
 
 // generic in-place 2-D transform of `howmany` n0 x n1 arrays
 int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t s);
+// in-place 2-D DFT of any size as batched complex matrix products (for
+// potential grids the line FFTs do not cover); scratch holds scratch_slices
+// n0 x n1 arrays
+int dft2d(float2* data, int n0, int n1, int howmany, bool inverse, float2* scratch, int scratch_slices,
+          cudaStream_t s);
 // inter-pass twiddle table of the length-n line transform (per-pass layout of
 // LineCfg), device-resident and cached per device and n; twiddle_host fills
 // the same table on the host

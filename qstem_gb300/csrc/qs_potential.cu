@@ -368,16 +368,19 @@ int launch_grating_from_real(const float* V, float2* trans, size_t n, double sca
     return QS_OK;
 }
 
+// The reference scales by fftScale = 1/(potNx*potNy) in double and stores
+// float (stem3/stemlib.cpp:2315-2329); the float product differs from that
+// by at most one rounding of the scale (none for power-of-two grids).
 __global__ void bandlimit_mask(float2* __restrict__ t, int slices, int potNx, int potNy,
                                const float* __restrict__ kx2, const float* __restrict__ ky2, float k2max,
-                               double fftScale) {
+                               float fftScale) {
     const size_t n = (size_t)slices * potNx * potNy;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const int iy = (int)(i % potNy);
         const int ix = (int)((i / potNy) % potNx);
         const float k2 = ky2[iy] + kx2[ix];
         float2 v = t[i];
-        if (k2 < k2max) v = make_float2((float)(v.x * fftScale), (float)(v.y * fftScale));
+        if (k2 < k2max) v = make_float2(v.x * fftScale, v.y * fftScale);
         else v = make_float2(0.f, 0.f);
         t[i] = v;
     }
@@ -388,7 +391,7 @@ int launch_bandlimit_mask(float2* trans, int slices, int potNx, int potNy, const
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    bandlimit_mask<<<sms * 8, 256, 0, s>>>(trans, slices, potNx, potNy, kx2, ky2, k2max, fftScale);
+    bandlimit_mask<<<sms * 8, 256, 0, s>>>(trans, slices, potNx, potNy, kx2, ky2, k2max, (float)fftScale);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;

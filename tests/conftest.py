@@ -58,7 +58,7 @@ class Golden:
         return self.z.files
 
 
-GOLDEN_CASES = ["sto64", "sto64q", "si64cbed", "si64tem"]
+GOLDEN_CASES = ["sto64", "sto64q", "sto64bl", "si64cbed", "si64tem"]
 
 
 @pytest.fixture(params=GOLDEN_CASES)

@@ -48,6 +48,12 @@ CASES = {
                    detectors=[(10.0, 40.0, "A"), (40.0, 80.0, "B")], alpha=15.0, outputInterval=4,
                    Cs_mm=0.5, defocus_nm=-5.0, czOffset=0.3, centerSlices=True, periodicXY=True,
                    mode="STEM", run=True),
+    # the transmission band limit on a 106 x 110 potential grid (sizes the
+    # line FFTs do not cover: the DFT-matrix path)
+    "sto64bl": dict(cell="sto", ncell=(3, 3, 4), nx=64, resolutionX=0.0915, v0=200.0, slices=6,
+                    sliceThickness=1.9525, scan=(3.905, 7.81, 3, 3.905, 8.2, 3),
+                    detectors=[(0.0, 20.0, "BF"), (40.0, 90.0, "HAADF")], alpha=20.0, bandlimit=True,
+                    mode="STEM", run=True),
     # CBED geometry (potential grid = wave grid) with the transmission band limit
     "si64cbed": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=5, sliceThickness=2.0,
                      scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
