@@ -7,7 +7,8 @@
  *
  *   qs_lut_build        getAtomPotential3D / getAtomPotentialOffset3D
  *                       (stem3/stemlib.h:51-52; stem3/stemlib.cpp:1342, :1548)
- *   qs_slices_build     make3DSlices + initSTEMSlices
+ *   qs_slices_build     make3DSlices + initSTEMSlices (qs_slab_build: one slab
+ *                       of a cell divided along z)
  *                       (stem3/stemlib.h:45, :39; stem3/stemlib.cpp:383, :2199)
  *   qs_probe            probe (stem3/stemlib.h:36; stem3/stemlib.cpp:1952)
  *   qs_multislice_run   the position loop of doSTEM/doCBED around runMulsSTEM,
@@ -55,7 +56,7 @@
 extern "C" {
 #endif
 
-#define QS_ABI_VERSION 1
+#define QS_ABI_VERSION 2
 
 /* status codes */
 #define QS_OK 0
@@ -69,6 +70,8 @@ extern "C" {
 #define QS_HOST_IO 1u           /* buffer pointers are host memory */
 #define QS_OUT_POTENTIAL 2u     /* qs_slices_build: stop after make3DSlices (V in .re) */
 #define QS_SYNC 4u              /* synchronise the stream before returning */
+#define QS_SLAB_STACKS 8u       /* qs_multislice_run with cellDiv > 1: trans holds one
+                                   slices-long stack per slab, back to back */
 
 /* run modes, same numbering as libs/stemtypes_fftw3.h:35-42 */
 #define QS_MODE_STEM 1
@@ -105,7 +108,7 @@ typedef struct qs_params {
     int nx, ny;             /* wave grid */
     int potNx, potNy;       /* potential/transmission grid */
     int slices;             /* slices per stack */
-    int cellDiv;            /* slab count (only 1 supported) */
+    int cellDiv;            /* slabs the cell is divided into along z (NCELLZ: n/cellDiv) */
     int outputInterval;     /* "slices between outputs" */
     int centerSlices, nonPeriod, nonPeriodZ, potential3D, fftpotential;
     int bandlimittrans, tds;
@@ -131,6 +134,9 @@ typedef struct qs_params {
     float electronScale;    /* beam current * dwell time * MILLISEC_PICOAMP */
     int detectorNum;
     qs_detector detectors[QS_MAX_DETECTORS];
+    /* readFile's equalDivs (stem3/stem3.cpp:930-931): with cellDiv > 1, every
+     * slab has the potential of slab 0, built once and reused */
+    int equalDivs;
 } qs_params;
 
 /* A batch of probe positions for qs_multislice_run.  Position p uses the
@@ -175,6 +181,13 @@ int qs_lut_build(qs_ctx *ctx, const qs_params *p, int Znum, double B, int charge
 int qs_slices_build(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom,
                     float *trans, unsigned flags);
 
+/* The same for slab `slab` (0 <= slab < cellDiv) of a cell divided into
+ * cellDiv slabs along z: make3DSlices' successive calls, which offset the
+ * atoms by -slab * slices * sliceThickness (stem3/stemlib.cpp:456-465,
+ * :709-713).  qs_slices_build is slab 0. */
+int qs_slab_build(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom, int slab,
+                  float *trans, unsigned flags);
+
 /* ----------------------------------------------------------------- probe */
 /* nx x ny c64 real-space probe centred at (dx, dy) A. */
 int qs_probe(qs_ctx *ctx, const qs_params *p, double dx, double dy, float *wave,
@@ -183,7 +196,11 @@ int qs_probe(qs_ctx *ctx, const qs_params *p, double dx, double dy, float *wave,
 /* ------------------------------------------------------------ multislice */
 /* Run every position of `batch` through all slices of `trans` (device,
  * slices x potNx x potNy c64), starting from `probe` (device nx x ny c64,
- * NULL = build the centred probe).  Outputs (each may be NULL):
+ * NULL = build the centred probe).  With cellDiv > 1 the wave continues
+ * through cellDiv slabs (doSTEM's slab loop, stem3/stem3.cpp:2795-2949), the
+ * thickness slots counting absolute slices: `trans` is one stack reused for
+ * every slab, or with QS_SLAB_STACKS cellDiv stacks back to back
+ * (qs_slab_build).  Outputs (each may be NULL):
  *   det_images  [tCount+1][detectorNum][scanXN][scanYN] float, the
  *               detector images after the last slice of each thickness
  *               group (collectIntensity's overwrite semantics)

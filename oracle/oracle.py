@@ -43,6 +43,8 @@ def lib():
                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                               ctypes.POINTER(ctypes.c_int)]
         L.qso_potential.argtypes = [P, fp, ctypes.c_int, fp]
+        L.qso_potential_slab.argtypes = [P, fp, ctypes.c_int, ctypes.c_int, fp]
+        L.qso_stem_slabs.argtypes = [P, fp, ctypes.c_int, fp, ctypes.c_int, ctypes.c_int, fp, fp, fp, ctypes.c_int]
         L.qso_transmission.argtypes = [P, fp]
         L.qso_probe.argtypes = [P, ctypes.c_double, ctypes.c_double, fp]
         L.qso_run_position.argtypes = [P, fp, ctypes.c_int, ctypes.c_int, fp, fp, fp]
@@ -69,10 +71,11 @@ def lut(p, Z, B=0.0, charged=False):
     return out, ns.value
 
 
-def potential(p, atoms):
+def potential(p, atoms, slab=0):
+    """make3DSlices (slab `slab` of a cell divided into cellDiv slabs)."""
     out = np.zeros((p.slices, p.potNx, p.potNy, 2), np.float32)
     a = abi.atoms_to_numpy(atoms)
-    rc = lib().qso_potential(ctypes.byref(p), _ptr(a), len(a), _ptr(out))
+    rc = lib().qso_potential_slab(ctypes.byref(p), _ptr(a), len(a), int(slab), _ptr(out))
     assert rc == 0, rc
     return out
 
@@ -96,8 +99,9 @@ def probe(p, dx=None, dy=None):
 
 
 def stem(p, trans, probe_wave=None, p0=0, p1=None, det=True, diffpats=False, exit_waves=False,
-         nthreads=0):
-    """The doSTEM position loop for raster positions [p0, p1)."""
+         nthreads=0, slab_stacks=False):
+    """The doSTEM position loop for raster positions [p0, p1), through cellDiv
+    slabs (trans: one stack reused, or cellDiv stacks with slab_stacks)."""
     npix = p.scanXN * p.scanYN
     p1 = npix if p1 is None else p1
     nt = p.thickness_count()
@@ -106,7 +110,8 @@ def stem(p, trans, probe_wave=None, p0=0, p1=None, det=True, diffpats=False, exi
     ew = np.zeros((p1 - p0, p.nx, p.ny, 2), np.float32) if exit_waves else None
     t = np.ascontiguousarray(trans, dtype=np.float32)
     pw = None if probe_wave is None else np.ascontiguousarray(probe_wave, dtype=np.float32)
-    rc = lib().qso_stem(ctypes.byref(p), _ptr(t), _ptr(pw), p0, p1, _ptr(d), _ptr(dp), _ptr(ew), nthreads)
+    rc = lib().qso_stem_slabs(ctypes.byref(p), _ptr(t), int(bool(slab_stacks)), _ptr(pw), p0, p1, _ptr(d), _ptr(dp),
+                              _ptr(ew), nthreads)
     assert rc == 0, rc
     return d, dp, ew
 

@@ -243,7 +243,14 @@ static inline void add_column(float *col, size_t sliceStep, int iaz0, int iaz1, 
 }
 
 int qso_potential(const qs_params *p, const qs_atom *atoms_in, int natom, float *trans) {
-    if (!p->fftpotential || !p->potential3D || p->cellDiv != 1) return QS_ERR_UNSUPPORTED;
+    return qso_potential_slab(p, atoms_in, natom, 0, trans);
+}
+
+/* make3DSlices' call for slab `slab` of a cellDiv-divided cell: the atoms are
+ * offset by -slab * c, c = slices * sliceThickness (stem3/stemlib.cpp:456-465,
+ * :572, :709-713; divCount counts the slabs down from cellDiv - 1). */
+int qso_potential_slab(const qs_params *p, const qs_atom *atoms_in, int natom, int slab, float *trans) {
+    if (!p->fftpotential || !p->potential3D || slab < 0 || slab >= p->cellDiv) return QS_ERR_UNSUPPORTED;
     const int potNx = p->potNx, potNy = p->potNy, slices = p->slices;
     const size_t sliceStep = 2 * (size_t)potNx * potNy; /* floats */
     memset(trans, 0, sizeof(float) * sliceStep * slices);
@@ -265,8 +272,8 @@ int qso_potential(const qs_params *p, const qs_atom *atoms_in, int natom, float 
     for (int iatom = 0; iatom < natom; iatom++) {
         while (iatom < natom && atoms[iatom].Znum == 0) iatom++; /* vacancies, :680 */
         if (iatom >= natom) break;
-        /* :709-713 with cellDiv == 1 */
-        float atomZ = (float)((double)(atoms[iatom].z - c * 0.0f + p->czOffset) -
+        /* :709-713; c*(cellDiv-divCount-1) is c*slab */
+        float atomZ = (float)((double)(atoms[iatom].z - c * (float)slab + p->czOffset) -
                               0.5 * p->sliceThickness * (1 - p->centerSlices));
         atomZ -= p->sliceThickness;
         if (p->nonPeriodZ) { /* :716-731 */
@@ -274,7 +281,7 @@ int qso_potential(const qs_params *p, const qs_atom *atoms_in, int natom, float 
             do {
                 if (atomZ + p->atomRadius + p->sliceThickness >= 0) break;
                 ++iatom;
-                atomZ = (float)((double)(atoms[iatom].z - c * 0.0f + p->czOffset) -
+                atomZ = (float)((double)(atoms[iatom].z - c * (float)slab + p->czOffset) -
                                 0.5 * p->sliceThickness * (1 - p->centerSlices));
                 atomZ -= p->sliceThickness;
             } while (iatom < natom - 1);
@@ -531,8 +538,10 @@ static void prop_free(prop_tables *t) {
     free(t->kx2); free(t->ky2); free(t->pxr); free(t->pxi); free(t->pyr); free(t->pyi);
 }
 
+/* One runMulsSTEM call: the slices of one slab; slice0 = totalSliceCount,
+ * the absolute index of its first slice (stem3/stemlib.cpp:2405). */
 static void run_position(const qs_params *p, const prop_tables *pt, const float *trans, int iPosX,
-                         int iPosY, float *w, float *det, float *diffpat) {
+                         int iPosY, float *w, float *det, float *diffpat, int slice0) {
     const int nx = p->nx, ny = p->ny, potNy = p->potNy;
     const size_t N = (size_t)nx * ny;
     const size_t sliceElems = (size_t)p->potNx * potNy;
@@ -573,11 +582,12 @@ static void run_position(const qs_params *p, const prop_tables *pt, const float 
                 memset(wrow, 0, sizeof(float) * 2 * ny);
             }
         }
-        /* collectIntensity, :2576-2687, slice = islice */
+        /* collectIntensity, :2576-2687, slice = absolute_slice */
         {
+            const int aslice = slice0 + islice;
             int tt;
             if (p->outputInterval == 0) tt = 0;
-            else if (islice < p->slices * p->cellDiv - 1) tt = islice / p->outputInterval;
+            else if (aslice < p->slices * p->cellDiv - 1) tt = aslice / p->outputInterval;
             else tt = tCount;
             float img[QS_MAX_DETECTORS], err[QS_MAX_DETECTORS];
             for (int i = 0; i < p->detectorNum; i++) img[i] = err[i] = 0.0f;
@@ -618,7 +628,7 @@ int qso_run_position(const qs_params *p, const float *trans, int iPosX, int iPos
                      float *det, float *diffpat) {
     prop_tables pt;
     prop_init(p, &pt);
-    run_position(p, &pt, trans, iPosX, iPosY, wave, det, diffpat);
+    run_position(p, &pt, trans, iPosX, iPosY, wave, det, diffpat, 0);
     prop_free(&pt);
     return QS_OK;
 }
@@ -635,6 +645,17 @@ void qso_scan_offsets(const qs_params *p, int ix, int iy, int *iPosX, int *iPosY
 
 int qso_stem(const qs_params *p, const float *trans, const float *probe_in, int p0, int p1,
              float *det_images, float *diffpats, float *exit_waves, int nthreads) {
+    return qso_stem_slabs(p, trans, 0, probe_in, p0, p1, det_images, diffpats, exit_waves, nthreads);
+}
+
+/* doSTEM's slab loop (stem3/stem3.cpp:2795-2949): cellDiv runMulsSTEM calls
+ * per position, the wave carried from one slab to the next (through
+ * mulswav files in the reference), totalSliceCount advancing by slices.
+ * trans: one stack reused for every slab (equal divisions), or with
+ * slab_stacks cellDiv stacks back to back. */
+int qso_stem_slabs(const qs_params *p, const float *trans, int slab_stacks, const float *probe_in, int p0,
+                   int p1, float *det_images, float *diffpats, float *exit_waves, int nthreads) {
+    const size_t stackFloats = 2 * (size_t)p->slices * p->potNx * p->potNy;
     const int nx = p->nx, ny = p->ny;
     const size_t N = (size_t)nx * ny;
     const int nt = qso_thickness_count(p);
@@ -662,7 +683,9 @@ int qso_stem(const qs_params *p, const float *trans, const float *probe_in, int 
             memcpy(w, probe, sizeof(float) * 2 * N);
             memset(det, 0, sizeof(float) * (size_t)nt * (ndet > 0 ? ndet : 1));
             float *dp = diffpats ? diffpats + (size_t)(pos - p0) * N : NULL;
-            run_position(p, &pt, trans, iPosX, iPosY, w, det, dp);
+            for (int k = 0; k < p->cellDiv; k++)
+                run_position(p, &pt, trans + (slab_stacks ? stackFloats * k : 0), iPosX, iPosY, w, det, dp,
+                             k * p->slices);
             if (det_images)
                 for (int t = 0; t < nt; t++)
                     for (int i = 0; i < ndet; i++)

@@ -39,6 +39,8 @@ int qso_lut(const qs_params *p, int Znum, double B, int charged, float *out, int
  * trans: slices*potNx*potNy c64, overwritten with V in .re and 0 in .im.
  * atoms is not modified (a sorted copy is used). */
 int qso_potential(const qs_params *p, const qs_atom *atoms, int natom, float *trans);
+/* the same for slab `slab` of a cell divided into cellDiv slabs along z */
+int qso_potential_slab(const qs_params *p, const qs_atom *atoms, int natom, int slab, float *trans);
 
 /* initSTEMSlices, stem3/stemlib.cpp:2199-2357: V -> exp(i lambda gamma V),
  * band limit when p->bandlimittrans. */
@@ -59,6 +61,10 @@ int qso_run_position(const qs_params *p, const float *trans, int iPosX, int iPos
  * [p0, p1) of the raster p = ix*scanYN + iy, OpenMP over positions.
  * det_images: [tCount+1][ndet][scanXN][scanYN] (may be NULL);
  * diffpats/exit_waves: per position in [p0,p1) (may be NULL). */
+/* doSTEM's slab loop over cellDiv slabs; trans holds cellDiv stacks when
+ * slab_stacks, else one stack reused for every slab. */
+int qso_stem_slabs(const qs_params *p, const float *trans, int slab_stacks, const float *probe, int p0, int p1,
+                   float *det_images, float *diffpats, float *exit_waves, int nthreads);
 int qso_stem(const qs_params *p, const float *trans, const float *probe, int p0, int p1,
              float *det_images, float *diffpats, float *exit_waves, int nthreads);
 

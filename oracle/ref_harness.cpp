@@ -103,6 +103,22 @@ int main(int argc, char **argv) {
     initSTEMSlices(&muls, muls.slices);
     dump("trans.bin", muls.trans[0][0], ntrans * sizeof(fftwf_complex));
 
+    /* A cell divided into unequal slabs: make3DSlices builds slab k on its
+     * k-th call (a static counter, stem3/stemlib.cpp:456-465).  Capture the
+     * other slabs too; after cellDiv calls the counter is back where doSTEM
+     * expects it, so its first call builds slab 0 again. */
+    if (muls.cellDiv > 1 && !muls.equalDivs) {
+        for (int k = 1; k < muls.cellDiv; k++) {
+            char nm[64];
+            make3DSlices(&muls, muls.slices, muls.atomPosFile, NULL);
+            snprintf(nm, sizeof nm, "potential_%d.bin", k);
+            dump(nm, muls.trans[0][0], ntrans * sizeof(fftwf_complex));
+            initSTEMSlices(&muls, muls.slices);
+            snprintf(nm, sizeof nm, "trans_%d.bin", k);
+            dump(nm, muls.trans[0][0], ntrans * sizeof(fftwf_complex));
+        }
+    }
+
     {
         WavePtr wave = WavePtr(new WAVEFUNC(muls.nx, muls.ny, muls.resolutionX, muls.resolutionY));
         probe(&muls, wave, muls.nx / 2 * muls.resolutionX, muls.ny / 2 * muls.resolutionY);
@@ -125,8 +141,8 @@ int main(int argc, char **argv) {
             muls.scanYStop, muls.scanYN);
     fprintf(m, "v0 = %.9g\nalpha = %.9g\nCs = %.9g\nC5 = %.9g\ndf0 = %.9g\n", muls.v0,
             muls.alpha, muls.Cs, muls.C5, muls.df0);
-    fprintf(m, "electronScale = %.9g\noutputInterval = %d\ncellDiv = %d\n", muls.electronScale,
-            muls.outputInterval, muls.cellDiv);
+    fprintf(m, "electronScale = %.9g\noutputInterval = %d\ncellDiv = %d\nequalDivs = %d\n", muls.electronScale,
+            muls.outputInterval, muls.cellDiv, muls.equalDivs);
     fprintf(m, "atomRadius = %.9g\nnonPeriod = %d\nnonPeriodZ = %d\ncenterSlices = %d\n",
             muls.atomRadius, muls.nonPeriod, muls.nonPeriodZ, muls.centerSlices);
     fprintf(m, "bandlimittrans = %d\ntds = %d\nismoth = %d\ndetectorNum = %d\n",

@@ -17,6 +17,7 @@ QS_ERR_TIMEOUT = -5
 QS_HOST_IO = 1
 QS_OUT_POTENTIAL = 2
 QS_SYNC = 4
+QS_SLAB_STACKS = 8
 
 QS_MODE_STEM = 1
 QS_MODE_CBED = 2
@@ -61,7 +62,7 @@ class QsParams(ctypes.Structure):
                  ("scanYStart", ctypes.c_float), ("scanYStop", ctypes.c_float),
                  ("scanXN", ctypes.c_int), ("scanYN", ctypes.c_int),
                  ("electronScale", ctypes.c_float), ("detectorNum", ctypes.c_int),
-                 ("detectors", QsDetector * QS_MAX_DETECTORS)])
+                 ("detectors", QsDetector * QS_MAX_DETECTORS), ("equalDivs", ctypes.c_int)])
 
     def copy(self):
         out = QsParams()

@@ -140,10 +140,12 @@ def make_params(*, mode=abi.QS_MODE_STEM, nx, ny=None, resolutionX, resolutionY=
                 astig_nm=0.0, astig_deg=0.0, outputInterval=None, czOffset=0.0,
                 centerSlices=False, periodicXY=False, periodicZ=False, bandlimit=False,
                 atomRadius=5.0, smooth=True, gaussian=None, aAIS=0.0, beamCurrent=1.0,
-                dwellTime=1.6021773e-4, tds=False):
+                dwellTime=1.6021773e-4, tds=False, cellDiv=1, nCellZ=None):
     """qs_params as stem3's readFile would fill them from the corresponding
     .qsc keys (units as in the .qsc: mm, nm, mrad, deg).
-    scan = (x_start, x_stop, x_pixels, y_start, y_stop, y_pixels) in A."""
+    scan = (x_start, x_stop, x_pixels, y_start, y_stop, y_pixels) in A.
+    cellDiv, nCellZ: "NCELLZ: nCellZ/cellDiv" (slabs along z); nCellZ is only
+    needed for readFile's equalDivs test."""
     ny = nx if ny is None else ny
     resolutionY = resolutionX if resolutionY is None else resolutionY
     p = abi.QsParams()
@@ -154,7 +156,11 @@ def make_params(*, mode=abi.QS_MODE_STEM, nx, ny=None, resolutionX, resolutionY=
     p.slices = slices + (1 if centerSlices else 0)
     p.sliceThickness = F32(sliceThickness)
     p.centerSlices = int(bool(centerSlices))
-    p.cellDiv = 1
+    p.cellDiv = max(1, int(cellDiv))
+    # stem3/stem3.cpp:930-931, in the reference's float fields
+    ncz = p.cellDiv if nCellZ is None else int(nCellZ)
+    p.equalDivs = int((not tds) and ncz % p.cellDiv == 0 and
+                      abs(float(F32(F32(p.slices) * F32(sliceThickness)) - F32(F32(c) / F32(p.cellDiv)))) < 1e-5)
     p.outputInterval = p.slices if (outputInterval is None or outputInterval < 1) else outputInterval
     p.czOffset = F32(czOffset)
     p.ax, p.by, p.c = F32(ax), F32(by), F32(c)
@@ -249,13 +255,14 @@ def scan_offsets(p):
 def write_qsc(path, *, cfg_file, ncell, nx, resolutionX, v0, slices, sliceThickness, scan=None,
               detectors=(), alpha=20.0, Cs_mm=0.0, C5_mm=0.0, defocus_nm=0.0, outputInterval=None,
               mode="STEM", bandlimit=False, periodicXY=False, periodicZ=False, folder="out",
-              saveLevel=0, smooth=True, czOffset=0.0, atomRadius=5.0, centerSlices=False):
+              saveLevel=0, smooth=True, czOffset=0.0, atomRadius=5.0, centerSlices=False, cellDiv=1):
     """A stem3 input file for the same run make_params describes."""
     yn = lambda b: "yes" if b else "no"
     L = ["mode: %s" % mode, "print level: 1", "save level: %d" % saveLevel,
          "filename: %s" % cfg_file, "resolutionX: %r" % float(resolutionX),
          "resolutionY: %r" % float(resolutionX), "NCELLX: %d" % ncell[0], "NCELLY: %d" % ncell[1],
-         "NCELLZ: %d" % ncell[2], "v0: %r" % float(v0), "tds: no",
+         ("NCELLZ: %d/%d" % (ncell[2], cellDiv) if cellDiv > 1 else "NCELLZ: %d" % ncell[2]),
+         "v0: %r" % float(v0), "tds: no",
          "slice-thickness: %r" % float(sliceThickness), "slices: %d" % slices,
          "center slices: %s" % yn(centerSlices)]
     if outputInterval:

@@ -96,7 +96,7 @@ static int check_params(const qs_params* p) {
         set_error("resolution, slice thickness and v0 must be positive");
         return QS_ERR_ARG;
     }
-    if (p->cellDiv != 1) { set_error("cellDiv > 1 (slab decomposition) is not supported"); return QS_ERR_UNSUPPORTED; }
+    if (p->cellDiv < 1) { set_error("cellDiv must be >= 1"); return QS_ERR_ARG; }
     if (p->outputInterval < 1) { set_error("outputInterval must be >= 1"); return QS_ERR_ARG; }
     if (p->detectorNum < 0 || p->detectorNum > QS_MAX_DETECTORS) { set_error("detectorNum out of range"); return QS_ERR_ARG; }
     return QS_OK;
@@ -145,7 +145,7 @@ static int thickness_count(const qs_params& p) { return (p.slices * p.cellDiv) /
 // Debye-Waller factor of the element's first contributing atom, as the
 // reference's per-element LUT cache keeps it (:1417).
 static void plan_atoms(const qs_params& P, const qs_atom* atoms, int natom, std::vector<AtomJob>& jobs,
-                       std::vector<std::pair<int, double>>& lutKeys) {
+                       std::vector<std::pair<int, double>>& lutKeys, int slab = 0) {
     std::vector<int> order(natom);
     for (int i = 0; i < natom; i++) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return atoms[a].z < atoms[b].z; });
@@ -159,7 +159,9 @@ static void plan_atoms(const qs_params& P, const qs_atom* atoms, int natom, std:
     lutKeys.clear();
     std::map<int, int> lutIndex;          // key Z*2+charged -> index
     auto atomz = [&](int i) {
-        float z = (float)((double)(at[i].z - cz * 0.0f + P.czOffset) - 0.5 * P.sliceThickness * (1 - P.centerSlices));
+        // slab `slab` sees the atoms shifted down by slab * cz (stem3/stemlib.cpp:709-713)
+        float z = (float)((double)(at[i].z - cz * (float)slab + P.czOffset) -
+                          0.5 * P.sliceThickness * (1 - P.centerSlices));
         z -= P.sliceThickness;
         return z;
     };
@@ -386,8 +388,17 @@ int qs_lut_build(qs_ctx* c, const qs_params* p, int Z, double B, int charged, fl
 
 int qs_slices_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, float* trans_out,
                     unsigned flags) {
+    return qs_slab_build(c, p, atoms, natom, 0, trans_out, flags);
+}
+
+int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, int slab, float* trans_out,
+                  unsigned flags) {
     if (!c || !trans_out || (natom > 0 && !atoms)) { set_error("null argument"); return QS_ERR_ARG; }
     QS_TRY(check_params(p));
+    if (slab < 0 || slab >= p->cellDiv) {
+        set_error("slab " + std::to_string(slab) + " outside 0.." + std::to_string(p->cellDiv - 1));
+        return QS_ERR_ARG;
+    }
     if (!p->fftpotential || !p->potential3D) {
         set_error("only the 3-D FFT-integrated potential (one time integration, potential3D) is supported");
         return QS_ERR_UNSUPPORTED;
@@ -405,7 +416,7 @@ int qs_slices_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int nat
 
     std::vector<AtomJob> jobs;
     std::vector<std::pair<int, double>> lutKeys;
-    plan_atoms(P, atoms, natom, jobs, lutKeys);
+    plan_atoms(P, atoms, natom, jobs, lutKeys, slab);
 
     if (!jobs.empty()) {
         int Nz = 0, Nr = 0, ns = 0;
@@ -587,12 +598,17 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     }
     const int ntiles = (int)tiles.size();
 
-    // output slices: slice s writes thickness slot tOf[s] (collectIntensity's
+    // absolute slices: cellDiv slabs of S slices (doSTEM's slab loop,
+    // stem3/stem3.cpp:2795-2949, with runMulsSTEM's absolute_slice =
+    // totalSliceCount + islice, stem3/stemlib.cpp:2405)
+    const int D = P.cellDiv, SA = S * D;
+    const bool slabStacks = D > 1 && (flags & QS_SLAB_STACKS);
+    // output slices: slice a writes thickness slot tOf[a] (collectIntensity's
     // t, stem3/stemlib.cpp:2597-2610); a slot keeps its last writer only
-    std::vector<int> lastWriter(nT, -1), slotOf(S, -1);
-    for (int sl = 0; sl < S; sl++) {
-        const int t = (sl < S * P.cellDiv - 1) ? sl / P.outputInterval : nT - 1;
-        lastWriter[t] = sl;
+    std::vector<int> lastWriter(nT, -1), slotOf(SA, -1);
+    for (int a = 0; a < SA; a++) {
+        const int t = (a < SA - 1) ? a / P.outputInterval : nT - 1;
+        if (t < nT) lastWriter[t] = a;
     }
     for (int t = 0; t < nT; t++) if (lastWriter[t] >= 0) slotOf[lastWriter[t]] = t;
     const bool wantDet = ndet > 0 && det_images != nullptr;
@@ -624,7 +640,7 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     QS_CUDA_TRY(cudaMemcpyAsync(d_dy_pos, dyp.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
 
     // transmission and probe
-    const size_t nTrans = (size_t)S * P.potNx * P.potNy;
+    const size_t nTrans = (size_t)S * P.potNx * P.potNy * (slabStacks ? D : 1);
     const float2* trans = (const float2*)trans_in;
     if (host) {
         void* d = nullptr;
@@ -737,17 +753,19 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
             }
             return QS_OK;
         };
-        ra.trans_slice = transChunk;
+        // stack slice of absolute slice a
+        auto sliceOf = [&](int a) { return transChunk + (size_t)(slabStacks ? a : a % S) * P.potNx * P.potNy; };
+        ra.trans_slice = sliceOf(0);
         QS_TRY(rows(ROW_FIRST));
-        for (int sl = 0; sl < S; sl++) {
-            const int slot = slotOf[sl];
+        for (int a = 0; a < SA; a++) {
+            const int slot = slotOf[a];
             ca.ndet = (wantDet && slot >= 0) ? ndet : 0;
             ca.partial = (double*)dpart + (slot >= 0 ? (size_t)slot * partPerT : 0);
-            ca.diffpat = (sl == S - 1) ? dpOut : nullptr;
-            ca.inverse = (sl < S - 1 || ewOut) ? 1 : 0;
+            ca.diffpat = (a == SA - 1) ? dpOut : nullptr;
+            ca.inverse = (a < SA - 1 || ewOut) ? 1 : 0;
             QS_TRY(cols());
-            if (sl < S - 1) {
-                ra.trans_slice = transChunk + (size_t)(sl + 1) * P.potNx * P.potNy;
+            if (a < SA - 1) {
+                ra.trans_slice = sliceOf(a + 1);
                 QS_TRY(rows(ROW_MID));
             }
         }
@@ -782,10 +800,14 @@ int qs_stem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, 
     QS_TRY(check_params(p));
     QS_CUDA_TRY(cudaSetDevice(c->device));
     const size_t nTrans = (size_t)p->slices * p->potNx * p->potNy;
+    // doSTEM builds slab 0 once when the slabs are equal, else every slab
+    // (stem3/stem3.cpp:2795-2812)
+    const int nslab = (p->cellDiv > 1 && !p->equalDivs) ? p->cellDiv : 1;
     void* dstack = nullptr;
-    // B_DIFF_IN doubles as the configuration's transmission stack here
-    QS_TRY(ensure(c, B_DIFF_IN, sizeof(float2) * nTrans, &dstack));
-    QS_TRY(qs_slices_build(c, p, atoms, natom, (float*)dstack, 0));
+    // B_DIFF_IN doubles as the configuration's transmission stacks here
+    QS_TRY(ensure(c, B_DIFF_IN, sizeof(float2) * nTrans * nslab, &dstack));
+    for (int k = 0; k < nslab; k++)
+        QS_TRY(qs_slab_build(c, p, atoms, natom, k, (float*)dstack + 2 * nTrans * k, 0));
     const qs_params& P = *p;
     const int nT = thickness_count(P);
     const int npix = P.scanXN * P.scanYN;
@@ -802,7 +824,8 @@ int qs_stem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, 
         QS_TRY(ensure(c, B_OUT2, sizeof(float) * N * batch->npos, &d));
         ddp = (float*)d;
     }
-    QS_TRY(qs_multislice_run(c, p, (const float*)dstack, nullptr, batch, ddet, ddp, nullptr, 0));
+    QS_TRY(qs_multislice_run(c, p, (const float*)dstack, nullptr, batch, ddet, ddp, nullptr,
+                             nslab > 1 ? QS_SLAB_STACKS : 0));
     if (ddet)
         QS_CUDA_TRY(cudaMemcpyAsync(det_images, ddet, sizeof(float) * (size_t)nT * P.detectorNum * npix,
                                     cudaMemcpyDeviceToHost, c->stream));
@@ -858,6 +881,10 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
         if (P.potNx != P.nx || P.potNy != P.ny) {
             set_error("job " + std::to_string(i) + ": CBED needs the potential grid equal to the wave grid");
             return QS_ERR_ARG;
+        }
+        if (P.cellDiv != 1) {
+            set_error("job " + std::to_string(i) + ": cells divided into slabs (cellDiv > 1) are not supported");
+            return QS_ERR_UNSUPPORTED;
         }
         if (!line_supported(P.nx) || !line_supported(P.ny)) {
             set_error("job " + std::to_string(i) + ": nx, ny must be in {64,128,256,384,512,768,1024}");
@@ -1085,6 +1112,10 @@ int qs_tem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, const int* n
     if (ndef > 0 && ctf_images && (!ctf || !defoci)) { set_error("CTF images need ctf and defoci"); return QS_ERR_ARG; }
     QS_TRY(check_params(p));
     const qs_params& P = *p;
+    if (P.cellDiv != 1) {
+        set_error("TEM: cells divided into slabs (cellDiv > 1) are not supported");
+        return QS_ERR_UNSUPPORTED;
+    }
     QS_CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
     const int nx = P.nx, ny = P.ny;
@@ -1193,6 +1224,10 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     }
     if (P.bandlimittrans) {
         set_error("adjoint: band-limited transmission functions are not supported");
+        return QS_ERR_UNSUPPORTED;
+    }
+    if (P.cellDiv != 1) {
+        set_error("adjoint: cells divided into slabs (cellDiv > 1) are not supported");
         return QS_ERR_UNSUPPORTED;
     }
     const int npos = batch->npos, S = P.slices, nx = P.nx, ny = P.ny;
@@ -1388,6 +1423,10 @@ int qs_atoms_grad(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
     QS_TRY(check_params(p));
     if (!p->fftpotential || !p->potential3D) {
         set_error("only the 3-D FFT-integrated potential is supported");
+        return QS_ERR_UNSUPPORTED;
+    }
+    if (p->cellDiv != 1) {
+        set_error("atom gradients: cells divided into slabs (cellDiv > 1) are not supported");
         return QS_ERR_UNSUPPORTED;
     }
     QS_CUDA_TRY(cudaSetDevice(c->device));

@@ -23,7 +23,7 @@ EXPORTS = ["qs_ctx_create", "qs_ctx_destroy", "qs_last_error", "qs_abi_version",
            "qs_params_finalize", "qs_thickness_count", "qs_lut_build", "qs_slices_build", "qs_probe",
            "qs_multislice_run", "qs_collect", "qs_stem_run", "qs_ctx_profile", "qs_ctx_stats",
            "qs_multislice_run_noalloc", "qs_phase_grating", "qs_adjoint_run", "qs_atoms_grad", "qs_tem_run",
-           "qs_cbed_batch_run"]
+           "qs_cbed_batch_run", "qs_slab_build"]
 
 _lib = None
 
@@ -56,6 +56,7 @@ def load(path=LIB_PATH):
                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                ctypes.POINTER(ctypes.c_int), ctypes.c_uint]
     L.qs_slices_build.argtypes = [vp, P, vp, ctypes.c_int, vp, ctypes.c_uint]
+    L.qs_slab_build.argtypes = [vp, P, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_uint]
     L.qs_probe.argtypes = [vp, P, ctypes.c_double, ctypes.c_double, vp, ctypes.c_uint]
     L.qs_multislice_run.argtypes = [vp, P, vp, vp, ctypes.POINTER(abi.QsBatch), vp, vp, vp, ctypes.c_uint]
     L.qs_collect.argtypes = [vp, P, vp, vp, vp, ctypes.c_uint]
@@ -145,14 +146,15 @@ class Context:
         return out, ns.value
 
     # ------------------------------------------------------------ slices
-    def slices(self, p, atoms, out=None, potential_only=False, sync=True):
-        """make3DSlices + initSTEMSlices -> trans[slices][potNx][potNy][2]."""
+    def slices(self, p, atoms, out=None, potential_only=False, sync=True, slab=0):
+        """make3DSlices + initSTEMSlices -> trans[slices][potNx][potNy][2]
+        (slab `slab` of a cell divided into cellDiv slabs)."""
         a = abi.atoms_to_numpy(atoms)
         if out is None:
             out = np.zeros((p.slices, p.potNx, p.potNy, 2), np.float32)
         flags = _io_flags(out) | (abi.QS_OUT_POTENTIAL if potential_only else 0) | (abi.QS_SYNC if sync else 0)
-        _check(self.lib.qs_slices_build(self.h, ctypes.byref(p), a.ctypes.data_as(ctypes.c_void_p), len(a),
-                                        _ptr(out), flags))
+        _check(self.lib.qs_slab_build(self.h, ctypes.byref(p), a.ctypes.data_as(ctypes.c_void_p), len(a),
+                                      int(slab), _ptr(out), flags))
         return out
 
     # ------------------------------------------------------------- probe
@@ -169,7 +171,7 @@ class Context:
 
     # -------------------------------------------------------- multislice
     def multislice(self, p, trans, probe=None, positions=None, det=None, diffpats=None, exit_waves=None,
-                   want_det=True, want_diffpats=False, want_exit_waves=False, sync=True):
+                   want_det=True, want_diffpats=False, want_exit_waves=False, sync=True, slab_stacks=False):
         """Run probe positions through the slice stack.
 
         positions: None (the full scan raster) or (iPosX, iPosY, detPosX, detPosY) int arrays.
@@ -184,7 +186,8 @@ class Context:
             diffpats = np.zeros((npos, p.nx, p.ny), np.float32) if host else None
         if exit_waves is None and want_exit_waves:
             exit_waves = np.zeros((npos, p.nx, p.ny, 2), np.float32) if host else None
-        flags = _io_flags(trans, probe, det, diffpats, exit_waves) | (abi.QS_SYNC if sync else 0)
+        flags = (_io_flags(trans, probe, det, diffpats, exit_waves) | (abi.QS_SYNC if sync else 0) |
+                 (abi.QS_SLAB_STACKS if slab_stacks else 0))
         _check(self.lib.qs_multislice_run(self.h, ctypes.byref(p), _ptr(trans), _ptr(probe), ctypes.byref(bx),
                                           _ptr(det), _ptr(diffpats), _ptr(exit_waves), flags))
         del keep

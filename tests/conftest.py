@@ -24,7 +24,8 @@ def params_from_dict(d):
     for name, _ in abi.QsParams._fields_:
         if name == "detectors":
             continue
-        setattr(p, name, d[name])
+        # fixtures made before a field existed hold its default
+        setattr(p, name, d.get(name, 0))
     for i, (rin, rout, sx, sy) in enumerate(d["detectors"]):
         p.detectors[i].rInside, p.detectors[i].rOutside = rin, rout
         p.detectors[i].shiftX, p.detectors[i].shiftY = sx, sy
@@ -58,12 +59,20 @@ class Golden:
         return self.z.files
 
 
-GOLDEN_CASES = ["sto64", "sto64q", "sto64bl", "si64cbed", "si64tem"]
+GOLDEN_CASES = ["sto64", "sto64q", "sto64bl", "sto64d2", "sto64d2u", "si64cbed", "si64tem"]
 
 
 @pytest.fixture(params=GOLDEN_CASES)
 def golden(request):
     return Golden(request.param)
+
+
+def scan_stack(golden):
+    """The transmission the scan of a fixture runs through: every slab's stack
+    of an unequally divided cell (with QS_SLAB_STACKS), else the one stack."""
+    if "T_slabs" in golden:
+        return np.ascontiguousarray(golden["T_slabs"]), True
+    return golden["T"], False
 
 
 def rel_l2(a, b):

@@ -14,6 +14,8 @@ as compressed .npz files:
   det       detector images after doSTEM (STEM cases that run)
   diffpat_* / wave_*   diffAvg_ix_iy.img / mulswav_ix_iy.img the reference
             wrote for the first positions (saveLevel 2)
+  V_slabs, T_slabs   every slab's potential/transmission of an unequally
+            divided cell (cellDiv > 1)
   cbed_diffpat  doCBED's diffraction pattern (diffAvg_1.img)
   exit_wave     doTEM's exit wave (wave.img)
 
@@ -54,6 +56,17 @@ CASES = {
                     sliceThickness=1.9525, scan=(3.905, 7.81, 3, 3.905, 8.2, 3),
                     detectors=[(0.0, 20.0, "BF"), (40.0, 90.0, "HAADF")], alpha=20.0, bandlimit=True,
                     mode="STEM", run=True),
+    # a cell divided into two equal slabs (NCELLZ: 4/2): slab 0's stack reused,
+    # thickness slots counted over both
+    "sto64d2": dict(cell="sto", ncell=(3, 3, 4), nx=64, resolutionX=0.0915, v0=200.0, slices=4,
+                    sliceThickness=1.9525, scan=(3.905, 7.81, 3, 3.905, 7.81, 3),
+                    detectors=[(0.0, 20.0, "BF"), (40.0, 90.0, "HAADF")], alpha=20.0, outputInterval=3,
+                    cellDiv=2, mode="STEM", run=True),
+    # two unequal slabs (NCELLZ: 3/2): every slab built from shifted atoms
+    "sto64d2u": dict(cell="sto", ncell=(3, 3, 3), nx=64, resolutionX=0.0915, v0=200.0, slices=3,
+                     sliceThickness=1.9525, scan=(3.905, 7.81, 3, 3.905, 7.81, 3),
+                     detectors=[(0.0, 20.0, "BF"), (40.0, 90.0, "HAADF")], alpha=20.0, cellDiv=2,
+                     mode="STEM", run=True),
     # CBED geometry (potential grid = wave grid) with the transmission band limit
     "si64cbed": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=5, sliceThickness=2.0,
                      scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
@@ -87,7 +100,8 @@ def params_for(case):
                            Cs_mm=case.get("Cs_mm", 0.0), defocus_nm=case.get("defocus_nm", 0.0),
                            outputInterval=case.get("outputInterval"), czOffset=case.get("czOffset", 0.0),
                            centerSlices=case.get("centerSlices", False),
-                           periodicXY=case.get("periodicXY", False), bandlimit=case.get("bandlimit", False))
+                           periodicXY=case.get("periodicXY", False), bandlimit=case.get("bandlimit", False),
+                           cellDiv=case.get("cellDiv", 1), nCellZ=case["ncell"][2])
     return cell, atoms, p
 
 
@@ -103,7 +117,7 @@ def run_case(name, case, workdir):
                      outputInterval=case.get("outputInterval"), mode=case["mode"],
                      bandlimit=case.get("bandlimit", False), periodicXY=case.get("periodicXY", False),
                      folder="out", saveLevel=case.get("saveLevel", 2 if case["run"] else 0), czOffset=case.get("czOffset", 0.0),
-                     centerSlices=case.get("centerSlices", False))
+                     centerSlices=case.get("centerSlices", False), cellDiv=case.get("cellDiv", 1))
     dump = os.path.join(workdir, "dump")
     oracle.run_reference(qsc, dump, run=case["run"])
     meta = dict(l.split(" = ", 1) for l in open(os.path.join(dump, "meta.txt")).read().strip().split("\n"))
@@ -114,6 +128,12 @@ def run_case(name, case, workdir):
     out["V"] = np.fromfile(os.path.join(dump, "potential.bin"), np.float32).reshape(shp)
     out["T"] = np.fromfile(os.path.join(dump, "trans.bin"), np.float32).reshape(shp)
     out["probe"] = np.fromfile(os.path.join(dump, "probe.bin"), np.float32).reshape(p.nx, p.ny, 2)
+    if p.cellDiv > 1 and not p.equalDivs:
+        # slabs 1..cellDiv-1 of an unequally divided cell
+        out["V_slabs"] = np.stack([out["V"]] + [np.fromfile(os.path.join(dump, "potential_%d.bin" % k), np.float32)
+                                                .reshape(shp) for k in range(1, p.cellDiv)])
+        out["T_slabs"] = np.stack([out["T"]] + [np.fromfile(os.path.join(dump, "trans_%d.bin" % k), np.float32)
+                                                .reshape(shp) for k in range(1, p.cellDiv)])
     for line in open(os.path.join(dump, "lut_dims.txt")):
         Z, Nz, Nr, ns = map(int, line.split())
         out["lut_%d" % Z] = np.fromfile(os.path.join(dump, "lut_%d.bin" % Z), np.float32).reshape(Nz, Nr, 2)[..., 0]

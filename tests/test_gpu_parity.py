@@ -11,7 +11,7 @@ Tolerances (relative L2 unless noted):
 import numpy as np
 import pytest
 
-from conftest import Golden, rel_l2
+from conftest import Golden, rel_l2, scan_stack
 from oracle import oracle
 from qstem_gb300 import config, lib
 
@@ -73,9 +73,11 @@ def test_multislice_vs_reference(ctx, golden):
     if "det" not in golden:
         pytest.skip("case does not run the scan")
     p = golden.params
-    det, dps, ews = ctx.multislice(p, golden["T"], golden["probe"], want_diffpats=True, want_exit_waves=True)
+    T, slabs = scan_stack(golden)
+    det, dps, ews = ctx.multislice(p, T, golden["probe"], want_diffpats=True, want_exit_waves=True,
+                                   slab_stacks=slabs)
     assert rel_l2(det, golden["det"]) <= TOL_MS
-    ocd, ocp, ocw = oracle.stem(p, golden["T"], golden["probe"], diffpats=True, exit_waves=True)
+    ocd, ocp, ocw = oracle.stem(p, T, golden["probe"], diffpats=True, exit_waves=True, slab_stacks=slabs)
     assert rel_l2(det, ocd) <= TOL_MS
     assert rel_l2(dps, ocp) <= TOL_MS
     assert rel_l2(ews, ocw) <= TOL_MS
@@ -85,6 +87,22 @@ def test_multislice_vs_reference(ctx, golden):
             pos = ix * p.scanYN + iy
             mine = dps[pos] if k.startswith("diffpat_") else ews[pos]
             assert rel_l2(mine, golden[k]) <= TOL_MS, k
+
+
+@pytest.mark.parametrize("name", ["sto64d2", "sto64d2u"])
+def test_slabs_from_atoms(ctx, name):
+    """Cells divided into slabs (NCELLZ n/2): every slab's stack against the
+    reference's, and qs_stem_run (atoms in, detector images out: slab 0 reused
+    for equal divisions, every slab built otherwise) against the reference's
+    detector images of every thickness slot."""
+    g = Golden(name)
+    p = g.params
+    refs = g["T_slabs"] if "T_slabs" in g else [g["T"]]
+    for k, ref in enumerate(refs):
+        assert rel_l2(ctx.slices(p, g["atoms"], slab=k), ref) <= TOL_BUILD, k
+    det = ctx.stem_run(p, g["atoms"])
+    assert det.shape == g["det"].shape
+    assert rel_l2(det, g["det"]) <= TOL_MS
 
 
 def test_end_to_end_from_atoms(ctx):

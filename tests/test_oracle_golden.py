@@ -5,7 +5,7 @@ machine's libm (cos/sin/exp of the host the tests run on)."""
 import numpy as np
 import pytest
 
-from conftest import rel_l2
+from conftest import rel_l2, scan_stack
 from oracle import oracle
 from qstem_gb300 import abi
 
@@ -50,6 +50,18 @@ def test_potential(golden):
     assert np.all(V[..., 1] == 0)
 
 
+def test_slab_potentials(golden):
+    if "V_slabs" not in golden:
+        pytest.skip("not an unequally divided cell")
+    p = golden.params
+    for k in range(p.cellDiv):
+        V = oracle.potential(p, golden["atoms"], slab=k)
+        ref = golden["V_slabs"][k]
+        assert np.abs(V - ref).max() <= TOL * np.abs(ref).max(), k
+        T = oracle.transmission(p, V)
+        assert np.abs(T - golden["T_slabs"][k]).max() <= TOL * 1.0, k
+
+
 def test_transmission(golden):
     T = oracle.transmission(golden.params, golden["V"])
     ref = golden["T"]
@@ -66,7 +78,8 @@ def test_stem_detectors_diffpats_waves(golden):
     if "det" not in golden:
         pytest.skip("case does not run the scan")
     p = golden.params
-    det, dps, ews = oracle.stem(p, golden["T"], golden["probe"], diffpats=True, exit_waves=True)
+    T, slabs = scan_stack(golden)
+    det, dps, ews = oracle.stem(p, T, golden["probe"], diffpats=True, exit_waves=True, slab_stacks=slabs)
     ref = golden["det"]
     assert det.shape == ref.shape
     assert rel_l2(det, ref) <= TOL
@@ -104,8 +117,12 @@ def test_atoms_match_readunitcell(golden):
 
 
 def test_thickness_slots(golden):
+    """tCount + 1 slots over all slices of all slabs (stem3/stemlib.cpp:2591),
+    and the reference's detector arrays have that many."""
     p = golden.params
-    assert p.thickness_count() == (p.slices // p.outputInterval) + 1
+    assert p.thickness_count() == (p.slices * p.cellDiv // p.outputInterval) + 1
+    if "det" in golden:
+        assert golden["det"].shape[0] == p.thickness_count()
 
 
 def cbed_probe_offset(p):
