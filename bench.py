@@ -28,7 +28,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from qstem_gb300 import abi, config  # noqa: E402
+from qstem_gb300 import abi, config, phonons  # noqa: E402
 
 WORKLOAD = "stem-batched-512: SrTiO3 10x10x20, 512^2, 40 slices, 64x64 positions, 4 detectors, frozen phonons"
 SEED = 20261203 + 100
@@ -46,13 +46,8 @@ def workload_params(npix=64):
 
 def phonon_atoms(atoms, j):
     """Configuration j: Gaussian displacements per Cartesian axis from
-    numpy.random.default_rng(SEED + j)."""
-    rng = np.random.default_rng(SEED + j)
-    a = atoms.copy()
-    sig = np.where(a["Znum"] == 8, 0.09, 0.08).astype(np.float64)
-    for k in ("x", "y", "z"):
-        a[k] = (a[k].astype(np.float64) + rng.standard_normal(len(a)) * sig).astype(np.float32)
-    return a
+    numpy.random.default_rng(SEED + j), 0.09 A for O and 0.08 A for Sr, Ti."""
+    return phonons.displaced(atoms, j, SEED, {8: 0.09, 38: 0.08, 22: 0.08})
 
 
 class ClockSampler:
@@ -299,10 +294,14 @@ def run_ours(args, rank, world):
     trans = torch.empty((p.slices, p.potNx, p.potNy, 2), dtype=torch.float32, device="cuda")
     det = torch.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), dtype=torch.float32, device="cuda")
     cfgs = [phonon_atoms(atoms, rank * (args.steps + args.warmup) + j) for j in range(args.warmup + args.steps)]
+    acc = phonons.ImageSum(det)
+    torch.cuda.synchronize()
 
     def step(j):
         ctx.slices(p, cfgs[j], out=trans, sync=False)
         ctx.multislice(p, trans, det=det, sync=False)
+        with torch.cuda.stream(stream):
+            acc.add(det)  # the frozen-phonon average over configurations
 
     for j in range(args.warmup):
         step(j)
@@ -329,7 +328,8 @@ def run_ours(args, rank, world):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = world * npos * args.steps / (ms / 1000.0)
-    result = det.cpu().numpy()
+    # mean images of every configuration of every rank (one all-reduce)
+    result = acc.mean().cpu().numpy()
     assert np.isfinite(result).all() and result[-1].sum() > 0
 
     # end to end through the C ABI: host atoms in, host detector images out
