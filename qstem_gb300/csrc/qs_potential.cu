@@ -139,40 +139,66 @@ __global__ void lut_fgrid(const double* __restrict__ tab, int nx, int nz, double
 }
 
 // backward DFT along x, keeping outputs ix' < nx/2 (FP64)
-__global__ void lut_dft_x(const float2* __restrict__ temp, int nx, int nz, double2* __restrict__ G) {
-    const int kx = blockIdx.x * blockDim.x + threadIdx.x;
+// exp(2 pi i k/n), k < n, the same sincospi values the direct sums used to
+// evaluate per term; the sums below read them from shared memory (FP64
+// transcendentals run at a small fraction of the FP32 rate on this part).
+__global__ void lut_twiddles(int n, double2* __restrict__ W) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double sn, cs;
+    sincospi(2.0 * k / n, &sn, &cs);
+    W[k] = make_double2(cs, sn);
+}
+
+// Inverse DFT along x of every z row, the kx < nx/2 half kept (FP64).
+__global__ void lut_dft_x(const float2* __restrict__ temp, const double2* __restrict__ Wx, int nx, int nz,
+                          double2* __restrict__ G) {
+    extern __shared__ double2 lsm[];
+    double2* w = lsm;
+    double2* row = lsm + nx;
     const int iz = blockIdx.y;
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        w[i] = Wx[i];
+        const float2 v = temp[(size_t)iz * nx + i];
+        row[i] = make_double2(v.x, v.y);
+    }
+    __syncthreads();
+    const int kx = blockIdx.x * blockDim.x + threadIdx.x;
     if (kx >= nx / 2) return;
     double re = 0, im = 0;
+    int k = 0;  // (ix * kx) mod nx
     for (int ix = 0; ix < nx; ix++) {
-        const float2 v = temp[(size_t)iz * nx + ix];
-        const int k = (int)(((long)ix * kx) % nx);
-        double sn, cs;
-        sincospi(2.0 * k / nx, &sn, &cs);
-        re += v.x * cs - v.y * sn;
-        im += v.x * sn + v.y * cs;
+        const double2 v = row[ix];
+        const double2 t = w[k];
+        re += v.x * t.x - v.y * t.y;
+        im += v.x * t.y + v.y * t.x;
+        k += kx;
+        if (k >= nx) k -= nx;
     }
     G[(size_t)iz * (nx / 2) + kx] = make_double2(re, im);
 }
 
-// backward DFT along z, real part of outputs iz' < nz/2, rounded to float as
-// the reference's single-precision transform stores it
-__global__ void lut_dft_z(const double2* __restrict__ G, int nxh, int nz, float* __restrict__ H) {
+// Inverse DFT along z, real part (FP64).
+__global__ void lut_dft_z(const double2* __restrict__ G, const double2* __restrict__ Wz, int nxh, int nz,
+                          float* __restrict__ H) {
+    extern __shared__ double2 lsm[];
+    for (int i = threadIdx.x; i < nz; i += blockDim.x) lsm[i] = Wz[i];
+    __syncthreads();
     const int kx = blockIdx.x * blockDim.x + threadIdx.x;
     const int kz = blockIdx.y;
     if (kx >= nxh) return;
     double re = 0;
+    int k = 0;  // (iz * kz) mod nz
     for (int iz = 0; iz < nz; iz++) {
         const double2 v = G[(size_t)iz * nxh + kx];
-        const int k = (int)(((long)iz * kz) % nz);
-        double sn, cs;
-        sincospi(2.0 * k / nz, &sn, &cs);
-        re += v.x * cs - v.y * sn;
+        const double2 t = lsm[k];
+        re += v.x * t.x - v.y * t.y;
+        k += kz;
+        if (k >= nz) k -= nz;
     }
     H[(size_t)kz * nxh + kx] = (float)re;
 }
 
-// sum over nzPerSlice sub-samples, clamp at 0, scale (:1503-1522)
 __global__ void lut_zsum(const float* __restrict__ H, int nxh, int nzh, int izOffset, double scale,
                          float* __restrict__ out) {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -218,6 +244,7 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
     const double dqy = charged ? g.dky : g.dkx;
 
     double* d_tab = nullptr;
+    double2* d_W = nullptr;
     float2* d_temp = nullptr;
     double2* d_G = nullptr;
     float* d_H = nullptr;
@@ -230,19 +257,27 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
     cudaError_t e;
     if ((e = cudaMallocAsync(&d_tab, sizeof(double) * 7 * NSF, s)) != cudaSuccess) { fail(e, "alloc"); return rc; }
     if ((e = cudaMallocAsync(&d_temp, sizeof(float2) * (size_t)g.nx * g.nz, s)) != cudaSuccess) fail(e, "alloc");
+    if (!rc && (e = cudaMallocAsync(&d_W, sizeof(double2) * (size_t)(g.nx + g.nz), s)) != cudaSuccess)
+        fail(e, "alloc");
     if (!rc && (e = cudaMallocAsync(&d_G, sizeof(double2) * (size_t)nxh * g.nz, s)) != cudaSuccess) fail(e, "alloc");
     if (!rc && (e = cudaMallocAsync(&d_H, sizeof(float) * (size_t)nxh * nzh, s)) != cudaSuccess) fail(e, "alloc");
     if (!rc) {
         cudaMemcpyAsync(d_tab, tab.data(), sizeof(double) * 7 * NSF, cudaMemcpyHostToDevice, s);
         lut_fgrid<<<dim3((g.nx + 127) / 128, g.nz), 128, 0, s>>>(d_tab, g.nx, g.nz, g.dkx, dqy, g.dkz, g.smax2, B,
                                                               g.zPos, d_temp);
-        lut_dft_x<<<dim3((nxh + 127) / 128, g.nz), 128, 0, s>>>(d_temp, g.nx, g.nz, d_G);
-        lut_dft_z<<<dim3((nxh + 127) / 128, nzh), 128, 0, s>>>(d_G, nxh, g.nz, d_H);
+        lut_twiddles<<<(g.nx + 127) / 128, 128, 0, s>>>(g.nx, d_W);
+        lut_twiddles<<<(g.nz + 127) / 128, 128, 0, s>>>(g.nz, d_W + g.nx);
+        const size_t smx = sizeof(double2) * 2 * (size_t)g.nx, smz = sizeof(double2) * (size_t)g.nz;
+        if (smx > 48 * 1024) cudaFuncSetAttribute(lut_dft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        if (smz > 48 * 1024) cudaFuncSetAttribute(lut_dft_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+        lut_dft_x<<<dim3((nxh + 127) / 128, g.nz), 128, smx, s>>>(d_temp, d_W, g.nx, g.nz, d_G);
+        lut_dft_z<<<dim3((nxh + 127) / 128, nzh), 128, smz, s>>>(d_G, d_W + g.nx, nxh, g.nz, d_H);
         const double scale = 47.8658 * g.dkx * g.dkz / (g.nz);
         lut_zsum<<<dim3((nxh + 127) / 128, nzh), 128, 0, s>>>(d_H, nxh, nzh, g.izOffset, scale, d_out);
         if ((e = cudaGetLastError()) != cudaSuccess) fail(e, "launch");
-        else count_launch(4);
+        else count_launch(6);
     }
+    cudaFreeAsync(d_W, s);
     cudaFreeAsync(d_H, s);
     cudaFreeAsync(d_G, s);
     cudaFreeAsync(d_temp, s);
