@@ -315,6 +315,18 @@ __device__ __forceinline__ void line_fft(float2 (&reg)[Cfg::E], const SM& sm, co
     });
 }
 
+// Register e of a line held by T threads (elements t + T*e) lies, for every
+// t, in [N/3 + 1, ceil(2N/3) - 1]: frequencies that the 2/3 band limit of
+// propagate_slow always removes (|k| < k_max <= N/3 grid steps in each
+// direction, whatever the cell; the margin of one step keeps the float
+// comparisons at |k| = N/3 out of it).  Kernels leave those registers
+// unstored or zero, and the compiler drops the butterfly outputs that only
+// fed them.
+template <int N, int T>
+__host__ __device__ constexpr bool always_out_of_band(int e) {
+    return T * e >= N / 3 + 1 && T * e + T - 1 <= (2 * N + 2) / 3 - 1;
+}
+
 // ------------------------------------------------------- size dispatching
 // One configuration per supported line length.
 template <int N>

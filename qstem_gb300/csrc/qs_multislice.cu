@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(line_threads(N) * ROW_LINES, row_min_blocks(N)
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int y = t + T * e;
-            if (y <= a.yA || y >= a.yB) dst[y] = reg[e];
+            if (!always_out_of_band<N, T>(e) && (y <= a.yA || y >= a.yB)) dst[y] = reg[e];
         }
     }
 }
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
         for (int e = 0; e < E; ++e) {
             const int kx = t + T * e;
             const float kx2 = __ldg(a.kx2 + kx);
-            if (kx2 < a.k2max && (kx2 + ky2) < a.k2max)
+            if (!always_out_of_band<N, T>(e) && kx2 < a.k2max && (kx2 + ky2) < a.k2max)
                 reg[e] = cmul(cmul(reg[e], pyv), __ldg(a.px + kx));
             else
                 reg[e] = make_float2(0.f, 0.f);
