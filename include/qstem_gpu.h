@@ -307,8 +307,9 @@ int qs_phase_grating(qs_ctx *ctx, const qs_params *p, const float *V, float *tra
  * dL/dV for every slice of the potential (device float,
  * slices x potNx x potNy, through t = exp(i*lambda*gamma*V)) and optionally
  * the forward patterns (device, [npos][nx][ny]).  Forward waves are kept every
- * `ckpt` slices and recomputed in between (1 = keep all).  All arrays are
- * device pointers; trans must not be band-limited. */
+ * `ckpt` slices and recomputed in between (1 = keep all; <= 0 = keep all when
+ * they fit in free device memory less 1 GiB, else the smallest interval that
+ * fits).  All arrays are device pointers; trans must not be band-limited. */
 int qs_adjoint_run(qs_ctx *ctx, const qs_params *p, const float *trans, const float *probe,
                    const qs_batch *batch, const float *target, int ckpt, double *loss, float *dL_dV,
                    float *diffpats, unsigned flags);

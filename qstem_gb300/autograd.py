@@ -17,7 +17,7 @@ from . import abi
 
 class MultisliceLoss(torch.autograd.Function):
     @staticmethod
-    def forward(fctx, V, qctx, p, probe, target, positions=None, ckpt=6):
+    def forward(fctx, V, qctx, p, probe, target, positions=None, ckpt=0):
         trans = qctx.phase_grating(p, V.contiguous())
         loss, dV, _ = qctx.adjoint(p, trans, probe, target, positions=positions, ckpt=ckpt)
         fctx.save_for_backward(dV)
@@ -31,7 +31,7 @@ class MultisliceLoss(torch.autograd.Function):
 
 class AtomsLoss(torch.autograd.Function):
     @staticmethod
-    def forward(fctx, xy, qctx, p, atoms, probe, target, positions=None, ckpt=6):
+    def forward(fctx, xy, qctx, p, atoms, probe, target, positions=None, ckpt=0):
         a = abi.atoms_to_numpy(atoms).copy()
         xyn = xy.detach().cpu().numpy()
         a["x"] = xyn[:, 0].astype(np.float32)

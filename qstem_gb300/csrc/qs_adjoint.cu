@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
         const int kx = t + T * e;
         const float kx2 = a.kx2[kx];
         const float2 pxv = a.px[kx];
-        const bool pass = inband && kx2 < a.k2max && (kx2 + ky2) < a.k2max;
+        const bool pass = !always_out_of_band<N, T>(e) && inband && kx2 < a.k2max && (kx2 + ky2) < a.k2max;
         const float2 Bp = pass ? cmul(cmul(reg[e], pyv), pxv) : make_float2(0.f, 0.f);
         const float I = (Bp.x * Bp.x + Bp.y * Bp.y) * sc;
         const size_t ik = (size_t)((kx + a.nx / 2) % a.nx) * a.ny;
@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES)
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int y = t + T * e;
-            if (y <= a.yA || y >= a.yB) grow[y] = cscale(g[e], a.norm);
+            if (!always_out_of_band<N, T>(e) && (y <= a.yA || y >= a.yB)) grow[y] = cscale(g[e], a.norm);
         }
     }
 }

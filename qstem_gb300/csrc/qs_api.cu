@@ -1232,7 +1232,20 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     }
     const int npos = batch->npos, S = P.slices, nx = P.nx, ny = P.ny;
     if (npos < 1) { set_error("batch has no positions"); return QS_ERR_ARG; }
-    if (ckpt < 1) ckpt = 1;
+    if (ckpt < 1) {
+        // automatic: every state kept when they fit (no recomputation), else
+        // the smallest interval whose checkpoints and segment states fit
+        size_t freeB = 0, totalB = 0;
+        QS_CUDA_TRY(cudaMemGetInfo(&freeB, &totalB));
+        const size_t reserve = (size_t)1 << 30;
+        const size_t budget = freeB > reserve ? freeB - reserve : 0;
+        const size_t wave = sizeof(float2) * (size_t)nx * ny * npos;
+        ckpt = S;
+        for (int k = 1; k < S; k++) {
+            const size_t nbufs = 4 + (size_t)((S + k - 1) / k - 1) + (size_t)(k - 1);
+            if (nbufs * wave <= budget) { ckpt = k; break; }
+        }
+    }
     if (ckpt > S) ckpt = S;
     QS_CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;

@@ -256,8 +256,10 @@ class Context:
         _check(self.lib.qs_phase_grating(self.h, ctypes.byref(p), _ptr(V), _ptr(out), abi.QS_SYNC))
         return out
 
-    def adjoint(self, p, trans, probe, target, positions=None, ckpt=6, want_diffpats=False):
-        """Loss sum (I - target)^2 and dL/dV (device torch tensors in and out)."""
+    def adjoint(self, p, trans, probe, target, positions=None, ckpt=0, want_diffpats=False):
+        """Loss sum (I - target)^2 and dL/dV (device torch tensors in and out).
+        ckpt: keep the forward waves every ckpt slices (1: all; 0: all when
+        they fit in device memory, else the smallest interval that fits)."""
         import torch
         bx, keep = _batch(p, positions)
         dV = torch.empty((p.slices, p.potNx, p.potNy), dtype=torch.float32, device=trans.device)

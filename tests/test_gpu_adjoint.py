@@ -78,7 +78,7 @@ def test_dLdV_matches_fp64_autograd(case):
 def test_checkpoint_interval_does_not_change_the_gradient(case):
     c = case
     ref = None
-    for ckpt in (1, 3, 8):
+    for ckpt in (1, 3, 8, 0):  # 0: the automatic interval (every state here)
         loss, dV, dps = c["ctx"].adjoint(c["p"], c["T"], c["probe"], c["target"], positions=c["pos"], ckpt=ckpt,
                                          want_diffpats=True)
         d = dV.cpu().numpy()
