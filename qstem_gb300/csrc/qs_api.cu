@@ -427,7 +427,10 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         QS_CUDA_TRY(cudaMemcpyAsync(dj, jobs.data(), sizeof(AtomJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream));
         // the host vector must outlive the async copy
         QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
-        QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), d_luts, Nz, Nr, ns, P, trans, c->stream));
+        bool charged = false;
+        for (const AtomJob& J : jobs) charged |= J.lutq >= 0;
+        QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), charged, d_luts, Nz, Nr, ns, P, trans,
+                              c->stream));
     }
 
     if (!(flags & QS_OUT_POTENTIAL)) {

@@ -295,19 +295,46 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
 // taken from the float value except within 2e-4 of a knot, where the double
 // computation decides it.  The interpolation weight and the sum then run in
 // float (~1e-7 relative).
+// Shared memory of a CTA: the LUT row offsets of the atom's slices (the same
+// for every pixel), then with STAGED those rows themselves (and the charged
+// table's), so that the interpolation reads shared memory instead of L2.
+template <bool STAGED>
 __global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts, int Nz,
                               int Nr, int nzSub, float dx, float dy, double dr, float drf, float dzs, int potNx,
-                              int potNy, int periodic, float2* __restrict__ trans) {
+                              int potNy, int periodic, int maxRows, float2* __restrict__ trans) {
+    extern __shared__ int s_mem[];
+    int* s_row = s_mem;                                     // [maxRows]
+    float* s_lut = reinterpret_cast<float*>(s_mem + maxRows);  // [maxRows][Nr] (+ [maxRows][Nr] charged)
     const AtomJob J = jobs[blockIdx.x];
     const float* lut = luts[J.lut];
     const float* lutq = J.lutq >= 0 ? luts[J.lutq] : nullptr;
     const float q = J.q;
     const int w = J.iay1 - J.iay0 + 1;
     const int npx = (J.iax1 - J.iax0 + 1) * w;
+    const int nrows = J.iaz1 - J.iaz0 + 1;
     const size_t sliceStep = (size_t)potNx * potNy;
     const int limHi = Nr * (Nz - 1), limLo = -Nr * (Nz - 1), step = nzSub * Nr;
     const double dOffsZ = (double)(((float)(J.iAtomZ + J.iaz0) - J.atomZ / dzs) * (float)nzSub);
     const int iOffsZ0 = ((int)(dOffsZ + 0.5)) * Nr;
+    for (int k = threadIdx.x; k < nrows; k += blockDim.x) {
+        const int iOffsZ = iOffsZ0 + k * step;
+        int row = -1;
+        if (iOffsZ < 0) {
+            if (iOffsZ > limLo) row = -iOffsZ + Nr;
+        } else if (iOffsZ < limHi) {
+            row = iOffsZ;
+        }
+        s_row[k] = row;
+    }
+    __syncthreads();
+    if constexpr (STAGED) {
+        for (int i = threadIdx.x; i < nrows * Nr; i += blockDim.x) {
+            const int k = i / Nr, j = i - k * Nr, row = s_row[k];
+            s_lut[i] = row >= 0 ? __ldg(lut + row + j) : 0.f;
+            if (lutq) s_lut[maxRows * Nr + i] = row >= 0 ? __ldg(lutq + row + j) : 0.f;
+        }
+        __syncthreads();
+    }
     for (int k = threadIdx.x; k < npx; k += blockDim.x) {
         const int iax = J.iax0 + k / w;
         const int iay = J.iay0 + k % w;
@@ -329,31 +356,47 @@ __global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* con
         const int cy = periodic ? ((iay % potNy) + potNy) % potNy : iay;
         float* dst = &trans[(size_t)(J.iAtomZ + J.iaz0) * sliceStep + (size_t)cx * potNy + cy].x;
         const float w0 = 1.f - ddr;
-        int iOffsZ = iOffsZ0;
-        for (int iaz = J.iaz0; iaz <= J.iaz1; iaz++) {
-            int row = -1;
-            if (iOffsZ < 0) {
-                if (iOffsZ > limLo) row = -iOffsZ + Nr;
-            } else if (iOffsZ < limHi) {
-                row = iOffsZ;
-            }
-            if (row >= 0) {
-                float v = w0 * __ldg(lut + row + ir) + ddr * __ldg(lut + row + ir + 1);
+        for (int r = 0; r < nrows; r++, dst += 2 * sliceStep) {
+            const int row = s_row[r];
+            if (row < 0) continue;
+            float v;
+            if constexpr (STAGED) {
+                const float* L = s_lut + r * Nr + ir;
+                v = w0 * L[0] + ddr * L[1];
+                if (lutq) v += q * (w0 * L[maxRows * Nr] + ddr * L[maxRows * Nr + 1]);
+            } else {
+                v = w0 * __ldg(lut + row + ir) + ddr * __ldg(lut + row + ir + 1);
                 if (lutq) v += q * (w0 * __ldg(lutq + row + ir) + ddr * __ldg(lutq + row + ir + 1));
-                if (v != 0.f) atomicAdd(dst, v);
             }
-            dst += 2 * sliceStep;
-            iOffsZ += step;
+            if (v != 0.f) atomicAdd(dst, v);
         }
     }
 }
 
-int launch_scatter(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
-                   const qs_params& p, float2* trans, cudaStream_t s) {
+int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* const* d_luts, int Nz, int Nr,
+                   int nzSub, const qs_params& p, float2* trans, cudaStream_t s) {
     if (njobs <= 0) return QS_OK;
     const double dr = p.resolutionX / OVERSAMP;
-    scatter_atoms<<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr, (float)dr,
-                                        p.sliceThickness, p.potNx, p.potNy, p.nonPeriod ? 0 : 1, trans);
+    // every atom's z range spans at most 2 iRadZ + 1 slices
+    const int maxRows = 2 * (int)ceilf(p.atomRadius / p.sliceThickness) + 1;
+    const size_t staged = sizeof(int) * maxRows + sizeof(float) * (size_t)maxRows * Nr * (charged ? 2 : 1);
+    const int periodic = p.nonPeriod ? 0 : 1;
+    if (staged <= 160 * 1024) {
+        static size_t attr = 0;
+        if (staged > attr) {
+            QS_CUDA_TRY(cudaFuncSetAttribute(scatter_atoms<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)staged));
+            attr = staged;
+        }
+        scatter_atoms<true><<<njobs, 256, staged, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY,
+                                                       dr, (float)dr, p.sliceThickness, p.potNx, p.potNy, periodic,
+                                                       maxRows, trans);
+    } else {
+        scatter_atoms<false><<<njobs, 256, sizeof(int) * maxRows, s>>>(d_jobs, d_luts, Nz, Nr, nzSub,
+                                                                        p.resolutionX, p.resolutionY, dr, (float)dr,
+                                                                        p.sliceThickness, p.potNx, p.potNy,
+                                                                        periodic, maxRows, trans);
+    }
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;
