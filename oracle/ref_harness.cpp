@@ -143,6 +143,10 @@ int main(int argc, char **argv) {
             muls.alpha, muls.Cs, muls.C5, muls.df0);
     fprintf(m, "electronScale = %.9g\noutputInterval = %d\ncellDiv = %d\nequalDivs = %d\n", muls.electronScale,
             muls.outputInterval, muls.cellDiv, muls.equalDivs);
+    fprintf(m, "astigMag = %.9g\nastigAngle = %.9g\na33 = %.9g\nphi33 = %.9g\nCc = %.9g\n",
+            muls.astigMag, muls.astigAngle, muls.a33, muls.phi33, muls.Cc);
+    fprintf(m, "aAIS = %.9g\ngaussFlag = %d\ngaussScale = %.9g\navgRuns = %d\n", muls.aAIS,
+            muls.gaussFlag, muls.gaussScale, muls.avgRuns);
     fprintf(m, "atomRadius = %.9g\nnonPeriod = %d\nnonPeriodZ = %d\ncenterSlices = %d\n",
             muls.atomRadius, muls.nonPeriod, muls.nonPeriodZ, muls.centerSlices);
     fprintf(m, "bandlimittrans = %d\ntds = %d\nismoth = %d\ndetectorNum = %d\n",

@@ -172,8 +172,33 @@ def run_case(name, case, workdir):
     return out
 
 
+def qsc_case():
+    """readFile on a hand-written .qsc + .cfg (tests/golden/qsc/): the MULS
+    fields it derives and the atoms of readUnitCell, with the input texts,
+    to pin qstem_gb300.qsc.read_qsc."""
+    src = os.path.join(HERE, "qsc")
+    work = tempfile.mkdtemp(prefix="qs_golden_")
+    try:
+        for f in ("run.qsc", "cell.cfg"):
+            shutil.copy(os.path.join(src, f), work)
+        dump = os.path.join(work, "dump")
+        oracle.run_reference(os.path.join(work, "run.qsc"), dump, run=False)
+        meta = dict(l.split(" = ", 1) for l in open(os.path.join(dump, "meta.txt")).read().strip().split("\n"))
+        out = {"atoms": np.fromfile(os.path.join(dump, "atoms.bin"), dtype=abi.ATOM_DTYPE),
+               "meta_json": np.array(json.dumps(meta)),
+               "qsc_text": np.array(open(os.path.join(src, "run.qsc")).read()),
+               "cfg_text": np.array(open(os.path.join(src, "cell.cfg")).read())}
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    path = os.path.join(HERE, "qscread.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 def main(names=None):
     oracle.build(quiet=False)
+    if not names or "qscread" in names:
+        qsc_case()
     for name, case in CASES.items():
         if names and name not in names:
             continue
