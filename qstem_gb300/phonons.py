@@ -26,11 +26,16 @@ def rank_configurations(nconf, rank, world):
 
 def displaced(atoms, j, seed, sigma):
     """Configuration j: Gaussian displacements per Cartesian axis.
-    sigma: one value for every atom, or a dict {Znum: sigma} (others 0)."""
+    sigma: one value for every atom, a dict {Znum: sigma} (others 0), or a
+    per-atom array (e.g. the Einstein model's, qsc.QscRun.einstein_sigma)."""
     rng = np.random.default_rng(seed + j)
     a = abi.atoms_to_numpy(atoms).copy()
     if isinstance(sigma, dict):
         sig = np.array([sigma.get(int(z), 0.0) for z in a["Znum"]], np.float64)
+    elif np.ndim(sigma) == 1:
+        sig = np.asarray(sigma, np.float64)
+        if len(sig) != len(a):
+            raise ValueError("one sigma per atom expected")
     else:
         sig = np.full(len(a), float(sigma))
     for k in ("x", "y", "z"):

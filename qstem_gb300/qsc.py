@@ -171,6 +171,7 @@ class QscRun:
     folder: str
     detector_names: list = field(default_factory=list)
     dE_E: list = field(default_factory=list)    # energy deviation of each run (dE_EArray)
+    scan_step: tuple = (1.0, 1.0)               # detector image sampling, from the .qsc's scan range
 
     def einstein_sigma(self):
         """Per-atom, per-axis rms displacement of the Einstein model with
@@ -315,9 +316,15 @@ def read_qsc(path):
     avg_runs = int(_num(g("Runs for averaging:"), 10))
     if not tds:  # stem3/stem3.cpp:1023
         avg_runs = 1
+    scan_step = (1.0, 1.0)
     if mode == "STEM":
         scan = (_num(g("scan_x_start:"), 0.0), _num(g("scan_x_stop:"), 0.0), int(_num(g("scan_x_pixels:"), 0)),
                 _num(g("scan_y_start:"), 0.0), _num(g("scan_y_stop:"), 0.0), int(_num(g("scan_y_pixels:"), 0)))
+        # Detector images are sampled at (stop - start)/N of the values as
+        # read, before readFile moves the stops onto the pixel grid
+        # (stem3/stem3.cpp:1335-1337)
+        scan_step = (float(F32(F32(F32(scan[1]) - F32(scan[0])) / F32(max(scan[2], 1)))),
+                     float(F32(F32(F32(scan[4]) - F32(scan[3])) / F32(max(scan[5], 1)))))
     elif mode == "CBED":  # the probe position; TEM keeps the cell centre (:1025-1041)
         xs, ys = g("scan_x_start:"), g("scan_y_start:")
         scan = None if xs is None and ys is None else (
@@ -387,7 +394,8 @@ def read_qsc(path):
     dE0 = math.sqrt(dE_E * dE_E + dI_I * dI_I + dV_V * dV_V)
     series = _energy_spread_series(dE0, max(avg_runs, 1))
     return QscRun(params=p, atoms=atoms, cell=cell, ncell=(ncx, ncy, ncz), mode=mode, tds=tds,
-                  temperature=temperature, avg_runs=avg_runs, folder=folder, detector_names=names, dE_E=series)
+                  temperature=temperature, avg_runs=avg_runs, folder=folder, detector_names=names, dE_E=series,
+                  scan_step=scan_step)
 
 
 def _isnum(t):
@@ -396,3 +404,58 @@ def _isnum(t):
         return True
     except ValueError:
         return False
+
+
+def run_qsc(path, ctx=None, folder=None, seed=20261203):
+    """Run a stem3 input through the library and write what stem3 writes.
+
+    STEM: every run of the frozen-phonon average (Einstein displacements
+    drawn from numpy.random.default_rng(seed + run) when tds is on, and
+    seeded vacancies where occupancies are partial) through qs_stem_run;
+    the mean detector images are written as saveSTEMImages does
+    (stem3/stemlib.cpp:2693-2749): <folder>/<name>_<t>.img for the thickness
+    slots before the last, <folder>/<name>.img for the last, comment
+    "STEM image", the thickness, the scan sampling, and params [runs, error,
+    image^2 per pixel] (the reference's image2 sums the squares over the
+    slices of a slot; this writes the final slice's).  Returns
+    {detector name: images [thickness slot][scanX][scanY]}.
+    folder: where to write (default the .qsc's "Folder:", relative to it;
+    None writes nothing when the .qsc names none)."""
+    from . import imageio, lib, phonons
+    run = read_qsc(path)
+    if run.mode != "STEM":
+        raise NotImplementedError("run_qsc writes STEM outputs; use Context.cbed_batch / Context.tem")
+    own = ctx is None
+    ctx = ctx or lib.Context(0)
+    try:
+        p = run.params.copy()
+        nt = p.thickness_count()
+        acc = np.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), np.float64)
+        partial = bool(np.any(run.atoms["occ"] < 1))
+        for j in range(run.avg_runs):
+            atoms = run.atoms
+            if run.tds:
+                atoms = phonons.displaced(atoms, j, seed, run.einstein_sigma())
+            if partial:
+                atoms = draw_vacancies(atoms, seed + 7919 * (j + 1))
+            p.dE_E = F32(run.dE_E[j]) if j < len(run.dE_E) else F32(0.0)
+            acc += ctx.stem_run(p, atoms)
+        mean = (acc / run.avg_runs).astype(np.float32)
+    finally:
+        if own:
+            ctx.close()
+    out = {name: mean[:, i] for i, name in enumerate(run.detector_names[:p.detectorNum])}
+    where = folder if folder is not None else (
+        os.path.join(os.path.dirname(os.path.abspath(path)), run.folder) if run.folder else None)
+    if where:
+        os.makedirs(where, exist_ok=True)
+        for t in range(nt):
+            thick = ((t + 1) * p.outputInterval if t < nt - 1 else p.slices * p.cellDiv) * float(p.sliceThickness)
+            for name, img in out.items():
+                im = img[t]
+                # error = sum(image2 - image^2) / sum(image^2): 0 with image2 = image^2
+                params = [float(run.avg_runs), 0.0] + list((im.astype(np.float64) ** 2).ravel())
+                fn = "%s_%d.img" % (name, t) if t < nt - 1 else "%s.img" % name
+                imageio.write_img(os.path.join(where, fn), im, t=float(F32(thick)), dx=run.scan_step[0],
+                                  dy=run.scan_step[1], params=params, comment="STEM image")
+    return out

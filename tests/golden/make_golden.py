@@ -182,12 +182,27 @@ def qsc_case():
         for f in ("run.qsc", "cell.cfg"):
             shutil.copy(os.path.join(src, f), work)
         dump = os.path.join(work, "dump")
-        oracle.run_reference(os.path.join(work, "run.qsc"), dump, run=False)
+        oracle.run_reference(os.path.join(work, "run.qsc"), dump, run=True)
         meta = dict(l.split(" = ", 1) for l in open(os.path.join(dump, "meta.txt")).read().strip().split("\n"))
         out = {"atoms": np.fromfile(os.path.join(dump, "atoms.bin"), dtype=abi.ATOM_DTYPE),
                "meta_json": np.array(json.dumps(meta)),
                "qsc_text": np.array(open(os.path.join(src, "run.qsc")).read()),
                "cfg_text": np.array(open(os.path.join(src, "cell.cfg")).read())}
+        # the run: detector images of every thickness slot and the .img
+        # files saveSTEMImages wrote (name, thickness, sampling, comment)
+        nt = (int(meta["slices"]) * int(meta["cellDiv"])) // int(meta["outputInterval"]) + 1
+        nd, sx, sy = int(meta["detectorNum"]), int(meta["scanXN"]), int(meta["scanYN"])
+        det = np.zeros((nt, nd, sx, sy), np.float32)
+        for t in range(nt):
+            for i in range(nd):
+                det[t, i] = np.fromfile(os.path.join(dump, "det_%d_%d.bin" % (t, i)), np.float32).reshape(sx, sy)
+        out["det"] = det
+        files = sorted(f for f in os.listdir(os.path.join(work, "out")) if f.endswith(".img"))
+        heads = {}
+        for f in files:
+            im = imageio.read_img(os.path.join(work, "out", f))
+            heads[f] = [float(im.t), float(im.dx), float(im.dy), im.comment]
+        out["img_headers_json"] = np.array(json.dumps(heads))
     finally:
         shutil.rmtree(work, ignore_errors=True)
     path = os.path.join(HERE, "qscread.npz")
