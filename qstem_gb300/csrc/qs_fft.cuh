@@ -272,7 +272,7 @@ __device__ __forceinline__ void line_sync() {
 template <class Cfg, bool INV, bool BLOCK = false, class SM>
 __device__ __forceinline__ void line_fft(float2 (&reg)[Cfg::E], const SM& sm, const float2* __restrict__ tw,
                                          int t) {
-    constexpr int N = Cfg::N, T = Cfg::T, E = Cfg::E;
+    constexpr int T = Cfg::T, E = Cfg::E;
     using RAD = typename Cfg::rad;
     sfor<0, Cfg::PASSES>([&](auto pi) {
         constexpr int p = decltype(pi)::value;
