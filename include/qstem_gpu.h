@@ -72,6 +72,8 @@ extern "C" {
 #define QS_SYNC 4u              /* synchronise the stream before returning */
 #define QS_SLAB_STACKS 8u       /* qs_multislice_run with cellDiv > 1: trans holds one
                                    slices-long stack per slab, back to back */
+#define QS_SERIES 16u           /* qs_multislice_run: diffpats and exit_waves hold one
+                                   array per thickness slot, [tCount+1][npos][nx][ny] */
 
 /* run modes, same numbering as libs/stemtypes_fftw3.h:35-42 */
 #define QS_MODE_STEM 1
@@ -207,6 +209,12 @@ int qs_probe(qs_ctx *ctx, const qs_params *p, double dx, double dy, float *wave,
  *   diffpats    [npos][nx][ny] float, fftshifted |psi(k)|^2/sqrt(nx*ny) of
  *               the final slice (wave->diffpat)
  *   exit_waves  [npos][nx][ny] c64 real-space exit waves
+ * With QS_SERIES diffpats and exit_waves get a leading thickness-slot axis
+ * ([tCount+1][npos][nx][ny]): slot t holds the pattern / real-space wave
+ * after the slice that writes detector slot t, i.e. collectIntensity's
+ * diff_<t>.img of CBED runs (stem3/stemlib.cpp:2663-2676) and, for the slots
+ * interimWave writes, its wave_<t>.img (stem3/stemlib.cpp:2538-2565); the
+ * last slot is the final slice's.
  * Buffers are device pointers, or host pointers with QS_HOST_IO. */
 int qs_multislice_run(qs_ctx *ctx, const qs_params *p, const float *trans, const float *probe,
                       const qs_batch *batch, float *det_images, float *diffpats,

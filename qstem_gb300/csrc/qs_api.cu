@@ -615,6 +615,9 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     }
     for (int t = 0; t < nT; t++) if (lastWriter[t] >= 0) slotOf[lastWriter[t]] = t;
     const bool wantDet = ndet > 0 && det_images != nullptr;
+    // QS_SERIES: one pattern / exit wave per thickness slot
+    const bool series = (flags & QS_SERIES) != 0;
+    const size_t nS = series ? (size_t)nT : 1;
 
     // device buffers: tables | tiles | positions
     void* dtab = nullptr;
@@ -678,7 +681,8 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     size_t freeB = 0, totalB = 0;
     QS_CUDA_TRY(cudaMemGetInfo(&freeB, &totalB));
     const size_t perWave = sizeof(float2) * N + (size_t)nT * ntiles * std::max(ndet, 1) * sizeof(double) +
-                           (host && diffpats ? sizeof(float) * N : 0) + (host && exit_waves ? sizeof(float2) * N : 0);
+                           (host && diffpats ? sizeof(float) * N * nS : 0) +
+                           (host && exit_waves ? sizeof(float2) * N * nS : 0);
     const size_t have = c->cap[B_WAVES] / (sizeof(float2) * N);
     const size_t budget = freeB > ((size_t)1 << 30) ? freeB - ((size_t)1 << 30) : freeB / 2;
     size_t chunk = std::min<size_t>((size_t)npos, std::max<size_t>(have, budget / perWave));
@@ -694,13 +698,13 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     float* dp_dev = nullptr;
     if (diffpats && host) {
         void* d = nullptr;
-        QS_TRY(ensure(c, B_OUT2, sizeof(float) * N * chunk, &d));
+        QS_TRY(ensure(c, B_OUT2, sizeof(float) * N * chunk * nS, &d));
         dp_dev = (float*)d;
     }
     float2* ew_dev = nullptr;
     if (exit_waves && host) {
         void* d = nullptr;
-        QS_TRY(ensure(c, B_OUT3, sizeof(float2) * N * chunk, &d));
+        QS_TRY(ensure(c, B_OUT3, sizeof(float2) * N * chunk * nS, &d));
         ew_dev = (float2*)d;
     }
     const float2* tw_y = twiddles(ny);
@@ -712,11 +716,15 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
         const int nb = (int)std::min(chunk, (size_t)npos - p0);
         float* dpOut = diffpats ? (host ? dp_dev : diffpats + p0 * N) : nullptr;
         float2* ewOut = exit_waves ? (host ? ew_dev : (float2*)exit_waves + p0 * N) : nullptr;
-        if (dpOut) QS_CUDA_TRY(cudaMemsetAsync(dpOut, 0, sizeof(float) * N * nb, s));
+        // distance between thickness slots of a series (elements)
+        const size_t slotStride = N * (host ? chunk : (size_t)npos);
+        if (dpOut)
+            for (size_t k = 0; k < nS; k++)
+                QS_CUDA_TRY(cudaMemsetAsync(dpOut + k * slotStride, 0, sizeof(float) * N * nb, s));
 
         RowArgs ra{};
         ra.nx = nx; ra.ny = ny; ra.potNx = P.potNx; ra.potNy = P.potNy;
-        ra.nwaves = nb; ra.waves = waves; ra.exit_waves = ewOut;
+        ra.nwaves = nb; ra.waves = waves; ra.exit_waves = nullptr;
         ra.probe = (const float2*)dprobe + p0 * probeStride;
         ra.probe_stride = probeStride;
         ra.trans_stride = transStride;
@@ -764,15 +772,26 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
             const int slot = slotOf[a];
             ca.ndet = (wantDet && slot >= 0) ? ndet : 0;
             ca.partial = (double*)dpart + (slot >= 0 ? (size_t)slot * partPerT : 0);
-            ca.diffpat = (a == SA - 1) ? dpOut : nullptr;
+            if (series)
+                ca.diffpat = (dpOut && slot >= 0) ? dpOut + (size_t)slot * slotStride : nullptr;
+            else
+                ca.diffpat = (a == SA - 1) ? dpOut : nullptr;
             ca.inverse = (a < SA - 1 || ewOut) ? 1 : 0;
             QS_TRY(cols());
+            if (series && ewOut && slot >= 0 && a < SA - 1) {
+                // the real-space wave after slice a, before the next transmit
+                ra.exit_waves = ewOut + (size_t)slot * slotStride;
+                QS_TRY(launch_rows(ra, ROW_LAST, s));
+            }
             if (a < SA - 1) {
                 ra.trans_slice = sliceOf(a + 1);
                 QS_TRY(rows(ROW_MID));
             }
         }
-        if (ewOut) QS_TRY(launch_rows(ra, ROW_LAST, s));
+        if (ewOut) {
+            ra.exit_waves = ewOut + (series ? (size_t)(nT - 1) * slotStride : 0);
+            QS_TRY(launch_rows(ra, ROW_LAST, s));
+        }
         if (wantDet)
             for (int t = 0; t < nT; t++) {
                 if (lastWriter[t] < 0) continue;
@@ -780,11 +799,14 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
                                            d_dx_pos + p0, d_dy_pos + p0, P.scanYN, npix,
                                            det_dev + (size_t)t * ndet * npix, s));
             }
-        if (host && diffpats)
-            QS_CUDA_TRY(cudaMemcpyAsync(diffpats + p0 * N, dpOut, sizeof(float) * N * nb, cudaMemcpyDeviceToHost, s));
-        if (host && exit_waves)
-            QS_CUDA_TRY(cudaMemcpyAsync(exit_waves + 2 * p0 * N, ewOut, sizeof(float2) * N * nb,
-                                        cudaMemcpyDeviceToHost, s));
+        for (size_t k = 0; k < nS; k++) {
+            if (host && diffpats)
+                QS_CUDA_TRY(cudaMemcpyAsync(diffpats + (k * npos + p0) * N, dpOut + k * slotStride,
+                                            sizeof(float) * N * nb, cudaMemcpyDeviceToHost, s));
+            if (host && exit_waves)
+                QS_CUDA_TRY(cudaMemcpyAsync(exit_waves + 2 * (k * npos + p0) * N, ewOut + k * slotStride,
+                                            sizeof(float2) * N * nb, cudaMemcpyDeviceToHost, s));
+        }
     }
     if (wantDet && host)
         QS_CUDA_TRY(cudaMemcpyAsync(det_images, det_dev, sizeof(float) * detElems, cudaMemcpyDeviceToHost, s));

@@ -171,23 +171,27 @@ class Context:
 
     # -------------------------------------------------------- multislice
     def multislice(self, p, trans, probe=None, positions=None, det=None, diffpats=None, exit_waves=None,
-                   want_det=True, want_diffpats=False, want_exit_waves=False, sync=True, slab_stacks=False):
+                   want_det=True, want_diffpats=False, want_exit_waves=False, sync=True, slab_stacks=False,
+                   series=False):
         """Run probe positions through the slice stack.
 
         positions: None (the full scan raster) or (iPosX, iPosY, detPosX, detPosY) int arrays.
-        Output buffers are allocated (numpy, host) when not given and requested."""
+        Output buffers are allocated (numpy, host) when not given and requested.
+        series: diffraction patterns and exit waves of every thickness slot
+        ([slot][position]...), not only the final slice's (QS_SERIES)."""
         bx, keep = _batch(p, positions)
         npos = bx.npos
         host = not _is_torch(trans)
         nt = p.thickness_count()
+        lead = (nt, npos) if series else (npos,)
         if det is None and want_det and p.detectorNum > 0:
             det = np.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), np.float32) if host else None
         if diffpats is None and want_diffpats:
-            diffpats = np.zeros((npos, p.nx, p.ny), np.float32) if host else None
+            diffpats = np.zeros(lead + (p.nx, p.ny), np.float32) if host else None
         if exit_waves is None and want_exit_waves:
-            exit_waves = np.zeros((npos, p.nx, p.ny, 2), np.float32) if host else None
+            exit_waves = np.zeros(lead + (p.nx, p.ny, 2), np.float32) if host else None
         flags = (_io_flags(trans, probe, det, diffpats, exit_waves) | (abi.QS_SYNC if sync else 0) |
-                 (abi.QS_SLAB_STACKS if slab_stacks else 0))
+                 (abi.QS_SLAB_STACKS if slab_stacks else 0) | (abi.QS_SERIES if series else 0))
         _check(self.lib.qs_multislice_run(self.h, ctypes.byref(p), _ptr(trans), _ptr(probe), ctypes.byref(bx),
                                           _ptr(det), _ptr(diffpats), _ptr(exit_waves), flags))
         del keep

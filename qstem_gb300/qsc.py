@@ -172,6 +172,8 @@ class QscRun:
     detector_names: list = field(default_factory=list)
     dE_E: list = field(default_factory=list)    # energy deviation of each run (dE_EArray)
     scan_step: tuple = (1.0, 1.0)               # detector image sampling, from the .qsc's scan range
+    save_level: int = 0                         # "save level:"
+    spread: tuple = (0.0, 0.0, 0.0)             # dE/E, dI/I, dV/V as read (CBED/TEM use them as such)
 
     def einstein_sigma(self):
         """Per-atom, per-axis rms displacement of the Einstein model with
@@ -242,7 +244,7 @@ def read_qsc(path):
     if mode not in ("STEM", "TEM", "CBED"):
         unsupported.append("mode %s" % mode)
     g("print level:")
-    g("save level:")
+    save_level = int(_num(g("save level:"), 0))
     cfg = _word(g("filename:"))
     ncx = int(_num(g("NCELLX:"), 1))
     ncy = int(_num(g("NCELLY:"), 1))
@@ -395,7 +397,7 @@ def read_qsc(path):
     series = _energy_spread_series(dE0, max(avg_runs, 1))
     return QscRun(params=p, atoms=atoms, cell=cell, ncell=(ncx, ncy, ncz), mode=mode, tds=tds,
                   temperature=temperature, avg_runs=avg_runs, folder=folder, detector_names=names, dE_E=series,
-                  scan_step=scan_step)
+                  scan_step=scan_step, save_level=save_level, spread=(dE_E, dI_I, dV_V))
 
 
 def _isnum(t):
@@ -406,51 +408,151 @@ def _isnum(t):
         return False
 
 
-def run_qsc(path, ctx=None, folder=None, seed=20261203):
-    """Run a stem3 input through the library and write what stem3 writes.
+def _slot_writers(SA, oi, nT):
+    """The absolute slice whose collectIntensity call a thickness slot keeps
+    (stem3/stemlib.cpp:2597-2610): slices before the last write slot a // oi,
+    the last slice slot nT - 1; -1 for a slot nothing writes."""
+    last = [-1] * nT
+    for a in range(SA):
+        t = a // oi if a < SA - 1 else nT - 1
+        if t < nT:
+            last[t] = a
+    return last
 
-    STEM: every run of the frozen-phonon average (Einstein displacements
-    drawn from numpy.random.default_rng(seed + run) when tds is on, and
-    seeded vacancies where occupancies are partial) through qs_stem_run;
-    the mean detector images are written as saveSTEMImages does
-    (stem3/stemlib.cpp:2693-2749): <folder>/<name>_<t>.img for the thickness
-    slots before the last, <folder>/<name>.img for the last, comment
-    "STEM image", the thickness, the scan sampling, and params [runs, error,
-    image^2 per pixel] (the reference's image2 sums the squares over the
-    slices of a slot; this writes the final slice's).  Returns
-    {detector name: images [thickness slot][scanX][scanY]}.
+
+def _interim_files(SA, oi):
+    """interimWave's writes (stem3/stemlib.cpp:2538-2565): file index -> the
+    last absolute slice writing wave_<index>.img (after slice a when a + 1 is
+    a multiple of oi, and after the last slice)."""
+    files = {}
+    for a in range(SA):
+        if a == SA - 1 or (a + 1) % oi == 0:
+            files[a // oi] = a
+    return files
+
+
+def _thick(n, dz):
+    """wave->thickness = n * sliceThickness in float (stem3/stemlib.cpp:2455)."""
+    return float(F32(F32(n) * F32(dz)))
+
+
+def _stacks(ctx, p, atoms):
+    """Every slab's slice stack (one, reused, for equal divisions), host."""
+    if p.cellDiv > 1 and not p.equalDivs:
+        return np.concatenate([ctx.slices(p, atoms, slab=k) for k in range(p.cellDiv)]), True
+    return ctx.slices(p, atoms), False
+
+
+def _run_atoms(run, j, seed):
+    atoms = run.atoms
+    if run.tds:
+        from . import phonons
+        atoms = phonons.displaced(atoms, j, seed, run.einstein_sigma())
+    if np.any(run.atoms["occ"] < 1):
+        atoms = draw_vacancies(atoms, seed + 7919 * (j + 1))
+    return atoms
+
+
+def _kspace_pattern(wave, scale):
+    """collectIntensity's diffpat of a wave (stem3/stemlib.cpp:2626-2630):
+    |psi|^2 at ((ix + nx/2) % nx, (iy + ny/2) % ny), times scale."""
+    w = np.asarray(wave, np.float32)
+    I = (w[..., 0] * w[..., 0] + w[..., 1] * w[..., 1]).astype(np.float64) * scale
+    return np.roll(I.astype(np.float32), (w.shape[0] // 2, w.shape[1] // 2), axis=(0, 1))
+
+
+def run_qsc(path, ctx=None, folder=None, seed=20261203, chunk=256):
+    """Run a stem3 input through the library and write what stem3 writes to
+    its output folder.
+
+    Every run of a frozen-phonon average draws its Einstein displacements
+    from numpy.random.default_rng(seed + run) when tds is on (and seeded
+    vacancies where occupancies are partial).  The files follow doSTEM,
+    doCBED and doTEM (stem3/stem3.cpp:2722-2961, 2048-2344, 2354-2710) and
+    runMulsSTEM's collectIntensity / interimWave (stem3/stemlib.cpp:
+    2538-2749); the writers below say which file comes from where.
+
     folder: where to write (default the .qsc's "Folder:", relative to it;
-    None writes nothing when the .qsc names none)."""
-    from . import imageio, lib, phonons
+    None writes nothing when the .qsc names none).  chunk: positions per
+    multislice call when per-position files are written (bounds host memory).
+    Returns a dict of the results (STEM: {detector name: images [slot][x][y]};
+    CBED: {"diffpat": mean final pattern, "series": mean slot patterns};
+    TEM: {"exit_intensity": mean |psi_exit|^2, "exit_wave": run 0's})."""
+    from . import lib
     run = read_qsc(path)
-    if run.mode != "STEM":
-        raise NotImplementedError("run_qsc writes STEM outputs; use Context.cbed_batch / Context.tem")
-    own = ctx is None
-    ctx = ctx or lib.Context(0)
-    try:
-        p = run.params.copy()
-        nt = p.thickness_count()
-        acc = np.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), np.float64)
-        partial = bool(np.any(run.atoms["occ"] < 1))
-        for j in range(run.avg_runs):
-            atoms = run.atoms
-            if run.tds:
-                atoms = phonons.displaced(atoms, j, seed, run.einstein_sigma())
-            if partial:
-                atoms = draw_vacancies(atoms, seed + 7919 * (j + 1))
-            p.dE_E = F32(run.dE_E[j]) if j < len(run.dE_E) else F32(0.0)
-            acc += ctx.stem_run(p, atoms)
-        mean = (acc / run.avg_runs).astype(np.float32)
-    finally:
-        if own:
-            ctx.close()
-    out = {name: mean[:, i] for i, name in enumerate(run.detector_names[:p.detectorNum])}
     where = folder if folder is not None else (
         os.path.join(os.path.dirname(os.path.abspath(path)), run.folder) if run.folder else None)
     if where:
         os.makedirs(where, exist_ok=True)
+    own = ctx is None
+    ctx = ctx or lib.Context(0)
+    try:
+        if run.mode == "STEM":
+            return _run_stem(ctx, run, where, seed, chunk)
+        if run.mode == "CBED":
+            return _run_cbed(ctx, run, where, seed)
+        return _run_tem(ctx, run, where, seed)
+    finally:
+        if own:
+            ctx.close()
+
+
+def _run_stem(ctx, run, where, seed, chunk):
+    """doSTEM: detector images averaged over the runs, saved as
+    saveSTEMImages does (stem3/stemlib.cpp:2693-2749): <name>_<t>.img for
+    the thickness slots before the last, <name>.img for the last, comment
+    "STEM image", the thickness, the scan sampling, and params [runs, error,
+    image^2 per pixel] (the reference's image2 sums the squares over the
+    slices of a slot; this writes the final slice's).  At save level > 0 also
+    each position's diffraction pattern, averaged over the runs in the file
+    itself as doSTEM does (diffAvg_<ix>_<iy>.img, "Average Array",
+    stem3/stem3.cpp:2890-2930), and at save level > 1 or with slabs its exit
+    wave (mulswav_<ix>_<iy>.img, runMulsSTEM's WriteWave,
+    stem3/stemlib.cpp:2525-2532; the last run's)."""
+    from . import imageio
+    p = run.params.copy()
+    nt = p.thickness_count()
+    SA = p.slices * p.cellDiv
+    want_dp = bool(where) and run.save_level > 0
+    want_ew = bool(where) and (run.save_level > 1 or p.cellDiv > 1)
+    per_pos = want_dp or want_ew
+    acc = np.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), np.float64)
+    offs = config.scan_offsets(p)
+    npos = len(offs[0])
+    t_end = _thick(SA, p.sliceThickness)
+    rk = (1.0 / float(F32(p.nx * F32(p.resolutionX))), 1.0 / float(F32(p.ny * F32(p.resolutionY))))
+    for j in range(run.avg_runs):
+        atoms = _run_atoms(run, j, seed)
+        p.dE_E = F32(run.dE_E[j]) if j < len(run.dE_E) else F32(0.0)
+        if not per_pos:
+            acc += ctx.stem_run(p, atoms)
+            continue
+        T, slabs = _stacks(ctx, p, atoms)
+        for c0 in range(0, npos, chunk):
+            pos = tuple(a[c0:c0 + chunk] for a in offs)
+            det, dps, ews = ctx.multislice(p, T, positions=pos, want_det=p.detectorNum > 0, want_diffpats=want_dp,
+                                           want_exit_waves=want_ew and j == run.avg_runs - 1,
+                                           slab_stacks=slabs)
+            if det is not None:
+                acc += det
+            for k in range(len(pos[0])):
+                ix, iy = int(pos[2][k]), int(pos[3][k])
+                if want_dp:
+                    fn = os.path.join(where, "diffAvg_%d_%d.img" % (ix, iy))
+                    avg = dps[k]
+                    if j > 0:  # (avgCount * avg + diffpat) / (avgCount + 1) in float
+                        old = imageio.read_img(fn).data.astype(np.float32)
+                        avg = ((F32(j) * old + dps[k]) / F32(j + 1)).astype(np.float32)
+                    imageio.write_img(fn, avg, t=t_end, dx=rk[0], dy=rk[1], comment="Average Array")
+                if ews is not None:
+                    imageio.write_img(os.path.join(where, "mulswav_%d_%d.img" % (ix, iy)), ews[k], t=t_end,
+                                      dx=float(F32(p.resolutionX)), dy=float(F32(p.resolutionY)),
+                                      comment="Wavefunction")
+    mean = (acc / run.avg_runs).astype(np.float32)
+    out = {name: mean[:, i] for i, name in enumerate(run.detector_names[:p.detectorNum])}
+    if where:
         for t in range(nt):
-            thick = ((t + 1) * p.outputInterval if t < nt - 1 else p.slices * p.cellDiv) * float(p.sliceThickness)
+            thick = ((t + 1) * p.outputInterval if t < nt - 1 else SA) * float(p.sliceThickness)
             for name, img in out.items():
                 im = img[t]
                 # error = sum(image2 - image^2) / sum(image^2): 0 with image2 = image^2
@@ -459,3 +561,171 @@ def run_qsc(path, ctx=None, folder=None, seed=20261203):
                 imageio.write_img(os.path.join(where, fn), im, t=float(F32(thick)), dx=run.scan_step[0],
                                   dy=run.scan_step[1], params=params, comment="STEM image")
     return out
+
+
+def _wave_params(p, spread):
+    """interimWave's nine header parameters (stem3/stemlib.cpp:2545-2556):
+    v0, Cs, df0, astigmatism and its angle, Cc * total energy spread, alpha,
+    beam tilt x and y (no beam tilt here)."""
+    dE, dI, dV = (float(F32(v)) for v in spread)
+    return [float(p.v0), float(p.Cs), float(p.df0), float(p.astigMag), float(p.astigAngle),
+            float(F32(float(p.Cc) * math.sqrt(dE * dE + dV * dV + dI * dI))), float(p.alpha), 0.0, 0.0]
+
+
+def _run_cbed(ctx, run, where, seed):
+    """doCBED: one probe at the scan start through every run's stack.
+
+    Files of the first run, as the reference writes them:
+      diff_<t>.img   save level > 0: collectIntensity's pattern of thickness
+                     slot t ("Diffraction Pattern"; the thickness is the
+                     wave's before the slice, as collectIntensity runs before
+                     runMulsSTEM updates it).  At save level > 1 runMulsSTEM's
+                     second, real-space collectIntensity overwrites it with
+                     the real-space intensity after the slice
+                     (stem3/stemlib.cpp:2475-2482, 2663-2676).
+      wave_<t>.img   save level > 1: interimWave's real-space wave.
+      wave_probe.img, wave_final.img   save level > 2: the probe and the
+                     final wave (stem3/stem3.cpp:2101-2104, 2210-2213).
+      diffAvg_1.img  the final pattern ("DEBUG Wave intensity",
+                     stem3/stem3.cpp:2224-2250).
+    Later runs (tds): diff_<t>.img hold the mean over the runs so far
+    ("Average Array"), diffAvg_<n>.img the mean of the first n runs'
+    final patterns ("Averaged Diffraction pattern, unit: 1/A", params
+    [tilt 0, 1/lambda]; the previous one is removed unless n - 1 is a
+    multiple of the save level) and avgresults.dat the mean squared change
+    of each step (stem3/stem3.cpp:2252-2295).  The reference's own averaging
+    re-reads the second run's pattern from a leftover diff.img for every
+    later run and averages every slice of a thickness group into diff_<t>;
+    the files here hold the plain means instead."""
+    from . import imageio
+    p = run.params.copy()
+    p.dE_E = F32(run.spread[0])
+    nx, ny = p.nx, p.ny
+    SA = p.slices * p.cellDiv
+    nT = p.thickness_count()
+    oi = p.outputInterval
+    writers = _slot_writers(SA, oi, nT)
+    sl = run.save_level
+    dz = float(p.sliceThickness)
+    t_end = _thick(SA, dz)
+    rx, ry = float(F32(p.resolutionX)), float(F32(p.resolutionY))
+    rk = (1.0 / float(F32(nx * F32(p.resolutionX))), 1.0 / float(F32(ny * F32(p.resolutionY))))
+    scale = 1.0 / math.sqrt(float(nx * ny))
+    # doCBED's probe position (stem3/stem3.cpp:2096-2100)
+    probe = ctx.probe(p, float(F32(F32(p.scanXStart) - F32(p.potOffsetX))),
+                      float(F32(F32(p.scanYStart) - F32(p.potOffsetY))))
+    pos = tuple(np.zeros(1, np.int32) for _ in range(4))
+    inv_lambda = 1.0 / config.wavelength(float(p.v0))
+    series_avg = [None] * nT
+    avg = None
+    chisq = []
+    for j in range(run.avg_runs):
+        atoms = _run_atoms(run, j, seed)
+        T, slabs = _stacks(ctx, p, atoms)
+        _, dps, ews = ctx.multislice(p, T, probe, positions=pos, want_det=False, want_diffpats=True,
+                                     want_exit_waves=sl > 1, slab_stacks=slabs, series=True)
+        # the pattern each slot's file ends the run with, and its thickness
+        slot_pat, slot_t = [None] * nT, [0.0] * nT
+        for t, a in enumerate(writers):
+            if a < 0:
+                continue
+            if sl > 1:
+                slot_pat[t], slot_t[t] = _kspace_pattern(ews[t, 0], scale), _thick(a + 1, dz)
+            else:
+                stale = t_end if (a == 0 and j > 0) else _thick(a, dz)
+                slot_pat[t], slot_t[t] = dps[t, 0], stale
+        final = slot_pat[nT - 1]
+        if where and sl > 2:
+            imageio.write_img(os.path.join(where, "wave_probe.img"), probe, t=0.0 if j == 0 else t_end, dx=rx,
+                              dy=ry, comment="Wavefunction")
+            if j == 0:
+                imageio.write_img(os.path.join(where, "wave_final.img"), ews[nT - 1, 0], t=t_end, dx=rx, dy=ry,
+                                  comment="Wavefunction")
+        if where and sl > 1:
+            for f, a in _interim_files(SA, oi).items():
+                t = nT - 1 if a == SA - 1 else a // oi
+                name = "wave_%d_%d.img" % (j, f) if run.tds else "wave_%d.img" % f
+                imageio.write_img(os.path.join(where, name), ews[t, 0], t=_thick(a + 1, dz), dx=rx, dy=ry,
+                                  params=_wave_params(p, run.spread), comment="Wave Function")
+        for t in range(nT):
+            if slot_pat[t] is None:
+                continue
+            series_avg[t] = slot_pat[t] if j == 0 else ((F32(j) * series_avg[t] + slot_pat[t]) / F32(j + 1)).astype(
+                np.float32)
+            if where and sl > 0:
+                imageio.write_img(os.path.join(where, "diff_%d.img" % t), series_avg[t], t=slot_t[t], dx=rk[0],
+                                  dy=rk[1], comment="Diffraction Pattern" if j == 0 else "Average Array")
+        if j == 0:
+            avg = final.copy()
+            if where:
+                imageio.write_img(os.path.join(where, "diffAvg_1.img"), avg, t=t_end, dx=rk[0], dy=rk[1],
+                                  comment="DEBUG Wave intensity")
+            continue
+        new = ((F32(j) * avg + final) / F32(j + 1)).astype(np.float32)
+        chisq.append(float(np.sum((avg.astype(np.float64) - new) ** 2)) / float(nx * ny))
+        avg = new
+        if where:
+            imageio.write_img(os.path.join(where, "diffAvg_%d.img" % (j + 1)), avg, t=t_end, dx=rk[0], dy=rk[1],
+                              params=[0.0, inv_lambda], comment="Averaged Diffraction pattern, unit: 1/A")
+            if sl == 0 or j % sl != 0:
+                prev = os.path.join(where, "diffAvg_%d.img" % j)
+                if os.path.exists(prev):
+                    os.remove(prev)
+            with open(os.path.join(where, "avgresults.dat"), "w") as fh:
+                for k, c in enumerate(chisq):
+                    fh.write("%d %g\n" % (k + 1, c))
+    return {"diffpat": avg, "series": series_avg}
+
+
+def _run_tem(ctx, run, where, seed):
+    """doTEM: an incident plane wave through every run's stack.
+
+    Files: interimWave's real-space waves wave_<t>.img ("Wave Function",
+    nine parameters; wave_<run>_<t>.img with tds) after the slices it writes
+    (stem3/stemlib.cpp:2538-2565), and the first run's exit wave wave.img
+    ("Exit face wave function for no TDS", or "Test wave function for run 0"
+    with tds; stem3/stem3.cpp:2494-2513).  The reference stops there: it
+    then reads a diff.img that TEM never writes (stem3/stem3.cpp:2545-2547).
+    This also writes the mean exit-wave intensity over all runs,
+    waveIntensity.img ("Wave intensity", params [runs]), which the
+    reference intends but never reaches; CTF images are Context.tem's."""
+    from . import imageio
+    p = run.params.copy()
+    nx, ny = p.nx, p.ny
+    SA = p.slices * p.cellDiv
+    nT = p.thickness_count()
+    oi = p.outputInterval
+    dz = float(p.sliceThickness)
+    t_end = _thick(SA, dz)
+    rx, ry = float(F32(p.resolutionX)), float(F32(p.resolutionY))
+    plane = np.zeros((nx, ny, 2), np.float32)
+    plane[..., 0] = 1.0  # stem3/stem3.cpp:2403-2407
+    pos = tuple(np.zeros(1, np.int32) for _ in range(4))
+    files = _interim_files(SA, oi)
+    acc = np.zeros((nx, ny), np.float64)
+    first = None
+    for j in range(run.avg_runs):
+        atoms = _run_atoms(run, j, seed)
+        T, slabs = _stacks(ctx, p, atoms)
+        _, _, ews = ctx.multislice(p, T, plane, positions=pos, want_det=False, want_exit_waves=True,
+                                   slab_stacks=slabs, series=True)
+        exit_wave = ews[nT - 1, 0]
+        acc += exit_wave[..., 0].astype(np.float64) ** 2 + exit_wave[..., 1].astype(np.float64) ** 2
+        if j == 0:
+            first = exit_wave
+        if not where:
+            continue
+        for f, a in files.items():
+            t = nT - 1 if a == SA - 1 else a // oi
+            name = "wave_%d_%d.img" % (j, f) if run.tds else "wave_%d.img" % f
+            imageio.write_img(os.path.join(where, name), ews[t, 0], t=_thick(a + 1, dz), dx=rx, dy=ry,
+                              params=_wave_params(p, run.spread), comment="Wave Function")
+        if j == 0:
+            imageio.write_img(os.path.join(where, "wave.img"), exit_wave, t=t_end, dx=rx, dy=ry,
+                              comment="Test wave function for run 0" if run.tds else
+                              "Exit face wave function for no TDS")
+    mean = (acc / run.avg_runs).astype(np.float32)
+    if where:
+        imageio.write_img(os.path.join(where, "waveIntensity.img"), mean, t=t_end, dx=rx, dy=ry,
+                          params=[float(run.avg_runs)], comment="Wave intensity")
+    return {"exit_intensity": mean, "exit_wave": first}

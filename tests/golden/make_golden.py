@@ -210,10 +210,70 @@ def qsc_case():
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+# whole stem3 runs whose output folders pin qstem_gb300.qsc.run_qsc: every
+# .img file the reference wrote (name, header, data)
+RUN_CASES = {
+    # CBED with a thickness series (diff_<t>.img, save level 1) and diffAvg_1.img
+    "qsccbed": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=5,
+                    sliceThickness=2.0, scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0,
+                    bandlimit=True, outputInterval=2, mode="CBED", saveLevel=1),
+    # CBED at save level 3: wave_probe.img, wave_final.img, and the patterns
+    # that runMulsSTEM's real-space collectIntensity overwrites
+    "qsccbed3": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=4,
+                     sliceThickness=2.0, scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0,
+                     bandlimit=True, outputInterval=3, mode="CBED", saveLevel=3),
+    # TEM: interimWave's wave_<t>.img and the exit wave wave.img
+    "qsctem": dict(cell="si", ncell=(4, 3, 4), nx=64, resolutionX=0.06, v0=300.0, slices=7, sliceThickness=2.0,
+                   scan=None, detectors=[], alpha=0.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
+                   outputInterval=3, mode="TEM", saveLevel=0),
+    # STEM at save level 2: per-position diffAvg_ix_iy.img and mulswav_ix_iy.img
+    "qscstem": dict(cell="sto", ncell=(3, 3, 4), nx=64, resolutionX=0.0915, v0=200.0, slices=8,
+                    sliceThickness=1.9525, scan=(3.905, 7.81, 2, 3.905, 7.81, 2),
+                    detectors=[(0.0, 20.0, "BF"), (40.0, 90.0, "HAADF")], alpha=20.0, outputInterval=4,
+                    mode="STEM", saveLevel=2),
+}
+
+
+def qsc_run_case(name, case):
+    """The reference run end to end on a .qsc written for `case`; stores the
+    input texts and every .img file of its output folder."""
+    work = tempfile.mkdtemp(prefix="qs_golden_")
+    try:
+        cell = cell_of(case["cell"])
+        config.write_cfg(cell, os.path.join(work, "cell.cfg"))
+        qsc = os.path.join(work, "run.qsc")
+        config.write_qsc(qsc, cfg_file="cell.cfg", ncell=case["ncell"], nx=case["nx"],
+                         resolutionX=case["resolutionX"], v0=case["v0"], slices=case["slices"],
+                         sliceThickness=case["sliceThickness"], scan=case["scan"], detectors=case["detectors"],
+                         alpha=case["alpha"], Cs_mm=case.get("Cs_mm", 0.0), defocus_nm=case.get("defocus_nm", 0.0),
+                         outputInterval=case.get("outputInterval"), mode=case["mode"],
+                         bandlimit=case.get("bandlimit", False), folder="out", saveLevel=case["saveLevel"])
+        oracle.run_reference(qsc, os.path.join(work, "dump"), run=True)
+        out = {"qsc_text": np.array(open(qsc).read()),
+               "cfg_text": np.array(open(os.path.join(work, "cell.cfg")).read())}
+        heads = {}
+        for f in sorted(os.listdir(os.path.join(work, "out"))):
+            if not f.endswith(".img"):
+                continue
+            im = imageio.read_img(os.path.join(work, "out", f))
+            heads[f] = [float(im.t), float(im.dx), float(im.dy), im.comment, [float(v) for v in im.params]]
+            d = im.data
+            out["img_" + f] = (np.stack([d.real, d.imag], -1) if np.iscomplexobj(d) else d).astype(np.float32)
+        out["img_headers_json"] = np.array(json.dumps(heads))
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes", sorted(heads))
+
+
 def main(names=None):
     oracle.build(quiet=False)
     if not names or "qscread" in names:
         qsc_case()
+    for name, case in RUN_CASES.items():
+        if not names or name in names:
+            qsc_run_case(name, case)
     for name, case in CASES.items():
         if names and name not in names:
             continue

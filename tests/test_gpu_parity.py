@@ -189,3 +189,28 @@ def test_errors_are_codes_not_exits(ctx):
     with pytest.raises(lib.QsError) as e:
         ctx.slices(p2, g["atoms"])
     assert e.value.code == -1
+
+
+def test_thickness_series(ctx):
+    """QS_SERIES: the pattern and real-space wave of every thickness slot
+    (collectIntensity's diff_<t>.img, interimWave's wave_<t>.img) against
+    the oracle run truncated after the slot's writer slice; the last slot
+    is bit-identical to the final outputs of a run without the flag."""
+    g = Golden("sto64")
+    p = g.params
+    T = g["T"]
+    _, dps, ews = ctx.multislice(p, T, g["probe"], want_det=False, want_diffpats=True, want_exit_waves=True,
+                                 series=True)
+    nt = p.thickness_count()
+    assert dps.shape == (nt, p.scanXN * p.scanYN, p.nx, p.ny) and ews.shape[:2] == dps.shape[:2]
+    _, dpf, ewf = ctx.multislice(p, T, g["probe"], want_det=False, want_diffpats=True, want_exit_waves=True)
+    np.testing.assert_array_equal(dps[-1], dpf)
+    np.testing.assert_array_equal(ews[-1], ewf)
+    S = p.slices
+    for t in range(nt):
+        a = min((t + 1) * p.outputInterval - 1, S - 2) if t < nt - 1 else S - 1
+        q = p.copy()
+        q.slices = q.outputInterval = a + 1
+        _, dpo, ewo = oracle.stem(q, T[:a + 1], g["probe"], det=False, diffpats=True, exit_waves=True)
+        assert rel_l2(dps[t], dpo) <= TOL_MS, t
+        assert rel_l2(ews[t], ewo) <= TOL_MS, t

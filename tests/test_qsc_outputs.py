@@ -1,0 +1,137 @@
+"""Host logic of qstem_gb300.qsc.run_qsc on the CPU: the files a stem3 run
+writes (names, headers, data) and the averaging over frozen-phonon runs,
+with the oracle standing in for the GPU library (tests/oracle_ctx.py).
+
+The folders are pinned against the reference's own runs (tests/golden/
+qsc*.npz); the oracle is bit-exact with the reference on these cases, so
+data agree to 1e-6 relative L2.  The multi-run cases check the averages
+against the per-run results the stand-in logged."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_l2
+from oracle import oracle
+from oracle_ctx import OracleContext
+from qstem_gb300 import imageio, qsc
+
+EXTRA = {"qsctem": {"waveIntensity.img"}}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle():
+    oracle.build()
+
+
+def _inputs(tmp_path, name, edit=None):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    texts = {"run.qsc": str(z["qsc_text"]), "cell.cfg": str(z["cfg_text"])}
+    if edit:
+        texts = edit(texts)
+    for fn, text in texts.items():
+        (tmp_path / fn).write_text(text)
+    return z, str(tmp_path / "run.qsc"), str(tmp_path / "out")
+
+
+def _read(folder, fn):
+    im = imageio.read_img(os.path.join(folder, fn))
+    d = im.data
+    return im, (np.stack([d.real, d.imag], -1) if np.iscomplexobj(d) else d)
+
+
+@pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsctem", "qscstem"])
+def test_output_folder_as_the_reference_writes_it(tmp_path, name):
+    z, path, out = _inputs(tmp_path, name)
+    qsc.run_qsc(path, ctx=OracleContext(), folder=out)
+    heads = json.loads(str(z["img_headers_json"]))
+    assert set(os.listdir(out)) == set(heads) | EXTRA.get(name, set())
+    for fn, (t, dx, dy, comment, params) in heads.items():
+        im, data = _read(out, fn)
+        assert (np.float32(im.t), np.float32(im.dx), np.float32(im.dy)) == (
+            np.float32(t), np.float32(dx), np.float32(dy)), fn
+        assert im.comment == comment, fn
+        if comment != "STEM image":
+            np.testing.assert_allclose(im.params, params, rtol=1e-6, err_msg=fn)
+        assert rel_l2(data, z["img_" + fn]) <= 1e-6, fn
+
+
+def _tds(runs, save_level):
+    def edit(texts):
+        q = texts["run.qsc"].replace("tds: no", "tds: yes\ntemperature: 300")
+        q = q.replace("Runs for averaging: 1", "Runs for averaging: %d" % runs)
+        q = "\n".join("save level: %d" % save_level if l.startswith("save level:") else l for l in q.split("\n"))
+        # a Debye-Waller factor, so that the Einstein displacements are not zero
+        c = texts["cell.cfg"].replace(" 0.0 1.0 0.0", " 0.5 1.0 0.0")
+        return {"run.qsc": q, "cell.cfg": c}
+    return edit
+
+
+def _running_mean(values):
+    avg = values[0]
+    for j, v in enumerate(values[1:], 1):
+        avg = ((np.float32(j) * avg + v) / np.float32(j + 1)).astype(np.float32)
+    return avg
+
+
+def test_cbed_runs_averaged(tmp_path):
+    _, path, out = _inputs(tmp_path, "qsccbed", _tds(3, 2))
+    ctx = OracleContext()
+    res = qsc.run_qsc(path, ctx=ctx, folder=out)
+    series = [entry for kind, entry in ctx.log if kind == "series"]
+    assert len(series) == 3
+    # save level 2: the patterns are the real-space intensities of the waves
+    finals = [qsc._kspace_pattern(ew[-1, 0], 1 / 64.0) for _, _, ew in series]
+    assert rel_l2(finals[1], finals[0]) > 1e-3  # the runs differ
+    files = set(os.listdir(out))
+    # diffAvg_2 stays (run index 2 is a multiple of the save level), diffAvg_1 does not
+    assert {"diffAvg_2.img", "diffAvg_3.img"} <= files and "diffAvg_1.img" not in files
+    im, data = _read(out, "diffAvg_3.img")
+    assert im.comment == "Averaged Diffraction pattern, unit: 1/A"
+    np.testing.assert_array_equal(data, _running_mean(finals))
+    np.testing.assert_allclose(data, np.mean(finals, 0), rtol=1e-5, atol=1e-6 * np.abs(data).max())
+    np.testing.assert_array_equal(res["diffpat"], data)
+    lines = open(os.path.join(out, "avgresults.dat")).read().split("\n")
+    assert [l.split()[0] for l in lines if l] == ["1", "2"]
+    # thickness series averaged over the runs; interimWave per run with tds
+    for t in range(3):
+        im, data = _read(out, "diff_%d.img" % t)
+        assert im.comment == "Average Array"
+        pats = [qsc._kspace_pattern(ew[t, 0], 1 / 64.0) for _, _, ew in series]
+        np.testing.assert_array_equal(data, _running_mean(pats))
+    for j in range(3):
+        for f in range(3):
+            assert "wave_%d_%d.img" % (j, f) in files
+
+
+def test_tem_runs_averaged(tmp_path):
+    _, path, out = _inputs(tmp_path, "qsctem", _tds(2, 0))
+    ctx = OracleContext()
+    res = qsc.run_qsc(path, ctx=ctx, folder=out)
+    waves = [entry[2][-1, 0].astype(np.float64) for kind, entry in ctx.log if kind == "series"]
+    assert len(waves) == 2
+    mean = np.mean([w[..., 0] ** 2 + w[..., 1] ** 2 for w in waves], 0)
+    im, data = _read(out, "waveIntensity.img")
+    assert im.params[0] == 2 and rel_l2(data, mean) <= 1e-6
+    assert rel_l2(res["exit_intensity"], mean) <= 1e-6
+    im, data = _read(out, "wave.img")
+    assert im.comment == "Test wave function for run 0" and rel_l2(data, waves[0]) <= 1e-6
+    files = set(os.listdir(out))
+    assert {"wave_%d_%d.img" % (j, f) for j in range(2) for f in range(3)} <= files
+
+
+def test_stem_position_patterns_averaged(tmp_path):
+    _, path, out = _inputs(tmp_path, "qscstem", _tds(2, 1))
+    ctx = OracleContext()
+    qsc.run_qsc(path, ctx=ctx, folder=out, chunk=3)  # two chunks of the 2 x 2 raster
+    runs = [entry for kind, entry in ctx.log if kind == "multislice"]
+    assert len(runs) == 4  # 2 runs x 2 chunks
+    pats = [np.concatenate([runs[2 * j][1], runs[2 * j + 1][1]]) for j in range(2)]
+    assert rel_l2(pats[1], pats[0]) > 1e-4
+    for k, (ix, iy) in enumerate([(0, 0), (0, 1), (1, 0), (1, 1)]):
+        im, data = _read(out, "diffAvg_%d_%d.img" % (ix, iy))
+        assert im.comment == "Average Array"
+        np.testing.assert_array_equal(data, _running_mean([pats[0][k], pats[1][k]]))
+    # save level 1, one slab: no exit waves
+    assert not any(f.startswith("mulswav") for f in os.listdir(out))
