@@ -42,12 +42,18 @@ def wavelength(kev):
 
 # --------------------------------------------------------------- unit cells
 class UnitCell:
-    """Orthogonal unit cell: a, b, c (A) and fractional atoms
-    (Z, fx, fy, fz, dw, occ, q)."""
+    """Unit cell: fractional atoms (Z, fx, fy, fz, dw, occ, q) and the cell
+    vectors as the rows of H (A); a, b, c are their lengths.  Orthogonal
+    cells are built from a, b, c alone."""
 
-    def __init__(self, a, b, c, atoms):
+    def __init__(self, a, b, c, atoms, H=None):
         self.a, self.b, self.c = float(a), float(b), float(c)
+        self.H = np.diag([self.a, self.b, self.c]) if H is None else np.asarray(H, dtype=np.float64)
         self.atoms = [tuple(t) for t in atoms]
+
+    @property
+    def orthogonal(self):
+        return bool(np.all(self.H == np.diag(np.diag(self.H))))
 
 
 def srtio3_cell(dw=0.0):
@@ -101,19 +107,45 @@ def _cmp_zyx_key(row):
     return (row[3], row[2], row[1])
 
 
-def replicate(cell, ncx, ncy, ncz):
-    """Cartesian atoms of an ncx x ncy x ncz super-cell, in the order and
-    float32 arithmetic of readUnitCell (libs/fileio_fftw3.cpp:1436-1612):
-    unit-cell atoms sorted by (z, y, x) of their fractional coordinates, then
-    replicated with index ((icz + icy*ncz + icx*ncy*ncz)*ncoord + i), then
-    scaled by the cell vectors in double and stored as float.
-    Returns (atoms[ATOM_DTYPE], ax, by, c) with the super-cell size as float32."""
+def _sorted_fractional(cell):
+    """The unit cell's atoms as records in fractional coordinates, sorted by
+    (z, y, x) as readUnitCell sorts them (libs/fileio_fftw3.cpp:1497-1500)."""
     n = len(cell.atoms)
     frac = np.zeros(n, dtype=abi.ATOM_DTYPE)
     for i, (Z, fx, fy, fz, dw, occ, q) in enumerate(cell.atoms):
         frac[i] = (fz, fy, fx, dw, occ, q, Z)
     order = sorted(range(n), key=lambda i: (frac["z"][i], frac["y"][i], frac["x"][i]))
-    frac = frac[order]
+    return frac[order]
+
+
+def rotation(phi_x, phi_y, phi_z):
+    """rotateVect's matrix (libs/matrixlib.cpp:599-635): rotations by
+    phi_x, phi_y, phi_z (rad) about x, then y, then z, in double with the
+    same products and sums."""
+    cx, sx = math.cos(phi_x), math.sin(phi_x)
+    cy, sy = math.cos(phi_y), math.sin(phi_y)
+    cz, sz = math.cos(phi_z), math.sin(phi_z)
+    return np.array([[cz * cy, cz * sy * sx - sz * cx, cz * sy * cx + sz * sx],
+                     [sz * cy, sz * sy * sx + cz * cx, sz * sy * cx - cz * sx],
+                     [-sy, cy * sx, cy * cx]])
+
+
+def _mat_vec(M, u0, u1, u2):
+    """M (3x3) times the vectors (u0, u1, u2), each row summed left to right."""
+    return [(M[i, 0] * u0 + M[i, 1] * u1) + M[i, 2] * u2 for i in range(3)]
+
+
+def supercell(cell, ncx, ncy, ncz, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0)):
+    """readUnitCell's NCELL mode (libs/fileio_fftw3.cpp:1512-1645): the unit
+    cell replicated ncx x ncy x ncz times in fractional coordinates (atom
+    j = (icz + icy*ncz + icx*ncy*ncz)*ncoord + i), converted to Cartesian by
+    the cell vectors, rotated by the crystal tilt about the centre of the
+    super-cell, shifted so that the bounding box of the (rotated) super-cell
+    starts at 0, then offset by (xOffset, yOffset).  Double arithmetic with
+    float32 storage where the reference stores floats.
+    Returns (atoms[ATOM_DTYPE], ax, by, c): the bounding box size, float32."""
+    frac = _sorted_fractional(cell)
+    n = len(frac)
     out = np.zeros(n * ncx * ncy * ncz, dtype=abi.ATOM_DTYPE)
     for icx in range(ncx):
         for icy in range(ncy):
@@ -124,13 +156,114 @@ def replicate(cell, ncx, ncy, ncz):
                 blk["x"] = (frac["x"].astype(np.float64) + icx).astype(F32)
                 blk["y"] = (frac["y"].astype(np.float64) + icy).astype(F32)
                 blk["z"] = (frac["z"].astype(np.float64) + icz).astype(F32)
-    out["x"] = (cell.a * out["x"].astype(np.float64)).astype(F32)
-    out["y"] = (cell.b * out["y"].astype(np.float64)).astype(F32)
-    out["z"] = (cell.c * out["z"].astype(np.float64)).astype(F32)
-    ax = F32(cell.a * ncx / 2.0 + cell.a * ncx / 2.0)
-    by = F32(cell.b * ncy / 2.0 + cell.b * ncy / 2.0)
-    cc = F32(cell.c * ncz / 2.0 + cell.c * ncz / 2.0)
-    return out, ax, by, cc
+    # Cartesian: x_j = sum_k Mm[k][j] * frac_k with Mm's rows the cell vectors
+    Mt = cell.H.T
+    fx, fy, fz = (out[k].astype(np.float64) for k in ("x", "y", "z"))
+    cart = _mat_vec(Mt, fx, fy, fz)
+    for k, v in zip(("x", "y", "z"), cart):
+        out[k] = v.astype(F32)
+    bc = (ncx / 2.0, ncy / 2.0, ncz / 2.0)
+    centre = _mat_vec(Mt, *bc)
+    R = rotation(*tilt)
+    lo, hi = None, None
+    for icx in (0, ncx):
+        for icy in (0, ncy):
+            for icz in (0, ncz):
+                u = _mat_vec(Mt, icx - bc[0], icy - bc[1], icz - bc[2])
+                u = _mat_vec(R, *u)
+                c = [u[k] + centre[k] for k in range(3)]
+                lo = list(c) if lo is None else [min(lo[k], c[k]) for k in range(3)]
+                hi = list(c) if hi is None else [max(hi[k], c[k]) for k in range(3)]
+    if any(t != 0 for t in tilt):
+        u = [out[k].astype(np.float64) - centre[i] for i, k in enumerate(("x", "y", "z"))]
+        u = _mat_vec(R, *u)
+        for i, k in enumerate(("x", "y", "z")):
+            out[k] = (u[i] + centre[i]).astype(F32)
+    for i, k in enumerate(("x", "y", "z")):
+        out[k] = (out[k].astype(np.float64) - lo[i]).astype(F32)
+    if offset[0] != 0 or offset[1] != 0:
+        out["x"] = (out["x"] + F32(offset[0])).astype(F32)
+        out["y"] = (out["y"] + F32(offset[1])).astype(F32)
+    return out, F32(hi[0] - lo[0]), F32(hi[1] - lo[1]), F32(hi[2] - lo[2])
+
+
+def cube(cell, size, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0), seed=None):
+    """tiltBoxed (libs/fileio_fftw3.cpp:1661-1940): the atoms of the crystal,
+    rotated by the crystal tilt about the origin and shifted by (xOffset,
+    yOffset), that fall inside the box [0, size] (the "Cube:" sizes).  Unit
+    cells are walked over the range that covers the box's corners; atoms are
+    listed per unit-cell atom (sorted as readUnitCell sorts them), then by
+    cell (x, y, z).  Unit-cell atoms at equal positions are one site: one of
+    them is kept per cell, chosen by a uniform draw over their occupancies
+    (numpy.random.default_rng(seed); the reference draws with ran1); the
+    first stays when the draw falls past a total occupancy below 1, as in
+    the reference.  Returns (atoms[ATOM_DTYPE], ax, by, c) = the box."""
+    frac = _sorted_fractional(cell)
+    n = len(frac)
+    cx, cy, cz = (F32(v) for v in size)
+    dx, dy, dz = float(F32(offset[0])), float(F32(offset[1])), 0.0
+    # rotateMatrix(Mm) with Mm the transposed cell matrix: Mrot * Mm, sums from 0
+    R = rotation(*tilt)
+    Mt = cell.H.T
+    M = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(3):
+            acc = 0.0
+            for k in range(3):
+                acc += R[i, k] * Mt[k, j]
+            M[i, j] = acc
+    Minv = np.linalg.inv(M)
+    b = Minv @ np.zeros(3)
+    nmin = [int(math.floor(b[0] - dx)), int(math.floor(b[1] - dy)), int(math.floor(b[2] - dz))]
+    nmax = list(nmin)
+    for ix in (0, 1):
+        for iy in (0, 1):
+            for iz in (0, 1):
+                b = Minv @ np.array([ix * float(cx) - dx, iy * float(cy) - dy, iz * float(cz) - dz])
+                for k in range(3):
+                    nmin[k] = min(nmin[k], int(math.floor(b[k])))
+                    nmax[k] = max(nmax[k], int(math.ceil(b[k])))
+    rng = np.random.default_rng(seed)
+    cells = np.array([(i, j, k) for i in range(nmin[0], nmax[0] + 1) for j in range(nmin[1], nmax[1] + 1)
+                      for k in range(nmin[2], nmax[2] + 1)], dtype=np.float64)
+    kept = []
+    i = 0
+    while i < n:
+        j = i + 1
+        occ = float(frac["occ"][i])
+        if frac["Znum"][i] > 0:
+            while j < n and all(abs(float(frac[k][j]) - float(frac[k][i])) < 1e-6 for k in ("x", "y", "z")):
+                occ += float(frac["occ"][j])
+                j += 1
+        else:
+            occ = 1.0
+        # ix + newAtom.x: an int plus a float, added in float
+        pos = [(cells[:, k].astype(F32) + frac[c][i]).astype(np.float64) for k, c in enumerate(("x", "y", "z"))]
+        cart = _mat_vec(M, *pos)
+        x, y, z = cart[0] + dx, cart[1] + dy, cart[2] + dz
+        inside = (x >= 0) & (x <= float(cx)) & (y >= 0) & (y <= float(cy)) & (z >= 0) & (z <= float(cz))
+        choice = np.full(len(cells), i)
+        if occ < 1.0 or j > i + 1:
+            u = rng.random(len(cells)) * (1.0 if occ < 1.0 else occ)
+            last = 0.0
+            for m in range(i, j):
+                o = float(frac["occ"][m])
+                choice[(u >= last) & (u < last + o)] = m
+                last += o
+        for c in np.nonzero(inside)[0]:
+            rec = frac[choice[c]].copy()
+            rec["x"], rec["y"], rec["z"] = F32(x[c]), F32(y[c]), F32(z[c])
+            kept.append(rec)
+        i = j
+    atoms = np.array(kept, dtype=abi.ATOM_DTYPE) if kept else np.zeros(0, abi.ATOM_DTYPE)
+    return atoms, cx, cy, cz
+
+
+def replicate(cell, ncx, ncy, ncz):
+    """Cartesian atoms of an ncx x ncy x ncz super-cell without tilt or
+    offset (supercell).  Returns (atoms[ATOM_DTYPE], ax, by, c) with the
+    super-cell size as float32."""
+    return supercell(cell, ncx, ncy, ncz)
 
 
 # ------------------------------------------------------------------ params

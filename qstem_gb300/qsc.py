@@ -99,9 +99,10 @@ def _yes(v, default=False):
 
 
 def read_cfg(path):
-    """A unit cell from an AtomEye .cfg (orthogonal H0 only): fractional
-    coordinates with the dw, occupancy and charge columns when present
-    (default dw = 0.45*28/mass, occupancy 1, charge 0)."""
+    """A unit cell from an AtomEye .cfg: the cell vectors H0 (rows, times
+    the length scale "A =") and fractional coordinates with the dw,
+    occupancy and charge columns when present (default dw = 0.45*28/mass,
+    occupancy 1, charge 0)."""
     pf = ParamFile(path, comment="#")
     ncoord = int(_num(pf.get("Number of particles ="), 0))
     scale = _num(pf.get("A ="), 1.0)
@@ -109,8 +110,6 @@ def read_cfg(path):
     for i in range(3):
         for j in range(3):
             H[i, j] = _num(pf.get("H0(%d,%d) =" % (i + 1, j + 1)), 0.0) * scale
-    if np.abs(H - np.diag(np.diag(H))).max() > 0:
-        raise NotImplementedError("%s: non-orthogonal cells are not supported" % path)
     # the atom lines follow the header: readNextCFGAtom reads on from the
     # "entry_count =" line (with .NO_VELOCITY., else 3 velocity columns too)
     pf.pos = 0
@@ -153,7 +152,7 @@ def read_cfg(path):
         atoms.append((Z, vals[0], vals[1], vals[2], dw, occ, q))
     if ncoord and len(atoms) != ncoord:
         raise ValueError("%s: %d atoms listed, %d announced" % (path, len(atoms), ncoord))
-    return config.UnitCell(H[0, 0], H[1, 1], H[2, 2], atoms)
+    return config.UnitCell(*(float(np.sqrt(np.dot(H[i], H[i]))) for i in range(3)), atoms, H=H)
 
 
 @dataclass
@@ -232,12 +231,25 @@ def _energy_spread_series(dE_E0, avg_runs):
     return arr[:avg_runs]
 
 
-def read_qsc(path):
+def read_qsc(path, seed=20261203):
     """Parse a stem3 .qsc (and the .cfg it names, relative to the .qsc's
-    folder) into a QscRun."""
+    folder) into a QscRun.  seed: the draw that picks one of several atoms
+    sharing a site in a "Cube:" box (the reference draws with ran1)."""
     pf = ParamFile(path)
     g = pf.get
     unsupported = []
+    # readFile parses yes/no answers into one buffer, `answer`; a key that
+    # is absent leaves the previous answer there, and "smooth:" is decided
+    # from whatever it holds (stem3/stem3.cpp:1262-1263)
+    answer = [""]
+
+    def ans(v, k=0, reset=False):
+        if reset:
+            answer[0] = ""
+        if v is not None and len(v.split()) > k:
+            answer[0] = v.split()[k]
+        return v
+
     mode_s = g("mode:") or ""
     mode = "STEM" if "STEM" in mode_s else "TEM" if "TEM" in mode_s else "CBED" if "CBED" in mode_s else (
         "NBED" if "NBED" in mode_s else "STEM" if not mode_s.strip() else mode_s.strip())
@@ -248,33 +260,46 @@ def read_qsc(path):
     cfg = _word(g("filename:"))
     ncx = int(_num(g("NCELLX:"), 1))
     ncy = int(_num(g("NCELLY:"), 1))
-    nz_s = _word(g("NCELLZ:"), "1")
+    nz_s = _word(ans(g("NCELLZ:")), "1")
     cellDiv = 1
     if "/" in nz_s:
         nz_s, d = nz_s.split("/", 1)
         cellDiv = int(float(d))
     ncz = int(float(nz_s))
-    for key in ("Beam tilt X:", "Beam tilt Y:", "Tilt back:", "Crystal tilt X:", "Crystal tilt Y:",
-                "Crystal tilt Z:"):
-        v = g(key)
+    for key in ("Beam tilt X:", "Beam tilt Y:", "Tilt back:"):
+        v = ans(g(key), 0 if key == "Tilt back:" else 1, reset=key != "Tilt back:")
         if key != "Tilt back:" and _num(v, 0.0) != 0.0:
             unsupported.append(key.rstrip(":"))
-    cube = g("Cube:")
-    if cube is not None and any(float(t) != 0 for t in cube.split()[:3] if _isnum(t)):
-        unsupported.append("Cube")
-    tds = _yes(g("tds:"))
+    # crystal tilt in rad, or in degrees with a unit word starting with "d"
+    # (stem3/stem3.cpp:723-743; the values are floats)
+    tilt = []
+    for key in ("Crystal tilt X:", "Crystal tilt Y:", "Crystal tilt Z:"):
+        v = ans(g(key), 1, reset=True)
+        t = F32(_num(v, 0.0))
+        words = (v or "").split()
+        if len(words) > 1 and words[1][:1].lower() == "d":
+            t = F32(float(t) * (3.1415926535897 / 180.0))
+        tilt.append(float(t))
+    cube_v = g("Cube:")
+    cube = None
+    if cube_v is not None:
+        vals = [float(F32(float(t))) for t in cube_v.split()[:3] if _isnum(t)]
+        if len(vals) == 3 and all(v > 0 for v in vals):
+            cube = vals
+    ans(g("Adjust cube size with tilt:"))
+    tds = _yes(ans(g("tds:")))
     temperature = _num(g("temperature:"), 300.0)
     if g("phonon-File:") is not None:
         unsupported.append("phonon-File")
     # the unit cell (readUnitCell: .cfg read, replicated, then shifted)
     cfg_path = os.path.join(os.path.dirname(os.path.abspath(path)), cfg)
     cell = read_cfg(cfg_path)
-    atoms, ax, by, c = config.replicate(cell, ncx, ncy, ncz)
     xoff = _num(g("xOffset:"), 0.0)
     yoff = _num(g("yOffset:"), 0.0)
-    if xoff != 0 or yoff != 0:  # libs/fileio_fftw3.cpp:1634-1640
-        atoms["x"] = (atoms["x"] + F32(xoff)).astype(F32)
-        atoms["y"] = (atoms["y"] + F32(yoff)).astype(F32)
+    if cube is not None:  # a box cut from the tilted crystal (tiltBoxed)
+        atoms, ax, by, c = config.cube(cell, cube, tuple(tilt), (xoff, yoff), seed=seed)
+    else:  # NCELL mode
+        atoms, ax, by, c = config.supercell(cell, ncx, ncy, ncz, tuple(tilt), (xoff, yoff))
     nx = int(_num(g("nx:"), 0))
     ny_v = g("ny:")
     ny = int(_num(ny_v, nx)) if ny_v is not None else nx
@@ -283,7 +308,7 @@ def read_qsc(path):
     v0 = _num(g("v0:"), 0.0)
     if nx < 1 or v0 <= 0:
         raise ValueError("%s: nx and v0 are required" % path)
-    centerSlices = _yes(g("center slices:"))
+    centerSlices = _yes(ans(g("center slices:")))
     dz_v = g("slice-thickness:")
     if dz_v is not None:
         dz = _num(dz_v, 0.0)
@@ -296,11 +321,20 @@ def read_qsc(path):
         sl_v = g("slices:")
         slices = int(_num(sl_v, 0))
         if slices == 1 and cellDiv == 1:
-            dz = float(F32(c)) if centerSlices else float(F32(c)) / cellDiv
+            if cube is not None:
+                dz = float(F32(2.0 * float(F32(c)) / cellDiv)) if centerSlices else float(F32(float(F32(c)) / cellDiv))
+            else:
+                dz = float(F32(c)) if centerSlices else float(F32(c)) / cellDiv
+        elif cube is not None:
+            dz = float(F32(F32(c) / F32(cellDiv * slices - int(centerSlices))))
         else:
             dz = float(F32(F32(c) / F32(cellDiv * slices)))
     if slices < 1:
         raise ValueError("%s: number of slices = 0" % path)
+    # only the slice-thickness branch adds the centre slice
+    # (stem3/stem3.cpp:880-892); make_params adds it, so take it off here
+    if dz_v is None:
+        slices -= int(centerSlices)
     out_v = g("slices between outputs:")
     outputInterval = int(_num(out_v, 0)) if out_v is not None else None
     czOffset = _num(g("zOffset:"), 0.0)
@@ -308,14 +342,17 @@ def read_qsc(path):
         resX = float(F32(float(F32(ax)) / nx))
     if resY == 0.0:
         resY = float(F32(float(F32(by)) / ny))
-    periodicXY = _yes(g("periodicXY:"))
-    periodicZ = _yes(g("periodicZ:"))
-    bandlimit = _yes(g("bandlimit f_trans:"), False)
-    g("one time integration:")
-    pot3d = g("potential3D:")
+    periodicXY = _yes(ans(g("periodicXY:")))
+    periodicZ = _yes(ans(g("periodicZ:")))
+    bandlimit = _yes(ans(g("bandlimit f_trans:")), True)  # on unless said otherwise
+    for key in ("read potential:", "save potential:", "save projected potential:", "plot V(r)*r:",
+                "one time integration:"):
+        ans(g(key))
+    pot3d = ans(g("potential3D:"))
     if pot3d is not None and not _yes(pot3d, True):
         unsupported.append("potential3D: no (the 2-D potential)")
     avg_runs = int(_num(g("Runs for averaging:"), 10))
+    ans(g("Store TDS diffr. patt. series:"))
     if not tds:  # stem3/stem3.cpp:1023
         avg_runs = 1
     scan_step = (1.0, 1.0)
@@ -339,7 +376,7 @@ def read_qsc(path):
     Cc = _num(g("Cc:"), 0.0)
     Cs = _num(g("Cs:"), 0.0)
     C5 = _num(g("C5:"), 0.0)
-    df = g("defocus:")
+    df = ans(g("defocus:"))
     df_w = _word(df)
     astig = _num(g("astigmatism:"), 0.0)
     astig_deg = _num(g("astigmatism angle:"), 0.0)
@@ -352,7 +389,8 @@ def read_qsc(path):
     aAIS = _num(g("AIS aperture:"), 0.0)
     beam = _num(g("beam current:"), 1.0)
     dwell = _num(g("dwell time:"), 1.0)
-    smooth = _yes(g("smooth:"), True)
+    ans(g("smooth:"))
+    smooth = answer[0][:1].lower() == "y"
     gv = g("gaussian:")
     gaussian = None
     if gv is not None and _yes(gv):

@@ -210,6 +210,32 @@ def qsc_case():
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+def qsc_geometry_case(name, qsc_file, cfg_file):
+    """readFile on a hand-written input of tests/golden/qsc/ (crystal tilt,
+    non-orthogonal cells, "Cube:" boxes): the MULS fields it derives and the
+    atoms readUnitCell builds, with the input texts."""
+    src = os.path.join(HERE, "qsc")
+    work = tempfile.mkdtemp(prefix="qs_golden_")
+    try:
+        for f in (qsc_file, cfg_file):
+            shutil.copy(os.path.join(src, f), work)
+        dump = os.path.join(work, "dump")
+        oracle.run_reference(os.path.join(work, qsc_file), dump, run=False)
+        meta = dict(l.split(" = ", 1) for l in open(os.path.join(dump, "meta.txt")).read().strip().split("\n"))
+        out = {"atoms": np.fromfile(os.path.join(dump, "atoms.bin"), dtype=abi.ATOM_DTYPE),
+               "meta_json": np.array(json.dumps(meta)),
+               "qsc_text": np.array(open(os.path.join(src, qsc_file)).read()),
+               "cfg_name": np.array(cfg_file),
+               "cfg_text": np.array(open(os.path.join(src, cfg_file)).read())}
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes", len(out["atoms"]), "atoms")
+
+
+GEOMETRY_CASES = {"qsctilt": ("tilt.qsc", "hex.cfg"), "qsccube": ("cube.qsc", "cell.cfg")}
+
 # whole stem3 runs whose output folders pin qstem_gb300.qsc.run_qsc: every
 # .img file the reference wrote (name, header, data)
 RUN_CASES = {
@@ -274,6 +300,9 @@ def main(names=None):
     for name, case in RUN_CASES.items():
         if not names or name in names:
             qsc_run_case(name, case)
+    for name, (q, c) in GEOMETRY_CASES.items():
+        if not names or name in names:
+            qsc_geometry_case(name, q, c)
     for name, case in CASES.items():
         if names and name not in names:
             continue

@@ -93,7 +93,7 @@ def test_fixture_inputs_read_back(name):
 def test_refused_inputs():
     z = np.load(os.path.join(GOLDEN, "qscread.npz"))
     base = str(z["qsc_text"])
-    for extra in ("Cube: 30 30 40", "Crystal tilt X: 0.01", "potential3D: no"):
+    for extra in ("Beam tilt X: 0.01", "phonon-File: modes.dat", "potential3D: no"):
         text = base.replace("print level: 1", extra + "\nprint level: 1")
         if extra.startswith("potential3D"):
             text = base.replace("potential3D: yes", extra)
@@ -124,3 +124,30 @@ def test_seeded_vacancies():
     # a shared Fe/Ni site keeps exactly one of the two
     fe, ni = atoms["Znum"] == 26, atoms["Znum"] == 28
     assert np.sum(a["Znum"][fe] == 26) + np.sum(a["Znum"][ni] == 28) == np.sum(fe)
+
+
+def _read_geometry(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = _write({"run.qsc": str(z["qsc_text"]), str(z["cfg_name"]): str(z["cfg_text"])})
+    return qsc.read_qsc(os.path.join(d, "run.qsc")), json.loads(str(z["meta_json"])), z["atoms"]
+
+
+@pytest.mark.parametrize("name", ["qsctilt", "qsccube"])
+def test_tilted_and_boxed_crystals_match_the_references_readfile(name):
+    """Crystal tilt about x and y of a non-orthogonal cell replicated in
+    NCELL mode, and a "Cube:" box cut from a crystal tilted about x and z
+    (with centre slices and no slice thickness): the atoms readUnitCell /
+    tiltBoxed produce, bit for bit, and the fields readFile derives."""
+    run, meta, atoms = _read_geometry(name)
+    assert len(run.atoms) == len(atoms) == int(meta["natom"])
+    for k in ("x", "y", "z", "dw", "occ", "q", "Znum"):
+        np.testing.assert_array_equal(run.atoms[k], atoms[k], err_msg=k)
+    p = run.params
+    for k, v in meta.items():
+        if k.startswith("det") or k in ("natom", "avgRuns"):
+            continue
+        got = getattr(p, k)
+        if isinstance(got, int):
+            assert got == int(v), k
+        else:
+            assert F32(got) == F32(float(v)), (k, got, v)
