@@ -220,13 +220,18 @@ def qsc_geometry_case(name, qsc_file, cfg_file):
         for f in (qsc_file, cfg_file):
             shutil.copy(os.path.join(src, f), work)
         dump = os.path.join(work, "dump")
-        oracle.run_reference(os.path.join(work, qsc_file), dump, run=False)
+        oracle.run_reference(os.path.join(work, qsc_file), dump, run=True)
         meta = dict(l.split(" = ", 1) for l in open(os.path.join(dump, "meta.txt")).read().strip().split("\n"))
         out = {"atoms": np.fromfile(os.path.join(dump, "atoms.bin"), dtype=abi.ATOM_DTYPE),
                "meta_json": np.array(json.dumps(meta)),
                "qsc_text": np.array(open(os.path.join(src, qsc_file)).read()),
                "cfg_name": np.array(cfg_file),
                "cfg_text": np.array(open(os.path.join(src, cfg_file)).read())}
+        # doSTEM's detector images of every thickness slot
+        nt = (int(meta["slices"]) * int(meta["cellDiv"])) // int(meta["outputInterval"]) + 1
+        nd, sx, sy = int(meta["detectorNum"]), int(meta["scanXN"]), int(meta["scanYN"])
+        out["det"] = np.stack([np.stack([np.fromfile(os.path.join(dump, "det_%d_%d.bin" % (t, i)), np.float32)
+                                         .reshape(sx, sy) for i in range(nd)]) for t in range(nt)])
     finally:
         shutil.rmtree(work, ignore_errors=True)
     path = os.path.join(HERE, name + ".npz")

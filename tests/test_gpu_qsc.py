@@ -84,3 +84,19 @@ def test_output_folder_matches_the_references(name):
         if np.iscomplexobj(data):
             data = np.stack([data.real, data.imag], -1)
         assert rel_l2(data, z["img_" + fn]) <= 1e-4, fn
+
+
+@pytest.mark.parametrize("name", ["qsctilt", "qsccube"])
+def test_tilted_and_boxed_crystals_end_to_end(name):
+    """A non-orthogonal cell tilted about x and y, and a Cube box cut from a
+    crystal tilted about x and z: run_qsc's detector images of every
+    thickness slot against the reference's doSTEM on the same input."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = tempfile.mkdtemp()
+    for fn, text in (("run.qsc", str(z["qsc_text"])), (str(z["cfg_name"]), str(z["cfg_text"]))):
+        with open(os.path.join(d, fn), "w") as f:
+            f.write(text)
+    out = qsc.run_qsc(os.path.join(d, "run.qsc"), folder=os.path.join(d, "out"))
+    ref = z["det"]
+    assert out["adf"].shape == ref[:, 0].shape
+    assert rel_l2(out["adf"], ref[:, 0]) <= 1e-4

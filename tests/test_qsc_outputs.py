@@ -135,3 +135,15 @@ def test_stem_position_patterns_averaged(tmp_path):
         np.testing.assert_array_equal(data, _running_mean([pats[0][k], pats[1][k]]))
     # save level 1, one slab: no exit waves
     assert not any(f.startswith("mulswav") for f in os.listdir(out))
+
+
+@pytest.mark.parametrize("name", ["qsctilt", "qsccube"])
+def test_tilted_and_boxed_crystals_through_the_oracle(tmp_path, name):
+    """The detector images of the tilted / boxed inputs through the oracle
+    stand-in match the reference's doSTEM (the atom front end feeds the
+    slice builder what readUnitCell feeds make3DSlices)."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    (tmp_path / "run.qsc").write_text(str(z["qsc_text"]))
+    (tmp_path / str(z["cfg_name"])).write_text(str(z["cfg_text"]))
+    out = qsc.run_qsc(str(tmp_path / "run.qsc"), ctx=OracleContext(), folder=str(tmp_path / "out"))
+    assert rel_l2(out["adf"], z["det"][:, 0]) <= 1e-6
