@@ -172,6 +172,8 @@ class QscRun:
     dE_E: list = field(default_factory=list)    # energy deviation of each run (dE_EArray)
     scan_step: tuple = (1.0, 1.0)               # detector image sampling, from the .qsc's scan range
     save_level: int = 0                         # "save level:"
+    beam_tilt: tuple = (0.0, 0.0)               # rad (TEM: a tilted incident plane wave)
+    tilt_back: bool = True                      # "Tilt back:" (TEM: wave.img tilted back)
     spread: tuple = (0.0, 0.0, 0.0)             # dE/E, dI/I, dV/V as read (CBED/TEM use them as such)
 
     def einstein_sigma(self):
@@ -266,10 +268,18 @@ def read_qsc(path, seed=20261203):
         nz_s, d = nz_s.split("/", 1)
         cellDiv = int(float(d))
     ncz = int(float(nz_s))
-    for key in ("Beam tilt X:", "Beam tilt Y:", "Tilt back:"):
-        v = ans(g(key), 0 if key == "Tilt back:" else 1, reset=key != "Tilt back:")
-        if key != "Tilt back:" and _num(v, 0.0) != 0.0:
-            unsupported.append(key.rstrip(":"))
+    # beam tilt in rad, or in degrees with a unit word starting with "d"
+    # (stem3/stem3.cpp:699-717; floats); tilt back on unless said otherwise
+    beam_tilt = []
+    for key in ("Beam tilt X:", "Beam tilt Y:"):
+        v = ans(g(key), 1, reset=True)
+        t = F32(_num(v, 0.0))
+        words = (v or "").split()
+        if len(words) > 1 and words[1][:1].lower() == "d":
+            t = F32(float(t) * (3.1415926535897 / 180.0))
+        beam_tilt.append(float(t))
+    tb = ans(g("Tilt back:"))
+    tilt_back = True if tb is None else _yes(tb)
     # crystal tilt in rad, or in degrees with a unit word starting with "d"
     # (stem3/stem3.cpp:723-743; the values are floats)
     tilt = []
@@ -435,7 +445,8 @@ def read_qsc(path, seed=20261203):
     series = _energy_spread_series(dE0, max(avg_runs, 1))
     return QscRun(params=p, atoms=atoms, cell=cell, ncell=(ncx, ncy, ncz), mode=mode, tds=tds,
                   temperature=temperature, avg_runs=avg_runs, folder=folder, detector_names=names, dE_E=series,
-                  scan_step=scan_step, save_level=save_level, spread=(dE_E, dI_I, dV_V))
+                  scan_step=scan_step, save_level=save_level, spread=(dE_E, dI_I, dV_V),
+                  beam_tilt=tuple(beam_tilt), tilt_back=tilt_back)
 
 
 def _isnum(t):
@@ -601,13 +612,29 @@ def _run_stem(ctx, run, where, seed, chunk):
     return out
 
 
-def _wave_params(p, spread):
+def _wave_params(p, spread, beam_tilt=(0.0, 0.0)):
     """interimWave's nine header parameters (stem3/stemlib.cpp:2545-2556):
     v0, Cs, df0, astigmatism and its angle, Cc * total energy spread, alpha,
-    beam tilt x and y (no beam tilt here)."""
+    beam tilt x and y."""
     dE, dI, dV = (float(F32(v)) for v in spread)
     return [float(p.v0), float(p.Cs), float(p.df0), float(p.astigMag), float(p.astigAngle),
-            float(F32(float(p.Cc) * math.sqrt(dE * dE + dV * dV + dI * dI))), float(p.alpha), 0.0, 0.0]
+            float(F32(float(p.Cc) * math.sqrt(dE * dE + dV * dV + dI * dI))), float(p.alpha),
+            float(beam_tilt[0]), float(beam_tilt[1])]
+
+
+def _beam_phase(p, beam_tilt, sign):
+    """The phase of doTEM's tilted plane wave per row ix
+    (stem3/stem3.cpp:2409-2419, and -tilt for the tilt back at :2498-2508):
+    k_t = sign * 2 pi sin(tilt) / lambda, x = dx (ix - nx/2), and y taken as
+    dy (ix - nx/2) as the reference does, so the wave is constant along y."""
+    lam = config.wavelength(float(F32(p.v0)))
+    pi = 3.1415926535897
+    ktx = sign * 2.0 * pi * math.sin(beam_tilt[0]) / lam
+    kty = sign * 2.0 * pi * math.sin(beam_tilt[1]) / lam
+    d = (np.arange(p.nx) - p.nx // 2).astype(F32)
+    x = (F32(p.resolutionX) * d).astype(F32).astype(np.float64)
+    y = (F32(p.resolutionY) * d).astype(F32).astype(np.float64)
+    return [ktx * a + kty * b for a, b in zip(x, y)]
 
 
 def _run_cbed(ctx, run, where, seed):
@@ -684,7 +711,7 @@ def _run_cbed(ctx, run, where, seed):
                 t = nT - 1 if a == SA - 1 else a // oi
                 name = "wave_%d_%d.img" % (j, f) if run.tds else "wave_%d.img" % f
                 imageio.write_img(os.path.join(where, name), ews[t, 0], t=_thick(a + 1, dz), dx=rx, dy=ry,
-                                  params=_wave_params(p, run.spread), comment="Wave Function")
+                                  params=_wave_params(p, run.spread, run.beam_tilt), comment="Wave Function")
         for t in range(nT):
             if slot_pat[t] is None:
                 continue
@@ -738,6 +765,11 @@ def _run_tem(ctx, run, where, seed):
     rx, ry = float(F32(p.resolutionX)), float(F32(p.resolutionY))
     plane = np.zeros((nx, ny, 2), np.float32)
     plane[..., 0] = 1.0  # stem3/stem3.cpp:2403-2407
+    tilted = run.beam_tilt[0] != 0 or run.beam_tilt[1] != 0
+    if tilted:
+        ph = _beam_phase(p, run.beam_tilt, 1.0)
+        plane[..., 0] = np.array([F32(math.cos(v)) for v in ph], np.float32)[:, None]
+        plane[..., 1] = np.array([F32(math.sin(v)) for v in ph], np.float32)[:, None]
     pos = tuple(np.zeros(1, np.int32) for _ in range(4))
     files = _interim_files(SA, oi)
     acc = np.zeros((nx, ny), np.float64)
@@ -757,9 +789,18 @@ def _run_tem(ctx, run, where, seed):
             t = nT - 1 if a == SA - 1 else a // oi
             name = "wave_%d_%d.img" % (j, f) if run.tds else "wave_%d.img" % f
             imageio.write_img(os.path.join(where, name), ews[t, 0], t=_thick(a + 1, dz), dx=rx, dy=ry,
-                              params=_wave_params(p, run.spread), comment="Wave Function")
+                              params=_wave_params(p, run.spread, run.beam_tilt), comment="Wave Function")
         if j == 0:
-            imageio.write_img(os.path.join(where, "wave.img"), exit_wave, t=t_end, dx=rx, dy=ry,
+            saved = exit_wave
+            if run.tilt_back and tilted:
+                # re *= cos(phase), im *= sin(phase): the reference scales the
+                # two parts separately (stem3/stem3.cpp:2498-2508)
+                ph = _beam_phase(p, run.beam_tilt, -1.0)
+                c = np.array([math.cos(v) for v in ph])[:, None]
+                sn = np.array([math.sin(v) for v in ph])[:, None]
+                saved = np.stack([(exit_wave[..., 0].astype(np.float64) * c).astype(F32),
+                                  (exit_wave[..., 1].astype(np.float64) * sn).astype(F32)], -1)
+            imageio.write_img(os.path.join(where, "wave.img"), saved, t=t_end, dx=rx, dy=ry,
                               comment="Test wave function for run 0" if run.tds else
                               "Exit face wave function for no TDS")
     mean = (acc / run.avg_runs).astype(np.float32)

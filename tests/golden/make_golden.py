@@ -257,6 +257,11 @@ RUN_CASES = {
     "qsctem": dict(cell="si", ncell=(4, 3, 4), nx=64, resolutionX=0.06, v0=300.0, slices=7, sliceThickness=2.0,
                    scan=None, detectors=[], alpha=0.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
                    outputInterval=3, mode="TEM", saveLevel=0),
+    # TEM with a tilted incident beam (and the exit wave tilted back)
+    "qsctemtilt": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06, v0=300.0, slices=5, sliceThickness=2.0,
+                       scan=None, detectors=[], alpha=0.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
+                       outputInterval=2, mode="TEM", saveLevel=0,
+                       extra=["Beam tilt X: 0.004", "Beam tilt Y: 0.2 deg", "Tilt back: yes"]),
     # STEM at save level 2: per-position diffAvg_ix_iy.img and mulswav_ix_iy.img
     "qscstem": dict(cell="sto", ncell=(3, 3, 4), nx=64, resolutionX=0.0915, v0=200.0, slices=8,
                     sliceThickness=1.9525, scan=(3.905, 7.81, 2, 3.905, 7.81, 2),
@@ -279,6 +284,9 @@ def qsc_run_case(name, case):
                          alpha=case["alpha"], Cs_mm=case.get("Cs_mm", 0.0), defocus_nm=case.get("defocus_nm", 0.0),
                          outputInterval=case.get("outputInterval"), mode=case["mode"],
                          bandlimit=case.get("bandlimit", False), folder="out", saveLevel=case["saveLevel"])
+        if case.get("extra"):
+            with open(qsc, "a") as f:
+                f.write("\n".join(case["extra"]) + "\n")
         oracle.run_reference(qsc, os.path.join(work, "dump"), run=True)
         out = {"qsc_text": np.array(open(qsc).read()),
                "cfg_text": np.array(open(os.path.join(work, "cell.cfg")).read())}
