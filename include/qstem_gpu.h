@@ -259,7 +259,9 @@ typedef struct qs_cbed_report {
  * their footprints (slice stacks + waves + probes + patterns) fits the budget:
  * the free device memory less 1 GiB, or max_bytes if that is smaller and not
  * 0.  An instance that alone does not fit is rejected (QS_ERR_NOMEM).
- * report may be NULL. */
+ * A cell divided into slabs (cellDiv > 1) runs through all of them, as
+ * doCBED's slab loop does: one stack per slab (slab 0's, copied, for equal
+ * divisions).  report may be NULL. */
 int qs_cbed_batch_run(qs_ctx *ctx, const qs_cbed_job *jobs, int njobs, size_t max_bytes,
                       qs_cbed_report *report);
 
@@ -286,8 +288,9 @@ typedef struct qs_ctf {
 /* doTEM for `nconf` frozen-phonon configurations (stem3/stem3.cpp:2354-2710).
  * atoms holds the configurations back to back, natoms[c] atoms each (host).
  * Every configuration gets its own slice stack (make3DSlices +
- * initSTEMSlices), and all of them run as one batch from doTEM's untilted
- * incident plane wave psi = 1 (:2403-2406) to their exit waves.
+ * initSTEMSlices; one per slab of a cell divided into unequal slabs), and
+ * all of them run as one batch from doTEM's untilted incident plane wave
+ * psi = 1 (:2403-2406) to their exit waves.
  * Outputs (HOST buffers, each may be NULL):
  *   mean_intensity  [nx][ny] float, the mean over configurations of
  *                   |psi_exit|^2 (doTEM's image.img holds (nx*ny)^2 times

@@ -883,6 +883,10 @@ struct CbedUnit {
 
 size_t rup256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// slices a wave passes through: cellDiv slabs of `slices` (doCBED's slab
+// loop, stem3/stem3.cpp:2188-2219)
+int abs_slices(const qs_params& P) { return P.slices * std::max(1, P.cellDiv); }
+
 // Device bytes of a unit of nb waves of grid N, slice stacks of smax slices.
 size_t cbed_unit_bytes(const qs_params& P, int nb, int smax) {
     const size_t N = (size_t)P.nx * P.ny, Pp = (size_t)P.potNx * P.potNy;
@@ -906,10 +910,6 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
         if (P.potNx != P.nx || P.potNy != P.ny) {
             set_error("job " + std::to_string(i) + ": CBED needs the potential grid equal to the wave grid");
             return QS_ERR_ARG;
-        }
-        if (P.cellDiv != 1) {
-            set_error("job " + std::to_string(i) + ": cells divided into slabs (cellDiv > 1) are not supported");
-            return QS_ERR_UNSUPPORTED;
         }
         if (!line_supported(P.nx) || !line_supported(P.ny)) {
             set_error("job " + std::to_string(i) + ": nx, ny must be in {64,128,256,384,512,768,1024}");
@@ -936,17 +936,17 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
     for (auto& g : groups) {
         std::vector<int>& v = g.second;
         std::stable_sort(v.begin(), v.end(),
-                         [&](int a, int b) { return jobs[a].params.slices > jobs[b].params.slices; });
+                         [&](int a, int b) { return abs_slices(jobs[a].params) > abs_slices(jobs[b].params); });
         CbedUnit u;
         for (int i : v) {
             const qs_params& P = jobs[i].params;
-            const int smax = u.jobs.empty() ? P.slices : u.smax;
+            const int smax = u.jobs.empty() ? abs_slices(P) : u.smax;
             const size_t b = cbed_unit_bytes(P, (int)u.jobs.size() + 1, smax);
             if (!u.jobs.empty() && b > budget) {
                 units.push_back(u);
                 u = CbedUnit();
             }
-            if (u.jobs.empty()) u.smax = P.slices;
+            if (u.jobs.empty()) u.smax = abs_slices(P);
             u.jobs.push_back(i);
             u.bytes = cbed_unit_bytes(P, (int)u.jobs.size(), u.smax);
             if (u.bytes > budget) {
@@ -1027,8 +1027,17 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
                 C.zeros = (int*)take(sizeof(int) * (P0.ny + nb));
                 for (int w = 0; w < nb; w++) {
                     const qs_cbed_job& J = jobs[u.jobs[w]];
-                    QS_TRY(qs_slices_build(c, &J.params, J.atoms, J.natom, (float*)(C.stacks + (size_t)w * u.smax * Pp),
-                                           0));
+                    // one stack per slab, back to back (slab 0's copied for
+                    // equal divisions, which the reference reuses)
+                    const int D = std::max(1, J.params.cellDiv), Sj = J.params.slices;
+                    float2* st0 = C.stacks + (size_t)w * u.smax * Pp;
+                    for (int slab = 0; slab < D; slab++) {
+                        float2* dst = st0 + (size_t)slab * Sj * Pp;
+                        if (slab > 0 && J.params.equalDivs)
+                            QS_CUDA_TRY(cudaMemcpyAsync(dst, st0, sizeof(float2) * Sj * Pp, cudaMemcpyDeviceToDevice, s));
+                        else
+                            QS_TRY(qs_slab_build(c, &J.params, J.atoms, J.natom, slab, (float*)dst, 0));
+                    }
                     // doCBED's probe position (stem3/stem3.cpp:2096-2100)
                     const double dx = (double)(J.params.scanXStart - J.params.potOffsetX);
                     const double dy = (double)(J.params.scanYStart - J.params.potOffsetY);
@@ -1070,7 +1079,7 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
                 const int nb = (int)u.jobs.size(), nx = P0.nx, ny = P0.ny;
                 const size_t N = (size_t)nx * ny, Pp = (size_t)P0.potNx * P0.potNy;
                 std::vector<int> S(nb);
-                for (int w = 0; w < nb; w++) S[w] = jobs[u.jobs[w]].params.slices;
+                for (int w = 0; w < nb; w++) S[w] = abs_slices(jobs[u.jobs[w]].params);
                 RowArgs ra{};
                 ra.nx = nx; ra.ny = ny; ra.potNx = P0.potNx; ra.potNy = P0.potNy;
                 ra.probe = C.probes; ra.probe_stride = N; ra.trans_stride = (size_t)u.smax * Pp;
@@ -1137,15 +1146,15 @@ int qs_tem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, const int* n
     if (ndef > 0 && ctf_images && (!ctf || !defoci)) { set_error("CTF images need ctf and defoci"); return QS_ERR_ARG; }
     QS_TRY(check_params(p));
     const qs_params& P = *p;
-    if (P.cellDiv != 1) {
-        set_error("TEM: cells divided into slabs (cellDiv > 1) are not supported");
-        return QS_ERR_UNSUPPORTED;
-    }
     QS_CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
     const int nx = P.nx, ny = P.ny;
     const size_t N = (size_t)nx * ny;
-    const size_t stack = (size_t)P.slices * P.potNx * P.potNy;
+    // a cell divided into slabs: one stack per slab unless they are equal
+    // (doTEM's slab loop, stem3/stem3.cpp:2473-2537)
+    const int nslab = (P.cellDiv > 1 && !P.equalDivs) ? P.cellDiv : 1;
+    const size_t slabStack = (size_t)P.slices * P.potNx * P.potNy;
+    const size_t stack = slabStack * nslab;
     const int nimg = (ctf_images && ndef > 0) ? ndef : 0;
     size_t natomTotal = 0;
     for (int k = 0; k < nconf; k++) {
@@ -1192,13 +1201,14 @@ int qs_tem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, const int* n
     for (int c0 = 0; c0 < nconf; c0 += chunk) {
         const int nb = std::min(chunk, nconf - c0);
         for (int k = 0; k < nb; k++) {
-            QS_TRY(qs_slices_build(c, p, atoms ? atoms + atomOff : nullptr, natoms[c0 + k],
-                                   (float*)(stacks + (size_t)k * stack), 0));
+            for (int slab = 0; slab < nslab; slab++)
+                QS_TRY(qs_slab_build(c, p, atoms ? atoms + atomOff : nullptr, natoms[c0 + k], slab,
+                                     (float*)(stacks + (size_t)k * stack + (size_t)slab * slabStack), 0));
             atomOff += (size_t)natoms[c0 + k];
         }
         qs_batch bt{nb, zeros.data(), zeros.data(), zeros.data(), zeros.data()};
         QS_TRY(multislice_run_ex(c, p, (const float*)stacks, stack, (const float*)plane, 0, &bt, nullptr, nullptr,
-                                 (float*)ew, 0));
+                                 (float*)ew, nslab > 1 ? QS_SLAB_STACKS : 0));
         QS_TRY(launch_acc_intensity(ew, nb, N, inv, acc, s));
         if (exit_waves)
             QS_CUDA_TRY(cudaMemcpyAsync(exit_waves + 2 * (size_t)c0 * N, ew, waveB * nb, cudaMemcpyDeviceToHost, s));

@@ -262,6 +262,15 @@ RUN_CASES = {
                        scan=None, detectors=[], alpha=0.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
                        outputInterval=2, mode="TEM", saveLevel=0,
                        extra=["Beam tilt X: 0.004", "Beam tilt Y: 0.2 deg", "Tilt back: yes"]),
+    # CBED through two unequal slabs (NCELLZ: 3/2): every slab's stack
+    "qsccbedd2u": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=3,
+                       sliceThickness=2.0, scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0,
+                       bandlimit=True, outputInterval=2, mode="CBED", saveLevel=1, cellDiv=2),
+    # TEM through two equal slabs (NCELLZ: 4/2, slab 0's stack reused)
+    "qsctemd2": dict(cell="si", ncell=(4, 3, 4), nx=64, resolutionX=0.06, v0=300.0, slices=4,
+                     sliceThickness=float(np.float32(np.float32(4 * 5.431 / np.sqrt(2)) / np.float32(8))),
+                     scan=None, detectors=[], alpha=0.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
+                     outputInterval=3, mode="TEM", saveLevel=0, cellDiv=2),
     # STEM at save level 2: per-position diffAvg_ix_iy.img and mulswav_ix_iy.img
     "qscstem": dict(cell="sto", ncell=(3, 3, 4), nx=64, resolutionX=0.0915, v0=200.0, slices=8,
                     sliceThickness=1.9525, scan=(3.905, 7.81, 2, 3.905, 7.81, 2),
@@ -283,7 +292,8 @@ def qsc_run_case(name, case):
                          sliceThickness=case["sliceThickness"], scan=case["scan"], detectors=case["detectors"],
                          alpha=case["alpha"], Cs_mm=case.get("Cs_mm", 0.0), defocus_nm=case.get("defocus_nm", 0.0),
                          outputInterval=case.get("outputInterval"), mode=case["mode"],
-                         bandlimit=case.get("bandlimit", False), folder="out", saveLevel=case["saveLevel"])
+                         bandlimit=case.get("bandlimit", False), folder="out", saveLevel=case["saveLevel"],
+                         cellDiv=case.get("cellDiv", 1))
         if case.get("extra"):
             with open(qsc, "a") as f:
                 f.write("\n".join(case["extra"]) + "\n")

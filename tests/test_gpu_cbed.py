@@ -90,3 +90,31 @@ def test_instance_larger_than_the_cap_is_rejected(ctx, mixed):
     with pytest.raises(lib.QsError) as e:
         ctx.cbed_batch(mixed, max_bytes=100 << 10)
     assert e.value.code == abi.QS_ERR_NOMEM
+
+
+def test_slabs_pattern_matches_reference(ctx):
+    """Two unequal slabs (NCELLZ 3/2): every slab built from its shifted
+    atoms; the pattern against the reference's diffAvg_1.img, alone and in
+    a batch with an undivided instance of the same grid."""
+    import os
+    import tempfile
+    from conftest import GOLDEN
+    from qstem_gb300 import qsc
+    z = np.load(os.path.join(GOLDEN, "qsccbedd2u.npz"))
+    d = tempfile.mkdtemp()
+    for fn, key in (("run.qsc", "qsc_text"), ("cell.cfg", "cfg_text")):
+        with open(os.path.join(d, fn), "w") as f:
+            f.write(str(z[key]))
+    run = qsc.read_qsc(os.path.join(d, "run.qsc"))
+    p = run.params
+    assert p.cellDiv == 2 and not p.equalDivs
+    p.dE_E = np.float32(run.spread[0])
+    ref = z["img_diffAvg_1.img"]
+    (dp,), _ = ctx.cbed_batch([(p, run.atoms)])
+    assert rel_l2(dp, ref) <= TOL
+    q = p.copy()
+    q.cellDiv = 1
+    (dp2, dq), _ = ctx.cbed_batch([(p, run.atoms), (q, run.atoms)])
+    assert rel_l2(dp2, ref) <= TOL
+    (dq1,), _ = ctx.cbed_batch([(q, run.atoms)])
+    assert rel_l2(dq, dq1) <= 1e-6

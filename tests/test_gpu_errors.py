@@ -47,7 +47,6 @@ def test_argument_and_support_errors(case):
     target = T.new_zeros((p.scanXN * p.scanYN, p.nx, p.ny, 2))[..., 0].contiguous()
     probe = T.new_zeros((p.nx, p.ny, 2))
     expect(abi.QS_ERR_UNSUPPORTED, ctx.adjoint, q, T, probe, target)
-    expect(abi.QS_ERR_UNSUPPORTED, ctx.tem, q, [g["atoms"]])
     r = p.copy()
     r.bandlimittrans = 1
     expect(abi.QS_ERR_UNSUPPORTED, ctx.adjoint, r, T, probe, target)

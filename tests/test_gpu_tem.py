@@ -65,3 +65,25 @@ def test_ctf_images_match_oracle(case):
 def test_identity_transfer_gives_the_exit_intensity(case):
     mean, imgs, _ = case["ctx"].tem(case["p"], case["configs"], ctf={}, defoci=[0.0])
     assert rel_l2(imgs[0], mean) <= 1e-5
+
+
+def _qsc_run(name):
+    import os
+    import tempfile
+    from conftest import GOLDEN
+    from qstem_gb300 import qsc
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = tempfile.mkdtemp()
+    for fn, key in (("run.qsc", "qsc_text"), ("cell.cfg", "cfg_text")):
+        with open(os.path.join(d, fn), "w") as f:
+            f.write(str(z[key]))
+    return qsc.read_qsc(os.path.join(d, "run.qsc")), z
+
+
+def test_slabs_exit_wave_matches_reference(case):
+    """A cell divided into two equal slabs (NCELLZ 4/2): qs_tem_run's exit
+    wave against the reference's wave.img of the same input."""
+    run, z = _qsc_run("qsctemd2")
+    assert run.params.cellDiv == 2 and run.params.equalDivs
+    _, _, ew = case["ctx"].tem(run.params, [run.atoms], want_exit_waves=True)
+    assert rel_l2(ew[0], z["img_wave.img"]) <= TOL

@@ -17,7 +17,7 @@ from oracle import oracle
 from oracle_ctx import OracleContext
 from qstem_gb300 import imageio, qsc
 
-EXTRA = {"qsctem": {"waveIntensity.img"}, "qsctemtilt": {"waveIntensity.img"}}
+EXTRA = {"qsctem": {"waveIntensity.img"}, "qsctemtilt": {"waveIntensity.img"}, "qsctemd2": {"waveIntensity.img"}}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -41,7 +41,7 @@ def _read(folder, fn):
     return im, (np.stack([d.real, d.imag], -1) if np.iscomplexobj(d) else d)
 
 
-@pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsctem", "qsctemtilt", "qscstem"])
+@pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsccbedd2u", "qsctem", "qsctemtilt", "qsctemd2", "qscstem"])
 def test_output_folder_as_the_reference_writes_it(tmp_path, name):
     z, path, out = _inputs(tmp_path, name)
     qsc.run_qsc(path, ctx=OracleContext(), folder=out)
