@@ -107,6 +107,21 @@ def _cmp_zyx_key(row):
     return (row[3], row[2], row[1])
 
 
+def cell_vectors(ax, by, c, alpha, beta, gamma):
+    """makeCellVectMuls (libs/matrixlib.cpp:722-747): cell vectors (rows)
+    from lengths and angles (degrees) held as floats, as the reference
+    builds them -- including its b vector of (b cos(gamma), b cos(gamma), 0)
+    for non-orthogonal cells."""
+    ax, by, c, al, be, ga = (float(F32(v)) for v in (ax, by, c, alpha, beta, gamma))
+    if al == 90 and be == 90 and ga == 90:
+        return np.diag([ax, by, c])
+    d = 1.7453292519943e-2  # PI180
+    ca, cb, cg, sg = math.cos(al * d), math.cos(be * d), math.cos(ga * d), math.sin(ga * d)
+    return np.array([[ax, 0.0, 0.0],
+                     [by * cg, by * cg, 0.0],
+                     [c * cb, c * (ca - cb * cg) / sg, c * (math.sqrt(1 - ca * ca - cb * cb + 2 * ca * cb * cg) / sg)]])
+
+
 def _sorted_fractional(cell):
     """The unit cell's atoms as records in fractional coordinates, sorted by
     (z, y, x) as readUnitCell sorts them (libs/fileio_fftw3.cpp:1497-1500)."""

@@ -1,5 +1,5 @@
-"""Read unmodified stem3 inputs: a .qsc parameter file and its AtomEye .cfg
-unit cell, into qs_params and the replicated atom list.
+"""Read unmodified stem3 inputs: a .qsc parameter file and its unit cell
+(AtomEye .cfg, .dat or .cssr), into qs_params and the atom list.
 
 The parameter file is read the way the reference's readFile does
 (stem3/stem3.cpp:600-1460): every key is looked up with readparam's rule
@@ -9,12 +9,14 @@ anywhere in the line -- in readFile's order, so that a key such as "slices:"
 resolves to the same line it does there (it is also a substring of
 "center slices:").  The derived fields (potential grid, offsets, k^2 of the
 detectors, ...) then come from config.make_params, which follows the rest of
-readFile.  The unit cell is read as readCFGCellParams / readNextCFGAtom read
-it (libs/fileio_fftw3.cpp:721-989) and replicated as readUnitCell does.
+readFile.  The unit cell is read as readCFGCellParams / readNextCFGAtom
+(and the .dat / .cssr readers) read it (libs/fileio_fftw3.cpp:664-1051) and
+built as readUnitCell builds it: NCELL replication with crystal tilt, or a
+"Cube:" box cut from the tilted crystal (config.supercell, config.cube).
 
 Inputs that need parts of the reference outside this library are refused
-with NotImplementedError: a "Cube" box, crystal or beam tilt, phonon files,
-the 2-D potential, and non-orthogonal cells.
+with NotImplementedError: phonon files, the 2-D potential (potential3D: no)
+and modes other than STEM, CBED and TEM.
 """
 import math
 import os
@@ -153,6 +155,85 @@ def read_cfg(path):
     if ncoord and len(atoms) != ncoord:
         raise ValueError("%s: %d atoms listed, %d announced" % (path, len(atoms), ncoord))
     return config.UnitCell(*(float(np.sqrt(np.dot(H[i], H[i]))) for i in range(3)), atoms, H=H)
+
+
+def _element(field):
+    """getZNumber (libs/fileio_fftw3.cpp:2299-2321): the first two characters
+    of a symbol field, a digit or line end in the second read as a blank,
+    looked up case-sensitively; 0 when unknown."""
+    f = (field + "  ")[:2]
+    if f[1].isdigit() or f[1] in "\n\r\0 ":
+        f = f[0] + " "
+    sym = f.rstrip()
+    return _SYMBOLS.index(sym) if sym in _SYMBOLS and sym else 0
+
+
+def read_dat(path):
+    """A unit cell from a .dat file (readDATCellParams / readNextDATAtom,
+    libs/fileio_fftw3.cpp:664-707, 825-890): "a =", "b =", "c =" and the
+    angles after "Number of atoms =" ('#' comments), then one atom per line
+    after the "gamma =" line -- element in the first two characters,
+    fractional x y z -- with dw = 0.45*28/(2 Z), occupancy 1, charge 0.  The
+    reference stores alpha as the cell's gamma and gamma as its alpha."""
+    pf = ParamFile(path, comment="#")
+    ncoord = int(_num(pf.get("Number of atoms ="), 0))
+    a = _num(pf.get("a ="), 0.0)
+    b = _num(pf.get("b ="), 0.0)
+    c = _num(pf.get("c ="), 0.0)
+    al = _num(pf.get("alpha ="), 90.0)
+    be = _num(pf.get("beta ="), 90.0)
+    ga = _num(pf.get("gamma ="), 90.0)
+    H = config.cell_vectors(a, b, c, ga, be, al)
+    pf.pos = 0
+    pf.get("gamma =")
+    atoms = []
+    for line in pf.lines[pf.pos:]:
+        Z = _element(line[:2]) if line else 0
+        if Z == 0:
+            continue
+        tok = line[2:].split()
+        if len(tok) < 3:
+            raise ValueError("%s: incomplete atom line %r" % (path, line))
+        atoms.append((Z, float(tok[0]), float(tok[1]), float(tok[2]), 0.45 * 28.0 / (2.0 * Z), 1.0, 0.0))
+        if len(atoms) == ncoord:
+            break
+    if ncoord and len(atoms) != ncoord:
+        raise ValueError("%s: %d atoms listed, %d announced" % (path, len(atoms), ncoord))
+    return config.UnitCell(*(float(np.sqrt(np.dot(H[i], H[i]))) for i in range(3)), atoms, H=H)
+
+
+def read_cssr(path):
+    """A unit cell from a .cssr file (readCSSRCellParams / readNextCSSRAtom,
+    libs/fileio_fftw3.cpp:785-815, 998-1051): lengths on line 1, angles on
+    line 2 (space group 1 only), the atom count on line 3, atoms from line 5
+    as "n element x y z" + 8 integers + dw; occupancy 1, charge 0."""
+    with open(path) as fh:
+        lines = fh.read().split("\n")
+    a, b, c = (float(t) for t in lines[0].split()[:3])
+    al, be, ga = (float(t) for t in lines[1].split()[:3])
+    if "SPGR =" in lines[1]:
+        grp = lines[1].split("SPGR =")[1].split()
+        if grp and grp[0].isdigit() and int(grp[0]) != 1:
+            raise NotImplementedError("%s: space group %s" % (path, grp[0]))
+    ncoord = int(lines[2].split()[0])
+    H = config.cell_vectors(a, b, c, al, be, ga)
+    atoms = []
+    for line in lines[4:4 + ncoord]:
+        tok = line.split()
+        dw = float(tok[13]) if len(tok) > 13 else 0.0
+        atoms.append((_element(tok[1]), float(tok[2]), float(tok[3]), float(tok[4]), dw, 1.0, 0.0))
+    return config.UnitCell(*(float(np.sqrt(np.dot(H[i], H[i]))) for i in range(3)), atoms, H=H)
+
+
+def read_cell(path):
+    """readUnitCell's formats by file extension: .cfg, .dat, .cssr."""
+    if path.endswith(".cssr"):
+        return read_cssr(path)
+    if path.endswith(".dat"):
+        return read_dat(path)
+    if path.endswith(".cfg"):
+        return read_cfg(path)
+    raise NotImplementedError("%s: unit cell format not supported (.cfg, .dat, .cssr)" % path)
 
 
 @dataclass
@@ -303,7 +384,7 @@ def read_qsc(path, seed=20261203):
         unsupported.append("phonon-File")
     # the unit cell (readUnitCell: .cfg read, replicated, then shifted)
     cfg_path = os.path.join(os.path.dirname(os.path.abspath(path)), cfg)
-    cell = read_cfg(cfg_path)
+    cell = read_cell(cfg_path)
     xoff = _num(g("xOffset:"), 0.0)
     yoff = _num(g("yOffset:"), 0.0)
     if cube is not None:  # a box cut from the tilted crystal (tiltBoxed)

@@ -239,7 +239,8 @@ def qsc_geometry_case(name, qsc_file, cfg_file):
     print("wrote", path, os.path.getsize(path), "bytes", len(out["atoms"]), "atoms")
 
 
-GEOMETRY_CASES = {"qsctilt": ("tilt.qsc", "hex.cfg"), "qsccube": ("cube.qsc", "cell.cfg")}
+GEOMETRY_CASES = {"qsctilt": ("tilt.qsc", "hex.cfg"), "qsccube": ("cube.qsc", "cell.cfg"),
+                  "qscdat": ("dat.qsc", "cell.dat"), "qsccssr": ("cssr.qsc", "cell.cssr")}
 
 # whole stem3 runs whose output folders pin qstem_gb300.qsc.run_qsc: every
 # .img file the reference wrote (name, header, data)

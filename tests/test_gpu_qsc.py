@@ -86,7 +86,7 @@ def test_output_folder_matches_the_references(name):
         assert rel_l2(data, z["img_" + fn]) <= 1e-4, fn
 
 
-@pytest.mark.parametrize("name", ["qsctilt", "qsccube"])
+@pytest.mark.parametrize("name", ["qsctilt", "qsccube", "qscdat", "qsccssr"])
 def test_tilted_and_boxed_crystals_end_to_end(name):
     """A non-orthogonal cell tilted about x and y, and a Cube box cut from a
     crystal tilted about x and z: run_qsc's detector images of every

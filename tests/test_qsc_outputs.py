@@ -137,7 +137,7 @@ def test_stem_position_patterns_averaged(tmp_path):
     assert not any(f.startswith("mulswav") for f in os.listdir(out))
 
 
-@pytest.mark.parametrize("name", ["qsctilt", "qsccube"])
+@pytest.mark.parametrize("name", ["qsctilt", "qsccube", "qscdat", "qsccssr"])
 def test_tilted_and_boxed_crystals_through_the_oracle(tmp_path, name):
     """The detector images of the tilted / boxed inputs through the oracle
     stand-in match the reference's doSTEM (the atom front end feeds the
