@@ -500,6 +500,20 @@ def read_qsc(path, seed=20261203):
         names.append(t[2])
     pf.pos = 0
     atomRadius = _num(g("atom radius:"), 5.0)
+    # stacking sequences (doSTEM/doTEM/doCBED's "sequence: m1 m2" loop,
+    # stem3/stem3.cpp:2761-2790): m1 repeats the stack inside runMulsSTEM,
+    # m2 the slab loop, each line restarts it.  Only the plain "1 1" is
+    # supported.  (Without any sequence line the reference runs no scan at
+    # all; this reader runs the one pass.)
+    seqs = pf.all("sequence: ")
+    if len(seqs) > 1:
+        unsupported.append("%d stacking-sequence lines" % len(seqs))
+    elif seqs:
+        tok = seqs[0].split()
+        if tok and tok[0][:1].isalnum():
+            m = [int(float(t)) if _isnum(t) else 0 for t in tok[:2]] + [1, 1]
+            if m[0] != 1 or max(m[1], 1) != 1:
+                unsupported.append("sequence: %s" % seqs[0].strip())
     if unsupported:
         raise NotImplementedError("%s: not supported by this library: %s" % (path, ", ".join(unsupported)))
 

@@ -93,12 +93,14 @@ def test_fixture_inputs_read_back(name):
 def test_refused_inputs():
     z = np.load(os.path.join(GOLDEN, "qscread.npz"))
     base = str(z["qsc_text"])
-    for extra in ("phonon-File: modes.dat", "potential3D: no", "mode: NBED"):
+    for extra in ("phonon-File: modes.dat", "potential3D: no", "mode: NBED", "sequence: 1 3"):
         text = base.replace("print level: 1", extra + "\nprint level: 1")
         if extra.startswith("potential3D"):
             text = base.replace("potential3D: yes", extra)
         if extra.startswith("mode"):
             text = base.replace("mode: STEM", extra)
+        if extra.startswith("sequence"):
+            text = base.replace("sequence: 1 1", extra)
         d = _write({"run.qsc": text, "cell.cfg": str(z["cfg_text"])})
         with pytest.raises(NotImplementedError):
             qsc.read_qsc(os.path.join(d, "run.qsc"))
