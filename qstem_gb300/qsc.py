@@ -646,8 +646,10 @@ def _run_stem(ctx, run, where, seed, chunk):
     saveSTEMImages does (stem3/stemlib.cpp:2693-2749): <name>_<t>.img for
     the thickness slots before the last, <name>.img for the last, comment
     "STEM image", the thickness, the scan sampling, and params [runs, error,
-    image^2 per pixel] (the reference's image2 sums the squares over the
-    slices of a slot; this writes the final slice's).  At save level > 0 also
+    image2 per pixel] with image2 = image^2 and error 0: the values of a
+    single-threaded reference run (collectIntensity squares a detector sum
+    that its OpenMP threads share, stem3/stemlib.cpp:2614-2681, so threaded
+    runs write racy ones).  At save level > 0 also
     each position's diffraction pattern, averaged over the runs in the file
     itself as doSTEM does (diffAvg_<ix>_<iy>.img, "Average Array",
     stem3/stem3.cpp:2890-2930), and at save level > 1 or with slabs its exit

@@ -75,8 +75,8 @@ def test_output_folder_matches_the_references(name):
         assert np.float32(im.dx) == np.float32(dx) and np.float32(im.dy) == np.float32(dy), (fn, im.dx, dx)
         assert im.comment == comment, (fn, im.comment)
         if comment == "STEM image":
-            # [runs, error, image2...]: the reference's image2 sums the squares
-            # over the slices of a slot, this writes the final slice's
+            # [runs, error, image2...]: the reference's threads share the sum
+            # image2 squares, so only its run count is reproducible
             assert im.params[0] == params[0], fn
         else:
             np.testing.assert_allclose(im.params, params, rtol=1e-6, err_msg=fn)
