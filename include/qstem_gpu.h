@@ -304,6 +304,16 @@ int qs_tem_run(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, const int 
                const qs_ctf *ctf, int ndef, const double *defoci, float *mean_intensity,
                float *ctf_images, float *exit_waves);
 
+/* qs_tem_run with doTEM's tilted incident plane wave (beam tilt btiltx,
+ * btilty in rad, held as floats as MULS holds them;
+ * stem3/stem3.cpp:2409-2419): psi(ix, iy) = exp(i k_t.(x, y)) with
+ * k_t = 2 pi sin(tilt) / lambda, x = dx (ix - nx/2) and -- as the reference
+ * forms it -- y = dy (ix - nx/2).  Exit waves are returned as propagated;
+ * doTEM's tilt-back applies to the wave.img file only. */
+int qs_tem_run_tilted(qs_ctx *ctx, const qs_params *p, double btiltx, double btilty, const qs_atom *atoms,
+                      const int *natoms, int nconf, const qs_ctf *ctf, int ndef, const double *defoci,
+                      float *mean_intensity, float *ctf_images, float *exit_waves);
+
 /* ------------------------------------------------------------ gradients */
 /* initSTEMSlices' phase grating for a given potential stack V
  * (stem3/stemlib.cpp:2280-2299): trans = exp(i*lambda*gamma*V), V a device

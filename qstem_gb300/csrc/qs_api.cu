@@ -1142,6 +1142,13 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
 
 int qs_tem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, const int* natoms, int nconf, const qs_ctf* ctf,
                int ndef, const double* defoci, float* mean_intensity, float* ctf_images, float* exit_waves) {
+    return qs_tem_run_tilted(c, p, 0.0, 0.0, atoms, natoms, nconf, ctf, ndef, defoci, mean_intensity, ctf_images,
+                             exit_waves);
+}
+
+int qs_tem_run_tilted(qs_ctx* c, const qs_params* p, double btiltx, double btilty, const qs_atom* atoms,
+                      const int* natoms, int nconf, const qs_ctf* ctf, int ndef, const double* defoci,
+                      float* mean_intensity, float* ctf_images, float* exit_waves) {
     if (!c || !natoms || nconf < 1) { set_error("null argument or no configurations"); return QS_ERR_ARG; }
     if (ndef > 0 && ctf_images && (!ctf || !defoci)) { set_error("CTF images need ctf and defoci"); return QS_ERR_ARG; }
     QS_TRY(check_params(p));
@@ -1192,6 +1199,25 @@ int qs_tem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, const int* n
     QS_CUDA_TRY(cudaMemsetAsync(acc, 0, sizeof(float) * N * (1 + nimg), s));
     // doTEM's incident wave without beam tilt (stem3/stem3.cpp:2403-2406)
     QS_TRY(launch_fill(plane, N, 1.f, 0.f, s));
+    std::vector<float2> tilted;
+    if (btiltx != 0.0 || btilty != 0.0) {
+        // doTEM's tilted plane wave (stem3/stem3.cpp:2409-2419): phase
+        // k_t.(x, y) with k_t = 2 pi sin(tilt) / lambda in double, x =
+        // dx (ix - nx/2) in float, and y formed from ix as the reference forms
+        // it, so every row ix is constant along y
+        const double pi = 3.1415926535897;
+        const double lam = wavelength(P.v0);
+        const double ktx = 2.0 * pi * std::sin((double)(float)btiltx) / lam;
+        const double kty = 2.0 * pi * std::sin((double)(float)btilty) / lam;
+        tilted.resize(N);
+        for (int ix = 0; ix < nx; ix++) {
+            const double x = (double)(P.resolutionX * (float)(ix - nx / 2));
+            const double y = (double)(P.resolutionY * (float)(ix - nx / 2));
+            const float2 v = make_float2((float)std::cos(ktx * x + kty * y), (float)std::sin(ktx * x + kty * y));
+            for (int iy = 0; iy < ny; iy++) tilted[(size_t)ix * ny + iy] = v;
+        }
+        QS_CUDA_TRY(cudaMemcpyAsync(plane, tilted.data(), waveB, cudaMemcpyHostToDevice, s));
+    }
 
     const double lambda = wavelength(P.v0);
     const float inv = 1.0f / (float)nconf;

@@ -23,7 +23,7 @@ EXPORTS = ["qs_ctx_create", "qs_ctx_destroy", "qs_last_error", "qs_abi_version",
            "qs_params_finalize", "qs_thickness_count", "qs_lut_build", "qs_slices_build", "qs_probe",
            "qs_multislice_run", "qs_collect", "qs_stem_run", "qs_ctx_profile", "qs_ctx_stats",
            "qs_multislice_run_noalloc", "qs_phase_grating", "qs_adjoint_run", "qs_atoms_grad", "qs_tem_run",
-           "qs_cbed_batch_run", "qs_slab_build"]
+           "qs_cbed_batch_run", "qs_slab_build", "qs_tem_run_tilted"]
 
 _lib = None
 
@@ -62,6 +62,8 @@ def load(path=LIB_PATH):
     L.qs_collect.argtypes = [vp, P, vp, vp, vp, ctypes.c_uint]
     L.qs_stem_run.argtypes = [vp, P, vp, ctypes.c_int, ctypes.POINTER(abi.QsBatch), vp, vp]
     L.qs_tem_run.argtypes = [vp, P, vp, vp, ctypes.c_int, ctypes.POINTER(abi.QsCtf), ctypes.c_int, vp, vp, vp, vp]
+    L.qs_tem_run_tilted.argtypes = [vp, P, ctypes.c_double, ctypes.c_double, vp, vp, ctypes.c_int,
+                                    ctypes.POINTER(abi.QsCtf), ctypes.c_int, vp, vp, vp, vp]
     L.qs_cbed_batch_run.argtypes = [vp, vp, ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(abi.QsCbedReport)]
     L.qs_ctx_profile.argtypes = [vp, ctypes.c_int]
     L.qs_ctx_stats.argtypes = [vp, ctypes.POINTER(abi.QsStats)]
@@ -231,8 +233,9 @@ class Context:
         del keep
         return outs, {n: getattr(rep, n) for n, _ in abi.QsCbedReport._fields_}
 
-    def tem(self, p, configs, ctf=None, defoci=(), want_exit_waves=False):
-        """doTEM over frozen-phonon configurations (qs_tem_run).
+    def tem(self, p, configs, ctf=None, defoci=(), want_exit_waves=False, beam_tilt=(0.0, 0.0)):
+        """doTEM over frozen-phonon configurations (qs_tem_run, or
+        qs_tem_run_tilted with a beam tilt in rad).
 
         configs: list of atom arrays (abi.ATOM_DTYPE), one per configuration.
         ctf: abi.QsCtf or a dict of its fields; defoci: defocus per CTF image
@@ -246,10 +249,14 @@ class Context:
         imgs = np.zeros((len(defs), p.nx, p.ny), np.float32) if len(defs) else None
         ew = np.zeros((len(arrs), p.nx, p.ny, 2), np.float32) if want_exit_waves else None
         c = ctf if isinstance(ctf, abi.QsCtf) else abi.QsCtf(**(ctf or {}))
-        _check(self.lib.qs_tem_run(self.h, ctypes.byref(p), cat.ctypes.data_as(ctypes.c_void_p),
-                                   nat.ctypes.data_as(ctypes.c_void_p), len(arrs), ctypes.byref(c), len(defs),
-                                   defs.ctypes.data_as(ctypes.c_void_p) if len(defs) else None, _ptr(mean),
-                                   _ptr(imgs), _ptr(ew)))
+        args = (cat.ctypes.data_as(ctypes.c_void_p), nat.ctypes.data_as(ctypes.c_void_p), len(arrs),
+                ctypes.byref(c), len(defs), defs.ctypes.data_as(ctypes.c_void_p) if len(defs) else None, _ptr(mean),
+                _ptr(imgs), _ptr(ew))
+        if beam_tilt[0] or beam_tilt[1]:
+            _check(self.lib.qs_tem_run_tilted(self.h, ctypes.byref(p), float(beam_tilt[0]), float(beam_tilt[1]),
+                                              *args))
+        else:
+            _check(self.lib.qs_tem_run(self.h, ctypes.byref(p), *args))
         return mean, imgs, ew
 
     def phase_grating(self, p, V, out=None):

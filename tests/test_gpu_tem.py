@@ -87,3 +87,15 @@ def test_slabs_exit_wave_matches_reference(case):
     assert run.params.cellDiv == 2 and run.params.equalDivs
     _, _, ew = case["ctx"].tem(run.params, [run.atoms], want_exit_waves=True)
     assert rel_l2(ew[0], z["img_wave.img"]) <= TOL
+
+
+def test_beam_tilt_exit_wave_matches_reference(case):
+    """qs_tem_run_tilted: doTEM's tilted incident wave (beam tilt 0.004 rad
+    and 0.2 degrees) through the reference's input; the exit wave against
+    interimWave's wave_<last>.img (wave.img itself is tilted back)."""
+    run, z = _qsc_run("qsctemtilt")
+    assert run.beam_tilt[0] != 0 and run.beam_tilt[1] != 0
+    _, _, ew = case["ctx"].tem(run.params, [run.atoms], want_exit_waves=True, beam_tilt=run.beam_tilt)
+    assert rel_l2(ew[0], z["img_wave_2.img"]) <= TOL
+    _, _, flat = case["ctx"].tem(run.params, [run.atoms], want_exit_waves=True)
+    assert rel_l2(flat[0], z["img_wave_2.img"]) > 10 * TOL  # the tilt matters
