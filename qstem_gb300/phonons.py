@@ -1,5 +1,5 @@
-"""Frozen-phonon configurations across ranks, and the average of their
-detector images.
+"""Frozen-phonon configurations and scan tiles across ranks, and the
+reduction of their detector images.
 
 doSTEM repeats the scan for `avgRuns` thermally displaced configurations
 (stem3/stem3.cpp:2722-2961), each with its own make3DSlices; the images of
@@ -10,7 +10,10 @@ configuration and a run is reproducible.
 
 With N ranks (one GPU each) configuration j runs on rank j mod N; the only
 exchange is one all-reduce (sum) of the per-rank image sums and counts at
-the end, which is also all the averaging needs.
+the end, which is also all the averaging needs.  A single configuration's
+scan can be split the same way: contiguous tiles of scan rows per rank
+(rank_positions), each rank holding the whole slice stack, and one
+all-reduce of the images (scan_images).
 """
 import numpy as np
 
@@ -22,6 +25,46 @@ def rank_configurations(nconf, rank, world):
     if world < 1 or not 0 <= rank < world:
         raise ValueError("rank %d outside a world of %d" % (rank, world))
     return list(range(rank, nconf, world))
+
+
+def rank_positions(p, rank, world):
+    """A contiguous tile of the scan raster for `rank` among `world` ranks:
+    raster positions i = ix*scanYN + iy, split into whole scan rows as evenly
+    as the rows allow (rank r gets rows [r*R/W, (r+1)*R/W)).  Returns the
+    positions as (iPosX, iPosY, detPosX, detPosY) int32 arrays, as
+    qs_multislice_run takes them (config.scan_offsets)."""
+    from . import config
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("rank %d outside a world of %d" % (rank, world))
+    rows = p.scanXN
+    r0, r1 = rank * rows // world, (rank + 1) * rows // world
+    offs = config.scan_offsets(p)
+    return tuple(a[r0 * p.scanYN:r1 * p.scanYN] for a in offs)
+
+
+def scan_images(ctx, p, trans, rank=0, world=1, group=None, probe=None):
+    """One configuration's scan split across ranks (each rank holds the same
+    slice stack): this rank's tile of positions through qs_multislice_run,
+    then one all-reduce (sum) of the detector images, where every pixel has
+    exactly one writer.  trans and probe may be device (torch) or host
+    (numpy) arrays; returns the full images [slot][detector][x][y] as a
+    float32 torch tensor on the trans device (CPU for numpy input)."""
+    import torch
+    import torch.distributed as dist
+    pos = rank_positions(p, rank, world)
+    nt = p.thickness_count()
+    on_device = isinstance(trans, torch.Tensor) and trans.is_cuda
+    det = torch.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), dtype=torch.float32,
+                      device=trans.device if on_device else "cpu")
+    if len(pos[0]) and on_device:
+        torch.cuda.synchronize()  # the zeroed buffer before the library's stream writes it
+        ctx.multislice(p, trans, probe, positions=pos, det=det)
+    elif len(pos[0]):
+        out, _, _ = ctx.multislice(p, trans, probe, positions=pos)
+        det = torch.from_numpy(np.ascontiguousarray(out))
+    if dist.is_available() and dist.is_initialized():
+        dist.all_reduce(det, op=dist.ReduceOp.SUM, group=group)
+    return det
 
 
 def displaced(atoms, j, seed, sigma):

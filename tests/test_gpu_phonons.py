@@ -26,3 +26,22 @@ def test_average_equals_mean_of_single_configurations():
         assert rel_l2(singles[0], singles[1]) > 1e-4  # the configurations differ
     finally:
         ctx.close()
+
+
+def test_scan_tiles_sum_to_the_whole_scan():
+    """The row tiles of every rank of a 3-rank split, each run through the
+    library (one after another on this GPU, no collective), sum to the
+    whole scan's detector images bit for bit, and match the reference's."""
+    import torch
+    g = Golden("sto64")
+    p = g.params
+    ctx = lib.Context(0)
+    try:
+        T = torch.from_numpy(np.ascontiguousarray(g["T"])).cuda()
+        probe = torch.from_numpy(np.ascontiguousarray(g["probe"])).cuda()
+        whole, _, _ = ctx.multislice(p, g["T"], g["probe"])
+        tiles = [phonons.scan_images(ctx, p, T, r, 3, probe=probe).cpu().numpy() for r in range(3)]
+        assert np.array_equal(np.sum(tiles, axis=0), whole)
+        assert rel_l2(whole, g["det"]) <= 1e-4
+    finally:
+        ctx.close()

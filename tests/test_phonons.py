@@ -72,3 +72,55 @@ def test_single_process_mean_without_distributed():
     assert torch.allclose(acc.mean(), torch.full((3,), 3.0))
     with pytest.raises(ValueError):
         phonons.ImageSum(torch.zeros(1)).mean()
+
+
+def test_rank_positions_tile_the_raster():
+    """Every raster position on exactly one rank, in whole scan rows, in
+    raster order within a rank."""
+    from qstem_gb300 import config
+    p = config.make_params(nx=64, resolutionX=0.1, v0=200, slices=4, sliceThickness=2.0, ax=20.0, by=20.0, c=8.0,
+                           scan=(2.0, 8.0, 7, 2.0, 8.0, 5), detectors=[(40, 100, "A")])
+    full = config.scan_offsets(p)
+    for world in (1, 2, 3, 4, 7, 9):
+        parts = [phonons.rank_positions(p, r, world) for r in range(world)]
+        for k in range(4):
+            assert np.array_equal(np.concatenate([q[k] for q in parts]), full[k])
+        for q in parts:
+            assert len(q[0]) % p.scanYN == 0
+    with pytest.raises(ValueError):
+        phonons.rank_positions(p, 2, 2)
+
+
+def _scan_rank_main(rank, world, port, out):
+    import torch.distributed as dist
+    from oracle import oracle
+    from oracle_ctx import OracleContext
+    from conftest import Golden
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        oracle.build()
+        g = Golden("sto64")
+        det = phonons.scan_images(OracleContext(), g.params, g["T"], rank, world, probe=g["probe"])
+        np.save(out % rank, det.numpy())
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.timeout(180)
+def test_scan_split_across_two_gloo_ranks():
+    """One configuration's scan split into row tiles on two ranks (the
+    oracle stands in for each rank's GPU) and all-reduced: every rank ends
+    with the reference's detector images of the whole raster."""
+    import tempfile
+
+    import torch.multiprocessing as mp
+    from conftest import Golden
+    d = tempfile.mkdtemp()
+    out = os.path.join(d, "det_%d.npy")
+    mp.start_processes(_scan_rank_main, args=(2, _free_port(), out), nprocs=2, join=True, start_method="spawn")
+    want = Golden("sto64")["det"]
+    for r in range(2):
+        got = np.load(out % r)
+        assert got.shape == want.shape
+        assert np.linalg.norm(got - want) <= 1e-6 * np.linalg.norm(want)
