@@ -188,6 +188,72 @@ def tem_measure(ctx, reps=2):
             "mean_intensity": float(mean.mean()), "ctf_image_mean": float(imgs[0].mean())}
 
 
+def stem256_workload():
+    """Plain STEM HAADF (configuration 1): SrTiO3 5x5x10, 256^2 at 0.0763 A,
+    20 slices of 1.9525 A, 200 kV, 20 mrad, 16x16 positions over one unit
+    cell, one 70-200 mrad detector, no thermal displacement."""
+    atoms, ax, by, c = config.replicate(config.srtio3_cell(), 5, 5, 10)
+    a = 3.905
+    p = config.make_params(nx=256, resolutionX=0.0763, v0=200, slices=20, sliceThickness=1.9525, ax=ax, by=by, c=c,
+                           scan=(2 * a, 3 * a, 16, 2 * a, 3 * a, 16), detectors=[(70, 200, "HAADF")], alpha=20)
+    return p, atoms
+
+
+def stem256_measure(ctx, torch, cpu=True, reps=5):
+    """Configuration 1 whole: qs_stem_run end to end (host atoms in, host
+    image out: LUT from the context's cache, slice stack, probe, 256-position
+    scan), the scan alone launched and replayed as a CUDA graph (device
+    buffers), and the oracle port on the same whole run on the host cores."""
+    p, atoms = stem256_workload()
+    npos = p.scanXN * p.scanYN
+    img = ctx.stem_run(p, atoms)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        img = ctx.stem_run(p, atoms)
+        t = time.perf_counter() - t0
+        best = t if best is None else min(best, t)
+    T = torch.empty((p.slices, p.potNx, p.potNy, 2), dtype=torch.float32, device="cuda")
+    ctx.slices(p, atoms, out=T)
+    probe = torch.from_numpy(ctx.probe(p)).cuda()
+    det = torch.zeros((p.thickness_count(), p.detectorNum, p.scanXN, p.scanYN), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream_handle)
+
+    def scan_ms(graph):
+        for _ in range(3):
+            ctx.multislice(p, T, probe, det=det, graph=graph)
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            ctx.multislice(p, T, probe, det=det, graph=graph, sync=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1)
+            best = t if best is None else min(best, t)
+        return best
+
+    launched, graphed = scan_ms(False), scan_ms(True)
+    out = {"workload": "stem-haadf-256: SrTiO3 5x5x10, 256^2, 20 slices, 16x16 positions, HAADF 70-200 mrad, "
+                       "no thermal displacement",
+           "e2e_ms": best * 1e3, "positions_per_s": npos / best, "scan_ms": launched, "scan_graph_ms": graphed,
+           "scan_positions_per_s": npos / (graphed * 1e-3), "haadf_mean": float(img.mean())}
+    if cpu:
+        from oracle import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        To = oracle.transmission(p, oracle.potential(p, atoms))
+        dref, _, _ = oracle.stem(p, To, nthreads=threads)
+        tc = time.perf_counter() - t0
+        out["cpu_port"] = {"s": tc, "positions_per_s": npos / tc, "cores": threads,
+                           "relerr_vs_gpu": float(np.linalg.norm(img - dref) / np.linalg.norm(dref)),
+                           "sample": "the whole run: slice stack + 256 positions, oracle (bit-exact C restatement)"}
+        out["gpu_over_cpu_port_e2e"] = tc / best
+    return out
+
+
 def cbed_workload():
     """64 CBED instances from numpy.random.default_rng(20261203 + 200): grid
     uniform in {256, 384, 512, 768, 1024}^2, material uniform in {fcc Au
@@ -402,6 +468,9 @@ def run_ours(args, rank, world):
     cbed = None
     if not args.skip_cbed:
         cbed = cbed_measure(ctx)
+    stem256 = None
+    if not args.skip_stem256:
+        stem256 = stem256_measure(ctx, torch, cpu=not args.skip_cpu)
     line = {"metric": "probe-positions/s", "value": value, "unit": "positions/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded frozen-phonon SrTiO3)",
@@ -417,7 +486,7 @@ def run_ours(args, rank, world):
             "e2e": {"value": e2e, "unit": "positions/s", "h2d_bytes_per_step": int(cfgs[0].nbytes),
                     "d2h_bytes_per_step": int(host_det.nbytes)},
             "cpu_baseline": cpu, "plain_gpu": plain, "adjoint": adj, "tem": tem,
-            "cbed": cbed}
+            "cbed": cbed, "stem256": stem256}
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0
@@ -435,6 +504,7 @@ def main():
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--skip-tem", action="store_true")
     ap.add_argument("--skip-cbed", action="store_true")
+    ap.add_argument("--skip-stem256", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -74,6 +74,9 @@ extern "C" {
                                    slices-long stack per slab, back to back */
 #define QS_SERIES 16u           /* qs_multislice_run: diffpats and exit_waves hold one
                                    array per thickness slot, [tCount+1][npos][nx][ny] */
+#define QS_GRAPH 32u            /* qs_multislice_run with device buffers: replay the slice
+                                   loop as a CUDA graph (captured on the second call with
+                                   the same parameters, buffers and batch) */
 
 /* run modes, same numbering as libs/stemtypes_fftw3.h:35-42 */
 #define QS_MODE_STEM 1

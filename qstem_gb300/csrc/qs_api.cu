@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <string>
 #include <tuple>
@@ -39,6 +40,14 @@ struct qs_ctx {
         }
     };
     std::map<LutKey, float*> luts;
+    // QS_GRAPH: slice loops captured as CUDA graphs, keyed by every value
+    // their launches bake in (a few, oldest dropped first)
+    struct GraphEntry {
+        std::vector<unsigned char> key;
+        cudaGraphExec_t exec = nullptr;
+        int launches = 0;   // kernels in the graph
+    };
+    std::vector<GraphEntry> graphs;
 };
 
 namespace qs {
@@ -261,6 +270,17 @@ static int prepare_luts(qs_ctx* c, const qs_params& P, const std::vector<std::pa
     return QS_OK;
 }
 
+// Bytes of values, appended to a graph key.
+struct KeyBytes {
+    std::vector<unsigned char> b;
+    template <class T>
+    KeyBytes& add(const T& v) {
+        const unsigned char* q = reinterpret_cast<const unsigned char*>(&v);
+        b.insert(b.end(), q, q + sizeof(T));
+        return *this;
+    }
+};
+
 }  // namespace qs
 
 using namespace qs;
@@ -295,6 +315,8 @@ int qs_ctx_destroy(qs_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
+    for (auto& g : c->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto& kv : c->luts) cudaFree(kv.second);
     for (int i = 0; i < kMaxBufs; i++)
         if (c->buf[i]) cudaFree(c->buf[i]);
@@ -526,6 +548,57 @@ int qs_probe(qs_ctx* c, const qs_params* p, double dx, double dy, float* wave, u
 // one incident wave per wave of the batch (device arrays, consecutive waves
 // transStride / probeStride elements apart; 0 = shared by all waves), which
 // the TEM and CBED batch drivers use.
+
+// Issue `work` (kernel launches and memsets on stream s) directly, or with
+// QS_GRAPH through the context's graph cache: the first call with a key runs
+// eagerly (first-use set-up happens outside any capture), the second is
+// captured into a graph and launched, later ones replay the graph.
+static int run_graphed(qs_ctx* c, cudaStream_t s, bool graph, const std::vector<unsigned char>& key,
+                       const std::function<int()>& work) {
+    if (!graph) return work();
+    for (auto& g : c->graphs)
+        if (g.key == key) {
+            if (g.exec) {
+                QS_CUDA_TRY(cudaGraphLaunch(g.exec, s));
+                count_launch(g.launches);
+                return QS_OK;
+            }
+            const long long before = g_launches.load();
+            QS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            const int rc = work();
+            cudaGraph_t gr = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(s, &gr);
+            if (rc != QS_OK || e != cudaSuccess) {
+                if (gr) cudaGraphDestroy(gr);
+                cudaGetLastError();
+                if (rc == QS_OK) set_error(std::string("graph capture failed: ") + cudaGetErrorString(e));
+                return rc != QS_OK ? rc : QS_ERR_CUDA;
+            }
+            const cudaError_t ei = cudaGraphInstantiate(&g.exec, gr, 0);
+            cudaGraphDestroy(gr);
+            if (ei != cudaSuccess) {
+                cudaGetLastError();
+                g.exec = nullptr;
+                set_error(std::string("graph instantiation failed: ") + cudaGetErrorString(ei));
+                return QS_ERR_CUDA;
+            }
+            g.launches = (int)(g_launches.load() - before);
+            g_launches -= g.launches;  // captured, not yet launched
+            QS_CUDA_TRY(cudaGraphLaunch(g.exec, s));
+            count_launch(g.launches);
+            return QS_OK;
+        }
+    if (c->graphs.size() >= 8) {
+        if (c->graphs.front().exec) {
+            cudaStreamSynchronize(s);
+            cudaGraphExecDestroy(c->graphs.front().exec);
+        }
+        c->graphs.erase(c->graphs.begin());
+    }
+    c->graphs.push_back({key, nullptr, 0});
+    return work();
+}
+
 static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_in, size_t transStride,
                              const float* probe_in, size_t probeStride, const qs_batch* batch, float* det_images,
                              float* diffpats, float* exit_waves, unsigned flags) {
@@ -718,9 +791,6 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
         float2* ewOut = exit_waves ? (host ? ew_dev : (float2*)exit_waves + p0 * N) : nullptr;
         // distance between thickness slots of a series (elements)
         const size_t slotStride = N * (host ? chunk : (size_t)npos);
-        if (dpOut)
-            for (size_t k = 0; k < nS; k++)
-                QS_CUDA_TRY(cudaMemsetAsync(dpOut + k * slotStride, 0, sizeof(float) * N * nb, s));
 
         RowArgs ra{};
         ra.nx = nx; ra.ny = ny; ra.potNx = P.potNx; ra.potNy = P.potNy;
@@ -766,6 +836,11 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
         };
         // stack slice of absolute slice a
         auto sliceOf = [&](int a) { return transChunk + (size_t)(slabStacks ? a : a % S) * P.potNx * P.potNy; };
+        // the chunk's stream work: the slice loop and the detector sums
+        auto work = [&]() -> int {
+        if (dpOut)
+            for (size_t k = 0; k < nS; k++)
+                QS_CUDA_TRY(cudaMemsetAsync(dpOut + k * slotStride, 0, sizeof(float) * N * nb, s));
         ra.trans_slice = sliceOf(0);
         QS_TRY(rows(ROW_FIRST));
         for (int a = 0; a < SA; a++) {
@@ -799,6 +874,16 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
                                            d_dx_pos + p0, d_dy_pos + p0, P.scanYN, npix,
                                            det_dev + (size_t)t * ndet * npix, s));
             }
+        return QS_OK;
+        };
+        // QS_GRAPH (device buffers only): everything the launches bake in
+        const bool graph = (flags & QS_GRAPH) && !host && !c->profile;
+        KeyBytes key;
+        if (graph)
+            key.add(P).add(flags).add(trans_in).add(transStride).add(dprobe).add(probeStride).add(det_dev)
+                .add(diffpats).add(exit_waves).add(p0).add(nb).add(chunk).add(npos).add(waves).add(dpart).add(dtab)
+                .add(dtiles).add(dpos).add(tw_y).add(tw_x);
+        QS_TRY(run_graphed(c, s, graph, key.b, work));
         for (size_t k = 0; k < nS; k++) {
             if (host && diffpats)
                 QS_CUDA_TRY(cudaMemcpyAsync(diffpats + (k * npos + p0) * N, dpOut + k * slotStride,

@@ -174,13 +174,15 @@ class Context:
     # -------------------------------------------------------- multislice
     def multislice(self, p, trans, probe=None, positions=None, det=None, diffpats=None, exit_waves=None,
                    want_det=True, want_diffpats=False, want_exit_waves=False, sync=True, slab_stacks=False,
-                   series=False):
+                   series=False, graph=False):
         """Run probe positions through the slice stack.
 
         positions: None (the full scan raster) or (iPosX, iPosY, detPosX, detPosY) int arrays.
         Output buffers are allocated (numpy, host) when not given and requested.
         series: diffraction patterns and exit waves of every thickness slot
-        ([slot][position]...), not only the final slice's (QS_SERIES)."""
+        ([slot][position]...), not only the final slice's (QS_SERIES).
+        graph: replay the slice loop as a CUDA graph on repeated calls with
+        the same parameters and device buffers (QS_GRAPH)."""
         bx, keep = _batch(p, positions)
         npos = bx.npos
         host = not _is_torch(trans)
@@ -193,7 +195,8 @@ class Context:
         if exit_waves is None and want_exit_waves:
             exit_waves = np.zeros(lead + (p.nx, p.ny, 2), np.float32) if host else None
         flags = (_io_flags(trans, probe, det, diffpats, exit_waves) | (abi.QS_SYNC if sync else 0) |
-                 (abi.QS_SLAB_STACKS if slab_stacks else 0) | (abi.QS_SERIES if series else 0))
+                 (abi.QS_SLAB_STACKS if slab_stacks else 0) | (abi.QS_SERIES if series else 0) |
+                 (abi.QS_GRAPH if graph else 0))
         _check(self.lib.qs_multislice_run(self.h, ctypes.byref(p), _ptr(trans), _ptr(probe), ctypes.byref(bx),
                                           _ptr(det), _ptr(diffpats), _ptr(exit_waves), flags))
         del keep
