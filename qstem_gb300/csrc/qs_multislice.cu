@@ -22,14 +22,24 @@
 
 #include "qs_fft.cuh"
 #include "qs_internal.h"
+#include "qs_tuned.h"
 
 namespace qs {
 
 constexpr int ROW_LINES = 8;
 
-// CTAs per SM the row pass is compiled for (register budget); 512^2 runs
-// fastest with three 128-thread CTAs (168 registers) rather than two.
-constexpr int row_min_blocks(int n) { return n == 512 ? 3 : 1; }
+// CTAs per SM the row pass is compiled for (register budget), per line
+// length, from the measured table in qs_tuned.h
+constexpr int row_min_blocks(int n) {
+    return n == 64     ? QS_ROW_MIN_BLOCKS_64
+           : n == 128  ? QS_ROW_MIN_BLOCKS_128
+           : n == 256  ? QS_ROW_MIN_BLOCKS_256
+           : n == 384  ? QS_ROW_MIN_BLOCKS_384
+           : n == 512  ? QS_ROW_MIN_BLOCKS_512
+           : n == 768  ? QS_ROW_MIN_BLOCKS_768
+           : n == 1024 ? QS_ROW_MIN_BLOCKS_1024
+                       : 1;
+}
 
 template <int N, int MODE>
 __global__ void __launch_bounds__(line_threads(N) * ROW_LINES, row_min_blocks(N))
