@@ -25,10 +25,22 @@
 
 #include "qs_fft.cuh"
 #include "qs_internal.h"
+#include "qs_tuned.h"
 
 namespace qs {
 
 constexpr int ADJ_ROW_LINES = 8;
+// the row adjoint's register budget (qs_tuned.h)
+constexpr int adj_min_blocks(int n) {
+    return n == 64     ? QS_ADJ_MIN_BLOCKS_64
+           : n == 128  ? QS_ADJ_MIN_BLOCKS_128
+           : n == 256  ? QS_ADJ_MIN_BLOCKS_256
+           : n == 384  ? QS_ADJ_MIN_BLOCKS_384
+           : n == 512  ? QS_ADJ_MIN_BLOCKS_512
+           : n == 768  ? QS_ADJ_MIN_BLOCKS_768
+           : n == 1024 ? QS_ADJ_MIN_BLOCKS_1024
+                       : 1;
+}
 
 // ---------------------------------------------- last slice: loss and seed
 // One block per (wave, column tile), all tiles of the grid: forward FFT_x
@@ -104,7 +116,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
 
 // ------------------------------------------------------------ row adjoint
 template <int N, bool FIRST>
-__global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES)
+__global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES, adj_min_blocks(N))
     adj_rows(AdjRowArgs a) {
     using Cfg = typename Line<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E;

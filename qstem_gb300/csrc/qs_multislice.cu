@@ -109,8 +109,20 @@ __device__ __forceinline__ void cp_async_wait() {
 // next one is copied into the other shared-memory stage with cp.async; once a
 // thread has read its elements of the current stage into registers, that
 // stage serves as the FFT exchange scratch.
+// the column pass's register budget (qs_tuned.h)
+constexpr int col_min_blocks(int n) {
+    return n == 64     ? QS_COL_MIN_BLOCKS_64
+           : n == 128  ? QS_COL_MIN_BLOCKS_128
+           : n == 256  ? QS_COL_MIN_BLOCKS_256
+           : n == 384  ? QS_COL_MIN_BLOCKS_384
+           : n == 512  ? QS_COL_MIN_BLOCKS_512
+           : n == 768  ? QS_COL_MIN_BLOCKS_768
+           : n == 1024 ? QS_COL_MIN_BLOCKS_1024
+                       : 1;
+}
+
 template <int N, bool DET, bool INVERSE>
-__global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
+__global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_blocks(N))
     ms_cols(ColArgs a, long nitems) {
     using Cfg = typename Line<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();

@@ -1,16 +1,22 @@
-"""Autotune the row pass's register budget per line length.
+"""Autotune the register budget (CTAs per SM) of the slice-loop kernels per
+line length.
 
     python -m qstem_gb300.tune [--candidates 1,2,3,4,6,8] [--sizes 256,384,...] [--write]
 
-For each candidate k the row-pass translation unit (qs_multislice.cu) is
-compiled with every QS_ROW_MIN_BLOCKS_<N> = k and linked with the other
+Phase 1, row and column passes: for each candidate k the slice-loop
+translation unit (qs_multislice.cu) is compiled with every
+QS_ROW_MIN_BLOCKS_<N> = QS_COL_MIN_BLOCKS_<N> = k and linked with the other
 objects of the normal build into a variant library in a temporary folder
-(the candidates compile in parallel).  Each variant then times, in a fresh
+(the candidates compile in parallel).  Each variant times, in a fresh
 process on the GPU, the row and column passes of every line length through
 the library's own CUDA-event counters (qs_ctx_profile / qs_ctx_stats): a
 random slice stack of 8 slices, 1024 waves at 256^2 down to 128 at 1024^2,
-best of 4.  The fastest candidate per size is printed as a table and, with
---write, stored in csrc/qs_tuned.h (then rebuild).  Needs nvcc and a GPU.
+best of 4.  Phase 2, row adjoint: the row and column tables fixed at the
+phase-1 winners, qs_adjoint.cu is compiled with every
+QS_ADJ_MIN_BLOCKS_<N> = k and the whole adjoint (every state kept) is timed
+per size with CUDA events.  The fastest candidate per pass and size is
+printed and, with --write, stored in csrc/qs_tuned.h (then rebuild).  Needs
+nvcc and a GPU.
 """
 import argparse
 import concurrent.futures
@@ -26,18 +32,19 @@ SIZES = (256, 384, 512, 768, 1024)
 WAVES = {64: 2048, 128: 2048, 256: 1024, 384: 512, 512: 512, 768: 192, 1024: 128}
 
 
-def _variant(k, sizes, tmp):
-    """Compile the row pass with register budget k for all sizes; link a library."""
-    objs = [os.path.join(_build.BUILD, s.replace(".cu", ".o")) for s in _build.SOURCES if s != "qs_multislice.cu"]
-    obj = os.path.join(tmp, "qs_multislice_%d.o" % k)
-    defs = ["-DQS_ROW_MIN_BLOCKS_%d=%d" % (n, k) for n in sizes]
-    cmd = ([_build.nvcc()] + _build.ARCH + _build.FLAGS + defs +
-           ["-c", os.path.join(_build.SRC, "qs_multislice.cu"), "-o", obj])
+def _variant(tag, source, defs, tmp, extra_objs=()):
+    """Compile `source` with -D`defs` and link it with the normal build's
+    other objects (or `extra_objs` in their place) into a variant library."""
+    replaced = {os.path.basename(o).split("@")[0] for o in extra_objs} | {source}
+    objs = [os.path.join(_build.BUILD, s.replace(".cu", ".o")) for s in _build.SOURCES if s not in replaced]
+    obj = os.path.join(tmp, "%s@%s.o" % (source, tag))
+    cmd = ([_build.nvcc()] + _build.ARCH + _build.FLAGS + ["-D" + d for d in defs] +
+           ["-c", os.path.join(_build.SRC, source), "-o", obj])
     subprocess.run(cmd, check=True, capture_output=True)
-    lib = os.path.join(tmp, "libqstem_gpu_%d.so" % k)
-    subprocess.run([_build.nvcc()] + _build.ARCH + ["-shared", "-o", lib, obj] + objs + ["-lcudart"], check=True,
-                   capture_output=True)
-    return k, lib
+    lib = os.path.join(tmp, "libqstem_gpu_%s.so" % tag)
+    subprocess.run([_build.nvcc()] + _build.ARCH + ["-shared", "-o", lib, obj] + list(extra_objs) + objs +
+                   ["-lcudart"], check=True, capture_output=True)
+    return lib, obj
 
 
 def measure(lib_path, sizes, reps=4):
@@ -77,16 +84,61 @@ def measure(lib_path, sizes, reps=4):
     return out
 
 
+def measure_adjoint(lib_path, sizes, reps=3):
+    """{N: ms} of the adjoint (every state kept) of one library build."""
+    import numpy as np
+    import torch
+    from . import config, lib
+    lib.load(lib_path)
+    ctx = lib.Context(0)
+    out = {}
+    try:
+        stream = torch.cuda.ExternalStream(ctx.stream_handle)
+        for n in sizes:
+            dx = 0.05
+            ax = n * dx * 1.2
+            side = {64: 32, 128: 32, 256: 32, 384: 16, 512: 16, 768: 8, 1024: 8}[n]
+            p = config.make_params(nx=n, resolutionX=dx, v0=200, slices=8, sliceThickness=2.0, ax=ax, by=ax, c=16.0,
+                                   scan=(ax / 2, ax / 2 + 0.5, side, ax / 2, ax / 2 + 0.5, side), detectors=[],
+                                   alpha=20)
+            ph = np.random.default_rng(1).standard_normal((p.slices, p.potNx, p.potNy)).astype(np.float32) * 0.3
+            T = torch.from_numpy(np.stack([np.cos(ph), np.sin(ph)], -1)).cuda()
+            probe = torch.from_numpy(ctx.probe(p)).cuda()
+            target = torch.rand((side * side, n, n), device="cuda")
+            ctx.adjoint(p, T, probe, target, ckpt=1)
+            best = None
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record(stream)
+                ctx.adjoint(p, T, probe, target, ckpt=1)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                t = e0.elapsed_time(e1)
+                best = t if best is None else min(best, t)
+            out[n] = best
+    finally:
+        ctx.close()
+    return out
+
+
 def write_table(best):
-    """Store the chosen values as the defaults of csrc/qs_tuned.h."""
+    """Store the chosen values ({("ROW"|"COL"|"ADJ", N): k}) as the defaults
+    of csrc/qs_tuned.h."""
     path = os.path.join(_build.SRC, "qs_tuned.h")
     lines = open(path).read().split("\n")
     for i, line in enumerate(lines):
-        for n, k in best.items():
-            if line.startswith("#define QS_ROW_MIN_BLOCKS_%d " % n):
-                lines[i] = "#define QS_ROW_MIN_BLOCKS_%d %d" % (n, k)
+        for (kind, n), k in best.items():
+            if line.startswith("#define QS_%s_MIN_BLOCKS_%d " % (kind, n)):
+                lines[i] = "#define QS_%s_MIN_BLOCKS_%d %d" % (kind, n, k)
     with open(path, "w") as f:
         f.write("\n".join(lines))
+
+
+def _run_measure(mode, sizes, path):
+    r = subprocess.run([sys.executable, "-m", "qstem_gb300.tune", "--sizes", ",".join(map(str, sizes)), mode, path],
+                       capture_output=True, text=True, check=True, cwd=os.path.dirname(_build.HERE))
+    return {int(n): v for n, v in json.loads(r.stdout.strip().splitlines()[-1]).items()}
 
 
 def main(argv=None):
@@ -94,29 +146,46 @@ def main(argv=None):
     ap.add_argument("--candidates", default="1,2,3,4,6,8")
     ap.add_argument("--sizes", default=",".join(map(str, SIZES)))
     ap.add_argument("--write", action="store_true")
-    ap.add_argument("--measure", help=argparse.SUPPRESS)  # internal: time one library, print JSON
+    ap.add_argument("--measure", help=argparse.SUPPRESS)          # internal: time one library
+    ap.add_argument("--measure-adjoint", help=argparse.SUPPRESS)  # internal
     a = ap.parse_args(argv)
     sizes = [int(s) for s in a.sizes.split(",")]
     if a.measure:
         print(json.dumps(measure(a.measure, sizes)))
         return 0
+    if a.measure_adjoint:
+        print(json.dumps(measure_adjoint(a.measure_adjoint, sizes)))
+        return 0
     _build.build()
     cands = [int(k) for k in a.candidates.split(",")]
     tmp = tempfile.mkdtemp(prefix="qs_tune_")
-    with concurrent.futures.ThreadPoolExecutor(max_workers=len(cands)) as ex:
-        libs = dict(ex.map(lambda k: _variant(k, sizes, tmp), cands))
-    results = {}
-    for k, path in sorted(libs.items()):
-        r = subprocess.run([sys.executable, "-m", "qstem_gb300.tune", "--sizes", a.sizes, "--measure", path],
-                           capture_output=True, text=True, check=True, cwd=os.path.dirname(_build.HERE))
-        results[k] = {int(n): v for n, v in json.loads(r.stdout.strip().splitlines()[-1]).items()}
-    print("row pass, us per position-slice (candidate = CTAs per SM)")
-    print("N     " + "".join("%8d" % k for k in sorted(results)))
     best = {}
+    # phase 1: row and column passes
+    defs = {k: ["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, k) for n in sizes for kind in ("ROW", "COL")] for k in cands}
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(cands)) as ex:
+        libs = dict(zip(cands, ex.map(lambda k: _variant("rc%d" % k, "qs_multislice.cu", defs[k], tmp)[0], cands)))
+    res = {k: _run_measure("--measure", sizes, libs[k]) for k in cands}
+    for j, kind in ((0, "ROW"), (1, "COL")):
+        print("%s pass, us per position-slice (candidate = CTAs per SM)" % kind.lower())
+        print("N     " + "".join("%8d" % k for k in cands))
+        for n in sizes:
+            times = {k: res[k][n][j] for k in cands}
+            best[(kind, n)] = min(times, key=times.get)
+            print("%-6d" % n + "".join("%8.3f" % times[k] for k in cands) + "   -> %d" % best[(kind, n)])
+    # phase 2: row adjoint, with the phase-1 winners
+    fixed = ["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, best[(kind, n)]) for n in sizes for kind in ("ROW", "COL")]
+    _, ms_obj = _variant("fixed", "qs_multislice.cu", fixed, tmp)
+    adefs = {k: ["QS_ADJ_MIN_BLOCKS_%d=%d" % (n, k) for n in sizes] for k in cands}
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(cands)) as ex:
+        alibs = dict(zip(cands, ex.map(
+            lambda k: _variant("adj%d" % k, "qs_adjoint.cu", adefs[k], tmp, extra_objs=[ms_obj])[0], cands)))
+    ares = {k: _run_measure("--measure-adjoint", sizes, alibs[k]) for k in cands}
+    print("adjoint (every state kept, 8 slices), ms")
+    print("N     " + "".join("%8d" % k for k in cands))
     for n in sizes:
-        times = {k: results[k][n][0] for k in results}
-        best[n] = min(times, key=times.get)
-        print("%-6d" % n + "".join("%8.3f" % times[k] for k in sorted(times)) + "   -> %d" % best[n])
+        times = {k: ares[k][n] for k in cands}
+        best[("ADJ", n)] = min(times, key=times.get)
+        print("%-6d" % n + "".join("%8.3f" % times[k] for k in cands) + "   -> %d" % best[("ADJ", n)])
     if a.write:
         write_table(best)
         print("wrote", os.path.join(_build.SRC, "qs_tuned.h"))
