@@ -70,7 +70,7 @@ static int ev_record(qs_ctx* c, size_t* idx) {
 
 enum Buf {
     B_WAVES, B_PROBE, B_PARTIAL, B_POS, B_TABLES, B_TILES, B_TRANS, B_OUT1, B_OUT2, B_OUT3, B_JOBS, B_LUTS,
-    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, NBUF
+    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, B_BAND, NBUF
 };
 static_assert(NBUF <= kMaxBufs, "context buffer table too small");
 
@@ -489,14 +489,37 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
             k2max = (float)((2.0f / 3.0f) * k2max);
             k2max = k2max * k2max;
             void* dt = nullptr;
-            QS_TRY(ensure(c, B_TABLES, sizeof(float) * (nx + ny), &dt));
-            std::vector<float> both(kx2);
-            both.insert(both.end(), ky2.begin(), ky2.end());
-            QS_CUDA_TRY(cudaMemcpyAsync(dt, both.data(), sizeof(float) * both.size(), cudaMemcpyHostToDevice, c->stream));
-            QS_TRY(xform(false));
-            QS_TRY(launch_bandlimit_mask(trans, P.slices, nx, ny, (float*)dt, (float*)dt + nx, k2max,
-                                         1.0 / (nx * ny), c->stream));
-            QS_TRY(xform(true));
+            if (lines) {
+                // fused: FFT_y, one column pass (FFT_x, mask and 1/N, IFFT_x), IFFT_y
+                const int Cw = col_tile_width(nx), ntl = ny / Cw;
+                const size_t bytes = sizeof(float) * (nx + ny) + sizeof(float2) * (nx + ny) + sizeof(int) * ntl;
+                QS_TRY(ensure(c, B_BAND, bytes, &dt));
+                std::vector<unsigned char> host(bytes);
+                float* hk = (float*)host.data();
+                std::copy(kx2.begin(), kx2.end(), hk);
+                std::copy(ky2.begin(), ky2.end(), hk + nx);
+                float2* hp = (float2*)(hk + nx + ny);
+                const float sc = (float)(1.0 / (nx * ny));
+                for (int i = 0; i < nx; i++) hp[i] = make_float2(sc, 0.f);
+                for (int i = 0; i < ny; i++) hp[nx + i] = make_float2(1.f, 0.f);
+                int* ht = (int*)(hp + nx + ny);
+                for (int k = 0; k < ntl; k++) ht[k] = k * Cw;
+                QS_CUDA_TRY(cudaMemcpyAsync(dt, host.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+                const float* dk = (const float*)dt;
+                const float2* dp = (const float2*)(dk + nx + ny);
+                QS_TRY(bandlimit_lines(trans, nx, ny, P.slices, dk, dk + nx, dp, dp + nx, (const int*)(dp + nx + ny),
+                                       k2max, c->stream));
+            } else {
+                QS_TRY(ensure(c, B_TABLES, sizeof(float) * (nx + ny), &dt));
+                std::vector<float> both(kx2);
+                both.insert(both.end(), ky2.begin(), ky2.end());
+                QS_CUDA_TRY(cudaMemcpyAsync(dt, both.data(), sizeof(float) * both.size(), cudaMemcpyHostToDevice,
+                                            c->stream));
+                QS_TRY(xform(false));
+                QS_TRY(launch_bandlimit_mask(trans, P.slices, nx, ny, (float*)dt, (float*)dt + nx, k2max,
+                                             1.0 / (nx * ny), c->stream));
+                QS_TRY(xform(true));
+            }
             QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
         }
     }

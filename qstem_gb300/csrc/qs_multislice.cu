@@ -496,6 +496,47 @@ int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t 
     return QS_OK;
 }
 
+// The transmission band limit of initSTEMSlices (stem3/stemlib.cpp:2305-2336)
+// on every slice of `data` (howmany slices of n0 x n1) in three passes:
+// forward line FFTs along y, one column pass (FFT_x, the mask with its 1/N
+// scale as a separable "propagator" of (1/N, 0) x (1, 0) limited to
+// k^2 < k2max, IFFT_x; every column, so the out-of-band ones come out zero),
+// inverse line FFTs along y.  tab: device tables kx2[n0], ky2[n1],
+// px[n0] = (1/N, 0), py[n1] = (1, 0), tiles[n1 / column-tile width].
+int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2, const float* ky2,
+                    const float2* px, const float2* py, const int* tiles, float k2max, cudaStream_t s) {
+    if (!line_supported(n0) || !line_supported(n1)) {
+        set_error("band limit: size " + std::to_string(n0) + "x" + std::to_string(n1) + " not supported");
+        return QS_ERR_UNSUPPORTED;
+    }
+    const float2* tw = twiddles(n0);
+    if (!tw || !twiddles(n1)) {
+        set_error("twiddle table allocation failed");
+        return QS_ERR_NOMEM;
+    }
+    QS_TRY(fft_rows_any<false>(data, n1, (long)n0 * howmany, s));
+    ColArgs ca{};
+    ca.nx = n0;
+    ca.ny = n1;
+    ca.nwaves = howmany;
+    ca.waves = data;
+    ca.waves_out = nullptr;
+    ca.tw = tw;
+    ca.kx2 = kx2;
+    ca.ky2 = ky2;
+    ca.px = px;
+    ca.py = py;
+    ca.k2max = k2max;
+    ca.tiles = tiles;
+    ca.ntiles = n1 / col_tile_width(n0);
+    ca.inverse = 1;
+    ca.ndet = 0;
+    ca.diffpat = nullptr;
+    QS_TRY(launch_cols(ca, s));
+    QS_TRY(fft_rows_any<true>(data, n1, (long)n0 * howmany, s));
+    return QS_OK;
+}
+
 template <int N>
 static void fill_twiddles(std::vector<float2>& h) {
     using Cfg = typename Line<N>::cfg;
