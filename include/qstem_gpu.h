@@ -333,7 +333,11 @@ int qs_phase_grating(qs_ctx *ctx, const qs_params *p, const float *V, float *tra
  * the forward patterns (device, [npos][nx][ny]).  Forward waves are kept every
  * `ckpt` slices and recomputed in between (1 = keep all; <= 0 = keep all when
  * they fit in free device memory less 1 GiB, else the smallest interval that
- * fits).  All arrays are device pointers; trans must not be band-limited. */
+ * fits).  All arrays are device pointers; trans must not be band-limited.
+ * A cell divided into slabs (cellDiv > 1) runs through all of them: trans is
+ * one stack reused for every slab, whose dL/dV slices then sum the gradient
+ * of every use, or with QS_SLAB_STACKS cellDiv stacks back to back and as
+ * many dL/dV stacks. */
 int qs_adjoint_run(qs_ctx *ctx, const qs_params *p, const float *trans, const float *probe,
                    const qs_batch *batch, const float *target, int ckpt, double *loss, float *dL_dV,
                    float *diffpats, unsigned flags);
@@ -342,7 +346,10 @@ int qs_adjoint_run(qs_ctx *ctx, const qs_params *p, const float *trans, const fl
  * dL/dV (device): the adjoint of make3DSlices' scatter-sum
  * (stem3/stemlib.cpp:894-1213) through its radial linear interpolation.
  * Atoms that contribute to no slice get zero; z gradients are not returned
- * (the LUT is nearest-neighbour in z, stem3/stemlib.cpp:76). */
+ * (the LUT is nearest-neighbour in z, stem3/stemlib.cpp:76).  With
+ * cellDiv > 1 and QS_SLAB_STACKS, dL_dV holds one stack per slab and the
+ * gradients sum every slab's placement of the atoms (make3DSlices' offset
+ * of slab k); without it, slab 0's (the stack reused for every slab). */
 int qs_atoms_grad(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom, const float *dL_dV,
                   double *grad_xy, unsigned flags);
 

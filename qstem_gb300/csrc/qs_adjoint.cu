@@ -204,7 +204,8 @@ __global__ void adj_dv_partial(const float2* __restrict__ grad_t, int npos, int 
 }
 
 __global__ void adj_dv_finish(const float2* __restrict__ partial, int nchunks, int potNx, int potNy,
-                              const float2* __restrict__ trans_slice, double sigma, float* __restrict__ dV) {
+                              const float2* __restrict__ trans_slice, double sigma, int accumulate,
+                              float* __restrict__ dV) {
     const size_t n = (size_t)potNx * potNy;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         double gr = 0.0, gi = 0.0;
@@ -215,7 +216,8 @@ __global__ void adj_dv_finish(const float2* __restrict__ partial, int nchunks, i
         }
         const float2 tv = trans_slice[i];
         // Im(conj(G) t) = gr*t.y - gi*t.x
-        dV[i] = (float)(-2.0 * sigma * (gr * tv.y - gi * tv.x));
+        const float g = (float)(-2.0 * sigma * (gr * tv.y - gi * tv.x));
+        dV[i] = accumulate ? dV[i] + g : g;
     }
 }
 
@@ -398,7 +400,7 @@ size_t dv_partial_bytes(int npos, int potNx, int potNy) {
 
 int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, int potNy, const int* posX,
                      const int* posY, const float2* trans_slice, double sigma, void* partial, float* dV,
-                     cudaStream_t s) {
+                     bool accumulate, cudaStream_t s) {
     const int nchunks = (npos + DV_CHUNK - 1) / DV_CHUNK;
     adj_dv_partial<<<dim3((potNy + 127) / 128, potNx, nchunks), 128, 0, s>>>(grad_t, npos, nx, ny, potNx, potNy,
                                                                             posX, posY, (float2*)partial);
@@ -406,7 +408,8 @@ int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, 
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    adj_dv_finish<<<sms * 4, 256, 0, s>>>((const float2*)partial, nchunks, potNx, potNy, trans_slice, sigma, dV);
+    adj_dv_finish<<<sms * 4, 256, 0, s>>>((const float2*)partial, nchunks, potNx, potNy, trans_slice, sigma,
+                                          accumulate ? 1 : 0, dV);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(2);
     return QS_OK;

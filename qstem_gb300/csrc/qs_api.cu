@@ -1395,11 +1395,11 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
         set_error("adjoint: band-limited transmission functions are not supported");
         return QS_ERR_UNSUPPORTED;
     }
-    if (P.cellDiv != 1) {
-        set_error("adjoint: cells divided into slabs (cellDiv > 1) are not supported");
-        return QS_ERR_UNSUPPORTED;
-    }
-    const int npos = batch->npos, S = P.slices, nx = P.nx, ny = P.ny;
+    // absolute slices: cellDiv slabs of `slices` (doSTEM's slab loop); the
+    // stack is one per slab with QS_SLAB_STACKS, else one reused
+    const int npos = batch->npos, S0 = P.slices, D = std::max(1, P.cellDiv), S = S0 * D, nx = P.nx, ny = P.ny;
+    const bool slabStacks = D > 1 && (flags & QS_SLAB_STACKS);
+    auto stackIdx = [&](int a) { return slabStacks ? a : a % S0; };
     if (npos < 1) { set_error("batch has no positions"); return QS_ERR_ARG; }
     if (ckpt < 1) {
         // automatic: every state kept when they fit (no recomputation), else
@@ -1534,7 +1534,7 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
         for (int sl = s0; sl < last; sl++) {
             ra.waves = cur;
             ra.waves_out = work;
-            ra.trans_slice = trans + (size_t)sl * sliceElems;
+            ra.trans_slice = trans + (size_t)stackIdx(sl) * sliceElems;
             QS_TRY(launch_rows(ra, sl == 0 ? ROW_FIRST : ROW_MID, s));
             if (sl == S - 1) break;
             const int nxt = sl + 1;
@@ -1579,11 +1579,13 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
                 QS_TRY(launch_cols(ca, s));
             }
             ar.state = state_of(sl, s0);
-            ar.trans_slice = trans + (size_t)sl * sliceElems;
+            ar.trans_slice = trans + (size_t)stackIdx(sl) * sliceElems;
             QS_TRY(launch_adj_rows(ar, sl == 0, s));
+            // a reused stack's slice collects the gradient of every use; the
+            // backward meets its last use (the last slab) first
             QS_TRY(launch_dv_gather(grad_t, npos, nx, ny, P.potNx, P.potNy, d_pos, d_pos + npos,
-                                    trans + (size_t)sl * sliceElems, sigma, d_part, dL_dV + (size_t)sl * sliceElems,
-                                    s));
+                                    trans + (size_t)stackIdx(sl) * sliceElems, sigma, d_part,
+                                    dL_dV + (size_t)stackIdx(sl) * sliceElems, !slabStacks && sl < S - S0, s));
         }
     }
     if (loss) {
@@ -1607,30 +1609,36 @@ int qs_atoms_grad(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         set_error("only the 3-D FFT-integrated potential is supported");
         return QS_ERR_UNSUPPORTED;
     }
-    if (p->cellDiv != 1) {
-        set_error("atom gradients: cells divided into slabs (cellDiv > 1) are not supported");
-        return QS_ERR_UNSUPPORTED;
-    }
     QS_CUDA_TRY(cudaSetDevice(c->device));
-    (void)flags;
-    std::vector<AtomJob> jobs;
-    std::vector<std::pair<int, double>> lutKeys;
-    plan_atoms(*p, atoms, natom, jobs, lutKeys);
+    // a cell divided into slabs with one stack per slab: every slab's atom
+    // placement against its own dL/dV, summed; otherwise slab 0's (the stack
+    // the forward reused for every slab)
+    const int nslab = (p->cellDiv > 1 && (flags & QS_SLAB_STACKS)) ? p->cellDiv : 1;
+    const size_t stackElems = (size_t)p->slices * p->potNx * p->potNy;
+    std::vector<double> total(2 * (size_t)std::max(natom, 1), 0.0), part(total.size());
     void* dg = nullptr;
     QS_TRY(ensure(c, B_OUT3, sizeof(double) * 2 * std::max(natom, 1), &dg));
-    QS_CUDA_TRY(cudaMemsetAsync(dg, 0, sizeof(double) * 2 * std::max(natom, 1), c->stream));
-    if (!jobs.empty()) {
-        int Nz = 0, Nr = 0, ns = 0;
-        const float* const* d_luts = nullptr;
-        QS_TRY(prepare_luts(c, *p, lutKeys, &d_luts, &Nz, &Nr, &ns));
-        void* dj = nullptr;
-        QS_TRY(ensure(c, B_JOBS, sizeof(AtomJob) * jobs.size(), &dj));
-        QS_CUDA_TRY(cudaMemcpyAsync(dj, jobs.data(), sizeof(AtomJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream));
-        QS_TRY(launch_atoms_grad((const AtomJob*)dj, (int)jobs.size(), d_luts, Nz, Nr, ns, *p, dL_dV, (double*)dg,
-                                 c->stream));
+    for (int slab = 0; slab < nslab; slab++) {
+        std::vector<AtomJob> jobs;
+        std::vector<std::pair<int, double>> lutKeys;
+        plan_atoms(*p, atoms, natom, jobs, lutKeys, slab);
+        QS_CUDA_TRY(cudaMemsetAsync(dg, 0, sizeof(double) * 2 * std::max(natom, 1), c->stream));
+        if (!jobs.empty()) {
+            int Nz = 0, Nr = 0, ns = 0;
+            const float* const* d_luts = nullptr;
+            QS_TRY(prepare_luts(c, *p, lutKeys, &d_luts, &Nz, &Nr, &ns));
+            void* dj = nullptr;
+            QS_TRY(ensure(c, B_JOBS, sizeof(AtomJob) * jobs.size(), &dj));
+            QS_CUDA_TRY(cudaMemcpyAsync(dj, jobs.data(), sizeof(AtomJob) * jobs.size(), cudaMemcpyHostToDevice,
+                                        c->stream));
+            QS_TRY(launch_atoms_grad((const AtomJob*)dj, (int)jobs.size(), d_luts, Nz, Nr, ns, *p,
+                                     dL_dV + (size_t)slab * stackElems, (double*)dg, c->stream));
+        }
+        QS_CUDA_TRY(cudaMemcpyAsync(part.data(), dg, sizeof(double) * 2 * natom, cudaMemcpyDeviceToHost, c->stream));
+        QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        for (size_t i = 0; i < 2 * (size_t)natom; i++) total[i] += part[i];
     }
-    QS_CUDA_TRY(cudaMemcpyAsync(grad_xy, dg, sizeof(double) * 2 * natom, cudaMemcpyDeviceToHost, c->stream));
-    QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    std::copy(total.begin(), total.begin() + 2 * (size_t)natom, grad_xy);
     return QS_OK;
 }
 

@@ -157,6 +157,7 @@ int launch_adj_rows(const AdjRowArgs& a, bool first, cudaStream_t s);
 size_t dv_partial_bytes(int npos, int potNx, int potNy);
 int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, int potNy, const int* posX,
                      const int* posY, const float2* trans_slice, double sigma, void* partial, float* dV,
+                     bool accumulate,
                      cudaStream_t s);
 int launch_atoms_grad(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
                       const qs_params& p, const float* dV, double* grad, cudaStream_t s);

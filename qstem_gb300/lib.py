@@ -270,26 +270,30 @@ class Context:
         _check(self.lib.qs_phase_grating(self.h, ctypes.byref(p), _ptr(V), _ptr(out), abi.QS_SYNC))
         return out
 
-    def adjoint(self, p, trans, probe, target, positions=None, ckpt=0, want_diffpats=False):
+    def adjoint(self, p, trans, probe, target, positions=None, ckpt=0, want_diffpats=False, slab_stacks=False):
         """Loss sum (I - target)^2 and dL/dV (device torch tensors in and out).
         ckpt: keep the forward waves every ckpt slices (1: all; 0: all when
-        they fit in device memory, else the smallest interval that fits)."""
+        they fit in device memory, else the smallest interval that fits).
+        slab_stacks: trans holds one stack per slab of a cell divided into
+        cellDiv slabs (dL/dV then too); else one stack serves every slab."""
         import torch
         bx, keep = _batch(p, positions)
-        dV = torch.empty((p.slices, p.potNx, p.potNy), dtype=torch.float32, device=trans.device)
+        nst = p.cellDiv if (slab_stacks and p.cellDiv > 1) else 1
+        dV = torch.empty((p.slices * nst, p.potNx, p.potNy), dtype=torch.float32, device=trans.device)
         dps = torch.empty((bx.npos, p.nx, p.ny), dtype=torch.float32, device=trans.device) if want_diffpats else None
         loss = ctypes.c_double()
         _check(self.lib.qs_adjoint_run(self.h, ctypes.byref(p), _ptr(trans), _ptr(probe), ctypes.byref(bx),
                                        _ptr(target), int(ckpt), ctypes.byref(loss), _ptr(dV), _ptr(dps),
-                                       abi.QS_SYNC))
+                                       abi.QS_SYNC | (abi.QS_SLAB_STACKS if slab_stacks else 0)))
         del keep
         return loss.value, dV, dps
 
-    def atoms_grad(self, p, atoms, dV):
+    def atoms_grad(self, p, atoms, dV, slab_stacks=False):
         a = abi.atoms_to_numpy(atoms)
         g = np.zeros((len(a), 2), np.float64)
         _check(self.lib.qs_atoms_grad(self.h, ctypes.byref(p), a.ctypes.data_as(ctypes.c_void_p), len(a), _ptr(dV),
-                                      g.ctypes.data_as(ctypes.c_void_p), 0))
+                                      g.ctypes.data_as(ctypes.c_void_p),
+                                      abi.QS_SLAB_STACKS if slab_stacks else 0))
         return g
 
     def profile(self, enable=True):

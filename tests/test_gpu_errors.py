@@ -42,11 +42,8 @@ def test_argument_and_support_errors(case):
     # a slab index beyond cellDiv
     expect(abi.QS_ERR_ARG, ctx.slices, p, g["atoms"], slab=1)
     # options a driver does not implement
-    q = p.copy()
-    q.cellDiv = 2
     target = T.new_zeros((p.scanXN * p.scanYN, p.nx, p.ny, 2))[..., 0].contiguous()
     probe = T.new_zeros((p.nx, p.ny, 2))
-    expect(abi.QS_ERR_UNSUPPORTED, ctx.adjoint, q, T, probe, target)
     r = p.copy()
     r.bandlimittrans = 1
     expect(abi.QS_ERR_UNSUPPORTED, ctx.adjoint, r, T, probe, target)
