@@ -99,3 +99,26 @@ def test_atom_gradients_through_slab_stacks(ctx):
             fd[i, k] = (loss_of(ap) - loss_of(am)) / (float(ap[ax][j]) - float(am[ax][j]))
     assert np.abs(grad[pick]).max() > 0
     assert rel_l2(grad[pick], fd) <= 1e-2
+
+
+def test_autograd_through_slab_stacks(ctx):
+    """MultisliceLoss and AtomsLoss with slab stacks: the same loss and
+    gradients as the C entry points."""
+    import torch
+    from qstem_gb300 import autograd
+    g, p, q, atoms, pos, probe, stacks, tgt = _setup(ctx, "sto64d2u")
+    V = torch.from_numpy(np.concatenate([ctx.slices(p, atoms, potential_only=True, slab=k)[..., 0]
+                                         for k in range(p.cellDiv)])).cuda().requires_grad_(True)
+    L = autograd.MultisliceLoss.apply(V, ctx, p, probe, tgt, pos, 1, True)
+    L.backward()
+    Tst = torch.from_numpy(np.concatenate(stacks)).cuda()
+    loss, dV, _ = ctx.adjoint(p, Tst, probe, tgt, positions=pos, ckpt=1, slab_stacks=True)
+    assert abs(float(L.detach()) - loss) <= 1e-5 * abs(loss)
+    assert rel_l2(V.grad.cpu().numpy(), dV.cpu().numpy()) <= 1e-4
+    xy = torch.from_numpy(np.stack([atoms["x"], atoms["y"]], 1).astype(np.float64)).requires_grad_(True)
+    La = autograd.AtomsLoss.apply(xy, ctx, p, atoms, probe, tgt, pos, 1, True)
+    La.backward()
+    # the stacks are rebuilt from the atoms: the scatter's float reductions
+    # sum in a different order, ~1e-7 of the potential
+    assert abs(float(La.detach()) - loss) <= 1e-5 * abs(loss)
+    assert rel_l2(xy.grad.numpy(), ctx.atoms_grad(p, atoms, dV, slab_stacks=True)) <= 1e-4
