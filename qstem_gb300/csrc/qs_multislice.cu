@@ -26,7 +26,20 @@
 
 namespace qs {
 
+// lines per CTA of the plain line-FFT kernels (fft_rows)
 constexpr int ROW_LINES = 8;
+
+// lines per CTA of the row pass, per line length (qs_tuned.h)
+constexpr int row_lines(int n) {
+    return n == 64     ? QS_ROW_LINES_64
+           : n == 128  ? QS_ROW_LINES_128
+           : n == 256  ? QS_ROW_LINES_256
+           : n == 384  ? QS_ROW_LINES_384
+           : n == 512  ? QS_ROW_LINES_512
+           : n == 768  ? QS_ROW_LINES_768
+           : n == 1024 ? QS_ROW_LINES_1024
+                       : 8;
+}
 
 // CTAs per SM the row pass is compiled for (register budget), per line
 // length, from the measured table in qs_tuned.h
@@ -42,7 +55,7 @@ constexpr int row_min_blocks(int n) {
 }
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(line_threads(N) * ROW_LINES, row_min_blocks(N))
+__global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks(N))
     ms_rows(RowArgs a) {
     using Cfg = typename Line<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E;
@@ -50,11 +63,11 @@ __global__ void __launch_bounds__(line_threads(N) * ROW_LINES, row_min_blocks(N)
     float2* s_tw = dsm;
     float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
     const int tid = threadIdx.x + T * threadIdx.y;
-    for (int i = tid; i < Cfg::TW; i += T * ROW_LINES) s_tw[i] = a.tw[i];
+    for (int i = tid; i < Cfg::TW; i += T * row_lines(N)) s_tw[i] = a.tw[i];
     __syncthreads();
 
     const int t = threadIdx.x;
-    const long line = (long)blockIdx.x * ROW_LINES + threadIdx.y;
+    const long line = (long)blockIdx.x * row_lines(N) + threadIdx.y;
     const int b = (int)(line / a.nx);
     const int x = (int)(line - (long)b * a.nx);
     const SmemRow<Cfg::R0> sm{s_line};
@@ -242,8 +255,8 @@ __global__ void det_finalize(const double* __restrict__ partial, int nwaves, int
 
 // ------------------------------------------------------------- launchers
 template <int N>
-static size_t row_smem() {
-    return sizeof(float2) * (N + ROW_LINES * Line<N>::cfg::SMEM);
+static size_t row_smem(int lines = row_lines(N)) {
+    return sizeof(float2) * (N + (size_t)lines * Line<N>::cfg::SMEM);
 }
 template <int N>
 static size_t col_smem() {
@@ -264,12 +277,12 @@ static int rows_n(const RowArgs& a, cudaStream_t s) {
         attr = true;
     }
     const long lines = (long)a.nwaves * a.nx;
-    if (lines % ROW_LINES) {
-        set_error("row pass: nwaves*nx must be a multiple of 8");
+    if (lines % row_lines(N)) {
+        set_error("row pass: nwaves*nx must be a multiple of " + std::to_string(row_lines(N)));
         return QS_ERR_ARG;
     }
-    dim3 block(Cfg::T, ROW_LINES);
-    ms_rows<N, MODE><<<(unsigned)(lines / ROW_LINES), block, sm, s>>>(a);
+    dim3 block(Cfg::T, row_lines(N));
+    ms_rows<N, MODE><<<(unsigned)(lines / row_lines(N)), block, sm, s>>>(a);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;
@@ -421,7 +434,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
 template <int N, bool INV>
 static int fft_rows_n(float2* data, long nlines, cudaStream_t s) {
     static bool attr = false;
-    const size_t sm = row_smem<N>();
+    const size_t sm = row_smem<N>(ROW_LINES);
     if (!attr) {
         QS_CUDA_TRY(cudaFuncSetAttribute(fft_rows<N, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         attr = true;

@@ -3,8 +3,9 @@ line length.
 
     python -m qstem_gb300.tune [--candidates 1,2,3,4,6,8] [--sizes 256,384,...] [--write]
 
-Phase 1, row and column passes: for each candidate k the slice-loop
-translation unit (qs_multislice.cu) is compiled with every
+Phase 1, row and column passes: for each candidate budget k and row-pass
+shape L (line transforms per CTA, --lines) the slice-loop translation unit
+(qs_multislice.cu) is compiled with every QS_ROW_LINES_<N> = L and
 QS_ROW_MIN_BLOCKS_<N> = QS_COL_MIN_BLOCKS_<N> = k and linked with the other
 objects of the normal build into a variant library in a temporary folder
 (the candidates compile in parallel).  Each variant times, in a fresh
@@ -123,14 +124,15 @@ def measure_adjoint(lib_path, sizes, reps=3):
 
 
 def write_table(best):
-    """Store the chosen values ({("ROW"|"COL"|"ADJ", N): k}) as the defaults
-    of csrc/qs_tuned.h."""
+    """Store the chosen values ({("ROW"|"COL"|"ADJ"|"LINES", N): k}) as the
+    defaults of csrc/qs_tuned.h."""
     path = os.path.join(_build.SRC, "qs_tuned.h")
     lines = open(path).read().split("\n")
     for i, line in enumerate(lines):
         for (kind, n), k in best.items():
-            if line.startswith("#define QS_%s_MIN_BLOCKS_%d " % (kind, n)):
-                lines[i] = "#define QS_%s_MIN_BLOCKS_%d %d" % (kind, n, k)
+            name = "QS_ROW_LINES_%d" % n if kind == "LINES" else "QS_%s_MIN_BLOCKS_%d" % (kind, n)
+            if line.startswith("#define %s " % name):
+                lines[i] = "#define %s %d" % (name, k)
     with open(path, "w") as f:
         f.write("\n".join(lines))
 
@@ -145,6 +147,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--candidates", default="1,2,3,4,6,8")
     ap.add_argument("--sizes", default=",".join(map(str, SIZES)))
+    ap.add_argument("--lines", default="4,8")
     ap.add_argument("--write", action="store_true")
     ap.add_argument("--measure", help=argparse.SUPPRESS)          # internal: time one library
     ap.add_argument("--measure-adjoint", help=argparse.SUPPRESS)  # internal
@@ -161,19 +164,30 @@ def main(argv=None):
     tmp = tempfile.mkdtemp(prefix="qs_tune_")
     best = {}
     # phase 1: row and column passes
-    defs = {k: ["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, k) for n in sizes for kind in ("ROW", "COL")] for k in cands}
-    with concurrent.futures.ThreadPoolExecutor(max_workers=len(cands)) as ex:
-        libs = dict(zip(cands, ex.map(lambda k: _variant("rc%d" % k, "qs_multislice.cu", defs[k], tmp)[0], cands)))
-    res = {k: _run_measure("--measure", sizes, libs[k]) for k in cands}
-    for j, kind in ((0, "ROW"), (1, "COL")):
-        print("%s pass, us per position-slice (candidate = CTAs per SM)" % kind.lower())
-        print("N     " + "".join("%8d" % k for k in cands))
-        for n in sizes:
-            times = {k: res[k][n][j] for k in cands}
-            best[(kind, n)] = min(times, key=times.get)
-            print("%-6d" % n + "".join("%8.3f" % times[k] for k in cands) + "   -> %d" % best[(kind, n)])
+    shapes = [int(x) for x in a.lines.split(",")]
+    combos = [(L, k) for L in shapes for k in cands]
+    defs = {(L, k): ["QS_ROW_LINES_%d=%d" % (n, L) for n in sizes] +
+            ["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, k) for n in sizes for kind in ("ROW", "COL")] for L, k in combos}
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(combos)) as ex:
+        libs = dict(zip(combos, ex.map(
+            lambda c: _variant("rc%d_%d" % c, "qs_multislice.cu", defs[c], tmp)[0], combos)))
+    res = {c: _run_measure("--measure", sizes, libs[c]) for c in combos}
+    print("row pass, us per position-slice (lines per CTA x CTAs per SM)")
+    print("N     " + "".join("%8s" % ("%dx%d" % c) for c in combos))
+    for n in sizes:
+        times = {c: res[c][n][0] for c in combos}
+        L, k = min(times, key=times.get)
+        best[("ROW", n)], best[("LINES", n)] = k, L
+        print("%-6d" % n + "".join("%8.3f" % times[c] for c in combos) + "   -> %dx%d" % (L, k))
+    print("col pass, us per position-slice (CTAs per SM)")
+    print("N     " + "".join("%8d" % k for k in cands))
+    for n in sizes:
+        times = {k: min(res[(L, k)][n][1] for L in shapes) for k in cands}
+        best[("COL", n)] = min(times, key=times.get)
+        print("%-6d" % n + "".join("%8.3f" % times[k] for k in cands) + "   -> %d" % best[("COL", n)])
     # phase 2: row adjoint, with the phase-1 winners
-    fixed = ["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, best[(kind, n)]) for n in sizes for kind in ("ROW", "COL")]
+    fixed = (["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, best[(kind, n)]) for n in sizes for kind in ("ROW", "COL")] +
+             ["QS_ROW_LINES_%d=%d" % (n, best[("LINES", n)]) for n in sizes])
     _, ms_obj = _variant("fixed", "qs_multislice.cu", fixed, tmp)
     adefs = {k: ["QS_ADJ_MIN_BLOCKS_%d=%d" % (n, k) for n in sizes] for k in cands}
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(cands)) as ex:
