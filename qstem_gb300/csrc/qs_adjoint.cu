@@ -324,12 +324,8 @@ template <int N>
 static int last_n(const AdjLastArgs& a, cudaStream_t s) {
     using Cfg = typename Line<N>::cfg;
     constexpr int C = col_tile<N>();
-    static bool attr = false;
     const size_t sm = sizeof(float2) * (N + (size_t)N * C);
-    if (!attr) {
-        QS_CUDA_TRY(cudaFuncSetAttribute(adj_last_cols<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        attr = true;
-    }
+    QS_TRY(smem_attr((const void*)adj_last_cols<N>, sm));
     const long nblk = (long)a.nwaves * (a.ny / C);
     adj_last_cols<N><<<(unsigned)nblk, dim3(C, Cfg::T), sm, s>>>(a);
     QS_CUDA_TRY(cudaGetLastError());
@@ -358,12 +354,8 @@ int launch_adj_last(const AdjLastArgs& a, cudaStream_t s) {
 template <int N, bool FIRST>
 static int adj_rows_n(const AdjRowArgs& a, cudaStream_t s) {
     using Cfg = typename Line<N>::cfg;
-    static bool attr = false;
     const size_t sm = sizeof(float2) * (N + ADJ_ROW_LINES * Cfg::SMEM);
-    if (!attr) {
-        QS_CUDA_TRY(cudaFuncSetAttribute(adj_rows<N, FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        attr = true;
-    }
+    QS_TRY(smem_attr((const void*)adj_rows<N, FIRST>, sm));
     const long lines = (long)a.nwaves * a.nx;
     adj_rows<N, FIRST><<<(unsigned)(lines / ADJ_ROW_LINES), dim3(Cfg::T, ADJ_ROW_LINES), sm, s>>>(a);
     QS_CUDA_TRY(cudaGetLastError());

@@ -16,6 +16,11 @@ namespace qs {
 void set_error(const std::string& msg);
 // process-wide count of kernels this library launched (for measurement)
 void count_launch(int n);
+// Raise `func`'s dynamic shared-memory limit to `bytes` on the current
+// device (once per device and kernel; a limit is a property of one context).
+int smem_attr(const void* func, size_t bytes);
+// CTAs of `func` resident per SM on the current device, and its SM count.
+int resident_ctas(const void* func, int threads, size_t bytes, int* ctas, int* sms);
 #define QS_CUDA_TRY(expr)                                                               \
     do {                                                                                \
         cudaError_t _e = (expr);                                                        \

@@ -18,6 +18,8 @@
 #include <cmath>
 #include <map>
 #include <mutex>
+#include <tuple>
+#include <utility>
 #include <vector>
 
 #include "qs_fft.cuh"
@@ -254,6 +256,45 @@ __global__ void det_finalize(const double* __restrict__ partial, int nwaves, int
 }
 
 // ------------------------------------------------------------- launchers
+// A kernel's dynamic shared-memory limit belongs to one device's context:
+// set it once per (device, kernel), under a lock (contexts may run on
+// several threads and devices).
+static std::mutex g_attr_mu;
+static std::map<std::pair<int, const void*>, size_t> g_attr;
+static std::map<std::tuple<int, const void*, int, size_t>, std::pair<int, int>> g_occ;
+
+int smem_attr(const void* func, size_t bytes) {
+    int dev = 0;
+    QS_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    size_t& have = g_attr[{dev, func}];
+    if (bytes > have) {
+        QS_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        have = bytes;
+    }
+    return QS_OK;
+}
+
+// CTAs of `func` resident per SM on the current device for `threads` and
+// `bytes` of dynamic shared memory, and the device's SM count (cached).
+int resident_ctas(const void* func, int threads, size_t bytes, int* ctas, int* sms) {
+    int dev = 0;
+    QS_CUDA_TRY(cudaGetDevice(&dev));
+    QS_TRY(smem_attr(func, bytes));
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    auto key = std::make_tuple(dev, func, threads, bytes);
+    auto it = g_occ.find(key);
+    if (it == g_occ.end()) {
+        int r = 0, n = 0;
+        QS_CUDA_TRY(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+        QS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, func, threads, bytes));
+        it = g_occ.emplace(key, std::make_pair(r, n)).first;
+    }
+    *ctas = it->second.first;
+    *sms = it->second.second;
+    return QS_OK;
+}
+
 template <int N>
 static size_t row_smem(int lines = row_lines(N)) {
     return sizeof(float2) * (N + (size_t)lines * Line<N>::cfg::SMEM);
@@ -270,12 +311,8 @@ static size_t col_smem_plain() {
 template <int N, int MODE>
 static int rows_n(const RowArgs& a, cudaStream_t s) {
     using Cfg = typename Line<N>::cfg;
-    static bool attr = false;  // per-process; the attribute is per function
     const size_t sm = row_smem<N>();
-    if (!attr) {
-        QS_CUDA_TRY(cudaFuncSetAttribute(ms_rows<N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        attr = true;
-    }
+    QS_TRY(smem_attr((const void*)ms_rows<N, MODE>, sm));
     const long lines = (long)a.nwaves * a.nx;
     if (lines % row_lines(N)) {
         set_error("row pass: nwaves*nx must be a multiple of " + std::to_string(row_lines(N)));
@@ -316,20 +353,12 @@ int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s) {
 template <int N, bool DET, bool INV>
 static int cols_n3(const ColArgs& a, cudaStream_t s) {
     using Cfg = typename Line<N>::cfg;
-    static int resident = 0;  // CTAs per SM, from the occupancy calculator
-    static int sms = 0;
     const size_t sm = col_smem<N>();
-    if (!resident) {
-        QS_CUDA_TRY(cudaFuncSetAttribute(ms_cols<N, DET, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        int dev = 0;
-        QS_CUDA_TRY(cudaGetDevice(&dev));
-        QS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        QS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, ms_cols<N, DET, INV>,
-                                                                  col_tile<N>() * Cfg::T, sm));
-        if (resident < 1) {
-            set_error("column pass does not fit on an SM");
-            return QS_ERR_UNSUPPORTED;
-        }
+    int resident = 0, sms = 0;  // CTAs per SM (occupancy calculator), SMs
+    QS_TRY(resident_ctas((const void*)ms_cols<N, DET, INV>, col_tile<N>() * Cfg::T, sm, &resident, &sms));
+    if (resident < 1) {
+        set_error("column pass does not fit on an SM");
+        return QS_ERR_UNSUPPORTED;
     }
     dim3 block(col_tile<N>(), Cfg::T);
     const long nitems = (long)a.nwaves * a.ntiles;
@@ -433,12 +462,8 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
 
 template <int N, bool INV>
 static int fft_rows_n(float2* data, long nlines, cudaStream_t s) {
-    static bool attr = false;
     const size_t sm = row_smem<N>(ROW_LINES);
-    if (!attr) {
-        QS_CUDA_TRY(cudaFuncSetAttribute(fft_rows<N, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        attr = true;
-    }
+    QS_TRY(smem_attr((const void*)fft_rows<N, INV>, sm));
     dim3 block(Line<N>::cfg::T, ROW_LINES);
     fft_rows<N, INV><<<(unsigned)((nlines + ROW_LINES - 1) / ROW_LINES), block, sm, s>>>(data, nlines, twiddles(N));
     QS_CUDA_TRY(cudaGetLastError());
@@ -448,12 +473,8 @@ static int fft_rows_n(float2* data, long nlines, cudaStream_t s) {
 
 template <int N, bool INV>
 static int fft_cols_n(float2* data, int ncols, int howmany, cudaStream_t s) {
-    static bool attr = false;
     const size_t sm = col_smem_plain<N>();
-    if (!attr) {
-        QS_CUDA_TRY(cudaFuncSetAttribute(fft_cols<N, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        attr = true;
-    }
+    QS_TRY(smem_attr((const void*)fft_cols<N, INV>, sm));
     constexpr int C = col_tile<N>();
     dim3 block(C, Line<N>::cfg::T);
     dim3 grid((ncols + C - 1) / C, howmany);

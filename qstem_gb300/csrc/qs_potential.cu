@@ -254,6 +254,7 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
         set_error(std::string("qs_lut_build: ") + what + ": " + cudaGetErrorString(e));
         rc = QS_ERR_CUDA;
     };
+    const size_t smx = sizeof(double2) * 2 * (size_t)g.nx, smz = sizeof(double2) * (size_t)g.nz;
     cudaError_t e;
     if ((e = cudaMallocAsync(&d_tab, sizeof(double) * 7 * NSF, s)) != cudaSuccess) { fail(e, "alloc"); return rc; }
     if ((e = cudaMallocAsync(&d_temp, sizeof(float2) * (size_t)g.nx * g.nz, s)) != cudaSuccess) fail(e, "alloc");
@@ -267,9 +268,10 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
                                                               g.zPos, d_temp);
         lut_twiddles<<<(g.nx + 127) / 128, 128, 0, s>>>(g.nx, d_W);
         lut_twiddles<<<(g.nz + 127) / 128, 128, 0, s>>>(g.nz, d_W + g.nx);
-        const size_t smx = sizeof(double2) * 2 * (size_t)g.nx, smz = sizeof(double2) * (size_t)g.nz;
-        if (smx > 48 * 1024) cudaFuncSetAttribute(lut_dft_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
-        if (smz > 48 * 1024) cudaFuncSetAttribute(lut_dft_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+        rc = smem_attr((const void*)lut_dft_x, smx);
+        if (!rc) rc = smem_attr((const void*)lut_dft_z, smz);
+    }
+    if (!rc) {
         lut_dft_x<<<dim3((nxh + 127) / 128, g.nz), 128, smx, s>>>(d_temp, d_W, g.nx, g.nz, d_G);
         lut_dft_z<<<dim3((nxh + 127) / 128, nzh), 128, smz, s>>>(d_G, d_W + g.nx, nxh, g.nz, d_H);
         const double scale = 47.8658 * g.dkx * g.dkz / (g.nz);
@@ -382,12 +384,7 @@ int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* 
     const size_t staged = sizeof(int) * maxRows + sizeof(float) * (size_t)maxRows * Nr * (charged ? 2 : 1);
     const int periodic = p.nonPeriod ? 0 : 1;
     if (staged <= 160 * 1024) {
-        static size_t attr = 0;
-        if (staged > attr) {
-            QS_CUDA_TRY(cudaFuncSetAttribute(scatter_atoms<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)staged));
-            attr = staged;
-        }
+        QS_TRY(smem_attr((const void*)scatter_atoms<true>, staged));
         scatter_atoms<true><<<njobs, 256, staged, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY,
                                                        dr, (float)dr, p.sliceThickness, p.potNx, p.potNy, periodic,
                                                        maxRows, trans);
