@@ -127,14 +127,21 @@ def run_position(p, trans, iPosX, iPosY, wave):
     return w, det[:, :p.detectorNum], dp
 
 
-def run_reference(qsc_path, outdir, run=True):
-    """Run the reference's own CPU path on a .qsc through the harness."""
+def run_reference(qsc_path, outdir, run=True, clock=None):
+    """Run the reference's own CPU path on a .qsc through the harness.
+    clock: the value the reference's time() returns (its thermal
+    displacements and CBED source offsets are seeded with -time(NULL));
+    None leaves the real clock."""
     os.makedirs(outdir, exist_ok=True)
     args = [REF_HARNESS, os.path.basename(qsc_path), os.path.abspath(outdir)]
     if run:
         args.append("run")
+    env = dict(os.environ)
+    env.pop("QS_REF_CLOCK", None)
+    if clock is not None:
+        env["QS_REF_CLOCK"] = str(int(clock))
     r = subprocess.run(args, cwd=os.path.dirname(os.path.abspath(qsc_path)), stdin=subprocess.DEVNULL,
-                       capture_output=True, text=True)
+                       capture_output=True, text=True, env=env)
     if r.returncode != 0:
         raise RuntimeError("reference harness failed: " + r.stdout[-2000:] + r.stderr[-2000:])
     return outdir

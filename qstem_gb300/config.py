@@ -122,13 +122,16 @@ def cell_vectors(ax, by, c, alpha, beta, gamma):
                      [c * cb, c * (ca - cb * cg) / sg, c * (math.sqrt(1 - ca * ca - cb * cb + 2 * ca * cb * cg) / sg)]])
 
 
-def _sorted_fractional(cell):
+def sorted_fractional(cell):
     """The unit cell's atoms as records in fractional coordinates, sorted by
-    (z, y, x) as readUnitCell sorts them (libs/fileio_fftw3.cpp:1497-1500)."""
+    (z, y, x) as readUnitCell sorts them (libs/fileio_fftw3.cpp:1497-1500).
+    readUnitCell stores the file's atoms last to first (:1421) and sorts
+    with the C library's qsort, whose merge sort keeps atoms at equal
+    positions in that stored order."""
     n = len(cell.atoms)
     frac = np.zeros(n, dtype=abi.ATOM_DTYPE)
     for i, (Z, fx, fy, fz, dw, occ, q) in enumerate(cell.atoms):
-        frac[i] = (fz, fy, fx, dw, occ, q, Z)
+        frac[n - 1 - i] = (fz, fy, fx, dw, occ, q, Z)
     order = sorted(range(n), key=lambda i: (frac["z"][i], frac["y"][i], frac["x"][i]))
     return frac[order]
 
@@ -150,7 +153,7 @@ def _mat_vec(M, u0, u1, u2):
     return [(M[i, 0] * u0 + M[i, 1] * u1) + M[i, 2] * u2 for i in range(3)]
 
 
-def supercell(cell, ncx, ncy, ncz, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0)):
+def supercell(cell, ncx, ncy, ncz, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0), replicated=None):
     """readUnitCell's NCELL mode (libs/fileio_fftw3.cpp:1512-1645): the unit
     cell replicated ncx x ncy x ncz times in fractional coordinates (atom
     j = (icz + icy*ncz + icx*ncy*ncz)*ncoord + i), converted to Cartesian by
@@ -158,19 +161,24 @@ def supercell(cell, ncx, ncy, ncz, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0)):
     super-cell, shifted so that the bounding box of the (rotated) super-cell
     starts at 0, then offset by (xOffset, yOffset).  Double arithmetic with
     float32 storage where the reference stores floats.
+    replicated: the replicated fractional atoms in that order, when drawn
+    elsewhere (thermal.Replicator: vacancies and thermal displacements).
     Returns (atoms[ATOM_DTYPE], ax, by, c): the bounding box size, float32."""
-    frac = _sorted_fractional(cell)
-    n = len(frac)
-    out = np.zeros(n * ncx * ncy * ncz, dtype=abi.ATOM_DTYPE)
-    for icx in range(ncx):
-        for icy in range(ncy):
-            for icz in range(ncz):
-                j0 = (icz + icy * ncz + icx * ncy * ncz) * n
-                blk = out[j0:j0 + n]
-                blk[:] = frac
-                blk["x"] = (frac["x"].astype(np.float64) + icx).astype(F32)
-                blk["y"] = (frac["y"].astype(np.float64) + icy).astype(F32)
-                blk["z"] = (frac["z"].astype(np.float64) + icz).astype(F32)
+    if replicated is not None:
+        out = np.array(replicated, dtype=abi.ATOM_DTYPE)
+    else:
+        frac = sorted_fractional(cell)
+        n = len(frac)
+        out = np.zeros(n * ncx * ncy * ncz, dtype=abi.ATOM_DTYPE)
+        for icx in range(ncx):
+            for icy in range(ncy):
+                for icz in range(ncz):
+                    j0 = (icz + icy * ncz + icx * ncy * ncz) * n
+                    blk = out[j0:j0 + n]
+                    blk[:] = frac
+                    blk["x"] = (frac["x"].astype(np.float64) + icx).astype(F32)
+                    blk["y"] = (frac["y"].astype(np.float64) + icy).astype(F32)
+                    blk["z"] = (frac["z"].astype(np.float64) + icz).astype(F32)
     # Cartesian: x_j = sum_k Mm[k][j] * frac_k with Mm's rows the cell vectors
     Mt = cell.H.T
     fx, fy, fz = (out[k].astype(np.float64) for k in ("x", "y", "z"))
@@ -213,7 +221,7 @@ def cube(cell, size, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0), seed=None):
     (numpy.random.default_rng(seed); the reference draws with ran1); the
     first stays when the draw falls past a total occupancy below 1, as in
     the reference.  Returns (atoms[ATOM_DTYPE], ax, by, c) = the box."""
-    frac = _sorted_fractional(cell)
+    frac = sorted_fractional(cell)
     n = len(frac)
     cx, cy, cz = (F32(v) for v in size)
     dx, dy, dz = float(F32(offset[0])), float(F32(offset[1])), 0.0

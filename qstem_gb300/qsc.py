@@ -14,9 +14,15 @@ readFile.  The unit cell is read as readCFGCellParams / readNextCFGAtom
 built as readUnitCell builds it: NCELL replication with crystal tilt, or a
 "Cube:" box cut from the tilted crystal (config.supercell, config.cube).
 
+Thermal displacements (tds) follow the Einstein model or a phonon file
+("phonon-File:"), vacancies the occupancies; their random draws come from
+numpy's generator or, on request, from the reference's own clock-seeded
+generator in the reference's order (qstem_gb300.thermal).
+
 Inputs that need parts of the reference outside this library are refused
-with NotImplementedError: phonon files, the 2-D potential (potential3D: no)
-and modes other than STEM, CBED and TEM.
+with NotImplementedError: the 2-D potential (potential3D: no), stacking
+sequences other than "1 1", a phonon file with a "Cube:" box (the reference
+exits there) and modes other than STEM, CBED and TEM.
 """
 import math
 import os
@@ -254,6 +260,10 @@ class QscRun:
     scan_step: tuple = (1.0, 1.0)               # detector image sampling, from the .qsc's scan range
     save_level: int = 0                         # "save level:"
     beam_tilt: tuple = (0.0, 0.0)               # rad (TEM: a tilted incident plane wave)
+    tilt: tuple = (0.0, 0.0, 0.0)               # crystal tilt, rad
+    offset: tuple = (0.0, 0.0)                  # xOffset, yOffset
+    source_radius: float = 0.0                  # CBED probe source radius (A)
+    replicator: object = None                   # thermal.Replicator drawing the runs' atoms
     tilt_back: bool = True                      # "Tilt back:" (TEM: wave.img tilted back)
     spread: tuple = (0.0, 0.0, 0.0)             # dE/E, dI/I, dV/V as read (CBED/TEM use them as such)
 
@@ -314,10 +324,18 @@ def _energy_spread_series(dE_E0, avg_runs):
     return arr[:avg_runs]
 
 
-def read_qsc(path, seed=20261203):
+def read_qsc(path, seed=20261203, rng="numpy", clock=0):
     """Parse a stem3 .qsc (and the .cfg it names, relative to the .qsc's
-    folder) into a QscRun.  seed: the draw that picks one of several atoms
-    sharing a site in a "Cube:" box (the reference draws with ran1)."""
+    folder) into a QscRun.
+
+    rng "numpy": random draws from numpy.random.default_rng -- the thermal
+    displacements of run j from seed + j (phonons.displaced for the Einstein
+    model, thermal.Replicator for a phonon file), vacancies likewise, the
+    site choice of a "Cube:" box from seed.  rng "reference": the
+    reference's own generator, seeded as the reference seeds it from its
+    clock (time(NULL) = clock), drawing in the reference's order from
+    readFile on (thermal.Replicator), so that runs reproduce a reference run
+    made at that clock (NCELL mode)."""
     pf = ParamFile(path)
     g = pf.get
     unsupported = []
@@ -379,18 +397,43 @@ def read_qsc(path, seed=20261203):
             cube = vals
     ans(g("Adjust cube size with tilt:"))
     tds = _yes(ans(g("tds:")))
-    temperature = _num(g("temperature:"), 300.0)
-    if g("phonon-File:") is not None:
-        unsupported.append("phonon-File")
+    temperature = float(F32(_num(g("temperature:"), 300.0)))
+    here = os.path.dirname(os.path.abspath(path))
+    modes = None
+    pv = g("phonon-File:")
+    if pv is not None and pv.split():
+        # a file that cannot be opened leaves the Einstein model
+        # (libs/fileio_fftw3.cpp:500-504)
+        pfile = os.path.join(here, pv.split()[0])
+        if os.path.isfile(pfile):
+            from . import thermal
+            modes = thermal.read_phonon_file(pfile)
+    if rng not in ("numpy", "reference"):
+        raise ValueError("rng must be 'numpy' or 'reference'")
     # the unit cell (readUnitCell: .cfg read, replicated, then shifted)
-    cfg_path = os.path.join(os.path.dirname(os.path.abspath(path)), cfg)
-    cell = read_cell(cfg_path)
+    cell = read_cell(os.path.join(here, cfg))
     xoff = _num(g("xOffset:"), 0.0)
     yoff = _num(g("yOffset:"), 0.0)
+    replicator = None
     if cube is not None:  # a box cut from the tilted crystal (tiltBoxed)
+        if tds and modes is not None:
+            unsupported.append("phonon-File with Cube")  # tiltBoxed exits (libs/fileio_fftw3.cpp:1893-1896)
+        random_cell = tds or any(a[5] < 1 for a in cell.atoms) or len(
+            {(a[1], a[2], a[3]) for a in cell.atoms}) < len(cell.atoms)
+        if rng == "reference" and random_cell:
+            unsupported.append("the reference generator's draws in a Cube box")
         atoms, ax, by, c = config.cube(cell, cube, tuple(tilt), (xoff, yoff), seed=seed)
     else:  # NCELL mode
-        atoms, ax, by, c = config.supercell(cell, ncx, ncy, ncz, tuple(tilt), (xoff, yoff))
+        if rng == "reference" or (tds and modes is not None):
+            from . import thermal
+            replicator = thermal.Replicator(config.sorted_fractional(cell), (ncx, ncy, ncz), cell.H,
+                                            (cell.a, cell.b, cell.c), tds, temperature, modes=modes, rng=rng,
+                                            seed=seed, clock=clock)
+            if not unsupported:  # readFile's own configuration
+                atoms, ax, by, c = config.supercell(cell, ncx, ncy, ncz, tuple(tilt), (xoff, yoff),
+                                                    replicated=replicator.configuration(0))
+        if replicator is None or unsupported:
+            atoms, ax, by, c = config.supercell(cell, ncx, ncy, ncz, tuple(tilt), (xoff, yoff))
     nx = int(_num(g("nx:"), 0))
     ny_v = g("ny:")
     ny = int(_num(ny_v, nx)) if ny_v is not None else nx
@@ -480,6 +523,8 @@ def read_qsc(path, seed=20261203):
     aAIS = _num(g("AIS aperture:"), 0.0)
     beam = _num(g("beam current:"), 1.0)
     dwell = _num(g("dwell time:"), 1.0)
+    # doCBED's probe source: offsets of radius * normal draw * sqrt 2 per run
+    source_radius = float(F32(_num(g("Source Size (diameter):"), 0.0) / 2.0))
     ans(g("smooth:"))
     smooth = answer[0][:1].lower() == "y"
     gv = g("gaussian:")
@@ -541,7 +586,8 @@ def read_qsc(path, seed=20261203):
     return QscRun(params=p, atoms=atoms, cell=cell, ncell=(ncx, ncy, ncz), mode=mode, tds=tds,
                   temperature=temperature, avg_runs=avg_runs, folder=folder, detector_names=names, dE_E=series,
                   scan_step=scan_step, save_level=save_level, spread=(dE_E, dI_I, dV_V),
-                  beam_tilt=tuple(beam_tilt), tilt_back=tilt_back)
+                  beam_tilt=tuple(beam_tilt), tilt_back=tilt_back, tilt=tuple(tilt), offset=(xoff, yoff),
+                  source_radius=source_radius, replicator=replicator)
 
 
 def _isnum(t):
@@ -588,6 +634,14 @@ def _stacks(ctx, p, atoms):
 
 
 def _run_atoms(run, j, seed):
+    """The atoms of run j: readFile's for run 0, redrawn for later runs
+    (make3DSlices re-reads the cell, stem3/stemlib.cpp:465-485)."""
+    if run.replicator is not None:
+        if j == 0:
+            return run.atoms
+        atoms, _, _, _ = config.supercell(run.cell, *run.ncell, run.tilt, run.offset,
+                                          replicated=run.replicator.configuration(j))
+        return atoms
     atoms = run.atoms
     if run.tds:
         from . import phonons
@@ -605,7 +659,7 @@ def _kspace_pattern(wave, scale):
     return np.roll(I.astype(np.float32), (w.shape[0] // 2, w.shape[1] // 2), axis=(0, 1))
 
 
-def run_qsc(path, ctx=None, folder=None, seed=20261203, chunk=256):
+def run_qsc(path, ctx=None, folder=None, seed=20261203, chunk=256, rng="numpy", clock=0):
     """Run a stem3 input through the library and write what stem3 writes to
     its output folder.
 
@@ -616,6 +670,8 @@ def run_qsc(path, ctx=None, folder=None, seed=20261203, chunk=256):
     runMulsSTEM's collectIntensity / interimWave (stem3/stemlib.cpp:
     2538-2749); the writers below say which file comes from where.
 
+    rng, clock: the generator of the runs' random draws (read_qsc); with
+    "reference" a run reproduces the reference's run at that clock.
     folder: where to write (default the .qsc's "Folder:", relative to it;
     None writes nothing when the .qsc names none).  chunk: positions per
     multislice call when per-position files are written (bounds host memory).
@@ -623,7 +679,7 @@ def run_qsc(path, ctx=None, folder=None, seed=20261203, chunk=256):
     CBED: {"diffpat": mean final pattern, "series": mean slot patterns};
     TEM: {"exit_intensity": mean |psi_exit|^2, "exit_wave": run 0's})."""
     from . import lib
-    run = read_qsc(path)
+    run = read_qsc(path, seed=seed, rng=rng, clock=clock)
     where = folder if folder is not None else (
         os.path.join(os.path.dirname(os.path.abspath(path)), run.folder) if run.folder else None)
     if where:
@@ -774,14 +830,30 @@ def _run_cbed(ctx, run, where, seed):
     rk = (1.0 / float(F32(nx * F32(p.resolutionX))), 1.0 / float(F32(ny * F32(p.resolutionY))))
     scale = 1.0 / math.sqrt(float(nx * ny))
     # doCBED's probe position (stem3/stem3.cpp:2096-2100)
-    probe = ctx.probe(p, float(F32(F32(p.scanXStart) - F32(p.potOffsetX))),
-                      float(F32(F32(p.scanYStart) - F32(p.potOffsetY))))
+    probes = {}
+
+    def probe_at(off):
+        """doCBED's probe at the scan start moved by the run's source
+        offset (stem3/stem3.cpp:2096-2100), all positions floats."""
+        if off not in probes:
+            sx = F32(float(F32(p.scanXStart)) + off[0])
+            sy = F32(float(F32(p.scanYStart)) + off[1])
+            probes[off] = ctx.probe(p, float(F32(sx - F32(p.potOffsetX))), float(F32(sy - F32(p.potOffsetY))))
+        return probes[off]
     pos = tuple(np.zeros(1, np.int32) for _ in range(4))
     inv_lambda = 1.0 / config.wavelength(float(p.v0))
     series_avg = [None] * nT
     avg = None
     chisq = []
+    rep = run.replicator
     for j in range(run.avg_runs):
+        off = (0.0, 0.0)
+        if rep is not None and rep.rng == "reference":
+            off = rep.source_offset(j, run.source_radius)  # drawn at radius 0 too: it moves the generator on
+        elif run.source_radius > 0:
+            from . import thermal
+            off = thermal.source_offset(seed, j, run.source_radius)
+        probe = probe_at(off)
         atoms = _run_atoms(run, j, seed)
         T, slabs = _stacks(ctx, p, atoms)
         _, dps, ews = ctx.multislice(p, T, probe, positions=pos, want_det=False, want_diffpats=True,

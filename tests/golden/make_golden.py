@@ -242,6 +242,59 @@ def qsc_geometry_case(name, qsc_file, cfg_file):
 GEOMETRY_CASES = {"qsctilt": ("tilt.qsc", "hex.cfg"), "qsccube": ("cube.qsc", "cell.cfg"),
                   "qscdat": ("dat.qsc", "cell.dat"), "qsccssr": ("cssr.qsc", "cell.cssr")}
 
+
+def phonon_modes_fixture():
+    """The phonon file of tests/golden/qsc/phonon.qsc: a 2-atom cell (Al, N
+    masses) at 4 k-points, seeded eigenvectors (unit length per mode), the
+    three modes at k = 0 acoustic (omega 0)."""
+    from qstem_gb300 import thermal
+    rng = np.random.default_rng(20261203 + 400)
+    Nk, Ns = 4, 2
+    m = 3 * Ns
+    kv = np.array([[0, 0, 0], [0.5, 0, 0], [0, 0.25, 0.5], [0.25, 0.25, 0.25]], np.float32)
+    om = rng.uniform(3.0, 30.0, (Nk, m)).astype(np.float32)
+    om[0, :3] = 0.0
+    e = rng.standard_normal((Nk, m, m, 2))
+    e /= np.sqrt((e ** 2).sum(axis=(2, 3), keepdims=True))
+    return thermal.PhononModes(np.array([26.98, 14.007], np.float32), kv, om, e.astype(np.float32))
+
+
+# readFile and doSTEM with thermal displacements at a fixed reference clock
+# (the reference seeds them with time(NULL)): qsc file, its other inputs
+THERMAL_CLOCK = 1764000000
+THERMAL_CASES = {"qsctds": ("tds.qsc", ["vac.cfg"]), "qscphonon": ("phonon.qsc", ["ph.cfg", "modes.phonon"])}
+
+
+def qsc_thermal_case(name, qsc_file, others):
+    """readFile's atoms (thermal displacements and vacancies of the first
+    run), doSTEM's detector images (those of the last run: collectIntensity
+    overwrites them, Navg being 0) and its per-position patterns averaged
+    over the runs (diffAvg_<ix>_<iy>.img), with the reference's clock fixed."""
+    from qstem_gb300 import thermal
+    src = os.path.join(HERE, "qsc")
+    if "modes.phonon" in others:
+        thermal.write_phonon_file(os.path.join(src, "modes.phonon"), phonon_modes_fixture())
+    work = tempfile.mkdtemp(prefix="qs_golden_")
+    try:
+        for f in [qsc_file] + others:
+            shutil.copy(os.path.join(src, f), work)
+        dump = os.path.join(work, "dump")
+        oracle.run_reference(os.path.join(work, qsc_file), dump, run=True, clock=THERMAL_CLOCK)
+        meta = dict(l.split(" = ", 1) for l in open(os.path.join(dump, "meta.txt")).read().strip().split("\n"))
+        out = {"atoms": np.fromfile(os.path.join(dump, "atoms.bin"), dtype=abi.ATOM_DTYPE),
+               "meta_json": np.array(json.dumps(meta)), "clock": np.array(THERMAL_CLOCK)}
+        nt = (int(meta["slices"]) * int(meta["cellDiv"])) // int(meta["outputInterval"]) + 1
+        nd, sx, sy = int(meta["detectorNum"]), int(meta["scanXN"]), int(meta["scanYN"])
+        out["det"] = np.stack([np.stack([np.fromfile(os.path.join(dump, "det_%d_%d.bin" % (t, i)), np.float32)
+                                         .reshape(sx, sy) for i in range(nd)]) for t in range(nt)])
+        out["diffavg"] = np.stack([np.stack([imageio.read_img(os.path.join(work, "out", "diffAvg_%d_%d.img" % (ix, iy)))
+                                             .data.astype(np.float32) for iy in range(sy)]) for ix in range(sx)])
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes", len(out["atoms"]), "atoms")
+
 # whole stem3 runs whose output folders pin qstem_gb300.qsc.run_qsc: every
 # .img file the reference wrote (name, header, data)
 RUN_CASES = {
@@ -263,6 +316,12 @@ RUN_CASES = {
                        scan=None, detectors=[], alpha=0.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
                        outputInterval=2, mode="TEM", saveLevel=0,
                        extra=["Beam tilt X: 0.004", "Beam tilt Y: 0.2 deg", "Tilt back: yes"]),
+    # CBED from a probe source of finite size: doCBED's source offset, drawn
+    # with the reference's clock-seeded generator (fixed here)
+    "qsccbedsrc": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=5,
+                       sliceThickness=2.0, scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0,
+                       bandlimit=True, outputInterval=2, mode="CBED", saveLevel=1,
+                       extra=["Source Size (diameter): 0.9"], clock=1764000000),
     # CBED through two unequal slabs (NCELLZ: 3/2): every slab's stack
     "qsccbedd2u": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=3,
                        sliceThickness=2.0, scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0,
@@ -298,9 +357,11 @@ def qsc_run_case(name, case):
         if case.get("extra"):
             with open(qsc, "a") as f:
                 f.write("\n".join(case["extra"]) + "\n")
-        oracle.run_reference(qsc, os.path.join(work, "dump"), run=True)
+        oracle.run_reference(qsc, os.path.join(work, "dump"), run=True, clock=case.get("clock"))
         out = {"qsc_text": np.array(open(qsc).read()),
                "cfg_text": np.array(open(os.path.join(work, "cell.cfg")).read())}
+        if case.get("clock") is not None:
+            out["clock"] = np.array(case["clock"])
         heads = {}
         for f in sorted(os.listdir(os.path.join(work, "out"))):
             if not f.endswith(".img"):
@@ -327,6 +388,9 @@ def main(names=None):
     for name, (q, c) in GEOMETRY_CASES.items():
         if not names or name in names:
             qsc_geometry_case(name, q, c)
+    for name, (q, others) in THERMAL_CASES.items():
+        if not names or name in names:
+            qsc_thermal_case(name, q, others)
     for name, case in CASES.items():
         if names and name not in names:
             continue

@@ -52,7 +52,8 @@ def test_stem3_input_end_to_end():
 EXTRA = {"qsctem": {"waveIntensity.img"}, "qsctemtilt": {"waveIntensity.img"}, "qsctemd2": {"waveIntensity.img"}}
 
 
-@pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsccbedd2u", "qsctem", "qsctemtilt", "qsctemd2", "qscstem"])
+@pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsccbedsrc", "qsccbedd2u", "qsctem", "qsctemtilt",
+                                  "qsctemd2", "qscstem"])
 def test_output_folder_matches_the_references(name):
     """The whole output folder of a stem3 run: CBED thickness series
     (diff_<t>.img) at save level 1 and 3 (real-space overwrite, interimWave,
@@ -65,7 +66,10 @@ def test_output_folder_matches_the_references(name):
     for fn, key in (("run.qsc", "qsc_text"), ("cell.cfg", "cfg_text")):
         with open(os.path.join(d, fn), "w") as f:
             f.write(str(z[key]))
-    qsc.run_qsc(os.path.join(d, "run.qsc"), folder=os.path.join(d, "out"))
+    # a case made at a fixed reference clock (CBED source offsets) runs with
+    # the reference's generator
+    kw = {"rng": "reference", "clock": int(z["clock"])} if "clock" in z.files else {}
+    qsc.run_qsc(os.path.join(d, "run.qsc"), folder=os.path.join(d, "out"), **kw)
     heads = json.loads(str(z["img_headers_json"]))
     written = set(os.listdir(os.path.join(d, "out")))
     assert written == set(heads) | EXTRA.get(name, set())

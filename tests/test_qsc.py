@@ -93,7 +93,7 @@ def test_fixture_inputs_read_back(name):
 def test_refused_inputs():
     z = np.load(os.path.join(GOLDEN, "qscread.npz"))
     base = str(z["qsc_text"])
-    for extra in ("phonon-File: modes.dat", "potential3D: no", "mode: NBED", "sequence: 1 3"):
+    for extra in ("potential3D: no", "mode: NBED", "sequence: 1 3"):
         text = base.replace("print level: 1", extra + "\nprint level: 1")
         if extra.startswith("potential3D"):
             text = base.replace("potential3D: yes", extra)

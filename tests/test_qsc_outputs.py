@@ -41,10 +41,13 @@ def _read(folder, fn):
     return im, (np.stack([d.real, d.imag], -1) if np.iscomplexobj(d) else d)
 
 
-@pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsccbedd2u", "qsctem", "qsctemtilt", "qsctemd2", "qscstem"])
+@pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsccbedsrc", "qsccbedd2u", "qsctem", "qsctemtilt",
+                                  "qsctemd2", "qscstem"])
 def test_output_folder_as_the_reference_writes_it(tmp_path, name):
     z, path, out = _inputs(tmp_path, name)
-    qsc.run_qsc(path, ctx=OracleContext(), folder=out)
+    # a case made at a fixed reference clock runs with the reference's generator
+    kw = {"rng": "reference", "clock": int(z["clock"])} if "clock" in z.files else {}
+    qsc.run_qsc(path, ctx=OracleContext(), folder=out, **kw)
     heads = json.loads(str(z["img_headers_json"]))
     assert set(os.listdir(out)) == set(heads) | EXTRA.get(name, set())
     for fn, (t, dx, dy, comment, params) in heads.items():
