@@ -56,7 +56,7 @@
 extern "C" {
 #endif
 
-#define QS_ABI_VERSION 2
+#define QS_ABI_VERSION 3
 
 /* status codes */
 #define QS_OK 0
@@ -142,6 +142,13 @@ typedef struct qs_params {
     /* readFile's equalDivs (stem3/stem3.cpp:930-931): with cellDiv > 1, every
      * slab has the potential of slab 0, built once and reused */
     int equalDivs;
+    /* The stacking sequence "sequence: m1 m2" (stem3/stem3.cpp:2761-2790,
+     * stem3/stemlib.cpp:2403-2429): the wave passes m2 times through the
+     * cellDiv slabs, and through each slab's stack m1 times in a row.  The
+     * thickness slot of a step is collectIntensity's t of the index
+     * totalSliceCount + islice*(1 + repeat) the reference passes it.
+     * 0 reads as 1. */
+    int mulsRepeat1, mulsRepeat2;
 } qs_params;
 
 /* A batch of probe positions for qs_multislice_run.  Position p uses the

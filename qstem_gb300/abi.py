@@ -64,7 +64,8 @@ class QsParams(ctypes.Structure):
                  ("scanYStart", ctypes.c_float), ("scanYStop", ctypes.c_float),
                  ("scanXN", ctypes.c_int), ("scanYN", ctypes.c_int),
                  ("electronScale", ctypes.c_float), ("detectorNum", ctypes.c_int),
-                 ("detectors", QsDetector * QS_MAX_DETECTORS), ("equalDivs", ctypes.c_int)])
+                 ("detectors", QsDetector * QS_MAX_DETECTORS), ("equalDivs", ctypes.c_int),
+                 ("mulsRepeat1", ctypes.c_int), ("mulsRepeat2", ctypes.c_int)])
 
     def copy(self):
         out = QsParams()

@@ -318,6 +318,7 @@ def make_params(*, mode=abi.QS_MODE_STEM, nx, ny=None, resolutionX, resolutionY=
     p.equalDivs = int((not tds) and ncz % p.cellDiv == 0 and
                       abs(float(F32(F32(p.slices) * F32(sliceThickness)) - F32(F32(c) / F32(p.cellDiv)))) < 1e-5)
     p.outputInterval = p.slices if (outputInterval is None or outputInterval < 1) else outputInterval
+    p.mulsRepeat1 = p.mulsRepeat2 = 1  # "sequence: 1 1"
     p.czOffset = F32(czOffset)
     p.ax, p.by, p.c = F32(ax), F32(by), F32(c)
     p.nonPeriod = 0 if periodicXY else 1
@@ -411,8 +412,10 @@ def scan_offsets(p):
 def write_qsc(path, *, cfg_file, ncell, nx, resolutionX, v0, slices, sliceThickness, scan=None,
               detectors=(), alpha=20.0, Cs_mm=0.0, C5_mm=0.0, defocus_nm=0.0, outputInterval=None,
               mode="STEM", bandlimit=False, periodicXY=False, periodicZ=False, folder="out",
-              saveLevel=0, smooth=True, czOffset=0.0, atomRadius=5.0, centerSlices=False, cellDiv=1):
-    """A stem3 input file for the same run make_params describes."""
+              saveLevel=0, smooth=True, czOffset=0.0, atomRadius=5.0, centerSlices=False, cellDiv=1,
+              sequence=(1, 1)):
+    """A stem3 input file for the same run make_params describes
+    (sequence: the stacking sequence m1 m2)."""
     yn = lambda b: "yes" if b else "no"
     L = ["mode: %s" % mode, "print level: 1", "save level: %d" % saveLevel,
          "filename: %s" % cfg_file, "resolutionX: %r" % float(resolutionX),
@@ -442,6 +445,6 @@ def write_qsc(path, *, cfg_file, ncell, nx, resolutionX, v0, slices, sliceThickn
           "gaussian: no", "potential3D: yes", "atom radius: %r" % float(atomRadius),
           "bandlimit f_trans: %s" % yn(bandlimit), "one time integration: yes",
           'Folder: "%s"' % folder, "Runs for averaging: 1", "Structure Factors: WK",
-          "sequence: 1 1"]
+          "sequence: %d %d" % tuple(sequence)]
     with open(path, "w") as f:
         f.write("\n".join(L) + "\n")

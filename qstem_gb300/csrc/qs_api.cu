@@ -95,6 +95,10 @@ static int ensure(qs_ctx* c, int which, size_t bytes, void** out) {
     return QS_OK;
 }
 
+// A stacking sequence other than "1 1" (qs_multislice_run, qs_stem_run and
+// qs_tem_run walk it; the other entry points do not).
+static bool repeats(const qs_params& p) { return p.mulsRepeat1 > 1 || p.mulsRepeat2 > 1; }
+
 static int check_params(const qs_params* p) {
     if (!p) { set_error("params is NULL"); return QS_ERR_ARG; }
     if (p->nx < 1 || p->ny < 1 || p->slices < 1 || p->potNx < p->nx || p->potNy < p->ny) {
@@ -106,6 +110,7 @@ static int check_params(const qs_params* p) {
         return QS_ERR_ARG;
     }
     if (p->cellDiv < 1) { set_error("cellDiv must be >= 1"); return QS_ERR_ARG; }
+    if (p->mulsRepeat1 < 0 || p->mulsRepeat2 < 0) { set_error("mulsRepeat1/2 must be >= 0"); return QS_ERR_ARG; }
     if (p->outputInterval < 1) { set_error("outputInterval must be >= 1"); return QS_ERR_ARG; }
     if (p->detectorNum < 0 || p->detectorNum > QS_MAX_DETECTORS) { set_error("detectorNum out of range"); return QS_ERR_ARG; }
     return QS_OK;
@@ -697,16 +702,30 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     }
     const int ntiles = (int)tiles.size();
 
-    // absolute slices: cellDiv slabs of S slices (doSTEM's slab loop,
-    // stem3/stem3.cpp:2795-2949, with runMulsSTEM's absolute_slice =
-    // totalSliceCount + islice, stem3/stemlib.cpp:2405)
+    // the steps of the wave: mulsRepeat2 passes through the cellDiv slabs
+    // (doSTEM's slab loop, stem3/stem3.cpp:2795-2949), each slab's S
+    // slices mulsRepeat1 times (runMulsSTEM's repeat loop,
+    // stem3/stemlib.cpp:2403-2405); step a transmits stack slice
+    // stepSlice[a] and hands collectIntensity the index
+    // totalSliceCount + islice*(1 + repeat) (:2429)
     const int D = P.cellDiv, SA = S * D;
     const bool slabStacks = D > 1 && (flags & QS_SLAB_STACKS);
-    // output slices: slice a writes thickness slot tOf[a] (collectIntensity's
-    // t, stem3/stemlib.cpp:2597-2610); a slot keeps its last writer only
-    std::vector<int> lastWriter(nT, -1), slotOf(SA, -1);
-    for (int a = 0; a < SA; a++) {
-        const int t = (a < SA - 1) ? a / P.outputInterval : nT - 1;
+    std::vector<int> stepSlice, stepIndex;
+    const int R1 = std::max(1, P.mulsRepeat1), R2 = std::max(1, P.mulsRepeat2);
+    for (int pc = 0; pc < R2 * D; pc++)
+        for (int r = 0; r < R1; r++)
+            for (int i = 0; i < S; i++) {
+                stepSlice.push_back((slabStacks ? (pc % D) * S : 0) + i);
+                stepIndex.push_back(pc * S + i * (1 + r));
+            }
+    const int NS = (int)stepSlice.size();
+    // output steps: step a writes thickness slot t of its index
+    // (collectIntensity's t, stem3/stemlib.cpp:2597-2610); a slot keeps its
+    // last writer only
+    std::vector<int> lastWriter(nT, -1), slotOf(NS, -1);
+    for (int a = 0; a < NS; a++) {
+        const int x = stepIndex[a];
+        const int t = (x < SA - 1) ? x / P.outputInterval : nT - 1;
         if (t < nT) lastWriter[t] = a;
     }
     for (int t = 0; t < nT; t++) if (lastWriter[t] >= 0) slotOf[lastWriter[t]] = t;
@@ -857,8 +876,8 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
             }
             return QS_OK;
         };
-        // stack slice of absolute slice a
-        auto sliceOf = [&](int a) { return transChunk + (size_t)(slabStacks ? a : a % S) * P.potNx * P.potNy; };
+        // stack slice of step a
+        auto sliceOf = [&](int a) { return transChunk + (size_t)stepSlice[a] * P.potNx * P.potNy; };
         // the chunk's stream work: the slice loop and the detector sums
         auto work = [&]() -> int {
         if (dpOut)
@@ -866,22 +885,22 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
                 QS_CUDA_TRY(cudaMemsetAsync(dpOut + k * slotStride, 0, sizeof(float) * N * nb, s));
         ra.trans_slice = sliceOf(0);
         QS_TRY(rows(ROW_FIRST));
-        for (int a = 0; a < SA; a++) {
+        for (int a = 0; a < NS; a++) {
             const int slot = slotOf[a];
             ca.ndet = (wantDet && slot >= 0) ? ndet : 0;
             ca.partial = (double*)dpart + (slot >= 0 ? (size_t)slot * partPerT : 0);
             if (series)
                 ca.diffpat = (dpOut && slot >= 0) ? dpOut + (size_t)slot * slotStride : nullptr;
             else
-                ca.diffpat = (a == SA - 1) ? dpOut : nullptr;
-            ca.inverse = (a < SA - 1 || ewOut) ? 1 : 0;
+                ca.diffpat = (a == NS - 1) ? dpOut : nullptr;
+            ca.inverse = (a < NS - 1 || ewOut) ? 1 : 0;
             QS_TRY(cols());
-            if (series && ewOut && slot >= 0 && a < SA - 1) {
-                // the real-space wave after slice a, before the next transmit
+            if (series && ewOut && slot >= 0 && a < NS - 1) {
+                // the real-space wave after step a, before the next transmit
                 ra.exit_waves = ewOut + (size_t)slot * slotStride;
                 QS_TRY(launch_rows(ra, ROW_LAST, s));
             }
-            if (a < SA - 1) {
+            if (a < NS - 1) {
                 ra.trans_slice = sliceOf(a + 1);
                 QS_TRY(rows(ROW_MID));
             }
@@ -1018,6 +1037,10 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
         if (P.potNx != P.nx || P.potNy != P.ny) {
             set_error("job " + std::to_string(i) + ": CBED needs the potential grid equal to the wave grid");
             return QS_ERR_ARG;
+        }
+        if (repeats(P)) {
+            set_error("job " + std::to_string(i) + ": the CBED batch walks the sequence 1 1 only");
+            return QS_ERR_UNSUPPORTED;
         }
         if (!line_supported(P.nx) || !line_supported(P.ny)) {
             set_error("job " + std::to_string(i) + ": nx, ny must be in {64,128,256,384,512,768,1024}");
@@ -1387,6 +1410,10 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     if (!c || !trans_in || !probe_in || !batch || !target || !dL_dV) { set_error("null argument"); return QS_ERR_ARG; }
     QS_TRY(check_params(p));
     const qs_params& P = *p;
+    if (repeats(P)) {
+        set_error("adjoint: the stacking sequence 1 1 only");
+        return QS_ERR_UNSUPPORTED;
+    }
     if (!line_supported(P.nx) || !line_supported(P.ny)) {
         set_error("adjoint: nx, ny must be in {64,128,256,384,512,768,1024}");
         return QS_ERR_UNSUPPORTED;

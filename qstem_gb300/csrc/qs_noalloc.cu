@@ -111,7 +111,8 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
     }
     const qs_params& P = *p;
     if (P.nx < 1 || P.ny < 1 || P.slices < 1 || P.potNx < P.nx || P.potNy < P.ny || P.outputInterval < 1 ||
-        P.cellDiv != 1 || P.detectorNum < 0 || P.detectorNum > QS_MAX_DETECTORS) {
+        P.cellDiv != 1 || P.mulsRepeat1 > 1 || P.mulsRepeat2 > 1 || P.detectorNum < 0 ||
+        P.detectorNum > QS_MAX_DETECTORS) {
         set_error(std::string(fn) + "inconsistent parameters");
         return QS_ERR_ARG;
     }

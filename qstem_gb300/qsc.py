@@ -545,20 +545,29 @@ def read_qsc(path, seed=20261203, rng="numpy", clock=0):
         names.append(t[2])
     pf.pos = 0
     atomRadius = _num(g("atom radius:"), 5.0)
-    # stacking sequences (doSTEM/doTEM/doCBED's "sequence: m1 m2" loop,
-    # stem3/stem3.cpp:2761-2790): m1 repeats the stack inside runMulsSTEM,
-    # m2 the slab loop, each line restarts it.  Only the plain "1 1" is
-    # supported.  (Without any sequence line the reference runs no scan at
-    # all; this reader runs the one pass.)
+    # the stacking sequence (doSTEM/doTEM/doCBED's "sequence: m1 m2" loop,
+    # stem3/stem3.cpp:2761-2790): m1 repeats each slab's stack inside
+    # runMulsSTEM, m2 the slab loop (m2 < 1 reads as 1).  One line is
+    # supported (each further line restarts the scan; without any line the
+    # reference runs no scan at all, this reader runs the one pass).
     seqs = pf.all("sequence: ")
+    m1, m2 = 1, 1
     if len(seqs) > 1:
         unsupported.append("%d stacking-sequence lines" % len(seqs))
     elif seqs:
         tok = seqs[0].split()
         if tok and tok[0][:1].isalnum():
-            m = [int(float(t)) if _isnum(t) else 0 for t in tok[:2]] + [1, 1]
-            if m[0] != 1 or max(m[1], 1) != 1:
-                unsupported.append("sequence: %s" % seqs[0].strip())
+            m = [int(float(t)) if _isnum(t) else 1 for t in tok[:2]] + [1, 1]
+            m1, m2 = m[0], max(m[1], 1)
+            if m1 < 1:
+                unsupported.append("sequence: %s (no slices)" % seqs[0].strip())
+    if mode == "STEM" and cube is not None:
+        m2 = 1  # doSTEM ignores m2 with a Cube box (stem3/stem3.cpp:2788-2791)
+    if mode == "STEM" and m2 * cellDiv > 1 and not (save_level > 1 or cellDiv > 1):
+        # doSTEM continues every pass from mulswav_<ix>_<iy>.img, which
+        # runMulsSTEM writes only at save level > 1 or with slabs
+        unsupported.append("sequence: %d %d at save level %d (the reference reads wave files it did not "
+                           "write)" % (m1, m2, save_level))
     if unsupported:
         raise NotImplementedError("%s: not supported by this library: %s" % (path, ", ".join(unsupported)))
 
@@ -577,6 +586,7 @@ def read_qsc(path, seed=20261203, rng="numpy", clock=0):
                            centerSlices=centerSlices, periodicXY=periodicXY, periodicZ=periodicZ,
                            bandlimit=bandlimit, atomRadius=atomRadius, smooth=smooth, gaussian=gaussian, aAIS=aAIS,
                            beamCurrent=beam, dwellTime=dwell, tds=tds, cellDiv=cellDiv, nCellZ=ncz)
+    p.mulsRepeat1, p.mulsRepeat2 = m1, m2
     if df is not None and df_w[:1].lower() == "o":  # "optimum" defocus, stem3/stem3.cpp:1160-1163
         p.df0 = F32(-float(F32(math.sqrt(float(p.Cs) * config.wavelength(float(p.v0))))))
     for k, v in aberr.items():
@@ -619,6 +629,84 @@ def _interim_files(SA, oi):
         if a == SA - 1 or (a + 1) % oi == 0:
             files[a // oi] = a
     return files
+
+
+def _steps(p):
+    """The wave's steps through the stacking sequence: mulsRepeat2 passes
+    through the cellDiv slabs (the slab loop of doSTEM/doCBED/doTEM,
+    stem3/stem3.cpp:2795-2949), each slab's stack mulsRepeat1 times
+    (runMulsSTEM, stem3/stemlib.cpp:2403-2486).  Per step: (slab, slice,
+    collectIntensity's index totalSliceCount + islice*(1 + repeat),
+    interimWave's index absolute_slice*(1 + repeat), absolute_slice =
+    totalSliceCount + islice)."""
+    S, D = p.slices, p.cellDiv
+    out = []
+    for pc in range(max(1, p.mulsRepeat2) * D):
+        for r in range(max(1, p.mulsRepeat1)):
+            for i in range(S):
+                tsc = pc * S
+                out.append((pc % D, i, tsc + i * (1 + r), (tsc + i) * (1 + r), tsc + i))
+    return out
+
+
+def _slot(x, SA, oi, nT):
+    """collectIntensity's thickness slot of index x (stem3/stemlib.cpp:2597-2610)."""
+    return x // oi if x < SA - 1 else nT - 1
+
+
+def _repeats(p):
+    return max(1, p.mulsRepeat1) > 1 or max(1, p.mulsRepeat2) > 1
+
+
+# run CBED/TEM through _chain even without repeats (tests compare both paths)
+_ALWAYS_CHAIN = False
+
+
+def _chain(ctx, p, T, slabs, wave0, stops):
+    """The wave after chosen steps: one multislice call per stretch of steps
+    (their stack slices gathered into one stack), each starting from the
+    previous stretch's exit wave.  Returns {step: (k-space pattern after the
+    step, real-space wave after it)}."""
+    steps = _steps(p)
+    S = p.slices
+    pos = tuple(np.zeros(1, np.int32) for _ in range(4))
+    out, w, a0 = {}, wave0, 0
+    for stop in sorted(set(stops)):
+        seg = steps[a0:stop + 1]
+        stack = np.ascontiguousarray(T[[(st[0] * S if slabs else 0) + st[1] for st in seg]])
+        q = p.copy()
+        q.slices = q.outputInterval = len(seg)
+        q.cellDiv, q.equalDivs, q.mulsRepeat1, q.mulsRepeat2 = 1, 0, 1, 1
+        _, dps, ews = ctx.multislice(q, stack, w, positions=pos, want_det=False, want_diffpats=True,
+                                     want_exit_waves=True)
+        out[stop] = (dps[0], ews[0])
+        w, a0 = ews[0], stop + 1
+    return out
+
+
+def _wave_events(p, real_space, sl_diff):
+    """What runMulsSTEM writes step by step, reduced to each file's last
+    write: {("diff", t): (kind, step, thickness in slices)} for
+    collectIntensity's CBED patterns (sl_diff; kind "k" the k-space pattern,
+    written with the thickness before the step, "r" the real-space intensity
+    of the second collectIntensity), {("wave", f): (step, thickness)} for
+    interimWave (real_space: TEM, CBED at save level > 1;
+    stem3/stemlib.cpp:2429, 2475-2482, 2538-2565)."""
+    steps = _steps(p)
+    SA = p.slices * p.cellDiv
+    oi, nT = p.outputInterval, p.thickness_count()
+    last = {}
+    before = None  # thickness before the step: the previous step's
+    for a, (_, _, s1, s2, ab) in enumerate(steps):
+        if sl_diff:
+            last[("diff", _slot(s1, SA, oi, nT))] = ("k", a, before)
+        if real_space:
+            if s2 >= SA - 1 or (s2 + 1) % oi == 0:
+                last[("wave", s2 // oi)] = (a, ab + 1)
+            if sl_diff:
+                last[("diff", _slot(s2, SA, oi, nT))] = ("r", a, ab + 1)
+        before = ab + 1
+    return last, len(steps)
 
 
 def _thick(n, dz):
@@ -721,7 +809,7 @@ def _run_stem(ctx, run, where, seed, chunk):
     acc = np.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), np.float64)
     offs = config.scan_offsets(p)
     npos = len(offs[0])
-    t_end = _thick(SA, p.sliceThickness)
+    t_end = _thick(SA * max(1, p.mulsRepeat2), p.sliceThickness)
     rk = (1.0 / float(F32(p.nx * F32(p.resolutionX))), 1.0 / float(F32(p.ny * F32(p.resolutionY))))
     for j in range(run.avg_runs):
         atoms = _run_atoms(run, j, seed)
@@ -825,7 +913,7 @@ def _run_cbed(ctx, run, where, seed):
     writers = _slot_writers(SA, oi, nT)
     sl = run.save_level
     dz = float(p.sliceThickness)
-    t_end = _thick(SA, dz)
+    t_end = _thick(SA * max(1, p.mulsRepeat2), dz)  # the wave's thickness after its last step
     rx, ry = float(F32(p.resolutionX)), float(F32(p.resolutionY))
     rk = (1.0 / float(F32(nx * F32(p.resolutionX))), 1.0 / float(F32(ny * F32(p.resolutionY))))
     scale = 1.0 / math.sqrt(float(nx * ny))
@@ -856,30 +944,46 @@ def _run_cbed(ctx, run, where, seed):
         probe = probe_at(off)
         atoms = _run_atoms(run, j, seed)
         T, slabs = _stacks(ctx, p, atoms)
-        _, dps, ews = ctx.multislice(p, T, probe, positions=pos, want_det=False, want_diffpats=True,
-                                     want_exit_waves=sl > 1, slab_stacks=slabs, series=True)
-        # the pattern each slot's file ends the run with, and its thickness
+        # the pattern each slot's file ends the run with and its thickness,
+        # interimWave's files, the final wave
         slot_pat, slot_t = [None] * nT, [0.0] * nT
-        for t, a in enumerate(writers):
-            if a < 0:
-                continue
-            if sl > 1:
-                slot_pat[t], slot_t[t] = _kspace_pattern(ews[t, 0], scale), _thick(a + 1, dz)
-            else:
-                stale = t_end if (a == 0 and j > 0) else _thick(a, dz)
-                slot_pat[t], slot_t[t] = dps[t, 0], stale
-        final = slot_pat[nT - 1]
+        if _ALWAYS_CHAIN or _repeats(p):
+            ev, NS = _wave_events(p, sl > 1, True)
+            res = _chain(ctx, p, T, slabs, probe, {v[1] if k[0] == "diff" else v[0] for k, v in ev.items()} | {NS - 1})
+            for (kind, t), v in ev.items():
+                if kind == "diff" and v[0] == "k":
+                    slot_pat[t] = res[v[1]][0]
+                    slot_t[t] = t_end if (v[2] is None and j > 0) else _thick(v[2] or 0, dz)
+                elif kind == "diff":
+                    slot_pat[t], slot_t[t] = _kspace_pattern(res[v[1]][1], scale), _thick(v[2], dz)
+            last_wave = res[NS - 1][1]
+            final = _kspace_pattern(last_wave, scale) if sl > 1 else res[NS - 1][0]
+            wave_files = {k[1]: (res[v[0]][1], _thick(v[1], dz)) for k, v in ev.items() if k[0] == "wave"}
+        else:
+            _, dps, ews = ctx.multislice(p, T, probe, positions=pos, want_det=False, want_diffpats=True,
+                                         want_exit_waves=sl > 1, slab_stacks=slabs, series=True)
+            for t, a in enumerate(writers):
+                if a < 0:
+                    continue
+                if sl > 1:
+                    slot_pat[t], slot_t[t] = _kspace_pattern(ews[t, 0], scale), _thick(a + 1, dz)
+                else:
+                    stale = t_end if (a == 0 and j > 0) else _thick(a, dz)
+                    slot_pat[t], slot_t[t] = dps[t, 0], stale
+            final = slot_pat[nT - 1]
+            last_wave = ews[nT - 1, 0] if sl > 1 else None
+            wave_files = {f: (ews[nT - 1 if a == SA - 1 else a // oi, 0], _thick(a + 1, dz))
+                          for f, a in _interim_files(SA, oi).items()} if sl > 1 else {}
         if where and sl > 2:
             imageio.write_img(os.path.join(where, "wave_probe.img"), probe, t=0.0 if j == 0 else t_end, dx=rx,
                               dy=ry, comment="Wavefunction")
             if j == 0:
-                imageio.write_img(os.path.join(where, "wave_final.img"), ews[nT - 1, 0], t=t_end, dx=rx, dy=ry,
+                imageio.write_img(os.path.join(where, "wave_final.img"), last_wave, t=t_end, dx=rx, dy=ry,
                                   comment="Wavefunction")
         if where and sl > 1:
-            for f, a in _interim_files(SA, oi).items():
-                t = nT - 1 if a == SA - 1 else a // oi
+            for f, (w, th) in wave_files.items():
                 name = "wave_%d_%d.img" % (j, f) if run.tds else "wave_%d.img" % f
-                imageio.write_img(os.path.join(where, name), ews[t, 0], t=_thick(a + 1, dz), dx=rx, dy=ry,
+                imageio.write_img(os.path.join(where, name), w, t=th, dx=rx, dy=ry,
                                   params=_wave_params(p, run.spread, run.beam_tilt), comment="Wave Function")
         for t in range(nT):
             if slot_pat[t] is None:
@@ -930,7 +1034,7 @@ def _run_tem(ctx, run, where, seed):
     nT = p.thickness_count()
     oi = p.outputInterval
     dz = float(p.sliceThickness)
-    t_end = _thick(SA, dz)
+    t_end = _thick(SA * max(1, p.mulsRepeat2), dz)  # the wave's thickness after its last step
     rx, ry = float(F32(p.resolutionX)), float(F32(p.resolutionY))
     plane = np.zeros((nx, ny, 2), np.float32)
     plane[..., 0] = 1.0  # stem3/stem3.cpp:2403-2407
@@ -946,18 +1050,24 @@ def _run_tem(ctx, run, where, seed):
     for j in range(run.avg_runs):
         atoms = _run_atoms(run, j, seed)
         T, slabs = _stacks(ctx, p, atoms)
-        _, _, ews = ctx.multislice(p, T, plane, positions=pos, want_det=False, want_exit_waves=True,
-                                   slab_stacks=slabs, series=True)
-        exit_wave = ews[nT - 1, 0]
+        if _ALWAYS_CHAIN or _repeats(p):
+            ev, NS = _wave_events(p, True, False)
+            res = _chain(ctx, p, T, slabs, plane, {a for a, _ in ev.values()} | {NS - 1})
+            exit_wave = res[NS - 1][1]
+            wave_files = {f: (res[a][1], _thick(th, dz)) for (_, f), (a, th) in ev.items()}
+        else:
+            _, _, ews = ctx.multislice(p, T, plane, positions=pos, want_det=False, want_exit_waves=True,
+                                       slab_stacks=slabs, series=True)
+            exit_wave = ews[nT - 1, 0]
+            wave_files = {f: (ews[nT - 1 if a == SA - 1 else a // oi, 0], _thick(a + 1, dz)) for f, a in files.items()}
         acc += exit_wave[..., 0].astype(np.float64) ** 2 + exit_wave[..., 1].astype(np.float64) ** 2
         if j == 0:
             first = exit_wave
         if not where:
             continue
-        for f, a in files.items():
-            t = nT - 1 if a == SA - 1 else a // oi
+        for f, (w, th) in wave_files.items():
             name = "wave_%d_%d.img" % (j, f) if run.tds else "wave_%d.img" % f
-            imageio.write_img(os.path.join(where, name), ews[t, 0], t=_thick(a + 1, dz), dx=rx, dy=ry,
+            imageio.write_img(os.path.join(where, name), w, t=th, dx=rx, dy=ry,
                               params=_wave_params(p, run.spread, run.beam_tilt), comment="Wave Function")
         if j == 0:
             saved = exit_wave

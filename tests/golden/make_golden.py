@@ -322,6 +322,20 @@ RUN_CASES = {
                        sliceThickness=2.0, scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0,
                        bandlimit=True, outputInterval=2, mode="CBED", saveLevel=1,
                        extra=["Source Size (diameter): 0.9"], clock=1764000000),
+    # stacking sequences "sequence: m1 m2": each slab's stack m1 times in a
+    # row, the slab loop m2 times.  CBED at save level 1 (k-space patterns,
+    # their stale thicknesses) and 3 (interimWave and the real-space
+    # collectIntensity at absolute_slice*(1 + repeat), files past the
+    # thickness slots), TEM, STEM through two unequal slabs at save level 1
+    "qsccbedseq": dict(cell="si", ncell=(4, 3, 2), nx=64, resolutionX=0.06788, v0=300.0, slices=3,
+                       sliceThickness=2.0, scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0,
+                       bandlimit=True, outputInterval=2, mode="CBED", saveLevel=1, sequence=(2, 2)),
+    "qsccbedseq3": dict(cell="si", ncell=(4, 3, 2), nx=64, resolutionX=0.06788, v0=300.0, slices=3,
+                        sliceThickness=2.0, scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0,
+                        bandlimit=True, outputInterval=2, mode="CBED", saveLevel=3, sequence=(2, 2)),
+    "qsctemseq": dict(cell="si", ncell=(4, 3, 2), nx=64, resolutionX=0.06, v0=300.0, slices=4, sliceThickness=2.0,
+                      scan=None, detectors=[], alpha=0.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
+                      outputInterval=3, mode="TEM", saveLevel=0, sequence=(3, 2)),
     # CBED through two unequal slabs (NCELLZ: 3/2): every slab's stack
     "qsccbedd2u": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=3,
                        sliceThickness=2.0, scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0,
@@ -336,6 +350,11 @@ RUN_CASES = {
                     sliceThickness=1.9525, scan=(3.905, 7.81, 2, 3.905, 7.81, 2),
                     detectors=[(0.0, 20.0, "BF"), (40.0, 90.0, "HAADF")], alpha=20.0, outputInterval=4,
                     mode="STEM", saveLevel=2),
+    # STEM through a stacking sequence over two equal slabs
+    "qscstemseq": dict(cell="sto", ncell=(3, 3, 4), nx=64, resolutionX=0.0915, v0=200.0, slices=4,
+                       sliceThickness=1.9525, scan=(3.905, 7.81, 2, 3.905, 7.81, 2),
+                       detectors=[(0.0, 20.0, "BF"), (40.0, 90.0, "HAADF")], alpha=20.0, outputInterval=2,
+                       mode="STEM", saveLevel=1, cellDiv=2, sequence=(2, 2)),
 }
 
 
@@ -353,7 +372,7 @@ def qsc_run_case(name, case):
                          alpha=case["alpha"], Cs_mm=case.get("Cs_mm", 0.0), defocus_nm=case.get("defocus_nm", 0.0),
                          outputInterval=case.get("outputInterval"), mode=case["mode"],
                          bandlimit=case.get("bandlimit", False), folder="out", saveLevel=case["saveLevel"],
-                         cellDiv=case.get("cellDiv", 1))
+                         cellDiv=case.get("cellDiv", 1), sequence=case.get("sequence", (1, 1)))
         if case.get("extra"):
             with open(qsc, "a") as f:
                 f.write("\n".join(case["extra"]) + "\n")

@@ -35,7 +35,7 @@ def test_exports_every_declared_symbol(L):
 
 
 def test_abi_version(L):
-    assert L.qs_abi_version() == 2
+    assert L.qs_abi_version() == 3
 
 
 def test_struct_layouts():

@@ -49,11 +49,12 @@ def test_stem3_input_end_to_end():
 
 # this library's own addition to the TEM output folder (the reference stops
 # before it writes its averages)
-EXTRA = {"qsctem": {"waveIntensity.img"}, "qsctemtilt": {"waveIntensity.img"}, "qsctemd2": {"waveIntensity.img"}}
+EXTRA = {"qsctem": {"waveIntensity.img"}, "qsctemtilt": {"waveIntensity.img"}, "qsctemd2": {"waveIntensity.img"},
+         "qsctemseq": {"waveIntensity.img"}}
 
 
 @pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsccbedsrc", "qsccbedd2u", "qsctem", "qsctemtilt",
-                                  "qsctemd2", "qscstem"])
+                                  "qsctemd2", "qscstem", "qsccbedseq", "qsccbedseq3", "qsctemseq", "qscstemseq"])
 def test_output_folder_matches_the_references(name):
     """The whole output folder of a stem3 run: CBED thickness series
     (diff_<t>.img) at save level 1 and 3 (real-space overwrite, interimWave,

@@ -17,7 +17,8 @@ from oracle import oracle
 from oracle_ctx import OracleContext
 from qstem_gb300 import imageio, qsc
 
-EXTRA = {"qsctem": {"waveIntensity.img"}, "qsctemtilt": {"waveIntensity.img"}, "qsctemd2": {"waveIntensity.img"}}
+EXTRA = {"qsctem": {"waveIntensity.img"}, "qsctemtilt": {"waveIntensity.img"}, "qsctemd2": {"waveIntensity.img"},
+         "qsctemseq": {"waveIntensity.img"}}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -42,7 +43,7 @@ def _read(folder, fn):
 
 
 @pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsccbedsrc", "qsccbedd2u", "qsctem", "qsctemtilt",
-                                  "qsctemd2", "qscstem"])
+                                  "qsctemd2", "qscstem", "qsccbedseq", "qsccbedseq3", "qsctemseq", "qscstemseq"])
 def test_output_folder_as_the_reference_writes_it(tmp_path, name):
     z, path, out = _inputs(tmp_path, name)
     # a case made at a fixed reference clock runs with the reference's generator
@@ -58,6 +59,15 @@ def test_output_folder_as_the_reference_writes_it(tmp_path, name):
         if comment != "STEM image":
             np.testing.assert_allclose(im.params, params, rtol=1e-6, err_msg=fn)
         assert rel_l2(data, z["img_" + fn]) <= 1e-6, fn
+
+
+@pytest.mark.parametrize("name", ["qsccbed", "qsccbed3", "qsccbedd2u", "qsctem", "qsctemtilt", "qsctemd2"])
+def test_step_chaining_writes_the_same_folder(tmp_path, monkeypatch, name):
+    """The path run_qsc takes for stacking sequences -- every file's last
+    write found step by step, the wave run in stretches between those steps
+    -- on the cases without repeats: the same folder as the reference's."""
+    monkeypatch.setattr(qsc, "_ALWAYS_CHAIN", True)
+    test_output_folder_as_the_reference_writes_it(tmp_path, name)
 
 
 def _tds(runs, save_level):
