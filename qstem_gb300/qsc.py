@@ -19,10 +19,11 @@ Thermal displacements (tds) follow the Einstein model or a phonon file
 numpy's generator or, on request, from the reference's own clock-seeded
 generator in the reference's order (qstem_gb300.thermal).
 
-Inputs that need parts of the reference outside this library are refused
-with NotImplementedError: the 2-D potential (potential3D: no), stacking
-sequences other than "1 1", a phonon file with a "Cube:" box (the reference
-exits there) and modes other than STEM, CBED and TEM.
+Inputs that need parts of the reference outside this library, or that the
+reference cannot run, are refused with NotImplementedError: the 2-D
+potential (potential3D: no), more than one stacking-sequence line, a
+phonon file with a "Cube:" box (the reference exits there) and modes other
+than STEM, CBED and TEM.
 """
 import math
 import os

@@ -1,0 +1,45 @@
+"""Stacking sequences in the library (qs_multislice_run with mulsRepeat1/2):
+the wave's steps against the same steps unrolled into one stack.  A
+sequence m1 m2 over cellDiv slabs is m2 passes through the slabs, each
+slab's stack m1 times; the detector images of every thickness slot come
+from the step collectIntensity's index assigns it last.  Tolerance 1e-4
+relative L2 (1e-6 typical) for detector images, patterns and exit waves."""
+import numpy as np
+import pytest
+
+from conftest import Golden, rel_l2
+from oracle_ctx import OracleContext
+from qstem_gb300 import lib
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = lib.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("name,m1,m2", [("sto64", 3, 1), ("sto64d2u", 2, 2), ("sto64d2", 1, 3)])
+def test_sequence_walk_matches_the_unrolled_steps(ctx, name, m1, m2):
+    g = Golden(name)
+    p = g.params
+    p.mulsRepeat1, p.mulsRepeat2 = m1, m2
+    slabs = p.cellDiv > 1 and not p.equalDivs
+    T = np.concatenate([ctx.slices(p, g["atoms"], slab=k) for k in range(p.cellDiv)]) if slabs else np.asarray(g["T"])
+    probe = np.ascontiguousarray(g["probe"])
+    det, dps, ews = ctx.multislice(p, T, probe, want_diffpats=True, want_exit_waves=True, slab_stacks=slabs)
+    n = p.scanXN * p.scanYN
+    from qstem_gb300 import config
+    offs = config.scan_offsets(p)
+    rdet, rdp, rew = OracleContext().multislice(p, T, probe, positions=offs, want_diffpats=True,
+                                                want_exit_waves=True, slab_stacks=slabs)
+    assert det.shape == rdet.shape and len(dps) == n
+    assert rel_l2(det, rdet) <= 1e-4
+    assert rel_l2(dps, rdp) <= 1e-4 and rel_l2(ews, rew) <= 1e-4
+    # the repeats change the result
+    q = p.copy()
+    q.mulsRepeat1 = q.mulsRepeat2 = 1
+    det1, _, _ = ctx.multislice(q, T, probe, slab_stacks=slabs)
+    assert rel_l2(det1, det) > 1e-3
