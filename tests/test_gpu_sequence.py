@@ -43,3 +43,26 @@ def test_sequence_walk_matches_the_unrolled_steps(ctx, name, m1, m2):
     q.mulsRepeat1 = q.mulsRepeat2 = 1
     det1, _, _ = ctx.multislice(q, T, probe, slab_stacks=slabs)
     assert rel_l2(det1, det) > 1e-3
+
+
+def test_tem_through_a_sequence(ctx):
+    """qs_tem_run with a stacking sequence: the exit wave of the plane wave
+    through the sequence's steps equals the plane wave through the stack
+    repeated by hand (m1 = 2 over one slab, m2 = 2)."""
+    g = Golden("si64tem")
+    p = g.params
+    atoms = g["atoms"]
+    T = ctx.slices(p, atoms)
+    plane = np.zeros((p.nx, p.ny, 2), np.float32)
+    plane[..., 0] = 1.0
+    q = p.copy()
+    q.mulsRepeat1, q.mulsRepeat2 = 2, 2
+    _, _, ew = ctx.tem(q, [atoms], want_exit_waves=True)
+    r = p.copy()
+    r.slices = r.outputInterval = 4 * p.slices
+    pos = tuple(np.zeros(1, np.int32) for _ in range(4))
+    _, _, ref = ctx.multislice(r, np.concatenate([T] * 4), plane, positions=pos, want_det=False,
+                               want_exit_waves=True)
+    assert rel_l2(ew[0], ref[0]) <= 1e-5
+    _, _, once = ctx.tem(p, [atoms], want_exit_waves=True)
+    assert rel_l2(once[0], ref[0]) > 1e-3
