@@ -210,7 +210,7 @@ def supercell(cell, ncx, ncy, ncz, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0), repl
     return out, F32(hi[0] - lo[0]), F32(hi[1] - lo[1]), F32(hi[2] - lo[2])
 
 
-def cube(cell, size, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0), seed=None):
+def cube(cell, size, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0), seed=None, draws=None, displace=None):
     """tiltBoxed (libs/fileio_fftw3.cpp:1661-1940): the atoms of the crystal,
     rotated by the crystal tilt about the origin and shifted by (xOffset,
     yOffset), that fall inside the box [0, size] (the "Cube:" sizes).  Unit
@@ -220,7 +220,12 @@ def cube(cell, size, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0), seed=None):
     them is kept per cell, chosen by a uniform draw over their occupancies
     (numpy.random.default_rng(seed); the reference draws with ran1); the
     first stays when the draw falls past a total occupancy below 1, as in
-    the reference.  Returns (atoms[ATOM_DTYPE], ax, by, c) = the box."""
+    the reference.  draws / displace (thermal.Replicator): the site draws
+    from draws.cube_uniform() instead, and each (site, cell) moved by the
+    fractional displacement displace(dw) (drawn for every cell of the walk,
+    inside the box or not, and once more after it, as tiltBoxed calls
+    phononDisplacement; the box test uses the undisplaced position).
+    Returns (atoms[ATOM_DTYPE], ax, by, c) = the box."""
     frac = sorted_fractional(cell)
     n = len(frac)
     cx, cy, cz = (F32(v) for v in size)
@@ -265,6 +270,28 @@ def cube(cell, size, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0), seed=None):
         cart = _mat_vec(M, *pos)
         x, y, z = cart[0] + dx, cart[1] + dy, cart[2] + dz
         inside = (x >= 0) & (x <= float(cx)) & (y >= 0) & (y <= float(cy)) & (z >= 0) & (z <= float(cz))
+        if draws is not None or displace is not None:
+            for c in range(len(cells)):
+                jch = i
+                if occ < 1.0 or j > i + 1:
+                    ch = draws.cube_uniform() if draws is not None else rng.random()
+                    if occ >= 1.0:
+                        ch = occ * ch
+                    last = 0.0
+                    for m in range(i, j):
+                        o = float(frac["occ"][m])
+                        if last <= ch < last + o:
+                            jch = m
+                        last += o
+                u = displace(float(frac["dw"][jch])) if displace is not None else (0.0, 0.0, 0.0)
+                if inside[c]:
+                    b = _mat_vec(M, *(float(pos[k][c]) + u[k] for k in range(3)))
+                    rec = frac[jch].copy()
+                    rec["x"], rec["y"], rec["z"] = F32(b[0] + dx), F32(b[1] + dy), F32(b[2] + dz)
+                    kept.append(rec)
+            last_site = i
+            i = j
+            continue
         choice = np.full(len(cells), i)
         if occ < 1.0 or j > i + 1:
             u = rng.random(len(cells)) * (1.0 if occ < 1.0 else occ)
@@ -278,6 +305,8 @@ def cube(cell, size, tilt=(0.0, 0.0, 0.0), offset=(0.0, 0.0), seed=None):
             rec["x"], rec["y"], rec["z"] = F32(x[c]), F32(y[c]), F32(z[c])
             kept.append(rec)
         i = j
+    if displace is not None and n:
+        displace(float(frac["dw"][last_site]))  # tiltBoxed's closing phononDisplacement call (:1935)
     atoms = np.array(kept, dtype=abi.ATOM_DTYPE) if kept else np.zeros(0, abi.ATOM_DTYPE)
     return atoms, cx, cy, cz
 

@@ -265,6 +265,7 @@ class QscRun:
     offset: tuple = (0.0, 0.0)                  # xOffset, yOffset
     source_radius: float = 0.0                  # CBED probe source radius (A)
     replicator: object = None                   # thermal.Replicator drawing the runs' atoms
+    cube: tuple = None                          # "Cube:" box size (None: NCELL mode)
     tilt_back: bool = True                      # "Tilt back:" (TEM: wave.img tilted back)
     spread: tuple = (0.0, 0.0, 0.0)             # dE/E, dI/I, dV/V as read (CBED/TEM use them as such)
 
@@ -419,11 +420,15 @@ def read_qsc(path, seed=20261203, rng="numpy", clock=0):
     if cube is not None:  # a box cut from the tilted crystal (tiltBoxed)
         if tds and modes is not None:
             unsupported.append("phonon-File with Cube")  # tiltBoxed exits (libs/fileio_fftw3.cpp:1893-1896)
-        random_cell = tds or any(a[5] < 1 for a in cell.atoms) or len(
-            {(a[1], a[2], a[3]) for a in cell.atoms}) < len(cell.atoms)
-        if rng == "reference" and random_cell:
-            unsupported.append("the reference generator's draws in a Cube box")
-        atoms, ax, by, c = config.cube(cell, cube, tuple(tilt), (xoff, yoff), seed=seed)
+        if rng == "reference":
+            from . import thermal
+            replicator = thermal.Replicator(config.sorted_fractional(cell), (1, 1, 1), cell.H,
+                                            (cell.a, cell.b, cell.c), tds, temperature, rng=rng, seed=seed,
+                                            clock=clock)
+            atoms = replicator.cube_configuration(0, cell, cube, tuple(tilt), (xoff, yoff))
+            ax, by, c = (F32(v) for v in cube)
+        else:
+            atoms, ax, by, c = config.cube(cell, cube, tuple(tilt), (xoff, yoff), seed=seed)
     else:  # NCELL mode
         if rng == "reference" or (tds and modes is not None):
             from . import thermal
@@ -598,7 +603,8 @@ def read_qsc(path, seed=20261203, rng="numpy", clock=0):
                   temperature=temperature, avg_runs=avg_runs, folder=folder, detector_names=names, dE_E=series,
                   scan_step=scan_step, save_level=save_level, spread=(dE_E, dI_I, dV_V),
                   beam_tilt=tuple(beam_tilt), tilt_back=tilt_back, tilt=tuple(tilt), offset=(xoff, yoff),
-                  source_radius=source_radius, replicator=replicator)
+                  source_radius=source_radius, replicator=replicator,
+                  cube=tuple(cube) if cube is not None else None)
 
 
 def _isnum(t):
@@ -728,6 +734,8 @@ def _run_atoms(run, j, seed):
     if run.replicator is not None:
         if j == 0:
             return run.atoms
+        if run.cube is not None:
+            return run.replicator.cube_configuration(j, run.cell, run.cube, run.tilt, run.offset)
         atoms, _, _, _ = config.supercell(run.cell, *run.ncell, run.tilt, run.offset,
                                           replicated=run.replicator.configuration(j))
         return atoms

@@ -109,11 +109,15 @@ class _RefDraws:
         self.g = RefRandom()
         self.clock = int(clock)
         self.vac = [-1]
+        self.cube = [-1]  # tiltBoxed's own seed (libs/fileio_fftw3.cpp:1691)
         self.thermal = None
         self.cbed = None
 
     def uniform(self):
         return self.g.ran1(self.vac)
+
+    def cube_uniform(self):
+        return self.g.ran1(self.cube)
 
     def normal(self):
         if self.thermal is None:
@@ -144,6 +148,7 @@ class _NumpyDraws:
         return float(self._n.pop())
 
     source = normal
+    cube_uniform = uniform
 
 
 @dataclass
@@ -291,12 +296,36 @@ class Replicator:
     def configuration(self, j):
         """Fractional atoms (ATOM_DTYPE, readUnitCell's order, j = (icz +
         icy ncz + icx ncy ncz) ncoord + i) of configuration j."""
+        return self._walk(self._draws(j))
+
+    def cube_configuration(self, j, cell, size, tilt, offset):
+        """Cartesian atoms of configuration j of a "Cube:" box (tiltBoxed,
+        libs/fileio_fftw3.cpp:1661-1940): its site draws and Einstein
+        displacements in its order (config.cube)."""
+        from . import config
+        d = self._draws(j)
+        disp = (lambda dw: self._einstein(d, dw)) if self.tds else None
+        atoms, _, _, _ = config.cube(cell, size, tilt, offset, draws=d, displace=disp)
+        return atoms
+
+    def _draws(self, j):
         if self._ref is not None:
             if j != self._next:
                 raise ValueError("the reference generator draws configuration %d next, not %d" % (self._next, j))
             self._next += 1
-            return self._walk(self._ref)
-        return self._walk(_NumpyDraws(self.seed + j))
+            return self._ref
+        return _NumpyDraws(self.seed + j)
+
+    def _einstein(self, draws, dw):
+        """phononDisplacement's Einstein model (:586-607): three normal
+        draws scaled by sqrt(T/300) sqrt(dw / (8 pi^2)) / sqrt(3), turned
+        into fractional coordinates (u times the inverse cell matrix)."""
+        scale = float(F32(math.sqrt(self.temperature / 300.0)))
+        wob = scale * math.sqrt(dw * (1.0 / (8 * PID * PID)))
+        sq3 = 1.0 / math.sqrt(3.0)
+        g = [wob * sq3 * draws.normal() for _ in range(3)]
+        M = self.minv
+        return tuple(((0.0 + g[0] * M[k]) + g[1] * M[3 + k]) + g[2] * M[6 + k] for k in range(3))
 
     def source_offset(self, j, radius):
         """doCBED's probe offset of run j (stem3/stem3.cpp:2096-2097):
@@ -332,11 +361,6 @@ class Replicator:
         occ = [float(v) for v in f["occ"]]
         einstein = self.tds and self.modes is None
         phonon = self.tds and self.modes is not None
-        if einstein:
-            scale = float(F32(math.sqrt(self.temperature / 300.0)))
-            wob_scale = 1.0 / (8 * PID * PID)
-            sq3 = 1.0 / math.sqrt(3.0)
-            M = self.minv
         rec_src, rec_dst, rec_cell, rec_u = [], [], [], []
         ph_rec = []  # phonon mode: (record index, chosen atom, cell)
         q1 = q2 = None
@@ -360,9 +384,7 @@ class Replicator:
                                 last += occ[i2]
                         u = (0.0, 0.0, 0.0)
                         if einstein:
-                            wob = scale * math.sqrt(float(f["dw"][jch]) * wob_scale)
-                            g = [wob * sq3 * draws.normal() for _ in range(3)]
-                            u = tuple(((0.0 + g[0] * M[k]) + g[1] * M[3 + k]) + g[2] * M[6 + k] for k in range(3))
+                            u = self._einstein(draws, float(f["dw"][jch]))
                         elif phonon:
                             if jcell + i == natom - 1:
                                 q1, q2 = self._draw_modes(draws)

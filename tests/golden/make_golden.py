@@ -262,7 +262,8 @@ def phonon_modes_fixture():
 # readFile and doSTEM with thermal displacements at a fixed reference clock
 # (the reference seeds them with time(NULL)): qsc file, its other inputs
 THERMAL_CLOCK = 1764000000
-THERMAL_CASES = {"qsctds": ("tds.qsc", ["vac.cfg"]), "qscphonon": ("phonon.qsc", ["ph.cfg", "modes.phonon"])}
+THERMAL_CASES = {"qsctds": ("tds.qsc", ["vac.cfg"]), "qscphonon": ("phonon.qsc", ["ph.cfg", "modes.phonon"]),
+                  "qsctdscube": ("tdscube.qsc", ["vac.cfg"])}
 
 
 def qsc_thermal_case(name, qsc_file, others):

@@ -17,7 +17,8 @@ from qstem_gb300 import imageio, lib, qsc
 
 pytestmark = pytest.mark.gpu
 
-CASES = {"qsctds": ("tds.qsc", ["vac.cfg"]), "qscphonon": ("phonon.qsc", ["ph.cfg", "modes.phonon"])}
+CASES = {"qsctds": ("tds.qsc", ["vac.cfg"]), "qscphonon": ("phonon.qsc", ["ph.cfg", "modes.phonon"]),
+         "qsctdscube": ("tdscube.qsc", ["vac.cfg"])}
 
 
 class _Logged:

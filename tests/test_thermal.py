@@ -5,7 +5,8 @@ The reference seeds its thermal displacements with its clock
 (-time(NULL), libs/fileio_fftw3.cpp:496).  The fixtures qsctds / qscphonon
 were made by the reference with time() fixed (oracle/fixed_clock.c): its
 readFile atoms (Einstein displacements plus vacancy draws in a
-non-orthogonal cell; displacements from a phonon file), its doSTEM images
+non-orthogonal cell, in NCELL mode and in a tilted "Cube:" box;
+displacements from a phonon file), its doSTEM images
 (those of the last run: Navg stays 0, so collectIntensity overwrites them)
 and its per-position patterns averaged over two runs.  read_qsc with the
 reference generator at that clock must give readFile's atoms bit for bit,
@@ -23,7 +24,8 @@ from qstem_gb300 import config, qsc, thermal
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-CASES = {"qsctds": ("tds.qsc", ["vac.cfg"]), "qscphonon": ("phonon.qsc", ["ph.cfg", "modes.phonon"])}
+CASES = {"qsctds": ("tds.qsc", ["vac.cfg"]), "qscphonon": ("phonon.qsc", ["ph.cfg", "modes.phonon"]),
+         "qsctdscube": ("tdscube.qsc", ["vac.cfg"])}
 
 
 def _inputs(tmp_path, name):
