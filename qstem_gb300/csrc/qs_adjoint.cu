@@ -209,8 +209,11 @@ __global__ void adj_dv_finish(const float2* __restrict__ partial, int nchunks, i
     const size_t n = (size_t)potNx * potNy;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         double gr = 0.0, gi = 0.0;
+        // unrolled so that several chunks' loads are in flight; the adds
+        // stay in chunk order
+#pragma unroll 8
         for (int c = 0; c < nchunks; ++c) {
-            const float2 v = partial[(size_t)c * n + i];
+            const float2 v = __ldg(partial + (size_t)c * n + i);
             gr += v.x;
             gi += v.y;
         }
