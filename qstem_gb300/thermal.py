@@ -19,7 +19,7 @@ the chosen atom moves every atom of the site:
                made once per configuration (before the first atom's
                displacement), w the mode's Bose-Einstein amplitude at the
                temperature; u / (a, b, c) in fractional units.
-Positions are x + icx + u (double), stored as float.
+Positions are (x + icx) in float, plus u in double, stored as float.
 
 The draws come from a generator: the reference's own (RefRandom: ran1, the
 Park-Miller generator with a Bays-Durham shuffle, and gasdev, the polar
