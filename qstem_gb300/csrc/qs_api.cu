@@ -1010,9 +1010,12 @@ struct CbedUnit {
 
 size_t rup256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// slices a wave passes through: cellDiv slabs of `slices` (doCBED's slab
-// loop, stem3/stem3.cpp:2188-2219)
-int abs_slices(const qs_params& P) { return P.slices * std::max(1, P.cellDiv); }
+// steps a wave takes: mulsRepeat2 passes through cellDiv slabs of `slices`,
+// each slab's stack mulsRepeat1 times (doCBED's slab loop,
+// stem3/stem3.cpp:2188-2219, around runMulsSTEM's repeat loop)
+int abs_slices(const qs_params& P) {
+    return P.slices * std::max(1, P.cellDiv) * std::max(1, P.mulsRepeat1) * std::max(1, P.mulsRepeat2);
+}
 
 // Device bytes of a unit of nb waves of grid N, slice stacks of smax slices.
 size_t cbed_unit_bytes(const qs_params& P, int nb, int smax) {
@@ -1037,10 +1040,6 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
         if (P.potNx != P.nx || P.potNy != P.ny) {
             set_error("job " + std::to_string(i) + ": CBED needs the potential grid equal to the wave grid");
             return QS_ERR_ARG;
-        }
-        if (repeats(P)) {
-            set_error("job " + std::to_string(i) + ": the CBED batch walks the sequence 1 1 only");
-            return QS_ERR_UNSUPPORTED;
         }
         if (!line_supported(P.nx) || !line_supported(P.ny)) {
             set_error("job " + std::to_string(i) + ": nx, ny must be in {64,128,256,384,512,768,1024}");
@@ -1158,17 +1157,26 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
                 C.zeros = (int*)take(sizeof(int) * (P0.ny + nb));
                 for (int w = 0; w < nb; w++) {
                     const qs_cbed_job& J = jobs[u.jobs[w]];
-                    // one stack per slab, back to back (slab 0's copied for
-                    // equal divisions, which the reference reuses)
+                    // the instance's stack in step order: block b = pc*R1 + r
+                    // of its stacking sequence holds slab pc % cellDiv; each
+                    // slab is built at its first block and copied to the
+                    // others (slab 0 everywhere for equal divisions, which
+                    // the reference reuses)
                     const int D = std::max(1, J.params.cellDiv), Sj = J.params.slices;
+                    const int R1 = std::max(1, J.params.mulsRepeat1), R2 = std::max(1, J.params.mulsRepeat2);
                     float2* st0 = C.stacks + (size_t)w * u.smax * Pp;
-                    for (int slab = 0; slab < D; slab++) {
-                        float2* dst = st0 + (size_t)slab * Sj * Pp;
-                        if (slab > 0 && J.params.equalDivs)
-                            QS_CUDA_TRY(cudaMemcpyAsync(dst, st0, sizeof(float2) * Sj * Pp, cudaMemcpyDeviceToDevice, s));
-                        else
-                            QS_TRY(qs_slab_build(c, &J.params, J.atoms, J.natom, slab, (float*)dst, 0));
-                    }
+                    const size_t blk = (size_t)Sj * Pp;
+                    for (int slab = 0; slab < D; slab++)
+                        if (slab == 0 || !J.params.equalDivs)
+                            QS_TRY(qs_slab_build(c, &J.params, J.atoms, J.natom, slab,
+                                                 (float*)(st0 + (size_t)slab * R1 * blk), 0));
+                    for (int pc = 0; pc < R2 * D; pc++)
+                        for (int r = 0; r < R1; r++) {
+                            const int k = J.params.equalDivs ? 0 : pc % D;
+                            if (pc == k && r == 0) continue;  // the block the slab was built in
+                            QS_CUDA_TRY(cudaMemcpyAsync(st0 + ((size_t)pc * R1 + r) * blk, st0 + (size_t)k * R1 * blk,
+                                                        sizeof(float2) * blk, cudaMemcpyDeviceToDevice, s));
+                        }
                     // doCBED's probe position (stem3/stem3.cpp:2096-2100)
                     const double dx = (double)(J.params.scanXStart - J.params.potOffsetX);
                     const double dy = (double)(J.params.scanYStart - J.params.potOffsetY);

@@ -66,3 +66,25 @@ def test_tem_through_a_sequence(ctx):
     assert rel_l2(ew[0], ref[0]) <= 1e-5
     _, _, once = ctx.tem(p, [atoms], want_exit_waves=True)
     assert rel_l2(once[0], ref[0]) > 1e-3
+
+
+@pytest.mark.parametrize("m1,m2", [(2, 3), (1, 2)])
+def test_cbed_batch_through_a_sequence(ctx, m1, m2):
+    """qs_cbed_batch_run with a stacking sequence (the instance's stack laid
+    out in step order) gives the final pattern qs_multislice_run gives for
+    the same sequence; an instance without one in the same batch is
+    unchanged."""
+    g = Golden("si64cbed")
+    plain = g.params
+    p = plain.copy()
+    p.mulsRepeat1, p.mulsRepeat2 = m1, m2
+    T = ctx.slices(p, g["atoms"])
+    probe = ctx.probe(p, float(np.float32(np.float32(p.scanXStart) - np.float32(p.potOffsetX))),
+                      float(np.float32(np.float32(p.scanYStart) - np.float32(p.potOffsetY))))
+    pos = tuple(np.zeros(1, np.int32) for _ in range(4))
+    _, dps, _ = ctx.multislice(p, T, probe, positions=pos, want_det=False, want_diffpats=True)
+    _, ref1, _ = ctx.multislice(plain, T, probe, positions=pos, want_det=False, want_diffpats=True)
+    pats, _ = ctx.cbed_batch([(p, g["atoms"]), (plain, g["atoms"])])
+    assert rel_l2(pats[0], dps[0]) <= 1e-5
+    assert rel_l2(pats[1], ref1[0]) <= 1e-5
+    assert rel_l2(pats[0], pats[1]) > 1e-3
