@@ -147,9 +147,10 @@ typedef struct qs_params {
      * cellDiv slabs, and through each slab's stack m1 times in a row.  The
      * thickness slot of a step is collectIntensity's t of the index
      * totalSliceCount + islice*(1 + repeat) the reference passes it.
-     * qs_multislice_run, qs_stem_run, qs_tem_run and qs_cbed_batch_run walk
-     * the sequence; qs_adjoint_run and the no-allocation entry point take
-     * "1 1" only (QS_ERR_UNSUPPORTED / QS_ERR_ARG).  0 reads as 1. */
+     * qs_multislice_run, qs_stem_run, qs_tem_run, qs_cbed_batch_run and
+     * qs_adjoint_run (a stack slice's dL/dV sums all its steps) walk the
+     * sequence; the no-allocation entry point takes "1 1" only (QS_ERR_ARG).
+     * 0 reads as 1. */
     int mulsRepeat1, mulsRepeat2;
 } qs_params;
 

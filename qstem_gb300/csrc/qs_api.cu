@@ -95,10 +95,6 @@ static int ensure(qs_ctx* c, int which, size_t bytes, void** out) {
     return QS_OK;
 }
 
-// A stacking sequence other than "1 1" (qs_multislice_run, qs_stem_run and
-// qs_tem_run walk it; the other entry points do not).
-static bool repeats(const qs_params& p) { return p.mulsRepeat1 > 1 || p.mulsRepeat2 > 1; }
-
 static int check_params(const qs_params* p) {
     if (!p) { set_error("params is NULL"); return QS_ERR_ARG; }
     if (p->nx < 1 || p->ny < 1 || p->slices < 1 || p->potNx < p->nx || p->potNy < p->ny) {
@@ -1418,10 +1414,6 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     if (!c || !trans_in || !probe_in || !batch || !target || !dL_dV) { set_error("null argument"); return QS_ERR_ARG; }
     QS_TRY(check_params(p));
     const qs_params& P = *p;
-    if (repeats(P)) {
-        set_error("adjoint: the stacking sequence 1 1 only");
-        return QS_ERR_UNSUPPORTED;
-    }
     if (!line_supported(P.nx) || !line_supported(P.ny)) {
         set_error("adjoint: nx, ny must be in {64,128,256,384,512,768,1024}");
         return QS_ERR_UNSUPPORTED;
@@ -1430,11 +1422,21 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
         set_error("adjoint: band-limited transmission functions are not supported");
         return QS_ERR_UNSUPPORTED;
     }
-    // absolute slices: cellDiv slabs of `slices` (doSTEM's slab loop); the
-    // stack is one per slab with QS_SLAB_STACKS, else one reused
-    const int npos = batch->npos, S0 = P.slices, D = std::max(1, P.cellDiv), S = S0 * D, nx = P.nx, ny = P.ny;
+    // the steps: mulsRepeat2 passes through cellDiv slabs of `slices`, each
+    // slab's stack mulsRepeat1 times (doSTEM's slab loop around runMulsSTEM's
+    // repeats); the stack is one per slab with QS_SLAB_STACKS, else one
+    // reused.  Step a transmits stack slice stepStack[a]; a stack slice's
+    // dL/dV sums the gradients of all its steps.
+    const int npos = batch->npos, S0 = P.slices, D = std::max(1, P.cellDiv), nx = P.nx, ny = P.ny;
     const bool slabStacks = D > 1 && (flags & QS_SLAB_STACKS);
-    auto stackIdx = [&](int a) { return slabStacks ? a : a % S0; };
+    std::vector<int> stepStack;
+    for (int pc = 0; pc < std::max(1, P.mulsRepeat2) * D; pc++)
+        for (int r = 0; r < std::max(1, P.mulsRepeat1); r++)
+            for (int i = 0; i < S0; i++) stepStack.push_back((slabStacks ? (pc % D) * S0 : 0) + i);
+    const int S = (int)stepStack.size();
+    std::vector<int> lastUse(slabStacks ? D * S0 : S0, -1);
+    for (int a = 0; a < S; a++) lastUse[stepStack[a]] = a;
+    auto stackIdx = [&](int a) { return stepStack[a]; };
     if (npos < 1) { set_error("batch has no positions"); return QS_ERR_ARG; }
     if (ckpt < 1) {
         // automatic: every state kept when they fit (no recomputation), else
@@ -1617,10 +1619,10 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
             ar.trans_slice = trans + (size_t)stackIdx(sl) * sliceElems;
             QS_TRY(launch_adj_rows(ar, sl == 0, s));
             // a reused stack's slice collects the gradient of every use; the
-            // backward meets its last use (the last slab) first
+            // backward meets its last use first
             QS_TRY(launch_dv_gather(grad_t, npos, nx, ny, P.potNx, P.potNy, d_pos, d_pos + npos,
                                     trans + (size_t)stackIdx(sl) * sliceElems, sigma, d_part,
-                                    dL_dV + (size_t)stackIdx(sl) * sliceElems, !slabStacks && sl < S - S0, s));
+                                    dL_dV + (size_t)stackIdx(sl) * sliceElems, sl != lastUse[stackIdx(sl)], s));
         }
     }
     if (loss) {

@@ -54,12 +54,10 @@ def test_argument_and_support_errors(case):
     t = p.copy()
     t.cellDiv = 0
     expect(abi.QS_ERR_ARG, ctx.slices, t, g["atoms"])
-    # stacking sequences: negative repeats; the adjoint walks "1 1" only
+    # stacking sequences: negative repeats
     u = p.copy()
     u.mulsRepeat2 = -1
     expect(abi.QS_ERR_ARG, ctx.multislice, u, T)
-    u.mulsRepeat2, u.mulsRepeat1 = 1, 2
-    expect(abi.QS_ERR_UNSUPPORTED, ctx.adjoint, u, T, probe, target)
 
 
 def test_null_pointers_through_the_raw_abi(case):

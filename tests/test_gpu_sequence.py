@@ -88,3 +88,28 @@ def test_cbed_batch_through_a_sequence(ctx, m1, m2):
     assert rel_l2(pats[0], dps[0]) <= 1e-5
     assert rel_l2(pats[1], ref1[0]) <= 1e-5
     assert rel_l2(pats[0], pats[1]) > 1e-3
+
+
+@pytest.mark.parametrize("m1,m2,ckpt", [(2, 1, 1), (2, 2, 3)])
+def test_adjoint_through_a_sequence(ctx, m1, m2, ckpt):
+    """qs_adjoint_run through a stacking sequence equals the adjoint of the
+    stack repeated by hand: the same loss, and each stack slice's dL/dV
+    the sum over its steps.  Tolerances: loss 1e-6, dL/dV 1e-5 (relative)."""
+    import torch
+    g = Golden("sto64")
+    p = g.params
+    p.mulsRepeat1, p.mulsRepeat2 = m1, m2
+    from qstem_gb300 import config
+    pos = config.scan_offsets(p)
+    T = torch.from_numpy(np.ascontiguousarray(g["T"])).cuda()
+    probe = torch.from_numpy(np.ascontiguousarray(g["probe"])).cuda()
+    reps = m1 * m2
+    q = p.copy()
+    q.slices, q.mulsRepeat1, q.mulsRepeat2 = p.slices * reps, 1, 1
+    Tcat = torch.cat([T] * reps)
+    target = torch.rand((len(pos[0]), p.nx, p.ny), device="cuda")
+    loss, dV, _ = ctx.adjoint(p, T, probe, target, positions=pos, ckpt=ckpt)
+    lref, dref, _ = ctx.adjoint(q, Tcat, probe, target, positions=pos, ckpt=ckpt)
+    assert abs(loss - lref) <= 1e-6 * abs(lref)
+    dref = dref.cpu().numpy().reshape(reps, p.slices, p.potNx, p.potNy).sum(0)
+    assert rel_l2(dV.cpu().numpy(), dref) <= 1e-5
