@@ -160,3 +160,29 @@ def test_tilted_and_boxed_crystals_through_the_oracle(tmp_path, name):
     (tmp_path / str(z["cfg_name"])).write_text(str(z["cfg_text"]))
     out = qsc.run_qsc(str(tmp_path / "run.qsc"), ctx=OracleContext(), folder=str(tmp_path / "out"))
     assert rel_l2(out["adf"], z["det"][:, 0]) <= 1e-6
+
+
+def test_step_helpers_reduce_to_the_plain_slot_rule():
+    """Without repeats the steps are the absolute slices and the file writes
+    found step by step are the plain slot rule's last writers; with repeats
+    collectIntensity's index and interimWave's part ways once a pass starts
+    past slice 0 (totalSliceCount > 0)."""
+    from qstem_gb300 import config
+    p = config.make_params(nx=64, resolutionX=0.1, v0=200, slices=5, sliceThickness=2.0, ax=6.4, by=6.4, c=10.0,
+                           outputInterval=2, scan=(3.2, 3.2, 1, 3.2, 3.2, 1))
+    p.cellDiv = 2
+    steps = qsc._steps(p)
+    assert [s[4] for s in steps] == list(range(10)) and all(s[2] == s[3] == s[4] for s in steps)
+    nT, SA = p.thickness_count(), 10
+    ev, NS = qsc._wave_events(p, True, True)
+    writers = qsc._slot_writers(SA, 2, nT)
+    for t, a in enumerate(writers):
+        if a >= 0:
+            assert ev[("diff", t)][:2] == ("r", a)
+    assert {f for (k, f) in ev if k == "wave"} == set(qsc._interim_files(SA, 2))
+    p.mulsRepeat1, p.mulsRepeat2 = 2, 2
+    steps = qsc._steps(p)
+    assert len(steps) == 2 * 2 * 2 * 5
+    # second repeat of the second pass: index 5 + 2i against (5 + i) * 2
+    s = [st for st in steps if st[4] == 5 + 3][1]
+    assert (s[2], s[3]) == (5 + 3 * 2, (5 + 3) * 2)
