@@ -17,14 +17,17 @@ REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 _lib = None
 
 
-def build(quiet=True):
-    """Compile liboracle.so (and, when the reference tree is present, the
-    reference harness) with oracle/Makefile."""
+def build(quiet=True, ref_dir=None):
+    """Compile liboracle.so and, when the reference checkout is given (ref_dir,
+    else the QS_REFERENCE_DIR environment variable) and present, the
+    reference's own programs in _ref/ with oracle/Makefile."""
     out = subprocess.run(["make", "-C", HERE, "-j8"], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
-    if os.path.isdir(os.environ.get("QS_REFERENCE_DIR", "/root/reference")):
-        out = subprocess.run(["make", "-C", HERE, "-j8", "ref"], capture_output=True, text=True)
+    ref = ref_dir or os.environ.get("QS_REFERENCE_DIR")
+    if ref and os.path.isdir(ref):
+        out = subprocess.run(["make", "-C", HERE, "-j8", "ref", "REF=" + os.path.abspath(ref)], capture_output=True,
+                             text=True)
         if out.returncode != 0 and not quiet:
             print(out.stdout + out.stderr)
 

@@ -95,7 +95,7 @@ static int ensure(qs_ctx* c, int which, size_t bytes, void** out) {
     return QS_OK;
 }
 
-static int check_params(const qs_params* p) {
+int check_params(const qs_params* p) {
     if (!p) { set_error("params is NULL"); return QS_ERR_ARG; }
     if (p->nx < 1 || p->ny < 1 || p->slices < 1 || p->potNx < p->nx || p->potNy < p->ny) {
         set_error("inconsistent grid sizes (nx, ny, potNx, potNy, slices)");
@@ -112,15 +112,19 @@ static int check_params(const qs_params* p) {
     return QS_OK;
 }
 
-static double wavelength(double kev) { return 12.3984244 / std::sqrt(kev * (2 * 510.99906 + kev)); }
+int check_raster(const qs_params& p, const qs_batch& b, bool wantDetPixels) {
+    const bool needRaster = !(b.iPosX && b.iPosY) || (wantDetPixels && !(b.detPosX && b.detPosY));
+    if (needRaster && (p.scanXN < 1 || p.scanYN < 1)) {
+        set_error("the batch takes positions or detector pixels from the scan raster, which needs "
+                  "scanXN, scanYN >= 1");
+        return QS_ERR_ARG;
+    }
+    return QS_OK;
+}
 
-// propagate_slow's tables (stem3/stemlib.cpp:2783-2824), float arithmetic
-struct PropTables {
-    std::vector<float> kx2, ky2;
-    std::vector<float2> px, py;
-    float k2max;
-};
-static PropTables prop_tables(const qs_params& p) {
+double wavelength(double kev) { return 12.3984244 / std::sqrt(kev * (2 * 510.99906 + kev)); }
+
+PropTables prop_tables(const qs_params& p) {
     PropTables t;
     const int nx = p.nx, ny = p.ny;
     const float ax = p.resolutionX * nx, by = p.resolutionY * ny;
@@ -144,6 +148,22 @@ static PropTables prop_tables(const qs_params& p) {
     k2max = (float)(2.0 / 3.0 * k2max);
     t.k2max = k2max * k2max;
     return t;
+}
+
+Band band_tiles(const PropTables& t, int ny, int colTile) {
+    Band b;
+    b.yA = -1;
+    b.yB = ny;
+    for (int iy = 0; iy <= ny / 2; iy++) if (t.ky2[iy] < t.k2max) b.yA = iy;
+    for (int iy = ny - 1; iy > ny / 2; iy--) if (t.ky2[iy] < t.k2max) b.yB = iy;
+    for (int iy = 0; iy < ny; iy++)
+        if ((t.ky2[iy] < t.k2max) != (iy <= b.yA || iy >= b.yB)) { b.yA = ny; b.yB = ny; break; }
+    for (int c0 = 0; c0 < ny; c0 += colTile) {
+        bool any = false;
+        for (int k = c0; k < c0 + colTile && k < ny; k++) any |= (k <= b.yA || k >= b.yB);
+        if (any) b.tiles.push_back(c0);
+    }
+    return b;
 }
 
 static int thickness_count(const qs_params& p) { return (p.slices * p.cellDiv) / p.outputInterval + 1; }
@@ -644,6 +664,7 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
         }
     const int npos = batch->npos;
     if (npos < 1) { set_error("batch has no positions"); return QS_ERR_ARG; }
+    QS_TRY(check_raster(P, *batch, P.detectorNum > 0 && det_images != nullptr));
     QS_CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
     const int nx = P.nx, ny = P.ny, S = P.slices;
@@ -666,8 +687,9 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
             px[i] = std::min(x, P.potNx - nx);
             py[i] = std::min(y, P.potNy - ny);
         }
-        dxp[i] = batch->detPosX ? batch->detPosX[i] : i / P.scanYN;
-        dyp[i] = batch->detPosY ? batch->detPosY[i] : i % P.scanYN;
+        // raster pixels (check_raster: scanYN >= 1 whenever they are used)
+        dxp[i] = batch->detPosX ? batch->detPosX[i] : (P.scanYN > 0 ? i / P.scanYN : 0);
+        dyp[i] = batch->detPosY ? batch->detPosY[i] : (P.scanYN > 0 ? i % P.scanYN : 0);
         if (px[i] < 0 || py[i] < 0 || px[i] > P.potNx - nx || py[i] > P.potNy - ny) {
             set_error("position " + std::to_string(i) + " puts the window outside the potential array");
             return QS_ERR_ARG;
@@ -680,22 +702,9 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
 
     // propagator tables, band, column tiles
     PropTables tb = prop_tables(P);
-    int yA = -1, yB = ny;
-    for (int iy = 0; iy <= ny / 2; iy++) if (tb.ky2[iy] < tb.k2max) yA = iy;
-    for (int iy = ny - 1; iy > ny / 2; iy--) if (tb.ky2[iy] < tb.k2max) yB = iy;
-    bool contiguous = true;
-    for (int iy = 0; iy < ny; iy++) {
-        const bool in = tb.ky2[iy] < tb.k2max;
-        if (in != (iy <= yA || iy >= yB)) contiguous = false;
-    }
-    if (!contiguous) { yA = ny; yB = ny; }
-    const int C = col_tile_width(nx);
-    std::vector<int> tiles;
-    for (int c0 = 0; c0 < ny; c0 += C) {
-        bool any = false;
-        for (int k = c0; k < c0 + C && k < ny; k++) any |= (k <= yA || k >= yB);
-        if (any) tiles.push_back(c0);
-    }
+    const Band band = band_tiles(tb, ny, col_tile_width(nx));
+    const int yA = band.yA, yB = band.yB;
+    const std::vector<int>& tiles = band.tiles;
     const int ntiles = (int)tiles.size();
 
     // the steps of the wave: mulsRepeat2 passes through the cellDiv slabs
@@ -1180,18 +1189,10 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
                 }
                 C.tb = prop_tables(P0);
                 const int ny = P0.ny;
-                C.yA = -1;
-                C.yB = ny;
-                for (int iy = 0; iy <= ny / 2; iy++) if (C.tb.ky2[iy] < C.tb.k2max) C.yA = iy;
-                for (int iy = ny - 1; iy > ny / 2; iy--) if (C.tb.ky2[iy] < C.tb.k2max) C.yB = iy;
-                for (int iy = 0; iy < ny; iy++)
-                    if ((C.tb.ky2[iy] < C.tb.k2max) != (iy <= C.yA || iy >= C.yB)) { C.yA = ny; C.yB = ny; break; }
-                const int Cw = col_tile_width(P0.nx);
-                for (int c0 = 0; c0 < ny; c0 += Cw) {
-                    bool any = false;
-                    for (int q = c0; q < c0 + Cw; q++) any |= (q <= C.yA || q >= C.yB);
-                    if (any) C.tilesH.push_back(c0);
-                }
+                const Band band = band_tiles(C.tb, ny, col_tile_width(P0.nx));
+                C.yA = band.yA;
+                C.yB = band.yB;
+                C.tilesH = band.tiles;
                 QS_CUDA_TRY(cudaMemcpyAsync(C.kx2, C.tb.kx2.data(), sizeof(float) * P0.nx, cudaMemcpyHostToDevice, s));
                 QS_CUDA_TRY(cudaMemcpyAsync(C.ky2, C.tb.ky2.data(), sizeof(float) * ny, cudaMemcpyHostToDevice, s));
                 QS_CUDA_TRY(cudaMemcpyAsync(C.px, C.tb.px.data(), sizeof(float2) * P0.nx, cudaMemcpyHostToDevice, s));
@@ -1438,6 +1439,7 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     for (int a = 0; a < S; a++) lastUse[stepStack[a]] = a;
     auto stackIdx = [&](int a) { return stepStack[a]; };
     if (npos < 1) { set_error("batch has no positions"); return QS_ERR_ARG; }
+    QS_TRY(check_raster(P, *batch, false));
     if (ckpt < 1) {
         // automatic: every state kept when they fit (no recomputation), else
         // the smallest interval whose checkpoints and segment states fit
@@ -1475,18 +1477,10 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
         }
     }
     PropTables tb = prop_tables(P);
-    int yA = -1, yB = ny;
-    for (int iy = 0; iy <= ny / 2; iy++) if (tb.ky2[iy] < tb.k2max) yA = iy;
-    for (int iy = ny - 1; iy > ny / 2; iy--) if (tb.ky2[iy] < tb.k2max) yB = iy;
-    for (int iy = 0; iy < ny; iy++)
-        if ((tb.ky2[iy] < tb.k2max) != (iy <= yA || iy >= yB)) { yA = ny; yB = ny; break; }
     const int C = col_tile_width(nx);
-    std::vector<int> tiles;
-    for (int c0 = 0; c0 < ny; c0 += C) {
-        bool any = false;
-        for (int k = c0; k < c0 + C; k++) any |= (k <= yA || k >= yB);
-        if (any) tiles.push_back(c0);
-    }
+    const Band band = band_tiles(tb, ny, C);
+    const int yA = band.yA, yB = band.yB;
+    const std::vector<int>& tiles = band.tiles;
     const int ntiles = (int)tiles.size();
     std::vector<float2> pxc(tb.px), pyc(tb.py);
     for (auto& v : pxc) v.y = -v.y;

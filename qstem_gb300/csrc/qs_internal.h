@@ -35,6 +35,33 @@ int resident_ctas(const void* func, int threads, size_t bytes, int* ctas, int* s
         if (_rc != QS_OK) return _rc; \
     } while (0)
 
+// ------------------------------------------------- shared host-side checks
+// The checks every entry point makes on qs_params (grid, sampling, energy,
+// slabs, sequence, outputs, detectors).
+int check_params(const qs_params* p);
+// A batch without window offsets or without detector pixels takes them from
+// the scan raster, which then needs scanXN, scanYN >= 1.
+int check_raster(const qs_params& p, const qs_batch& b, bool wantDetPixels);
+// wavelength (stem3/stemutil.cpp:714-725), Angstrom
+double wavelength(double kev);
+
+// propagate_slow's tables (stem3/stemlib.cpp:2783-2824) in the reference's
+// float arithmetic
+struct PropTables {
+    std::vector<float> kx2, ky2;
+    std::vector<float2> px, py;
+    float k2max;
+};
+PropTables prop_tables(const qs_params& p);
+// The ky columns the 2/3 band limit keeps: iy <= yA || iy >= yB (yA = yB = ny
+// when the in-band set is not of that form, so that every column is kept),
+// and the starts of the column tiles of width `colTile` that hold one.
+struct Band {
+    int yA, yB;
+    std::vector<int> tiles;
+};
+Band band_tiles(const PropTables& t, int ny, int colTile);
+
 // ------------------------------------------------------ multislice step
 // Arguments of one row pass (transforms along y, the contiguous index).
 enum RowMode { ROW_FIRST = 0, ROW_MID = 1, ROW_LAST = 2 };

@@ -18,10 +18,17 @@
 // capture.  All calls on a device share the one array and it keeps the
 // previous call's contents: calls whose GPU work overlaps (different streams,
 // or different host threads) race on it and must be serialised by the caller.
+// The stream must belong to the device that is current when the call is made
+// (that device's copy of the array is the one the kernels are given).
+//
+// The call's small tables (twiddles, propagator, k^2, column tiles, window
+// offsets) reach the scratch as kernel arguments of a store kernel, so the
+// work it queues refers to no host memory once it has returned.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -70,31 +77,33 @@ struct Carve {
     }
 };
 
-// The reference's propagator and k^2 tables (propagate_slow,
-// stem3/stemlib.cpp:2783-2824) in its float arithmetic.
-void prop_tables(const qs_params& p, std::vector<float>& kx2, std::vector<float>& ky2, std::vector<float2>& px,
-                 std::vector<float2>& py, float& k2max) {
-    const int nx = p.nx, ny = p.ny;
-    const float ax = p.resolutionX * nx, by = p.resolutionY * ny;
-    const float scale = (float)(p.sliceThickness * 3.14159265358979);
-    const float wavlen = (float)(12.3984244 / std::sqrt(p.v0 * (2 * 510.99906 + p.v0)));
-    kx2.resize(nx); px.resize(nx); ky2.resize(ny); py.resize(ny);
-    for (int i = 0; i < nx; i++) {
-        float k = (i > nx / 2) ? (float)(i - nx) / ax : (float)i / ax;
-        kx2[i] = k * k;
-        float a = scale * (kx2[i] * wavlen);
-        px[i] = make_float2(cosf(a), -sinf(a));
+// Host values carried to the scratch inside a kernel's parameter block
+// (under the 4 KB parameter limit of every launch form), one launch per
+// chunk: the launch copies the values when it is queued.
+constexpr int kBlobWords = 960;
+struct Blob {
+    unsigned n;
+    unsigned w[kBlobWords];
+};
+
+__global__ void blob_store(unsigned* __restrict__ dst, Blob b) {
+    for (unsigned i = threadIdx.x; i < b.n; i += blockDim.x) dst[i] = b.w[i];
+}
+
+// Store `bytes` (a multiple of 4) of host data at device address dst.
+int upload(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    const unsigned char* q = (const unsigned char*)src;
+    unsigned* d = (unsigned*)dst;
+    for (size_t off = 0; off < bytes; off += sizeof(unsigned) * kBlobWords) {
+        Blob b;
+        const size_t chunk = std::min(bytes - off, sizeof(unsigned) * kBlobWords);
+        b.n = (unsigned)(chunk / sizeof(unsigned));
+        std::memcpy(b.w, q + off, chunk);
+        blob_store<<<1, 256, 0, s>>>(d + off / sizeof(unsigned), b);
+        QS_CUDA_TRY(cudaGetLastError());
+        qs::count_launch(1);
     }
-    for (int i = 0; i < ny; i++) {
-        float k = (i > ny / 2) ? (float)(i - ny) / by : (float)i / by;
-        ky2[i] = k * k;
-        float a = scale * (ky2[i] * wavlen);
-        py[i] = make_float2(cosf(a), -sinf(a));
-    }
-    float km = nx / (2.0f * ax);
-    if (ny / (2.0f * by) < km) km = ny / (2.0f * by);
-    km = (float)(2.0 / 3.0 * km);
-    k2max = km * km;
+    return QS_OK;
 }
 
 }  // namespace
@@ -109,11 +118,10 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
         set_error(std::string(fn) + "params, trans, probe and batch are required");
         return QS_ERR_ARG;
     }
+    QS_TRY(check_params(p));
     const qs_params& P = *p;
-    if (P.nx < 1 || P.ny < 1 || P.slices < 1 || P.potNx < P.nx || P.potNy < P.ny || P.outputInterval < 1 ||
-        P.cellDiv != 1 || P.mulsRepeat1 > 1 || P.mulsRepeat2 > 1 || P.detectorNum < 0 ||
-        P.detectorNum > QS_MAX_DETECTORS) {
-        set_error(std::string(fn) + "inconsistent parameters");
+    if (P.cellDiv != 1 || P.mulsRepeat1 > 1 || P.mulsRepeat2 > 1) {
+        set_error(std::string(fn) + "slabs (cellDiv > 1) and stacking sequences other than 1 1 are not supported");
         return QS_ERR_ARG;
     }
     if (!line_supported(P.nx) || !line_supported(P.ny)) {
@@ -130,13 +138,25 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
         set_error(std::string(fn) + "batch has no positions");
         return QS_ERR_ARG;
     }
-    cudaStream_t s = (cudaStream_t)stream_handle;
     const int nx = P.nx, ny = P.ny, S = P.slices;
     const size_t N = (size_t)nx * ny;
     const int nT = (P.slices * P.cellDiv) / P.outputInterval + 1;
     const int ndet = P.detectorNum;
     const int npix = P.scanXN * P.scanYN;
     const bool wantDet = ndet > 0 && det_images != nullptr;
+    QS_TRY(check_raster(P, *batch, wantDet));
+    cudaStream_t s = (cudaStream_t)stream_handle;
+    {
+        // the scratch address handed to the kernels is the current device's
+        int cur = 0, sdev = 0;
+        QS_CUDA_TRY(cudaGetDevice(&cur));
+        QS_CUDA_TRY(cudaStreamGetDevice(s, &sdev));
+        if (sdev != cur) {
+            set_error(std::string(fn) + "the stream belongs to device " + std::to_string(sdev) +
+                      ", the current device is " + std::to_string(cur));
+            return QS_ERR_ARG;
+        }
+    }
 
     // positions, as doSTEM computes them when the batch gives none
     std::vector<int> pos(4 * (size_t)npos);
@@ -152,8 +172,9 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
             px_[i] = std::min(x, P.potNx - nx);
             py_[i] = std::min(y, P.potNy - ny);
         }
-        dx_[i] = batch->detPosX ? batch->detPosX[i] : i / P.scanYN;
-        dy_[i] = batch->detPosY ? batch->detPosY[i] : i % P.scanYN;
+        // raster pixels (check_raster: scanYN >= 1 whenever they are used)
+        dx_[i] = batch->detPosX ? batch->detPosX[i] : (P.scanYN > 0 ? i / P.scanYN : 0);
+        dy_[i] = batch->detPosY ? batch->detPosY[i] : (P.scanYN > 0 ? i % P.scanYN : 0);
         if (px_[i] < 0 || py_[i] < 0 || px_[i] > P.potNx - nx || py_[i] > P.potNy - ny) {
             set_error(std::string(fn) + "position " + std::to_string(i) + " puts the window outside the potential");
             return QS_ERR_ARG;
@@ -164,24 +185,10 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
         }
     }
 
-    // band and column tiles
-    std::vector<float> kx2, ky2;
-    std::vector<float2> pxt, pyt;
-    float k2max = 0;
-    prop_tables(P, kx2, ky2, pxt, pyt, k2max);
-    int yA = -1, yB = ny;
-    for (int iy = 0; iy <= ny / 2; iy++) if (ky2[iy] < k2max) yA = iy;
-    for (int iy = ny - 1; iy > ny / 2; iy--) if (ky2[iy] < k2max) yB = iy;
-    for (int iy = 0; iy < ny; iy++)
-        if ((ky2[iy] < k2max) != (iy <= yA || iy >= yB)) { yA = ny; yB = ny; break; }
-    const int C = col_tile_width(nx);
-    std::vector<int> tiles;
-    for (int c0 = 0; c0 < ny; c0 += C) {
-        bool any = false;
-        for (int k = c0; k < c0 + C && k < ny; k++) any |= (k <= yA || k >= yB);
-        if (any) tiles.push_back(c0);
-    }
-    const int ntiles = (int)tiles.size();
+    // propagator tables, band and column tiles (the same as qs_multislice_run's)
+    const PropTables tb = prop_tables(P);
+    const Band band = band_tiles(tb, ny, col_tile_width(nx));
+    const int ntiles = (int)band.tiles.size();
     std::vector<int> lastWriter(nT, -1), slotOf(S, -1);
     for (int sl = 0; sl < S; sl++) lastWriter[(sl < S * P.cellDiv - 1) ? sl / P.outputInterval : nT - 1] = sl;
     for (int t = 0; t < nT; t++) if (lastWriter[t] >= 0) slotOf[lastWriter[t]] = t;
@@ -189,10 +196,10 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
     // scratch layout; the whole batch must fit
     const size_t partPerT = (size_t)npos * ntiles * std::max(ndet, 1);
     auto rup = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t need = rup(sizeof(float2) * (nx + ny)) + rup(sizeof(float) * (nx + ny)) +
-                        rup(sizeof(float2) * (nx + ny)) + rup(sizeof(int) * std::max(ntiles, 1)) +
-                        rup(sizeof(int) * 4 * (size_t)npos) + rup(sizeof(double) * partPerT * nT) +
-                        rup(sizeof(float2) * N * npos);
+    const size_t need = rup(sizeof(float2) * ny) + rup(sizeof(float2) * nx) + rup(sizeof(float) * nx) +
+                        rup(sizeof(float) * ny) + rup(sizeof(float2) * nx) + rup(sizeof(float2) * ny) +
+                        rup(sizeof(int) * std::max(ntiles, 1)) + rup(sizeof(int) * 4 * (size_t)npos) +
+                        rup(sizeof(double) * partPerT * nT) + rup(sizeof(float2) * N * npos);
     if (need > (size_t)QS_NOALLOC_SCRATCH_BYTES) {
         set_error(std::string(fn) + "this batch needs " + std::to_string(need) + " bytes of scratch; the fixed area holds " +
                   std::to_string((size_t)QS_NOALLOC_SCRATCH_BYTES) + " (split the positions into smaller batches)");
@@ -215,16 +222,14 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
     std::vector<float2> twy, twx;
     QS_TRY(twiddle_host(ny, twy));
     QS_TRY(twiddle_host(nx, twx));
-    // the host vectors are consumed by the copies before these pageable-memory
-    // cudaMemcpyAsync calls return
-    QS_CUDA_TRY(cudaMemcpyAsync(d_tw_y, twy.data(), sizeof(float2) * ny, cudaMemcpyHostToDevice, s));
-    QS_CUDA_TRY(cudaMemcpyAsync(d_tw_x, twx.data(), sizeof(float2) * nx, cudaMemcpyHostToDevice, s));
-    QS_CUDA_TRY(cudaMemcpyAsync(d_kx2, kx2.data(), sizeof(float) * nx, cudaMemcpyHostToDevice, s));
-    QS_CUDA_TRY(cudaMemcpyAsync(d_ky2, ky2.data(), sizeof(float) * ny, cudaMemcpyHostToDevice, s));
-    QS_CUDA_TRY(cudaMemcpyAsync(d_px, pxt.data(), sizeof(float2) * nx, cudaMemcpyHostToDevice, s));
-    QS_CUDA_TRY(cudaMemcpyAsync(d_py, pyt.data(), sizeof(float2) * ny, cudaMemcpyHostToDevice, s));
-    if (ntiles) QS_CUDA_TRY(cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, s));
-    QS_CUDA_TRY(cudaMemcpyAsync(d_pos, pos.data(), sizeof(int) * 4 * (size_t)npos, cudaMemcpyHostToDevice, s));
+    QS_TRY(upload(d_tw_y, twy.data(), sizeof(float2) * ny, s));
+    QS_TRY(upload(d_tw_x, twx.data(), sizeof(float2) * nx, s));
+    QS_TRY(upload(d_kx2, tb.kx2.data(), sizeof(float) * nx, s));
+    QS_TRY(upload(d_ky2, tb.ky2.data(), sizeof(float) * ny, s));
+    QS_TRY(upload(d_px, tb.px.data(), sizeof(float2) * nx, s));
+    QS_TRY(upload(d_py, tb.py.data(), sizeof(float2) * ny, s));
+    if (ntiles) QS_TRY(upload(d_tiles, band.tiles.data(), sizeof(int) * ntiles, s));
+    QS_TRY(upload(d_pos, pos.data(), sizeof(int) * 4 * (size_t)npos, s));
     // the previous call's waves are still in the area: clear them, and the
     // caller's outputs that are only partly written
     QS_CUDA_TRY(cudaMemsetAsync(waves, 0, sizeof(float2) * N * npos, s));
@@ -234,11 +239,11 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
     RowArgs ra{};
     ra.nx = nx; ra.ny = ny; ra.potNx = P.potNx; ra.potNy = P.potNy; ra.nwaves = npos;
     ra.probe = (const float2*)probe_in; ra.waves = waves; ra.exit_waves = (float2*)exit_waves;
-    ra.posX = d_pos; ra.posY = d_pos + npos; ra.tw = d_tw_y; ra.yA = yA; ra.yB = yB;
+    ra.posX = d_pos; ra.posY = d_pos + npos; ra.tw = d_tw_y; ra.yA = band.yA; ra.yB = band.yB;
     ra.norm = (float)(1.0 / (double)(nx * ny));
     ColArgs ca{};
     ca.nx = nx; ca.ny = ny; ca.nwaves = npos; ca.waves = waves; ca.tw = d_tw_x;
-    ca.kx2 = d_kx2; ca.ky2 = d_ky2; ca.px = d_px; ca.py = d_py; ca.k2max = k2max;
+    ca.kx2 = d_kx2; ca.ky2 = d_ky2; ca.px = d_px; ca.py = d_py; ca.k2max = tb.k2max;
     ca.tiles = d_tiles; ca.ntiles = ntiles;
     for (int d = 0; d < ndet; d++) {
         ca.k2in[d] = P.detectors[d].k2Inside;

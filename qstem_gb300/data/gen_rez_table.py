@@ -29,7 +29,13 @@ def parse_tables(text):
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/stem3/scatfactsRez.h"
+    if len(sys.argv) > 1:
+        src = sys.argv[1]
+    elif os.environ.get("QS_REFERENCE_DIR"):
+        src = os.path.join(os.environ["QS_REFERENCE_DIR"], "stem3", "scatfactsRez.h")
+    else:
+        raise SystemExit("usage: gen_rez_table.py <reference>/stem3/scatfactsRez.h "
+                         "(or set QS_REFERENCE_DIR to the reference checkout)")
     with open(src) as f:
         text = f.read()
     n_elem = int(re.search(r"#define\s+N_ELEM\s+(\d+)", text).group(1))

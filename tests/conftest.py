@@ -12,7 +12,8 @@ if ROOT not in sys.path:
 from qstem_gb300 import abi  # noqa: E402
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE = os.environ.get("QS_REFERENCE_DIR", "/root/reference")
+# the reference checkout, for the tests that read its shipped data files
+REFERENCE = os.environ.get("QS_REFERENCE_DIR", "")
 
 
 def pytest_configure(config):

@@ -19,8 +19,8 @@ as compressed .npz files:
   cbed_diffpat  doCBED's diffraction pattern (diffAvg_1.img)
   exit_wave     doTEM's exit wave (wave.img)
 
-Usage: python tests/golden/make_golden.py [case ...]   (needs the reference
-tree; the fixtures are committed so the tests do not)
+Usage: QS_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py [case ...]
+(the fixtures are committed so the tests do not need the reference)
 """
 import json
 import os
@@ -399,6 +399,8 @@ def qsc_run_case(name, case):
 
 
 def main(names=None):
+    if not os.environ.get("QS_REFERENCE_DIR"):
+        raise SystemExit("set QS_REFERENCE_DIR to the reference checkout")
     oracle.build(quiet=False)
     if not names or "qscread" in names:
         qsc_case()

@@ -91,3 +91,22 @@ def test_struct_sizes_and_offsets_match_the_c_compiler(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(ct), cname
         for f in ct._fields_:
             assert got[(cname, f[0])] == getattr(ct, f[0]).offset, (cname, f[0])
+
+
+def test_noalloc_refuses_bad_arguments_before_any_device_work(L):
+    """qs_multislice_run_noalloc checks its arguments on the host before it
+    touches a device: non-positive energy, sampling or slice thickness, and
+    a batch that takes its positions from an empty scan raster, come back as
+    QS_ERR_ARG (no arithmetic on a zero raster size)."""
+    from qstem_gb300 import config
+    p0 = config.make_params(nx=64, resolutionX=0.1, v0=200, slices=4, sliceThickness=2, ax=20, by=20, c=8,
+                            scan=(5, 9, 4, 5, 9, 4), detectors=[(70, 200, "HAADF")])
+    dummy = ctypes.c_void_p(16)  # never dereferenced: the checks fail first
+    for field, value in (("v0", 0.0), ("v0", -200.0), ("resolutionX", 0.0), ("sliceThickness", 0.0),
+                         ("scanYN", 0), ("scanXN", 0)):
+        p = p0.copy()
+        setattr(p, field, value)
+        b = abi.QsBatch(4, None, None, None, None)
+        rc = L.qs_multislice_run_noalloc(None, ctypes.byref(p), dummy, dummy, ctypes.byref(b), dummy, None, None)
+        assert rc == abi.QS_ERR_ARG, (field, value, rc)
+        assert L.qs_last_error()

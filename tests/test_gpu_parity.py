@@ -130,8 +130,12 @@ def sto_case(nx, res, slices, ncell, scan_px, dets, v0=200.0, alpha=20.0, out_ev
 
 
 @pytest.mark.parametrize("nx,res,ncell", [(256, 0.0763, (5, 5, 4)), (128, 0.0915, (4, 4, 4)),
-                                          (384, 0.0763, (7, 7, 3)), (512, 0.07627, (10, 10, 2))])
+                                          (384, 0.0763, (7, 7, 3)), (512, 0.07627, (10, 10, 2)),
+                                          (768, 0.0763, (15, 15, 2)), (1024, 0.0763, (20, 20, 2))])
 def test_larger_grids_vs_oracle(ctx, nx, res, ncell):
+    """Every line length the slice loop has a transform for, radix-3 ones
+    (384 = 8*6*8, 768 = 8*12*8) included, through both passes, the detector
+    sums, the patterns and the exit waves."""
     dets = [(0, 10, "BF"), (10, 25, "LA"), (25, 70, "MA"), (70, 200, "HAADF")]
     p, atoms = sto_case(nx, res, 2 * ncell[2], ncell, 2, dets, out_every=3)
     T = ctx.slices(p, atoms)
