@@ -148,12 +148,14 @@ def adjoint_measure(ctx, torch, reps=3):
     t_adj6, (loss, dV, _) = timed(lambda: ctx.adjoint(p, T, probe, target, ckpt=6))
     t_adj1, _ = timed(lambda: ctx.adjoint(p, T, probe, target, ckpt=1))
     t_adj0, _ = timed(lambda: ctx.adjoint(p, T, probe, target, ckpt=0))
+    t_adjd, _ = timed(lambda: ctx.adjoint(p, T, probe, target, ckpt=6, deterministic=True))
     t_atoms, _ = timed(lambda: ctx.atoms_grad(p, atoms, dV))
     return {"workload": "4D-STEM SrTiO3 6x6x20, 256^2, 40 slices, 32x32 positions, 25 mrad, potential %dx%d"
             % (p.potNx, p.potNy), "positions": npos, "forward_ms": t_fwd, "adjoint_ms": t_adj6,
             "adjoint_over_forward": t_adj6 / t_fwd, "checkpoint_every": 6, "adjoint_ms_all_states": t_adj1,
             "adjoint_over_forward_all_states": t_adj1 / t_fwd, "adjoint_ms_auto": t_adj0,
-            "adjoint_over_forward_auto": t_adj0 / t_fwd, "atoms_grad_ms": t_atoms, "loss": loss,
+            "adjoint_over_forward_auto": t_adj0 / t_fwd, "adjoint_ms_deterministic": t_adjd,
+            "adjoint_over_forward_deterministic": t_adjd / t_fwd, "atoms_grad_ms": t_atoms, "loss": loss,
             "adjoint_definition": "loss + dL/dV for all slices, forward included; forward = diffraction patterns"}
 
 

@@ -77,6 +77,8 @@ extern "C" {
 #define QS_GRAPH 32u            /* qs_multislice_run with device buffers: replay the slice
                                    loop as a CUDA graph (captured on the second call with
                                    the same parameters, buffers and batch) */
+#define QS_DETERMINISTIC 64u    /* qs_adjoint_run: sum dL/dV over positions in a fixed order
+                                   (bit-reproducible, slower) instead of with float atomics */
 
 /* run modes, same numbering as libs/stemtypes_fftw3.h:35-42 */
 #define QS_MODE_STEM 1
@@ -347,7 +349,9 @@ int qs_phase_grating(qs_ctx *ctx, const qs_params *p, const float *V, float *tra
  * A cell divided into slabs (cellDiv > 1) runs through all of them: trans is
  * one stack reused for every slab, whose dL/dV slices then sum the gradient
  * of every use, or with QS_SLAB_STACKS cellDiv stacks back to back and as
- * many dL/dV stacks. */
+ * many dL/dV stacks.  The sum of dL/dV over positions uses float atomics
+ * (the last bits depend on the order the GPU adds in); QS_DETERMINISTIC sums
+ * in a fixed order instead. */
 int qs_adjoint_run(qs_ctx *ctx, const qs_params *p, const float *trans, const float *probe,
                    const qs_batch *batch, const float *target, int ckpt, double *loss, float *dL_dV,
                    float *diffpats, unsigned flags);

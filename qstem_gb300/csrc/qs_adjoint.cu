@@ -115,7 +115,10 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
 }
 
 // ------------------------------------------------------------ row adjoint
-template <int N, bool FIRST>
+// SUM: add g_t = conj(psi) g_phi into the slice's window sum a.gsum with
+// float atomics (vector reductions into an L2-resident potNx x potNy array)
+// instead of storing every position's g_t for the two-kernel gather.
+template <int N, bool FIRST, bool SUM>
 __global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES, adj_min_blocks(N))
     adj_rows(AdjRowArgs a) {
     using Cfg = typename Line<N>::cfg;
@@ -157,13 +160,24 @@ __global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES, adj_min_block
 #pragma unroll
         for (int e = 0; e < E; ++e) psi[e] = cscale(psi[e], a.norm);
     }
-    const float2* tr = a.trans_slice + (size_t)(x + __ldg(a.posX + b)) * a.potNy + __ldg(a.posY + b);
-    float2* gt = a.grad_t + ((size_t)b * a.nx + x) * N;
+    const size_t win = (size_t)(x + __ldg(a.posX + b)) * a.potNy + __ldg(a.posY + b);
+    const float2* tr = a.trans_slice + win;
+    if constexpr (SUM) {
+        float2* gs = a.gsum + win;
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-        const float2 tv = __ldg(tr + t + T * e);
-        gt[t + T * e] = cmulc(g[e], psi[e]);  // conj(psi) g_phi
-        g[e] = cmulc(g[e], tv);               // conj(t) g_phi
+        for (int e = 0; e < E; ++e) {
+            const float2 tv = __ldg(tr + t + T * e);
+            atomicAdd(gs + t + T * e, cmulc(g[e], psi[e]));  // conj(psi) g_phi
+            g[e] = cmulc(g[e], tv);                          // conj(t) g_phi
+        }
+    } else {
+        float2* gt = a.grad_t + ((size_t)b * a.nx + x) * N;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const float2 tv = __ldg(tr + t + T * e);
+            gt[t + T * e] = cmulc(g[e], psi[e]);  // conj(psi) g_phi
+            g[e] = cmulc(g[e], tv);               // conj(t) g_phi
+        }
     }
     if constexpr (!FIRST) {
         line_fft<Cfg, false>(g, sm, s_tw, t);
@@ -221,6 +235,19 @@ __global__ void adj_dv_finish(const float2* __restrict__ partial, int nchunks, i
         // Im(conj(G) t) = gr*t.y - gi*t.x
         const float g = (float)(-2.0 * sigma * (gr * tv.y - gi * tv.x));
         dV[i] = accumulate ? dV[i] + g : g;
+    }
+}
+
+// dL/dV of one slice from the summed windows, and the sum cleared for the
+// next slice's row adjoint.
+__global__ void adj_dv_from_sum(float2* __restrict__ gsum, size_t n, const float2* __restrict__ trans_slice,
+                                float sigma2, int accumulate, float* __restrict__ dV) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 G = gsum[i], tv = trans_slice[i];
+        // Im(conj(G) t) = G.x t.y - G.y t.x
+        const float g = -sigma2 * (G.x * tv.y - G.y * tv.x);
+        dV[i] = accumulate ? dV[i] + g : g;
+        gsum[i] = make_float2(0.f, 0.f);
     }
 }
 
@@ -354,16 +381,21 @@ int launch_adj_last(const AdjLastArgs& a, cudaStream_t s) {
     return QS_ERR_UNSUPPORTED;
 }
 
-template <int N, bool FIRST>
-static int adj_rows_n(const AdjRowArgs& a, cudaStream_t s) {
+template <int N, bool FIRST, bool SUM>
+static int adj_rows_n3(const AdjRowArgs& a, cudaStream_t s) {
     using Cfg = typename Line<N>::cfg;
     const size_t sm = sizeof(float2) * (N + ADJ_ROW_LINES * Cfg::SMEM);
-    QS_TRY(smem_attr((const void*)adj_rows<N, FIRST>, sm));
+    QS_TRY(smem_attr((const void*)adj_rows<N, FIRST, SUM>, sm));
     const long lines = (long)a.nwaves * a.nx;
-    adj_rows<N, FIRST><<<(unsigned)(lines / ADJ_ROW_LINES), dim3(Cfg::T, ADJ_ROW_LINES), sm, s>>>(a);
+    adj_rows<N, FIRST, SUM><<<(unsigned)(lines / ADJ_ROW_LINES), dim3(Cfg::T, ADJ_ROW_LINES), sm, s>>>(a);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;
+}
+
+template <int N, bool FIRST>
+static int adj_rows_n(const AdjRowArgs& a, cudaStream_t s) {
+    return a.gsum ? adj_rows_n3<N, FIRST, true>(a, s) : adj_rows_n3<N, FIRST, false>(a, s);
 }
 
 template <bool FIRST>
@@ -382,7 +414,7 @@ static int adj_rows_any(const AdjRowArgs& a, cudaStream_t s) {
 }
 
 int launch_adj_rows(const AdjRowArgs& a, bool first, cudaStream_t s) {
-    if (!a.grad || !a.grad_t || (first ? !a.probe : !a.state)) {
+    if (!a.grad || !(a.grad_t || a.gsum) || (first ? !a.probe : !a.state)) {
         set_error("adjoint: row pass given a null buffer");
         return QS_ERR_ARG;
     }
@@ -407,6 +439,20 @@ int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, 
                                           accumulate ? 1 : 0, dV);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(2);
+    return QS_OK;
+}
+
+int launch_dv_from_sum(float2* gsum, int potNx, int potNy, const float2* trans_slice, double sigma, float* dV,
+                       bool accumulate, cudaStream_t s) {
+    const size_t n = (size_t)potNx * potNy;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long blocks = std::min<long>((long)sms * 4, (long)((n + 255) / 256));
+    adj_dv_from_sum<<<(unsigned)std::max<long>(blocks, 1), 256, 0, s>>>(gsum, n, trans_slice, (float)(2.0 * sigma),
+                                                                       accumulate ? 1 : 0, dV);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
     return QS_OK;
 }
 

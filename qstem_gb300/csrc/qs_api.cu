@@ -1493,9 +1493,14 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     auto rup = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t small = rup(sizeof(float) * (nx + ny)) + 2 * rup(sizeof(float2) * (nx + ny)) +
                          rup(sizeof(int) * std::max(ntiles, 1)) + rup(sizeof(int) * 2 * npos) + rup(sizeof(double) * nLoss);
-    // work, scratch state, grad, grad_t, checkpoints 1..nseg-1, segment states 1..ckpt-1
-    const size_t nbuf = 4 + (size_t)(nseg - 1) + (size_t)(ckpt - 1);
-    const size_t partBytes = dv_partial_bytes(npos, P.potNx, P.potNy);
+    // dL/dV summed over positions with float atomics into one L2-resident
+    // window sum per slice, or (QS_DETERMINISTIC) every position's g_t kept
+    // and gathered in a fixed order
+    const bool det = (flags & QS_DETERMINISTIC) != 0;
+    // work, scratch state, grad, [grad_t], checkpoints 1..nseg-1, segment states 1..ckpt-1
+    const size_t nbuf = (det ? 4 : 3) + (size_t)(nseg - 1) + (size_t)(ckpt - 1);
+    const size_t partBytes = det ? dv_partial_bytes(npos, P.potNx, P.potNy)
+                                 : sizeof(float2) * (size_t)P.potNx * P.potNy;
     void* base = nullptr;
     QS_TRY(ensure(c, B_ADJ, small + rup(partBytes) + nbuf * rup(waveBytes), &base));
     unsigned char* cur = (unsigned char*)base;
@@ -1513,7 +1518,7 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     float2* work = (float2*)take(waveBytes);
     float2* hscr = (float2*)take(waveBytes);
     float2* grad = (float2*)take(waveBytes);
-    float2* grad_t = (float2*)take(waveBytes);
+    float2* grad_t = det ? (float2*)take(waveBytes) : nullptr;
     std::vector<float2*> ck(nseg, nullptr), seg(ckpt, nullptr);
     for (int k = 1; k < nseg; k++) ck[k] = (float2*)take(waveBytes);
     for (int k = 1; k < ckpt; k++) seg[k] = (float2*)take(waveBytes);
@@ -1530,6 +1535,7 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     QS_CUDA_TRY(cudaMemsetAsync(work, 0, waveBytes, s));
     QS_CUDA_TRY(cudaMemsetAsync(hscr, 0, waveBytes, s));
     QS_CUDA_TRY(cudaMemsetAsync(grad, 0, waveBytes, s));
+    if (!det) QS_CUDA_TRY(cudaMemsetAsync(d_part, 0, partBytes, s));  // the window sum starts at zero
     const float2* tw_y = twiddles(ny);
     const float2* tw_x = twiddles(nx);
     if (!tw_y || !tw_x) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
@@ -1544,18 +1550,26 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     ColArgs ca{};
     ca.nx = nx; ca.ny = ny; ca.nwaves = npos; ca.tw = tw_x; ca.kx2 = d_kx2; ca.ky2 = d_ky2;
     ca.k2max = tb.k2max; ca.tiles = d_tiles; ca.ntiles = ntiles; ca.inverse = 1; ca.ndet = 0;
+    // Segments of ckpt slices, the remainder of S/ckpt first: segment k
+    // starts at segStart[k] (checkpoints every ckpt slices counted back from
+    // the end), so the segment the full run keeps whole -- the last, never
+    // recomputed -- is a full one and the short one is recomputed instead.
+    std::vector<int> segStart(nseg + 1, 0), ckOf(S + 1, -1);
+    for (int k = 1; k < nseg; k++) segStart[k] = S - (nseg - k) * ckpt;
+    segStart[nseg] = S;
+    for (int k = 1; k < nseg; k++) ckOf[segStart[k]] = k;
     // Forward through slices [s0, upto).  The row pass of slice s reads the
     // state h_s (the probe for s = 0) and writes `work`; the column pass reads
     // `work` and writes h_{s+1} straight into the buffer that keeps it, so no
     // state is ever copied.  The full run (full true) keeps the checkpoint
-    // states h_{k*ckpt} in ck[k] and the states of the last segment in seg,
-    // and ends after the last row pass (the last column pass is the loss
+    // states h_{segStart[k]} in ck[k] and the states of the last segment in
+    // seg, and ends after the last row pass (the last column pass is the loss
     // kernel).  A segment recompute writes h_s, s0 < s < upto, into seg.
-    const int lastS0 = (nseg - 1) * ckpt;
+    const int lastS0 = segStart[nseg - 1];
     auto state_of = [&](int sl, int s0) -> float2* {
         if (sl == 0) return nullptr;
         if (sl > s0) return seg[sl - s0];
-        return ck[sl / ckpt];
+        return ck[ckOf[sl]];
     };
     auto forward = [&](int s0, int upto, bool full) -> int {
         ca.px = d_px;
@@ -1571,7 +1585,7 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
             const int nxt = sl + 1;
             float2* dst;
             if (!full || nxt > lastS0) dst = seg[nxt - (full ? lastS0 : s0)];
-            else if (nxt % ckpt == 0) dst = ck[nxt / ckpt];
+            else if (ckOf[nxt] >= 0) dst = ck[ckOf[nxt]];
             else dst = hscr;
             ca.waves = work;
             ca.waves_out = dst;
@@ -1593,10 +1607,11 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     const double sigma = (double)(1.0f + P.v0 / 511.0f) * wavelength(P.v0);
     AdjRowArgs ar{};
     ar.nx = nx; ar.ny = ny; ar.potNx = P.potNx; ar.potNy = P.potNy; ar.nwaves = npos; ar.yA = yA; ar.yB = yB;
-    ar.grad = grad; ar.probe = probe; ar.grad_t = grad_t; ar.posX = d_pos; ar.posY = d_pos + npos; ar.tw = tw_y;
+    ar.grad = grad; ar.probe = probe; ar.grad_t = grad_t; ar.gsum = det ? nullptr : (float2*)d_part;
+    ar.posX = d_pos; ar.posY = d_pos + npos; ar.tw = tw_y;
     ar.norm = (float)(1.0 / (double)N);
     for (int sg = nseg - 1; sg >= 0; sg--) {
-        const int s0 = sg * ckpt, s1 = std::min(S, s0 + ckpt);
+        const int s0 = segStart[sg], s1 = segStart[sg + 1];
         // recompute the segment's states h_s, s0 < s < s1 (the full run kept
         // those of the last segment)
         if (sg < nseg - 1 && s1 - s0 > 1) QS_TRY(forward(s0, s1, false));
@@ -1614,9 +1629,14 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
             QS_TRY(launch_adj_rows(ar, sl == 0, s));
             // a reused stack's slice collects the gradient of every use; the
             // backward meets its last use first
-            QS_TRY(launch_dv_gather(grad_t, npos, nx, ny, P.potNx, P.potNy, d_pos, d_pos + npos,
-                                    trans + (size_t)stackIdx(sl) * sliceElems, sigma, d_part,
-                                    dL_dV + (size_t)stackIdx(sl) * sliceElems, sl != lastUse[stackIdx(sl)], s));
+            const float2* tsl = trans + (size_t)stackIdx(sl) * sliceElems;
+            float* dvs = dL_dV + (size_t)stackIdx(sl) * sliceElems;
+            const bool acc = sl != lastUse[stackIdx(sl)];
+            if (det)
+                QS_TRY(launch_dv_gather(grad_t, npos, nx, ny, P.potNx, P.potNy, d_pos, d_pos + npos, tsl, sigma,
+                                        d_part, dvs, acc, s));
+            else
+                QS_TRY(launch_dv_from_sum((float2*)d_part, P.potNx, P.potNy, tsl, sigma, dvs, acc, s));
         }
     }
     if (loss) {

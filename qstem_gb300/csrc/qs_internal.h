@@ -177,7 +177,9 @@ struct AdjRowArgs {
     const float2* state;         // h of this slice (not read for the first slice)
     const float2* probe;         // first slice
     const float2* trans_slice;
-    float2* grad_t;              // out: conj(psi) g_phi, [nwaves][nx][ny]
+    float2* grad_t;              // out: conj(psi) g_phi, [nwaves][nx][ny] (gsum == nullptr)
+    float2* gsum;                // or: conj(psi) g_phi added into its window of this
+                                 // potNx x potNy sum (float atomics, any order)
     const int *posX, *posY;
     const float2* tw;            // twiddles of the length-ny transform
     float norm;
@@ -191,6 +193,10 @@ int launch_dv_gather(const float2* grad_t, int npos, int nx, int ny, int potNx, 
                      const int* posY, const float2* trans_slice, double sigma, void* partial, float* dV,
                      bool accumulate,
                      cudaStream_t s);
+// dL/dV of one slice from the summed windows G (gsum of the row adjoint):
+// dV (=|+=) -2 sigma Im(conj(G) t), and G cleared for the next slice
+int launch_dv_from_sum(float2* gsum, int potNx, int potNy, const float2* trans_slice, double sigma, float* dV,
+                       bool accumulate, cudaStream_t s);
 int launch_atoms_grad(const AtomJob* d_jobs, int njobs, const float* const* d_luts, int Nz, int Nr, int nzSub,
                       const qs_params& p, const float* dV, double* grad, cudaStream_t s);
 int launch_grating_from_real(const float* V, float2* trans, size_t n, double scale, cudaStream_t s);

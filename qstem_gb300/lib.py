@@ -270,12 +270,15 @@ class Context:
         _check(self.lib.qs_phase_grating(self.h, ctypes.byref(p), _ptr(V), _ptr(out), abi.QS_SYNC))
         return out
 
-    def adjoint(self, p, trans, probe, target, positions=None, ckpt=0, want_diffpats=False, slab_stacks=False):
+    def adjoint(self, p, trans, probe, target, positions=None, ckpt=0, want_diffpats=False, slab_stacks=False,
+                deterministic=False):
         """Loss sum (I - target)^2 and dL/dV (device torch tensors in and out).
         ckpt: keep the forward waves every ckpt slices (1: all; 0: all when
         they fit in device memory, else the smallest interval that fits).
         slab_stacks: trans holds one stack per slab of a cell divided into
-        cellDiv slabs (dL/dV then too); else one stack serves every slab."""
+        cellDiv slabs (dL/dV then too); else one stack serves every slab.
+        deterministic: sum dL/dV over positions in a fixed order
+        (QS_DETERMINISTIC; bit-reproducible) instead of with float atomics."""
         import torch
         bx, keep = _batch(p, positions)
         nst = p.cellDiv if (slab_stacks and p.cellDiv > 1) else 1
@@ -284,7 +287,8 @@ class Context:
         loss = ctypes.c_double()
         _check(self.lib.qs_adjoint_run(self.h, ctypes.byref(p), _ptr(trans), _ptr(probe), ctypes.byref(bx),
                                        _ptr(target), int(ckpt), ctypes.byref(loss), _ptr(dV), _ptr(dps),
-                                       abi.QS_SYNC | (abi.QS_SLAB_STACKS if slab_stacks else 0)))
+                                       abi.QS_SYNC | (abi.QS_SLAB_STACKS if slab_stacks else 0) |
+                                       (abi.QS_DETERMINISTIC if deterministic else 0)))
         del keep
         return loss.value, dV, dps
 
