@@ -49,7 +49,7 @@ constexpr int adj_min_blocks(int n) {
 template <int N>
 __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
     adj_last_cols(AdjLastArgs a) {
-    using Cfg = typename Line<N>::cfg;
+    using Cfg = typename LineCol<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();
     constexpr int NT = C * T;
     constexpr int NWARPS = (NT + 31) / 32;
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(256) atoms_grad(const AtomJob* __restrict__ jo
 // --------------------------------------------------------------- launchers
 template <int N>
 static int last_n(const AdjLastArgs& a, cudaStream_t s) {
-    using Cfg = typename Line<N>::cfg;
+    using Cfg = typename LineCol<N>::cfg;
     constexpr int C = col_tile<N>();
     const size_t sm = sizeof(float2) * (N + (size_t)N * C);
     QS_TRY(smem_attr((const void*)adj_last_cols<N>, sm));

@@ -828,7 +828,7 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
         ew_dev = (float2*)d;
     }
     const float2* tw_y = twiddles(ny);
-    const float2* tw_x = twiddles(nx);
+    const float2* tw_x = twiddles(nx, true);
     if (!tw_y || !tw_x) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
     const double scaleDet = (double)P.electronScale / ((double)(nx * ny) * (double)(nx * ny));
 
@@ -1202,7 +1202,7 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
                                                 cudaMemcpyHostToDevice, s));
                 QS_CUDA_TRY(cudaMemsetAsync(C.zeros, 0, sizeof(int) * (P0.ny + nb), s));
                 QS_CUDA_TRY(cudaMemsetAsync(C.dp, 0, sizeof(float) * N * nb, s));
-                if (!twiddles(P0.nx) || !twiddles(P0.ny)) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
+                if (!twiddles(P0.nx, true) || !twiddles(P0.ny)) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
             }
             QS_CUDA_TRY(cudaEventRecord(evs[nstreams], s));
             // 2. the units' scans, concurrently on the side streams
@@ -1222,7 +1222,7 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
                 ra.waves = C.waves; ra.posX = C.zeros; ra.posY = C.zeros; ra.tw = twiddles(ny);
                 ra.yA = C.yA; ra.yB = C.yB; ra.norm = (float)(1.0 / (double)N);
                 ColArgs ca{};
-                ca.nx = nx; ca.ny = ny; ca.tw = twiddles(nx); ca.kx2 = C.kx2; ca.ky2 = C.ky2; ca.px = C.px;
+                ca.nx = nx; ca.ny = ny; ca.tw = twiddles(nx, true); ca.kx2 = C.kx2; ca.ky2 = C.ky2; ca.px = C.px;
                 ca.py = C.py; ca.k2max = C.tb.k2max; ca.tiles = C.tiles; ca.ntiles = (int)C.tilesH.size();
                 ca.scaleDiff = 1.0 / std::sqrt((double)N);
                 for (int sl = 0; sl < u.smax; sl++) {
@@ -1537,7 +1537,7 @@ int qs_adjoint_run(qs_ctx* c, const qs_params* p, const float* trans_in, const f
     QS_CUDA_TRY(cudaMemsetAsync(grad, 0, waveBytes, s));
     if (!det) QS_CUDA_TRY(cudaMemsetAsync(d_part, 0, partBytes, s));  // the window sum starts at zero
     const float2* tw_y = twiddles(ny);
-    const float2* tw_x = twiddles(nx);
+    const float2* tw_x = twiddles(nx, true);
     if (!tw_y || !tw_x) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
     const float2* trans = (const float2*)trans_in;
     const float2* probe = (const float2*)probe_in;

@@ -26,6 +26,8 @@
 #include <type_traits>
 #include <utility>
 
+#include "qs_tuned.h"
+
 namespace qs {
 
 // ---------------------------------------------------------------- complex
@@ -328,22 +330,56 @@ __host__ __device__ constexpr bool always_out_of_band(int e) {
 }
 
 // ------------------------------------------------------- size dispatching
-// One configuration per supported line length.
+// One configuration per supported line length.  Where several
+// factorisations fit the thread layout (each radix must divide E = N/T), the
+// row transforms (Line) and the column transforms (LineCol) pick one each:
+// QS_RADIX_ROW_<N> and QS_RADIX_COL_<N> in qs_tuned.h index the lists below.
+template <int... Rs>
+using rad_t = radices<Rs...>;
+template <int I, class... Alts>
+struct pick;
+template <class A, class... Rest>
+struct pick<0, A, Rest...> { using type = A; };
+template <int I, class A, class... Rest>
+struct pick<I, A, Rest...> { using type = typename pick<I - 1, Rest...>::type; };
+template <int I>
+using Rad384 = typename pick<I, rad_t<8, 6, 8>, rad_t<6, 8, 8>, rad_t<8, 8, 6>, rad_t<12, 4, 8>, rad_t<24, 4, 4>>::type;
+template <int I>
+using Rad512 = typename pick<I, rad_t<32, 16>, rad_t<16, 32>>::type;
+template <int I>
+using Rad768 = typename pick<I, rad_t<8, 12, 8>, rad_t<12, 8, 8>, rad_t<8, 8, 12>, rad_t<24, 4, 8>, rad_t<24, 8, 4>>::type;
+template <int I>
+using Rad1024 = typename pick<I, rad_t<32, 32>, rad_t<8, 16, 8>>::type;
+
+// (the product kernels size __launch_bounds__ with line_threads(N))
 template <int N>
 struct Line;
-// (the product kernels size __launch_bounds__ with line_threads(N))
 template <> struct Line<64> { using cfg = LineCfg<64, 8, radices<8, 8>>; };
 template <> struct Line<128> { using cfg = LineCfg<128, 8, radices<16, 8>>; };
 template <> struct Line<256> { using cfg = LineCfg<256, 16, radices<16, 16>>; };
-template <> struct Line<384> { using cfg = LineCfg<384, 16, radices<8, 6, 8>>; };
-template <> struct Line<512> { using cfg = LineCfg<512, 16, radices<32, 16>>; };
-template <> struct Line<768> { using cfg = LineCfg<768, 32, radices<8, 12, 8>>; };
-template <> struct Line<1024> { using cfg = LineCfg<1024, 32, radices<32, 32>>; };
+template <> struct Line<384> { using cfg = LineCfg<384, 16, Rad384<QS_RADIX_ROW_384>>; };
+template <> struct Line<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_ROW_512>>; };
+template <> struct Line<768> { using cfg = LineCfg<768, 32, Rad768<QS_RADIX_ROW_768>>; };
+template <> struct Line<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_ROW_1024>>; };
+// column transforms
+template <int N>
+struct LineCol { using cfg = typename Line<N>::cfg; };
+template <> struct LineCol<384> { using cfg = LineCfg<384, 16, Rad384<QS_RADIX_COL_384>>; };
+template <> struct LineCol<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_COL_512>>; };
+template <> struct LineCol<768> { using cfg = LineCfg<768, 32, Rad768<QS_RADIX_COL_768>>; };
+template <> struct LineCol<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_COL_1024>>; };
 
-// columns per column-pass tile (128-byte row segments; 64 bytes from 768 up)
+// columns per column-pass tile (qs_tuned.h: 16 = 128-byte row segments)
 template <int N>
 constexpr int col_tile() {
-    return N >= 768 ? 8 : 16;
+    return N == 64     ? QS_COL_TILE_64
+           : N == 128  ? QS_COL_TILE_128
+           : N == 256  ? QS_COL_TILE_256
+           : N == 384  ? QS_COL_TILE_384
+           : N == 512  ? QS_COL_TILE_512
+           : N == 768  ? QS_COL_TILE_768
+           : N == 1024 ? QS_COL_TILE_1024
+                       : 8;
 }
 
 template <int N>

@@ -121,11 +121,12 @@ int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2,
 // n0 x n1 arrays
 int dft2d(float2* data, int n0, int n1, int howmany, bool inverse, float2* scratch, int scratch_slices,
           cudaStream_t s);
-// inter-pass twiddle table of the length-n line transform (per-pass layout of
-// LineCfg), device-resident and cached per device and n; twiddle_host fills
-// the same table on the host
-const float2* twiddles(int n);
-int twiddle_host(int n, std::vector<float2>& h);
+// inter-pass twiddle table of the length-n row (col = false) or column
+// (col = true) line transform (per-pass layout of LineCfg), device-resident
+// and cached per device, n and kind; twiddle_host fills the same table on the
+// host
+const float2* twiddles(int n, bool col = false);
+int twiddle_host(int n, std::vector<float2>& h, bool col = false);
 
 // ---------------------------------------------------------- potentials
 struct LutTable {

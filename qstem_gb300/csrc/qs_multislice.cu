@@ -56,6 +56,18 @@ constexpr int row_min_blocks(int n) {
                        : 1;
 }
 
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+
+// Shared memory of the row pass: the twiddle table (N float2) and one padded
+// exchange line per line transform.
 template <int N, int MODE>
 __global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks(N))
     ms_rows(RowArgs a) {
@@ -109,16 +121,6 @@ __global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks
     }
 }
 
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int PENDING>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
-}
-
 // Column pass, persistent: each CTA walks the (wave, column tile) work items
 // blockIdx.x, blockIdx.x + gridDim.x, ...  While one tile is transformed, the
 // next one is copied into the other shared-memory stage with cp.async; once a
@@ -136,16 +138,30 @@ constexpr int col_min_blocks(int n) {
                        : 1;
 }
 
+// shared-memory tile stages of the column pass (qs_tuned.h)
+constexpr int col_stages(int n) {
+    return n == 64     ? QS_COL_STAGES_64
+           : n == 128  ? QS_COL_STAGES_128
+           : n == 256  ? QS_COL_STAGES_256
+           : n == 384  ? QS_COL_STAGES_384
+           : n == 512  ? QS_COL_STAGES_512
+           : n == 768  ? QS_COL_STAGES_768
+           : n == 1024 ? QS_COL_STAGES_1024
+                       : 2;
+}
+
 template <int N, bool DET, bool INVERSE>
 __global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_blocks(N))
     ms_cols(ColArgs a, long nitems) {
-    using Cfg = typename Line<N>::cfg;
+    using Cfg = typename LineCol<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();
     constexpr int NT = C * T;
     constexpr int NWARPS = (NT + 31) / 32;
+    constexpr int STAGES = col_stages(N);
+    static_assert(STAGES == 1 || STAGES == 2, "one or two tile stages");
     extern __shared__ float2 dsm[];
     float2* s_tw = dsm;
-    float2* s_stage = dsm + N;  // two stages of N*C
+    float2* s_stage = dsm + N;  // STAGES stages of N*C
     __shared__ double s_det[QS_MAX_DETECTORS][NWARPS];
     const int tid = threadIdx.x + C * threadIdx.y;
     const int c = threadIdx.x, t = threadIdx.y;
@@ -170,9 +186,14 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_block
     prefetch(item, 0);
     __syncthreads();
     for (int it = 0; item < nitems; ++it, item += gridDim.x) {
-        prefetch(item + gridDim.x, (it + 1) & 1);
-        cp_async_wait<1>();
-        float2* stage = s_stage + (it & 1) * N * C;
+        // every thread reads back only the elements it copied itself
+        if constexpr (STAGES == 2) {
+            prefetch(item + gridDim.x, (it + 1) & 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        float2* stage = s_stage + (STAGES == 2 ? (it & 1) : 0) * N * C;
         float2 reg[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) reg[e] = stage[(t + T * e) * C + c];
@@ -240,6 +261,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_block
             for (int e = 0; e < E; ++e) col[(size_t)(t + T * e) * a.ny] = reg[e];
         }
         __syncthreads();  // scratch and s_det reads done before the stage is refilled
+        if constexpr (STAGES == 1) prefetch(item + gridDim.x, 0);
     }
     cp_async_wait<0>();
 }
@@ -301,7 +323,7 @@ static size_t row_smem(int lines = row_lines(N)) {
 }
 template <int N>
 static size_t col_smem() {
-    return sizeof(float2) * (N + 2 * (size_t)N * col_tile<N>());
+    return sizeof(float2) * (N + (size_t)col_stages(N) * N * col_tile<N>());
 }
 template <int N>
 static size_t col_smem_plain() {
@@ -352,7 +374,7 @@ int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s) {
 
 template <int N, bool DET, bool INV>
 static int cols_n3(const ColArgs& a, cudaStream_t s) {
-    using Cfg = typename Line<N>::cfg;
+    using Cfg = typename LineCol<N>::cfg;
     const size_t sm = col_smem<N>();
     int resident = 0, sms = 0;  // CTAs per SM (occupancy calculator), SMs
     QS_TRY(resident_ctas((const void*)ms_cols<N, DET, INV>, col_tile<N>() * Cfg::T, sm, &resident, &sms));
@@ -395,7 +417,18 @@ int launch_cols(const ColArgs& a, cudaStream_t s) {
     return QS_ERR_UNSUPPORTED;
 }
 
-int col_tile_width(int nx) { return nx >= 768 ? 8 : 16; }
+int col_tile_width(int nx) {
+    switch (nx) {
+        case 64: return col_tile<64>();
+        case 128: return col_tile<128>();
+        case 256: return col_tile<256>();
+        case 384: return col_tile<384>();
+        case 512: return col_tile<512>();
+        case 768: return col_tile<768>();
+        case 1024: return col_tile<1024>();
+    }
+    return 8;
+}
 
 int launch_det_finalize(const double* partial, int nwaves, int ntiles, int ndet, double scale,
                         const int* detPosX, const int* detPosY, int scanYN, int npix, float* det_out,
@@ -438,7 +471,7 @@ template <int N, bool INV>
 __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
     fft_cols(float2* data, int ncols, const float2* tw) {
     // columns of length N, row stride ncols; blockIdx.y = array index
-    using Cfg = typename Line<N>::cfg;
+    using Cfg = typename LineCol<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();
     extern __shared__ float2 dsm[];
     float2* s_tw = dsm;
@@ -476,9 +509,9 @@ static int fft_cols_n(float2* data, int ncols, int howmany, cudaStream_t s) {
     const size_t sm = col_smem_plain<N>();
     QS_TRY(smem_attr((const void*)fft_cols<N, INV>, sm));
     constexpr int C = col_tile<N>();
-    dim3 block(C, Line<N>::cfg::T);
+    dim3 block(C, LineCol<N>::cfg::T);
     dim3 grid((ncols + C - 1) / C, howmany);
-    fft_cols<N, INV><<<grid, block, sm, s>>>(data, ncols, twiddles(N));
+    fft_cols<N, INV><<<grid, block, sm, s>>>(data, ncols, twiddles(N, true));
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;
@@ -543,7 +576,7 @@ int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2,
         set_error("band limit: size " + std::to_string(n0) + "x" + std::to_string(n1) + " not supported");
         return QS_ERR_UNSUPPORTED;
     }
-    const float2* tw = twiddles(n0);
+    const float2* tw = twiddles(n0, true);
     if (!tw || !twiddles(n1)) {
         set_error("twiddle table allocation failed");
         return QS_ERR_NOMEM;
@@ -571,10 +604,10 @@ int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2,
     return QS_OK;
 }
 
-template <int N>
+template <class Cfg>
 static void fill_twiddles(std::vector<float2>& h) {
-    using Cfg = typename Line<N>::cfg;
     using RAD = typename Cfg::rad;
+    constexpr int N = Cfg::N;
     h.assign(N, make_float2(0.f, 0.f));
     for (int p = 1; p < Cfg::PASSES; ++p) {
         const int R = RAD::at(p), Ns = RAD::prefix(p), off = Cfg::tw_offset(p);
@@ -589,31 +622,37 @@ static void fill_twiddles(std::vector<float2>& h) {
     }
 }
 
-int twiddle_host(int n, std::vector<float2>& h) {
+template <int N>
+static void fill_kind(std::vector<float2>& h, bool col) {
+    if (col) fill_twiddles<typename LineCol<N>::cfg>(h);
+    else fill_twiddles<typename Line<N>::cfg>(h);
+}
+
+int twiddle_host(int n, std::vector<float2>& h, bool col) {
     switch (n) {
-        case 64: fill_twiddles<64>(h); return QS_OK;
-        case 128: fill_twiddles<128>(h); return QS_OK;
-        case 256: fill_twiddles<256>(h); return QS_OK;
-        case 384: fill_twiddles<384>(h); return QS_OK;
-        case 512: fill_twiddles<512>(h); return QS_OK;
-        case 768: fill_twiddles<768>(h); return QS_OK;
-        case 1024: fill_twiddles<1024>(h); return QS_OK;
+        case 64: fill_kind<64>(h, col); return QS_OK;
+        case 128: fill_kind<128>(h, col); return QS_OK;
+        case 256: fill_kind<256>(h, col); return QS_OK;
+        case 384: fill_kind<384>(h, col); return QS_OK;
+        case 512: fill_kind<512>(h, col); return QS_OK;
+        case 768: fill_kind<768>(h, col); return QS_OK;
+        case 1024: fill_kind<1024>(h, col); return QS_OK;
     }
     set_error("no line transform of length " + std::to_string(n));
     return QS_ERR_UNSUPPORTED;
 }
 
-const float2* twiddles(int n) {
+const float2* twiddles(int n, bool col) {
     static std::mutex mu;
-    static std::map<std::pair<int, int>, float2*> cache;
+    static std::map<std::tuple<int, int, bool>, float2*> cache;
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(mu);
-    auto key = std::make_pair(dev, n);
+    auto key = std::make_tuple(dev, n, col);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
     std::vector<float2> h;
-    if (twiddle_host(n, h) != QS_OK) return nullptr;
+    if (twiddle_host(n, h, col) != QS_OK) return nullptr;
     float2* d = nullptr;
     if (cudaMalloc(&d, sizeof(float2) * n) != cudaSuccess) return nullptr;
     cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);

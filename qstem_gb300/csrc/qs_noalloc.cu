@@ -221,7 +221,7 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
 
     std::vector<float2> twy, twx;
     QS_TRY(twiddle_host(ny, twy));
-    QS_TRY(twiddle_host(nx, twx));
+    QS_TRY(twiddle_host(nx, twx, true));
     QS_TRY(upload(d_tw_y, twy.data(), sizeof(float2) * ny, s));
     QS_TRY(upload(d_tw_x, twx.data(), sizeof(float2) * nx, s));
     QS_TRY(upload(d_kx2, tb.kx2.data(), sizeof(float) * nx, s));

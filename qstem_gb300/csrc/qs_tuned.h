@@ -9,10 +9,12 @@
 // overridden with -D at build time.
 //
 // The tables below are the output of
-//   python -m qstem_gb300.tune --candidates 1,2,3,4,6,8 --lines 4,8 --sizes 256,384,512,768,1024
-// (the row adjoint's 5 at 256^2 from a sweep with 5 among the candidates)
-// on GB300 (it prints the whole sweep).  For the column pass a stated 1 (the compiler may use up to 255 registers) differs
-// from leaving the bound open, and measured faster at 384^2 and 768^2.
+//   python -m qstem_gb300.tune --write
+// (candidates 1,2,3,4,6,8, row shapes of 4 and 8 lines, sizes 256-1024) on
+// GB300: phase 0 picked the factorisations and column tiles, phase 1 the
+// row-pass shapes and the budgets of both passes, phase 2 the row adjoint's
+// budget (it prints the whole sweep).  For the column pass a stated 1 (the
+// compiler may use up to 255 registers) differs from leaving the bound open.
 #pragma once
 
 #ifndef QS_ROW_MIN_BLOCKS_64
@@ -31,7 +33,7 @@
 #define QS_ROW_MIN_BLOCKS_512 3
 #endif
 #ifndef QS_ROW_MIN_BLOCKS_768
-#define QS_ROW_MIN_BLOCKS_768 3
+#define QS_ROW_MIN_BLOCKS_768 4
 #endif
 #ifndef QS_ROW_MIN_BLOCKS_1024
 #define QS_ROW_MIN_BLOCKS_1024 4
@@ -46,7 +48,7 @@
 #define QS_COL_MIN_BLOCKS_256 2
 #endif
 #ifndef QS_COL_MIN_BLOCKS_384
-#define QS_COL_MIN_BLOCKS_384 1
+#define QS_COL_MIN_BLOCKS_384 4
 #endif
 #ifndef QS_COL_MIN_BLOCKS_512
 #define QS_COL_MIN_BLOCKS_512 2
@@ -64,7 +66,7 @@
 #define QS_ADJ_MIN_BLOCKS_128 1
 #endif
 #ifndef QS_ADJ_MIN_BLOCKS_256
-#define QS_ADJ_MIN_BLOCKS_256 5
+#define QS_ADJ_MIN_BLOCKS_256 4
 #endif
 #ifndef QS_ADJ_MIN_BLOCKS_384
 #define QS_ADJ_MIN_BLOCKS_384 3
@@ -98,4 +100,82 @@
 #endif
 #ifndef QS_ROW_LINES_1024
 #define QS_ROW_LINES_1024 4
+#endif
+
+// QS_COL_TILE_<N>: columns per column-pass tile (8 or 16; with two stages
+// the 16-column tile fits in shared memory only up to 768).
+#ifndef QS_COL_TILE_64
+#define QS_COL_TILE_64 16
+#endif
+#ifndef QS_COL_TILE_128
+#define QS_COL_TILE_128 16
+#endif
+#ifndef QS_COL_TILE_256
+#define QS_COL_TILE_256 16
+#endif
+#ifndef QS_COL_TILE_384
+#define QS_COL_TILE_384 8
+#endif
+#ifndef QS_COL_TILE_512
+#define QS_COL_TILE_512 16
+#endif
+#ifndef QS_COL_TILE_768
+#define QS_COL_TILE_768 16
+#endif
+#ifndef QS_COL_TILE_1024
+#define QS_COL_TILE_1024 8
+#endif
+
+// QS_COL_STAGES_<N>: shared-memory tile stages of the column pass: 2 copies
+// the next tile with cp.async while one is transformed, 1 leaves the overlap
+// to other CTAs (half the shared memory per CTA).
+#ifndef QS_COL_STAGES_64
+#define QS_COL_STAGES_64 2
+#endif
+#ifndef QS_COL_STAGES_128
+#define QS_COL_STAGES_128 2
+#endif
+#ifndef QS_COL_STAGES_256
+#define QS_COL_STAGES_256 2
+#endif
+#ifndef QS_COL_STAGES_384
+#define QS_COL_STAGES_384 1
+#endif
+#ifndef QS_COL_STAGES_512
+#define QS_COL_STAGES_512 2
+#endif
+#ifndef QS_COL_STAGES_768
+#define QS_COL_STAGES_768 1
+#endif
+#ifndef QS_COL_STAGES_1024
+#define QS_COL_STAGES_1024 1
+#endif
+
+// QS_RADIX_ROW_<N>, QS_RADIX_COL_<N>: which factorisation of the row and of
+// the column line transform (the lists of Line / LineCol in qs_fft.cuh;
+// 0 = the first).  Every translation unit must be compiled with the same
+// choice (the twiddle tables follow it).
+#ifndef QS_RADIX_ROW_384
+#define QS_RADIX_ROW_384 4
+#endif
+#ifndef QS_RADIX_ROW_512
+#define QS_RADIX_ROW_512 0
+#endif
+#ifndef QS_RADIX_ROW_768
+#define QS_RADIX_ROW_768 3
+#endif
+#ifndef QS_RADIX_ROW_1024
+#define QS_RADIX_ROW_1024 0
+#endif
+#ifndef QS_RADIX_COL_384
+#define QS_RADIX_COL_384 0
+#endif
+#ifndef QS_RADIX_COL_512
+#define QS_RADIX_COL_512 0
+#endif
+#ifndef QS_RADIX_COL_768
+#define QS_RADIX_COL_768 0
+#endif
+#ifndef QS_RADIX_COL_1024
+#define QS_RADIX_COL_1024 0
 #endif

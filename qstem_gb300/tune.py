@@ -1,7 +1,15 @@
-"""Autotune the register budget (CTAs per SM) of the slice-loop kernels per
-line length.
+"""Autotune the slice-loop kernels per line length: the factorisation of the
+row and of the column transforms, the column-pass tile, the row-pass shape
+and the register budgets (CTAs per SM).
 
     python -m qstem_gb300.tune [--candidates 1,2,3,4,6,8] [--sizes 256,384,...] [--write]
+
+Phase 0, factorisations and tiles: variant k compiles every line length
+with its k-th factorisation (QS_RADIX_ROW_<N> = QS_RADIX_COL_<N> = k, where
+that length has a k-th one; qs_fft.cuh lists them), plus one variant with
+16-column tiles wherever the double-buffered tile fits (QS_COL_TILE_<N>);
+the row transform keeps the factorisation with the fastest row pass, the
+column transform the one with the fastest column pass, independently.
 
 Phase 1, row and column passes: for each candidate budget k and row-pass
 shape L (line transforms per CTA, --lines) the slice-loop translation unit
@@ -31,6 +39,10 @@ from . import build as _build
 
 SIZES = (256, 384, 512, 768, 1024)
 WAVES = {64: 2048, 128: 2048, 256: 1024, 384: 512, 512: 512, 768: 192, 1024: 128}
+# factorisations per line length (the lists of qs_fft.cuh's Line / LineCol)
+RADIX_ALTS = {384: 5, 512: 2, 768: 5, 1024: 2}
+# lengths whose double-buffered 16-column tile fits in shared memory
+TILE16 = (64, 128, 256, 384, 512, 768)
 
 
 def _variant(tag, source, defs, tmp, extra_objs=()):
@@ -123,18 +135,55 @@ def measure_adjoint(lib_path, sizes, reps=3):
     return out
 
 
+MACRO = {"LINES": "QS_ROW_LINES_%d", "RROW": "QS_RADIX_ROW_%d", "RCOL": "QS_RADIX_COL_%d",
+         "TILE": "QS_COL_TILE_%d", "STAGES": "QS_COL_STAGES_%d"}
+
+
 def write_table(best):
-    """Store the chosen values ({("ROW"|"COL"|"ADJ"|"LINES", N): k}) as the
-    defaults of csrc/qs_tuned.h."""
+    """Store the chosen values ({(kind, N): k}, kind one of ROW, COL, ADJ
+    (register budgets), LINES, RROW, RCOL, TILE, STAGES) as the defaults of
+    csrc/qs_tuned.h."""
     path = os.path.join(_build.SRC, "qs_tuned.h")
     lines = open(path).read().split("\n")
     for i, line in enumerate(lines):
         for (kind, n), k in best.items():
-            name = "QS_ROW_LINES_%d" % n if kind == "LINES" else "QS_%s_MIN_BLOCKS_%d" % (kind, n)
+            name = (MACRO[kind] if kind in MACRO else "QS_" + kind + "_MIN_BLOCKS_%d") % n
             if line.startswith("#define %s " % name):
                 lines[i] = "#define %s %d" % (name, k)
     with open(path, "w") as f:
         f.write("\n".join(lines))
+
+
+def tune_factorisations(sizes, tmp):
+    """Phase 0: {("RROW"|"RCOL"|"TILE"|"STAGES", N): choice} and the defines fixing them."""
+    nalt = max([RADIX_ALTS.get(n, 1) for n in sizes])
+    variants = {"r%d" % k: ["QS_RADIX_ROW_%d=%d" % (n, k) for n in sizes if k < RADIX_ALTS.get(n, 1)] +
+                ["QS_RADIX_COL_%d=%d" % (n, k) for n in sizes if k < RADIX_ALTS.get(n, 1)] for k in range(nalt)}
+    # column tiles: (columns, stages); a double-buffered 16-column tile only
+    # where it fits
+    tiles = {"t8s2": (8, 2), "t16s2": (16, 2), "t8s1": (8, 1), "t16s1": (16, 1)}
+    for v, (c, st) in tiles.items():
+        variants[v] = ["QS_COL_TILE_%d=%d" % (n, c if (st == 1 or c == 8 or n in TILE16) else 8) for n in sizes] + \
+                      ["QS_COL_STAGES_%d=%d" % (n, st) for n in sizes]
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(variants)) as ex:
+        libs = dict(zip(variants, ex.map(lambda v: _variant(v, "qs_multislice.cu", variants[v], tmp)[0], variants)))
+    res = {v: _run_measure("--measure", sizes, libs[v]) for v in variants}
+    best = {}
+    print("factorisation k: row | column pass, us per position-slice")
+    print("N     " + "".join("%16s" % v for v in variants))
+    for n in sizes:
+        print("%-6d" % n + "".join("%8.3f%8.3f" % tuple(res[v][n]) for v in variants))
+        ks = range(RADIX_ALTS.get(n, 1))
+        if n in RADIX_ALTS:
+            best[("RROW", n)] = min(ks, key=lambda k: res["r%d" % k][n][0])
+            best[("RCOL", n)] = min(ks, key=lambda k: res["r%d" % k][n][1])
+        cand = [v for v in tiles if v != "t16s2" or n in TILE16]
+        tv = min(cand, key=lambda v: res[v][n][1])
+        best[("TILE", n)], best[("STAGES", n)] = tiles[tv]
+        print("      -> row factorisation %s, column factorisation %s, column tile %d x %d stage(s)" %
+              (best.get(("RROW", n), 0), best.get(("RCOL", n), 0), best[("TILE", n)], best[("STAGES", n)]))
+    defs = ["%s=%d" % (MACRO[kind] % n, k) for (kind, n), k in best.items()]
+    return best, defs
 
 
 def _run_measure(mode, sizes, path):
@@ -162,11 +211,12 @@ def main(argv=None):
     _build.build()
     cands = [int(k) for k in a.candidates.split(",")]
     tmp = tempfile.mkdtemp(prefix="qs_tune_")
-    best = {}
+    # phase 0: factorisations and column tiles
+    best, fdefs = tune_factorisations(sizes, tmp)
     # phase 1: row and column passes
     shapes = [int(x) for x in a.lines.split(",")]
     combos = [(L, k) for L in shapes for k in cands]
-    defs = {(L, k): ["QS_ROW_LINES_%d=%d" % (n, L) for n in sizes] +
+    defs = {(L, k): fdefs + ["QS_ROW_LINES_%d=%d" % (n, L) for n in sizes] +
             ["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, k) for n in sizes for kind in ("ROW", "COL")] for L, k in combos}
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(combos)) as ex:
         libs = dict(zip(combos, ex.map(
@@ -186,10 +236,12 @@ def main(argv=None):
         best[("COL", n)] = min(times, key=times.get)
         print("%-6d" % n + "".join("%8.3f" % times[k] for k in cands) + "   -> %d" % best[("COL", n)])
     # phase 2: row adjoint, with the phase-1 winners
-    fixed = (["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, best[(kind, n)]) for n in sizes for kind in ("ROW", "COL")] +
+    fixed = (fdefs + ["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, best[(kind, n)]) for n in sizes for kind in ("ROW", "COL")] +
              ["QS_ROW_LINES_%d=%d" % (n, best[("LINES", n)]) for n in sizes])
     _, ms_obj = _variant("fixed", "qs_multislice.cu", fixed, tmp)
-    adefs = {k: ["QS_ADJ_MIN_BLOCKS_%d=%d" % (n, k) for n in sizes] for k in cands}
+    # the adjoint's kernels share the factorisations and tiles (their twiddle
+    # tables come from the slice-loop object)
+    adefs = {k: fdefs + ["QS_ADJ_MIN_BLOCKS_%d=%d" % (n, k) for n in sizes] for k in cands}
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(cands)) as ex:
         alibs = dict(zip(cands, ex.map(
             lambda k: _variant("adj%d" % k, "qs_adjoint.cu", adefs[k], tmp, extra_objs=[ms_obj])[0], cands)))
