@@ -293,20 +293,34 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
 // interpolation at dr = dx/2, nearest sub-slice in z).  FP32 arithmetic
 // (FP64 runs at a small fraction of the FP32 rate on this part): the
 // reference forms r and r/dr in double (stem3/stemlib.cpp:944-952); the
-// float radius is within ~2e-7 relative of that, so the radial interval is
-// taken from the float value except within 2e-4 of a knot, where the double
-// computation decides it.  The interpolation weight and the sum then run in
-// float (~1e-7 relative).
-// Shared memory of a CTA: the LUT row offsets of the atom's slices (the same
-// for every pixel), then with STAGED those rows themselves (and the charged
-// table's), so that the interpolation reads shared memory instead of L2.
+// float r/dr (reciprocal square root, within ~4e-7 relative of it) is off by
+// less than 1e-4 of an interval anywhere in the box, so the radial interval
+// is taken from it except within 2e-4 of a knot, where the double
+// computation decides it.  The interpolation weight and the sum run in float.
+//
+// The LUT rows an atom touches are the same for every pixel of its box: the
+// CTA finds the contiguous run of reachable rows once (the reference's
+// iOffsZ tests) and stages them in shared memory as (value, slope) pairs
+// L[ir], L[ir+1] - L[ir], the charge-dependent table already added in with
+// the atom's charge (the interpolation is linear in both), so that a slice
+// costs one shared load, one FMA and one reduction per pixel.  The box pixel
+// advances by fixed quotient/remainder steps instead of a division.
+__device__ __forceinline__ int lut_row(int iOffsZ, int Nr, int limLo, int limHi) {
+    if (iOffsZ < 0) return iOffsZ > limLo ? -iOffsZ + Nr : -1;
+    return iOffsZ < limHi ? iOffsZ : -1;
+}
+
+// CTAs per SM the scatter is compiled for (its register budget): 4 measured
+// fastest on the 512^2 STEM and the largest CBED stacks, within 1 % on TEM
+#ifndef QS_SCATTER_MIN_BLOCKS
+#define QS_SCATTER_MIN_BLOCKS 4
+#endif
 template <bool STAGED>
-__global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts, int Nz,
-                              int Nr, int nzSub, float dx, float dy, double dr, float drf, float dzs, int potNx,
+__global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts, int Nz,
+                              int Nr, int nzSub, float dx, float dy, double dr, float inv_dr, float dzs, int potNx,
                               int potNy, int periodic, int maxRows, float2* __restrict__ trans) {
-    extern __shared__ int s_mem[];
-    int* s_row = s_mem;                                     // [maxRows]
-    float* s_lut = reinterpret_cast<float*>(s_mem + maxRows);  // [maxRows][Nr] (+ [maxRows][Nr] charged)
+    extern __shared__ float2 s_pair[];  // STAGED: [maxRows][Nr - 1] (value, slope)
+    __shared__ int s_run[2];            // first reachable row (relative to iaz0), count
     const AtomJob J = jobs[blockIdx.x];
     const float* lut = luts[J.lut];
     const float* lutq = J.lutq >= 0 ? luts[J.lutq] : nullptr;
@@ -318,34 +332,54 @@ __global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* con
     const int limHi = Nr * (Nz - 1), limLo = -Nr * (Nz - 1), step = nzSub * Nr;
     const double dOffsZ = (double)(((float)(J.iAtomZ + J.iaz0) - J.atomZ / dzs) * (float)nzSub);
     const int iOffsZ0 = ((int)(dOffsZ + 0.5)) * Nr;
-    for (int k = threadIdx.x; k < nrows; k += blockDim.x) {
-        const int iOffsZ = iOffsZ0 + k * step;
-        int row = -1;
-        if (iOffsZ < 0) {
-            if (iOffsZ > limLo) row = -iOffsZ + Nr;
-        } else if (iOffsZ < limHi) {
-            row = iOffsZ;
-        }
-        s_row[k] = row;
+    if (threadIdx.x == 0) {
+        // the reachable rows form one run: iOffsZ grows by `step` per slice
+        // and the reachable ones lie strictly between limLo and limHi
+        int first = -1, count = 0;
+        for (int k = 0; k < nrows; k++)
+            if (lut_row(iOffsZ0 + k * step, Nr, limLo, limHi) >= 0) {
+                if (first < 0) first = k;
+                count = k - first + 1;
+            }
+        s_run[0] = first;
+        s_run[1] = first < 0 ? 0 : count;
     }
     __syncthreads();
+    const int r0 = s_run[0], nr = s_run[1];
+    if (nr == 0) return;
     if constexpr (STAGED) {
-        for (int i = threadIdx.x; i < nrows * Nr; i += blockDim.x) {
-            const int k = i / Nr, j = i - k * Nr, row = s_row[k];
-            s_lut[i] = row >= 0 ? __ldg(lut + row + j) : 0.f;
-            if (lutq) s_lut[maxRows * Nr + i] = row >= 0 ? __ldg(lutq + row + j) : 0.f;
+        const int P = Nr - 1;
+        for (int i = threadIdx.x; i < nr * P; i += blockDim.x) {
+            const int k = i / P, j = i - k * P;
+            const float* L = lut + lut_row(iOffsZ0 + (r0 + k) * step, Nr, limLo, limHi) + j;
+            float v0 = __ldg(L), v1 = __ldg(L + 1);
+            if (lutq) {
+                const float* Lq = lutq + (L - lut);
+                v0 += q * __ldg(Lq);
+                v1 += q * __ldg(Lq + 1);
+            }
+            s_pair[i] = make_float2(v0, v1 - v0);
         }
         __syncthreads();
     }
+    const int sx = blockDim.x / w, sy = blockDim.x - sx * w;
+    int qx = threadIdx.x / w, qy = threadIdx.x - qx * w;
+    float* const base = &trans[(size_t)(J.iAtomZ + J.iaz0 + r0) * sliceStep].x;
     for (int k = threadIdx.x; k < npx; k += blockDim.x) {
-        const int iax = J.iax0 + k / w;
-        const int iay = J.iay0 + k % w;
+        const int iax = J.iax0 + qx, iay = J.iay0 + qy;
+        qx += sx;
+        qy += sy;
+        if (qy >= w) {
+            qy -= w;
+            ++qx;
+        }
         // x2 = iax*dx - atomX in float as the reference forms it
-        // (stem3/stemlib.cpp:931-938), rounded step by step (no FMA)
+        // (stem3/stemlib.cpp:935-938), rounded step by step (no FMA)
         const float ddx = __fsub_rn(__fmul_rn((float)iax, dx), J.atomX);
         const float ddy = __fsub_rn(__fmul_rn((float)iay, dy), J.atomY);
-        const float rr = __fsqrt_rn(__fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy))) / drf;
-        int ir = (int)floorf(rr);
+        const float r2 = fmaf(ddx, ddx, ddy * ddy);
+        const float rr = r2 > 0.f ? r2 * rsqrtf(r2) * inv_dr : 0.f;
+        int ir = (int)rr;
         float ddr = rr - (float)ir;
         if (ddr < 2e-4f || ddr > 1.f - 2e-4f) {
             const double x2 = (double)ddx * ddx, y2 = (double)ddy * ddy;
@@ -356,21 +390,22 @@ __global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* con
         if (ir >= Nr - 1) continue;
         const int cx = periodic ? ((iax % potNx) + potNx) % potNx : iax;
         const int cy = periodic ? ((iay % potNy) + potNy) % potNy : iay;
-        float* dst = &trans[(size_t)(J.iAtomZ + J.iaz0) * sliceStep + (size_t)cx * potNy + cy].x;
-        const float w0 = 1.f - ddr;
-        for (int r = 0; r < nrows; r++, dst += 2 * sliceStep) {
-            const int row = s_row[r];
-            if (row < 0) continue;
-            float v;
-            if constexpr (STAGED) {
-                const float* L = s_lut + r * Nr + ir;
-                v = w0 * L[0] + ddr * L[1];
-                if (lutq) v += q * (w0 * L[maxRows * Nr] + ddr * L[maxRows * Nr + 1]);
-            } else {
-                v = w0 * __ldg(lut + row + ir) + ddr * __ldg(lut + row + ir + 1);
-                if (lutq) v += q * (w0 * __ldg(lutq + row + ir) + ddr * __ldg(lutq + row + ir + 1));
+        float* dst = base + 2 * ((size_t)cx * potNy + cy);
+        if constexpr (STAGED) {
+            const float2* pr = s_pair + ir;
+#pragma unroll 4
+            for (int r = 0; r < nr; r++, dst += 2 * sliceStep, pr += Nr - 1) {
+                const float2 ls = *pr;
+                atomicAdd(dst, fmaf(ddr, ls.y, ls.x));
             }
-            if (v != 0.f) atomicAdd(dst, v);
+        } else {
+            const float w0 = 1.f - ddr;
+            for (int r = 0; r < nr; r++, dst += 2 * sliceStep) {
+                const int row = lut_row(iOffsZ0 + (r0 + r) * step, Nr, limLo, limHi);
+                float v = w0 * __ldg(lut + row + ir) + ddr * __ldg(lut + row + ir + 1);
+                if (lutq) v += q * (w0 * __ldg(lutq + row + ir) + ddr * __ldg(lutq + row + ir + 1));
+                atomicAdd(dst, v);
+            }
         }
     }
 }
@@ -378,21 +413,22 @@ __global__ void scatter_atoms(const AtomJob* __restrict__ jobs, const float* con
 int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* const* d_luts, int Nz, int Nr,
                    int nzSub, const qs_params& p, float2* trans, cudaStream_t s) {
     if (njobs <= 0) return QS_OK;
+    (void)charged;
     const double dr = p.resolutionX / OVERSAMP;
     // every atom's z range spans at most 2 iRadZ + 1 slices
     const int maxRows = 2 * (int)ceilf(p.atomRadius / p.sliceThickness) + 1;
-    const size_t staged = sizeof(int) * maxRows + sizeof(float) * (size_t)maxRows * Nr * (charged ? 2 : 1);
+    const size_t staged = sizeof(float2) * (size_t)maxRows * (Nr - 1);
     const int periodic = p.nonPeriod ? 0 : 1;
+    const float inv_dr = (float)(1.0 / dr);
     if (staged <= 160 * 1024) {
         QS_TRY(smem_attr((const void*)scatter_atoms<true>, staged));
         scatter_atoms<true><<<njobs, 256, staged, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY,
-                                                       dr, (float)dr, p.sliceThickness, p.potNx, p.potNy, periodic,
+                                                       dr, inv_dr, p.sliceThickness, p.potNx, p.potNy, periodic,
                                                        maxRows, trans);
     } else {
-        scatter_atoms<false><<<njobs, 256, sizeof(int) * maxRows, s>>>(d_jobs, d_luts, Nz, Nr, nzSub,
-                                                                        p.resolutionX, p.resolutionY, dr, (float)dr,
-                                                                        p.sliceThickness, p.potNx, p.potNy,
-                                                                        periodic, maxRows, trans);
+        scatter_atoms<false><<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr,
+                                                   inv_dr, p.sliceThickness, p.potNx, p.potNy, periodic, maxRows,
+                                                   trans);
     }
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
