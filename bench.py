@@ -98,16 +98,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def adjoint_workload():
+def adjoint_workload(npix=32):
     """Differentiable 4D-STEM: SrTiO3 6x6x20, 256^2 at 0.09152 A, 40 slices of
     1.9525 A, 200 kV, 25 mrad, 32x32 positions over one unit cell (potential
-    298^2).  Returns (params, atoms, target atoms): the target structure has
-    its atoms displaced by N(0, 0.05^2) A in x and y from
+    298^2; npix: scan raster edge, 32 for the workload, smaller only for
+    profiling captures).  Returns (params, atoms, target atoms): the target
+    structure has its atoms displaced by N(0, 0.05^2) A in x and y from
     numpy.random.default_rng(20261203 + 300)."""
     atoms, ax, by, c = config.replicate(config.srtio3_cell(), 6, 6, 20)
     a = 3.905
     p = config.make_params(nx=256, resolutionX=0.09152, v0=200, slices=40, sliceThickness=1.9525, ax=ax, by=by, c=c,
-                           scan=(3 * a, 4 * a, 32, 3 * a, 4 * a, 32), detectors=[], alpha=25)
+                           scan=(3 * a, 4 * a, npix, 3 * a, 4 * a, npix), detectors=[], alpha=25)
     rng = np.random.default_rng(20261203 + 300)
     tgt_atoms = atoms.copy()
     for k in ("x", "y"):
@@ -115,11 +116,11 @@ def adjoint_workload():
     return p, atoms, tgt_atoms
 
 
-def adjoint_measure(ctx, torch, reps=3):
+def adjoint_measure(ctx, torch, reps=3, npix=32):
     """Differentiable 4D-STEM (adjoint_workload): forward diffraction patterns
     vs the adjoint run (loss + dL/dV), checkpoints every 6 slices and every
     slice, plus dL/d(x,y) of the atoms."""
-    p, atoms, tgt_atoms = adjoint_workload()
+    p, atoms, tgt_atoms = adjoint_workload(npix)
     npos = p.scanXN * p.scanYN
     probe = torch.from_numpy(ctx.probe(p)).cuda()
     T = torch.empty((p.slices, p.potNx, p.potNy, 2), dtype=torch.float32, device="cuda")
@@ -376,9 +377,30 @@ def run_reference(args, rank, world):
     return 0
 
 
+def run_only(args):
+    """One measurement leg alone (for profiling captures of that workload):
+    prints {leg: result} as one JSON line."""
+    import torch
+    from qstem_gb300 import lib
+    ctx = lib.Context(0)
+    if args.only == "adjoint":
+        out = adjoint_measure(ctx, torch, npix=args.adjoint_npix)
+    elif args.only == "tem":
+        out = tem_measure(ctx)
+    elif args.only == "cbed":
+        out = cbed_measure(ctx)
+    else:
+        out = stem256_measure(ctx, torch, cpu=False)
+    print(json.dumps({args.only: out}), flush=True)
+    ctx.close()
+    return 0
+
+
 def run_ours(args, rank, world):
     import torch
     from qstem_gb300 import lib
+    if args.only:
+        return run_only(args)
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     p, atoms = workload_params(args.npix)
@@ -530,6 +552,10 @@ def main():
     ap.add_argument("--skip-tem", action="store_true")
     ap.add_argument("--skip-cbed", action="store_true")
     ap.add_argument("--skip-stem256", action="store_true")
+    ap.add_argument("--only", choices=["adjoint", "tem", "cbed", "stem256"],
+                    help="run one measurement leg alone (profiling captures)")
+    ap.add_argument("--adjoint-npix", type=int, default=32,
+                    help="with --only adjoint: scan raster edge (32 is the workload)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -70,7 +70,7 @@ static int ev_record(qs_ctx* c, size_t* idx) {
 
 enum Buf {
     B_WAVES, B_PROBE, B_PARTIAL, B_POS, B_TABLES, B_TILES, B_TRANS, B_OUT1, B_OUT2, B_OUT3, B_JOBS, B_LUTS,
-    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, B_BAND, NBUF
+    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, B_BAND, B_VREAL, NBUF
 };
 static_assert(NBUF <= kMaxBufs, "context buffer table too small");
 
@@ -455,7 +455,12 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         QS_TRY(ensure(c, B_TRANS, sizeof(float2) * nTrans, &d));
         trans = (float2*)d;
     }
-    QS_CUDA_TRY(cudaMemsetAsync(trans, 0, sizeof(float2) * nTrans, c->stream));
+    // make3DSlices' sums go to a real array first (the phase grating, or
+    // for QS_OUT_POTENTIAL a plain copy, fills the complex stack from it)
+    void* dvr = nullptr;
+    QS_TRY(ensure(c, B_VREAL, sizeof(float) * nTrans, &dvr));
+    float* Vr = (float*)dvr;
+    QS_CUDA_TRY(cudaMemsetAsync(Vr, 0, sizeof(float) * nTrans, c->stream));
 
     std::vector<AtomJob> jobs;
     std::vector<std::pair<int, double>> lutKeys;
@@ -472,14 +477,16 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
         bool charged = false;
         for (const AtomJob& J : jobs) charged |= J.lutq >= 0;
-        QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), charged, d_luts, Nz, Nr, ns, P, trans,
+        QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), charged, d_luts, Nz, Nr, ns, P, Vr,
                               c->stream));
     }
 
-    if (!(flags & QS_OUT_POTENTIAL)) {
+    if (flags & QS_OUT_POTENTIAL) {
+        QS_TRY(launch_expand_real(Vr, trans, nTrans, c->stream));
+    } else {
         // initSTEMSlices (stem3/stemlib.cpp:2280-2336)
         const double mm0 = (double)(1.0f + P.v0 / 511.0f);
-        QS_TRY(launch_phase_grating(trans, nTrans, mm0 * wavelength(P.v0), c->stream));
+        QS_TRY(launch_grating_from_real(Vr, trans, nTrans, mm0 * wavelength(P.v0), c->stream));
         if (P.bandlimittrans) {
             const int nx = P.potNx, ny = P.potNy;
             // line FFTs where they exist, DFT matrix products otherwise

@@ -145,10 +145,12 @@ struct AtomJob {
     int iAtomZ;
     int lut, lutq;               // LUT indices (-1: none)
 };
+// the scatter-sum into V[slices][potNx][potNy] (float, zeroed by the caller);
 // charged: some job has a charge LUT (lutq >= 0)
 int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* const* d_luts, int Nz, int Nr,
-                   int nzSub, const qs_params& p, float2* trans, cudaStream_t s);
-int launch_phase_grating(float2* trans, size_t n, double scale, cudaStream_t s);
+                   int nzSub, const qs_params& p, float* V, cudaStream_t s);
+// trans = (V, 0)
+int launch_expand_real(const float* V, float2* trans, size_t n, cudaStream_t s);
 int launch_bandlimit_mask(float2* trans, int slices, int potNx, int potNy, const float* kx2,
                           const float* ky2, float k2max, double fftScale, cudaStream_t s);
 

@@ -304,7 +304,9 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
 // L[ir], L[ir+1] - L[ir], the charge-dependent table already added in with
 // the atom's charge (the interpolation is linear in both), so that a slice
 // costs one shared load, one FMA and one reduction per pixel.  The box pixel
-// advances by fixed quotient/remainder steps instead of a division.
+// advances by fixed quotient/remainder steps instead of a division.  The sums
+// go to a real array (unit stride: a warp's reductions cover half the
+// sectors of the complex stack's real parts); the phase grating expands it.
 __device__ __forceinline__ int lut_row(int iOffsZ, int Nr, int limLo, int limHi) {
     if (iOffsZ < 0) return iOffsZ > limLo ? -iOffsZ + Nr : -1;
     return iOffsZ < limHi ? iOffsZ : -1;
@@ -318,7 +320,7 @@ __device__ __forceinline__ int lut_row(int iOffsZ, int Nr, int limLo, int limHi)
 template <bool STAGED>
 __global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts, int Nz,
                               int Nr, int nzSub, float dx, float dy, double dr, float inv_dr, float dzs, int potNx,
-                              int potNy, int periodic, int maxRows, float2* __restrict__ trans) {
+                              int potNy, int periodic, int maxRows, float* __restrict__ V) {
     extern __shared__ float2 s_pair[];  // STAGED: [maxRows][Nr - 1] (value, slope)
     __shared__ int s_run[2];            // first reachable row (relative to iaz0), count
     const AtomJob J = jobs[blockIdx.x];
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(cons
     }
     const int sx = blockDim.x / w, sy = blockDim.x - sx * w;
     int qx = threadIdx.x / w, qy = threadIdx.x - qx * w;
-    float* const base = &trans[(size_t)(J.iAtomZ + J.iaz0 + r0) * sliceStep].x;
+    float* const base = V + (size_t)(J.iAtomZ + J.iaz0 + r0) * sliceStep;
     for (int k = threadIdx.x; k < npx; k += blockDim.x) {
         const int iax = J.iax0 + qx, iay = J.iay0 + qy;
         qx += sx;
@@ -390,17 +392,17 @@ __global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(cons
         if (ir >= Nr - 1) continue;
         const int cx = periodic ? ((iax % potNx) + potNx) % potNx : iax;
         const int cy = periodic ? ((iay % potNy) + potNy) % potNy : iay;
-        float* dst = base + 2 * ((size_t)cx * potNy + cy);
+        float* dst = base + (size_t)cx * potNy + cy;
         if constexpr (STAGED) {
             const float2* pr = s_pair + ir;
 #pragma unroll 4
-            for (int r = 0; r < nr; r++, dst += 2 * sliceStep, pr += Nr - 1) {
+            for (int r = 0; r < nr; r++, dst += sliceStep, pr += Nr - 1) {
                 const float2 ls = *pr;
                 atomicAdd(dst, fmaf(ddr, ls.y, ls.x));
             }
         } else {
             const float w0 = 1.f - ddr;
-            for (int r = 0; r < nr; r++, dst += 2 * sliceStep) {
+            for (int r = 0; r < nr; r++, dst += sliceStep) {
                 const int row = lut_row(iOffsZ0 + (r0 + r) * step, Nr, limLo, limHi);
                 float v = w0 * __ldg(lut + row + ir) + ddr * __ldg(lut + row + ir + 1);
                 if (lutq) v += q * (w0 * __ldg(lutq + row + ir) + ddr * __ldg(lutq + row + ir + 1));
@@ -411,7 +413,7 @@ __global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(cons
 }
 
 int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* const* d_luts, int Nz, int Nr,
-                   int nzSub, const qs_params& p, float2* trans, cudaStream_t s) {
+                   int nzSub, const qs_params& p, float* V, cudaStream_t s) {
     if (njobs <= 0) return QS_OK;
     (void)charged;
     const double dr = p.resolutionX / OVERSAMP;
@@ -424,11 +426,11 @@ int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* 
         QS_TRY(smem_attr((const void*)scatter_atoms<true>, staged));
         scatter_atoms<true><<<njobs, 256, staged, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY,
                                                        dr, inv_dr, p.sliceThickness, p.potNx, p.potNy, periodic,
-                                                       maxRows, trans);
+                                                       maxRows, V);
     } else {
         scatter_atoms<false><<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr,
                                                    inv_dr, p.sliceThickness, p.potNx, p.potNy, periodic, maxRows,
-                                                   trans);
+                                                   V);
     }
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
@@ -441,31 +443,29 @@ int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* 
 // sincosf (within 2 ulp) evaluates it: for the phases of real potentials
 // (|scale V| of order 10 rad) the result differs by ~1e-6 absolute, and FP64
 // transcendentals run at a small fraction of the FP32 rate on this part.
-__global__ void phase_grating(float2* __restrict__ t, size_t n, float scale) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        float sn, cs;
-        sincosf(t[i].x * scale, &sn, &cs);
-        t[i] = make_float2(cs, sn);
-    }
-}
-
-int launch_phase_grating(float2* trans, size_t n, double scale, cudaStream_t s) {
-    if (!n) return QS_OK;
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    phase_grating<<<sms * 8, 256, 0, s>>>(trans, n, (float)scale);
-    QS_CUDA_TRY(cudaGetLastError());
-    count_launch(1);
-    return QS_OK;
-}
-
 __global__ void grating_from_real(const float* __restrict__ V, float2* __restrict__ t, size_t n, float scale) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         float sn, cs;
         sincosf(V[i] * scale, &sn, &cs);
         t[i] = make_float2(cs, sn);
     }
+}
+
+// trans = (V, 0): the potential itself in the complex stack's layout
+__global__ void expand_real(const float* __restrict__ V, float2* __restrict__ t, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        t[i] = make_float2(V[i], 0.f);
+}
+
+int launch_expand_real(const float* V, float2* trans, size_t n, cudaStream_t s) {
+    if (!n) return QS_OK;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    expand_real<<<sms * 8, 256, 0, s>>>(V, trans, n);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
 }
 
 int launch_grating_from_real(const float* V, float2* trans, size_t n, double scale, cudaStream_t s) {
