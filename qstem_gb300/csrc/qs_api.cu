@@ -48,6 +48,16 @@ struct qs_ctx {
         int launches = 0;   // kernels in the graph
     };
     std::vector<GraphEntry> graphs;
+    // pinned host staging of uploads: one buffer per kind, refilled once the
+    // copy queued from it (the event recorded after it) has run, so that the
+    // host can plan the next call while the device still works on this one
+    struct Pinned {
+        void* p = nullptr;
+        size_t cap = 0;
+        cudaEvent_t ev = nullptr;
+        bool pending = false;
+    };
+    Pinned pin[4];
 };
 
 namespace qs {
@@ -73,6 +83,44 @@ enum Buf {
     B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, B_BAND, B_VREAL, NBUF
 };
 static_assert(NBUF <= kMaxBufs, "context buffer table too small");
+enum Pin { P_JOBS, P_LUTPTR, P_BAND, P_TABLES };
+
+// Pinned host memory of `bytes` for staging kind `which`; waits only for the
+// previous copy from the same buffer.
+static int stage(qs_ctx* c, int which, size_t bytes, void** out) {
+    qs_ctx::Pinned& b = c->pin[which];
+    if (b.pending) {
+        QS_CUDA_TRY(cudaEventSynchronize(b.ev));
+        b.pending = false;
+    }
+    if (b.cap < bytes) {
+        if (b.p) cudaFreeHost(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+        QS_CUDA_TRY(cudaMallocHost(&b.p, bytes));
+        b.cap = bytes;
+    }
+    if (!b.ev) QS_CUDA_TRY(cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming));
+    *out = b.p;
+    return QS_OK;
+}
+
+// Queue the copy of `bytes` from staging buffer `which` (filled by the caller
+// after stage()) to device address dst.
+static int stage_copy(qs_ctx* c, int which, void* dst, size_t bytes) {
+    qs_ctx::Pinned& b = c->pin[which];
+    QS_CUDA_TRY(cudaMemcpyAsync(dst, b.p, bytes, cudaMemcpyHostToDevice, c->stream));
+    QS_CUDA_TRY(cudaEventRecord(b.ev, c->stream));
+    b.pending = true;
+    return QS_OK;
+}
+
+static int upload(qs_ctx* c, int which, void* dst, const void* src, size_t bytes) {
+    void* h = nullptr;
+    QS_TRY(stage(c, which, bytes, &h));
+    std::memcpy(h, src, bytes);
+    return stage_copy(c, which, dst, bytes);
+}
 
 static int ensure(qs_ctx* c, int which, size_t bytes, void** out) {
     if (bytes == 0) bytes = 16;
@@ -281,12 +329,13 @@ static int prepare_luts(qs_ctx* c, const qs_params& P, const std::vector<std::pa
                 return rc;
             }
             it = c->luts.emplace(key, d).first;
+            // build_lut's host tables (once per element and sampling) must
+            // outlive its copies
+            QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
         }
         ptrs[k] = it->second;
     }
-    if (!ptrs.empty())
-        QS_CUDA_TRY(cudaMemcpyAsync(dp, ptrs.data(), sizeof(float*) * ptrs.size(), cudaMemcpyHostToDevice, c->stream));
-    QS_CUDA_TRY(cudaStreamSynchronize(c->stream));  // the host vector must outlive the copy
+    if (!ptrs.empty()) QS_TRY(upload(c, P_LUTPTR, dp, ptrs.data(), sizeof(float*) * ptrs.size()));
     *d_ptrs = (const float* const*)dp;
     return QS_OK;
 }
@@ -339,6 +388,10 @@ int qs_ctx_destroy(qs_ctx* c) {
     for (auto& g : c->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto& kv : c->luts) cudaFree(kv.second);
+    for (auto& b : c->pin) {
+        if (b.p) cudaFreeHost(b.p);
+        if (b.ev) cudaEventDestroy(b.ev);
+    }
     for (int i = 0; i < kMaxBufs; i++)
         if (c->buf[i]) cudaFree(c->buf[i]);
     cudaStreamDestroy(c->stream);
@@ -472,9 +525,7 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         QS_TRY(prepare_luts(c, P, lutKeys, &d_luts, &Nz, &Nr, &ns));
         void* dj = nullptr;
         QS_TRY(ensure(c, B_JOBS, sizeof(AtomJob) * jobs.size(), &dj));
-        QS_CUDA_TRY(cudaMemcpyAsync(dj, jobs.data(), sizeof(AtomJob) * jobs.size(), cudaMemcpyHostToDevice, c->stream));
-        // the host vector must outlive the async copy
-        QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        QS_TRY(upload(c, P_JOBS, dj, jobs.data(), sizeof(AtomJob) * jobs.size()));
         bool charged = false;
         for (const AtomJob& J : jobs) charged |= J.lutq >= 0;
         QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), charged, d_luts, Nz, Nr, ns, P, Vr,
@@ -522,8 +573,9 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
                 const int Cw = col_tile_width(nx), ntl = ny / Cw;
                 const size_t bytes = sizeof(float) * (nx + ny) + sizeof(float2) * (nx + ny) + sizeof(int) * ntl;
                 QS_TRY(ensure(c, B_BAND, bytes, &dt));
-                std::vector<unsigned char> host(bytes);
-                float* hk = (float*)host.data();
+                void* hbuf = nullptr;
+                QS_TRY(stage(c, P_BAND, bytes, &hbuf));
+                float* hk = (float*)hbuf;
                 std::copy(kx2.begin(), kx2.end(), hk);
                 std::copy(ky2.begin(), ky2.end(), hk + nx);
                 float2* hp = (float2*)(hk + nx + ny);
@@ -532,7 +584,7 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
                 for (int i = 0; i < ny; i++) hp[nx + i] = make_float2(1.f, 0.f);
                 int* ht = (int*)(hp + nx + ny);
                 for (int k = 0; k < ntl; k++) ht[k] = k * Cw;
-                QS_CUDA_TRY(cudaMemcpyAsync(dt, host.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+                QS_TRY(stage_copy(c, P_BAND, dt, bytes));
                 const float* dk = (const float*)dt;
                 const float2* dp = (const float2*)(dk + nx + ny);
                 QS_TRY(bandlimit_lines(trans, nx, ny, P.slices, dk, dk + nx, dp, dp + nx, (const int*)(dp + nx + ny),
@@ -541,14 +593,12 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
                 QS_TRY(ensure(c, B_TABLES, sizeof(float) * (nx + ny), &dt));
                 std::vector<float> both(kx2);
                 both.insert(both.end(), ky2.begin(), ky2.end());
-                QS_CUDA_TRY(cudaMemcpyAsync(dt, both.data(), sizeof(float) * both.size(), cudaMemcpyHostToDevice,
-                                            c->stream));
+                QS_TRY(upload(c, P_TABLES, dt, both.data(), sizeof(float) * both.size()));
                 QS_TRY(xform(false));
                 QS_TRY(launch_bandlimit_mask(trans, P.slices, nx, ny, (float*)dt, (float*)dt + nx, k2max,
                                              1.0 / (nx * ny), c->stream));
                 QS_TRY(xform(true));
             }
-            QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
         }
     }
     if (flags & QS_HOST_IO) {
