@@ -57,7 +57,10 @@ struct qs_ctx {
         cudaEvent_t ev = nullptr;
         bool pending = false;
     };
-    Pinned pin[4];
+    Pinned pin[5];
+    // the scatter's knot thresholds in B_KNOTS were made for this (dr, Nr)
+    double knots_dr = -1.0;
+    int knots_Nr = 0;
 };
 
 namespace qs {
@@ -80,10 +83,10 @@ static int ev_record(qs_ctx* c, size_t* idx) {
 
 enum Buf {
     B_WAVES, B_PROBE, B_PARTIAL, B_POS, B_TABLES, B_TILES, B_TRANS, B_OUT1, B_OUT2, B_OUT3, B_JOBS, B_LUTS,
-    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, B_BAND, B_VREAL, NBUF
+    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, B_BAND, B_VREAL, B_KNOTS, NBUF
 };
 static_assert(NBUF <= kMaxBufs, "context buffer table too small");
-enum Pin { P_JOBS, P_LUTPTR, P_BAND, P_TABLES };
+enum Pin { P_JOBS, P_LUTPTR, P_BAND, P_TABLES, P_KNOTS };
 
 // Pinned host memory of `bytes` for staging kind `which`; waits only for the
 // previous copy from the same buffer.
@@ -526,10 +529,20 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         void* dj = nullptr;
         QS_TRY(ensure(c, B_JOBS, sizeof(AtomJob) * jobs.size(), &dj));
         QS_TRY(upload(c, P_JOBS, dj, jobs.data(), sizeof(AtomJob) * jobs.size()));
+        void* dk = nullptr;
+        QS_TRY(ensure(c, B_KNOTS, sizeof(double) * (Nr + 1), &dk));
+        const double dr = (double)(P.resolutionX / 2);  // make3DSlices' dr (stem3/stemlib.cpp:576)
+        if (c->knots_dr != dr || c->knots_Nr != Nr) {
+            std::vector<double> knots;
+            scatter_knots(dr, Nr, knots);
+            QS_TRY(upload(c, P_KNOTS, dk, knots.data(), sizeof(double) * knots.size()));
+            c->knots_dr = dr;
+            c->knots_Nr = Nr;
+        }
         bool charged = false;
         for (const AtomJob& J : jobs) charged |= J.lutq >= 0;
-        QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), charged, d_luts, Nz, Nr, ns, P, Vr,
-                              c->stream));
+        QS_TRY(launch_scatter((const AtomJob*)dj, (int)jobs.size(), charged, d_luts, Nz, Nr, ns, P,
+                              (const double*)dk, Vr, c->stream));
     }
 
     if (flags & QS_OUT_POTENTIAL) {

@@ -148,7 +148,10 @@ struct AtomJob {
 // the scatter-sum into V[slices][potNx][potNy] (float, zeroed by the caller);
 // charged: some job has a charge LUT (lutq >= 0)
 int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* const* d_luts, int Nz, int Nr,
-                   int nzSub, const qs_params& p, float* V, cudaStream_t s);
+                   int nzSub, const qs_params& p, const double* d_knots, float* V, cudaStream_t s);
+// knots[k], k = 0..Nr: the smallest s = x^2 + y^2 (double) whose radial
+// interval floor(fl(fl(sqrt(s)) / dr)) in make3DSlices is at least k
+void scatter_knots(double dr, int Nr, std::vector<double>& knots);
 // trans = (V, 0)
 int launch_expand_real(const float* V, float2* trans, size_t n, cudaStream_t s);
 int launch_bandlimit_mask(float2* trans, int slices, int potNx, int potNy, const float* kx2,

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
@@ -292,11 +293,16 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
 // interpolation follows stem3/stemlib.cpp:935-1028 (radial linear
 // interpolation at dr = dx/2, nearest sub-slice in z).  FP32 arithmetic
 // (FP64 runs at a small fraction of the FP32 rate on this part): the
-// reference forms r and r/dr in double (stem3/stemlib.cpp:944-952); the
-// float r/dr (reciprocal square root, within ~4e-7 relative of it) is off by
-// less than 1e-4 of an interval anywhere in the box, so the radial interval
-// is taken from it except within 2e-4 of a knot, where the double
-// computation decides it.  The interpolation weight and the sum run in float.
+// reference forms s = x2 + y2, r = sqrt(s) and r/dr in double
+// (stem3/stemlib.cpp:935-943); the float r/dr (reciprocal square root,
+// within ~4e-7 relative of it) is off by less than 1e-4 of an interval
+// anywhere in the box, so the radial interval is taken from it except within
+// 2e-4 of a knot.  There the reference's own decision is reproduced without a
+// double square root or division: its interval index floor(fl(sqrt(s))/dr)
+// never decreases as s grows, so it reaches knot k exactly when s is at
+// least the smallest double that reaches it (scatter_knots, found on the host
+// by bisection), and s itself costs one double product and one double FMA.
+// The interpolation weight and the sum run in float.
 //
 // The LUT rows an atom touches are the same for every pixel of its box: the
 // CTA finds the contiguous run of reachable rows once (the reference's
@@ -307,6 +313,28 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
 // advances by fixed quotient/remainder steps instead of a division.  The sums
 // go to a real array (unit stride: a warp's reductions cover half the
 // sectors of the complex stack's real parts); the phase grating expands it.
+void scatter_knots(double dr, int Nr, std::vector<double>& T) {
+    // T[k] = min{s >= 0 : floor(fl(fl(sqrt(s)) / dr)) >= k}; non-negative
+    // doubles order like their bit patterns, so bisect over those
+    T.assign(Nr + 1, 0.0);
+    auto reaches = [&](double v, int k) { return std::floor(std::sqrt(v) / dr) >= (double)k; };
+    for (int k = 1; k <= Nr; k++) {
+        const double hi0 = ((double)k + 1.0) * dr * ((double)k + 1.0) * dr;
+        uint64_t lo, hi;
+        const double zero = 0.0;
+        std::memcpy(&lo, &zero, 8);
+        std::memcpy(&hi, &hi0, 8);
+        while (hi - lo > 1) {  // invariant: !reaches(lo), reaches(hi)
+            const uint64_t mid = lo + (hi - lo) / 2;
+            double v;
+            std::memcpy(&v, &mid, 8);
+            if (reaches(v, k)) hi = mid;
+            else lo = mid;
+        }
+        std::memcpy(&T[k], &hi, 8);
+    }
+}
+
 __device__ __forceinline__ int lut_row(int iOffsZ, int Nr, int limLo, int limHi) {
     if (iOffsZ < 0) return iOffsZ > limLo ? -iOffsZ + Nr : -1;
     return iOffsZ < limHi ? iOffsZ : -1;
@@ -319,8 +347,8 @@ __device__ __forceinline__ int lut_row(int iOffsZ, int Nr, int limLo, int limHi)
 #endif
 template <bool STAGED>
 __global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(const AtomJob* __restrict__ jobs, const float* const* __restrict__ luts, int Nz,
-                              int Nr, int nzSub, float dx, float dy, double dr, float inv_dr, float dzs, int potNx,
-                              int potNy, int periodic, int maxRows, float* __restrict__ V) {
+                              int Nr, int nzSub, float dx, float dy, const double* __restrict__ knots, float inv_dr,
+                              float dzs, int potNx, int potNy, int periodic, int maxRows, float* __restrict__ V) {
     extern __shared__ float2 s_pair[];  // STAGED: [maxRows][Nr - 1] (value, slope)
     __shared__ int s_run[2];            // first reachable row (relative to iaz0), count
     const AtomJob J = jobs[blockIdx.x];
@@ -384,10 +412,15 @@ __global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(cons
         int ir = (int)rr;
         float ddr = rr - (float)ir;
         if (ddr < 2e-4f || ddr > 1.f - 2e-4f) {
-            const double x2 = (double)ddx * ddx, y2 = (double)ddy * ddy;
-            const double dd = sqrt(x2 + y2) / dr;
-            ir = (int)floor(dd);
-            ddr = (float)(dd - (double)ir);
+            // the knot k nearest to rr: the interval is k - 1 or k
+            const int k = (int)(rr + 0.5f);
+            if (k > 0 && k <= Nr) {
+                const double s2 = fma((double)ddx, (double)ddx, (double)ddy * (double)ddy);
+                ir = s2 < __ldg(knots + k) ? k - 1 : k;
+            } else {
+                ir = k;
+            }
+            ddr = fminf(fmaxf(rr - (float)ir, 0.f), 1.f);
         }
         if (ir >= Nr - 1) continue;
         const int cx = periodic ? ((iax % potNx) + potNx) % potNx : iax;
@@ -413,7 +446,7 @@ __global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(cons
 }
 
 int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* const* d_luts, int Nz, int Nr,
-                   int nzSub, const qs_params& p, float* V, cudaStream_t s) {
+                   int nzSub, const qs_params& p, const double* d_knots, float* V, cudaStream_t s) {
     if (njobs <= 0) return QS_OK;
     (void)charged;
     const double dr = p.resolutionX / OVERSAMP;
@@ -425,12 +458,12 @@ int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* 
     if (staged <= 160 * 1024) {
         QS_TRY(smem_attr((const void*)scatter_atoms<true>, staged));
         scatter_atoms<true><<<njobs, 256, staged, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY,
-                                                       dr, inv_dr, p.sliceThickness, p.potNx, p.potNy, periodic,
-                                                       maxRows, V);
+                                                       d_knots, inv_dr, p.sliceThickness, p.potNx, p.potNy,
+                                                       periodic, maxRows, V);
     } else {
-        scatter_atoms<false><<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY, dr,
-                                                   inv_dr, p.sliceThickness, p.potNx, p.potNy, periodic, maxRows,
-                                                   V);
+        scatter_atoms<false><<<njobs, 256, 0, s>>>(d_jobs, d_luts, Nz, Nr, nzSub, p.resolutionX, p.resolutionY,
+                                                   d_knots, inv_dr, p.sliceThickness, p.potNx, p.potNy, periodic,
+                                                   maxRows, V);
     }
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
