@@ -26,10 +26,13 @@ def build(quiet=True, ref_dir=None):
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     ref = ref_dir or os.environ.get("QS_REFERENCE_DIR")
     if ref and os.path.isdir(ref):
-        out = subprocess.run(["make", "-C", HERE, "-j8", "ref", "REF=" + os.path.abspath(ref)], capture_output=True,
-                             text=True)
-        if out.returncode != 0 and not quiet:
-            print(out.stdout + out.stderr)
+        # the reference's programs, and its stem3 with the drop-in adapter
+        # (this one links the GPU library, built before the oracle)
+        for target in ("ref", "adapter"):
+            out = subprocess.run(["make", "-C", HERE, "-j8", target, "REF=" + os.path.abspath(ref)],
+                                 capture_output=True, text=True)
+            if out.returncode != 0 and not quiet:
+                print(out.stdout + out.stderr)
 
 
 def lib():
