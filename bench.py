@@ -291,14 +291,22 @@ def cbed_workload():
     return jobs
 
 
-def cbed_measure(ctx):
+def cbed_measure(ctx, reps=2):
     """qs_cbed_batch_run end to end (host atoms in, host patterns out) on the
-    64-instance workload, against the same instances run one call each."""
+    64-instance workload, against the same instances run one call each.
+    The first call (e2e_ms_first) also builds the projected-potential tables
+    of every element and sampling, which the context keeps; e2e_ms is the
+    best of `reps` later calls."""
     jobs = cbed_workload()
-    ctx.cbed_batch(jobs[:2])
     t0 = time.perf_counter()
     dps, rep = ctx.cbed_batch(jobs)
-    t_batch = time.perf_counter() - t0
+    t_first = time.perf_counter() - t0
+    t_batch = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        dps, rep = ctx.cbed_batch(jobs)
+        t = time.perf_counter() - t0
+        t_batch = t if t_batch is None else min(t_batch, t)
     t0 = time.perf_counter()
     for j in jobs:
         ctx.cbed_batch([j])
@@ -306,8 +314,8 @@ def cbed_measure(ctx):
     ss = sum(p.slices for p, _ in jobs)
     by = sum(40.0 * p.nx * p.ny * p.slices for p, _ in jobs)
     return {"workload": "uneven CBED: 64 instances, grids 256-1024, Au/Si/SrTiO3, 5-50 nm, 5-25 mrad, 200 kV",
-            "e2e_ms": t_batch * 1e3, "instances_per_s": len(jobs) / t_batch, "slice_steps": ss,
-            "slice_steps_per_s": ss / t_batch, "multislice_GBps_model": by / t_batch / 1e9,
+            "e2e_ms": t_batch * 1e3, "e2e_ms_first": t_first * 1e3, "instances_per_s": len(jobs) / t_batch,
+            "slice_steps": ss, "slice_steps_per_s": ss / t_batch, "multislice_GBps_model": by / t_batch / 1e9,
             "one_call_per_instance_ms": t_single * 1e3, "batched_over_one_call": t_single / t_batch,
             "report": rep, "pattern_sum_mean": float(np.mean([d.sum() for d in dps]))}
 

@@ -259,24 +259,26 @@ typedef struct qs_cbed_job {
 
 /* What the scheduler did. */
 typedef struct qs_cbed_report {
-    int groups;              /* batches of instances sharing grid, sampling, slice thickness and energy */
+    int groups;              /* batches of instances sharing a grid */
     int rounds;              /* admission rounds */
     int streams;             /* CUDA streams the groups of a round ran on */
     double admitted_bytes;   /* largest device footprint of a round */
     double budget_bytes;     /* the admission budget used */
 } qs_cbed_report;
 
-/* Run `njobs` independent CBED instances.  Instances with the same grid,
- * sampling, slice thickness and energy share propagator tables and run as
- * one batch (per-instance slice stacks and probes, each wave stopping after
- * its own slice count); the batches of a round run concurrently on separate
+/* Run `njobs` independent CBED instances.  Instances with the same grid run
+ * as one batch, one launch per pass and step for all of them: each wave has
+ * its own slice stack, probe, propagator and k^2 tables (its sampling, slice
+ * thickness and energy), band, thickness and stacking, and stops after its
+ * own number of steps; the batches of a round run concurrently on separate
  * streams.  A round admits whole batches, largest first, while the sum of
- * their footprints (slice stacks + waves + probes + patterns) fits the budget:
- * the free device memory less 1 GiB, or max_bytes if that is smaller and not
- * 0.  An instance that alone does not fit is rejected (QS_ERR_NOMEM).
- * A cell divided into slabs (cellDiv > 1) runs through all of them, as
- * doCBED's slab loop does: one stack per slab (slab 0's, copied, for equal
- * divisions).  report may be NULL. */
+ * their footprints (slice stacks + waves + probes + patterns + tables) fits
+ * the budget: the free device memory less 1 GiB, or max_bytes if that is
+ * smaller and not 0.  An instance that alone does not fit is rejected
+ * (QS_ERR_NOMEM).  A cell divided into slabs (cellDiv > 1) runs through all
+ * of them and a stacking sequence through its passes, as doCBED's slab loop
+ * does: one stack is kept per slab (slab 0's alone for equal divisions) and
+ * the steps index it.  report may be NULL. */
 int qs_cbed_batch_run(qs_ctx *ctx, const qs_cbed_job *jobs, int njobs, size_t max_bytes,
                       qs_cbed_report *report);
 

@@ -1066,20 +1066,22 @@ int qs_stem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, 
 // ------------------------------------------------------------- CBED batch
 namespace {
 
-// Instances that can share one batched scan: the propagator tables, the band
-// and the column tiles depend on exactly these fields.
+// Instances that share one batched scan: the same grid (the line transforms
+// and launch shapes follow it).  Sampling, slice thickness, energy, optics,
+// thickness, slabs and stacking sequence differ per wave: every wave carries
+// its own propagator and k^2 tables, band, column-tile work items and
+// step-to-slice table.
 struct GridKey {
     int nx, ny, potNx, potNy;
-    float rx, ry, dz, v0;
     bool operator<(const GridKey& o) const {
-        return std::tie(nx, ny, potNx, potNy, rx, ry, dz, v0) <
-               std::tie(o.nx, o.ny, o.potNx, o.potNy, o.rx, o.ry, o.dz, o.v0);
+        return std::tie(nx, ny, potNx, potNy) < std::tie(o.nx, o.ny, o.potNx, o.potNy);
     }
 };
 
 struct CbedUnit {
-    std::vector<int> jobs;   // sorted by slice count, descending
-    int smax = 0;
+    std::vector<int> jobs;   // sorted by step count, descending
+    int smax = 0;            // steps of the longest wave
+    int kmax = 0;            // stack slices stored for the widest wave
     size_t bytes = 0;
 };
 
@@ -1092,12 +1094,33 @@ int abs_slices(const qs_params& P) {
     return P.slices * std::max(1, P.cellDiv) * std::max(1, P.mulsRepeat1) * std::max(1, P.mulsRepeat2);
 }
 
-// Device bytes of a unit of nb waves of grid N, slice stacks of smax slices.
-size_t cbed_unit_bytes(const qs_params& P, int nb, int smax) {
+// stack slices an instance stores: one stack per slab, slab 0's alone when
+// the divisions are equal (the reference reuses it)
+int stored_slices(const qs_params& P) {
+    const int D = std::max(1, P.cellDiv);
+    return P.slices * ((D > 1 && !P.equalDivs) ? D : 1);
+}
+
+// the stored slice each step transmits
+void step_slices(const qs_params& P, std::vector<int>& out) {
+    const int D = std::max(1, P.cellDiv), R1 = std::max(1, P.mulsRepeat1), R2 = std::max(1, P.mulsRepeat2);
+    const bool perSlab = D > 1 && !P.equalDivs;
+    out.clear();
+    for (int pc = 0; pc < R2 * D; pc++)
+        for (int r = 0; r < R1; r++)
+            for (int i = 0; i < P.slices; i++) out.push_back((perSlab ? pc % D : 0) * P.slices + i);
+}
+
+// Device bytes of a unit of nb waves of one grid: stacks of kmax slices,
+// probes, waves, patterns, per-wave tables, work items, step table.
+size_t cbed_unit_bytes(const qs_params& P, int nb, int kmax, int smax) {
     const size_t N = (size_t)P.nx * P.ny, Pp = (size_t)P.potNx * P.potNy;
-    return rup256(sizeof(float2) * Pp * smax * nb) + 2 * rup256(sizeof(float2) * N * nb) +
-           rup256(sizeof(float) * N * nb) + rup256(sizeof(float) * (P.nx + P.ny)) +
-           rup256(sizeof(float2) * (P.nx + P.ny)) + 2 * rup256(sizeof(int) * (P.ny + nb));
+    const int C = col_tile_width(P.nx), tmax = (P.ny + C - 1) / C;
+    return rup256(sizeof(float2) * Pp * kmax * nb) + 2 * rup256(sizeof(float2) * N * nb) +
+           rup256(sizeof(float) * N * nb) + 2 * rup256(sizeof(float) * (size_t)(P.nx + P.ny) * nb) +
+           2 * rup256(sizeof(float2) * (size_t)(P.nx + P.ny) * nb) + rup256(sizeof(float) * nb) +
+           rup256(sizeof(int2) * nb) + rup256(sizeof(int2) * (size_t)nb * tmax) + rup256(sizeof(int) * (size_t)smax * nb) +
+           rup256(sizeof(int) * nb);
 }
 
 }  // namespace
@@ -1124,12 +1147,11 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
     QS_CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
 
-    // batches of compatible instances, longest first inside each
+    // batches of instances of one grid, longest first inside each
     std::map<GridKey, std::vector<int>> groups;
     for (int i = 0; i < njobs; i++) {
         const qs_params& P = jobs[i].params;
-        groups[GridKey{P.nx, P.ny, P.potNx, P.potNy, P.resolutionX, P.resolutionY, P.sliceThickness, P.v0}]
-            .push_back(i);
+        groups[GridKey{P.nx, P.ny, P.potNx, P.potNy}].push_back(i);
     }
     size_t freeB = 0, totalB = 0;
     QS_CUDA_TRY(cudaMemGetInfo(&freeB, &totalB));
@@ -1146,14 +1168,18 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
         for (int i : v) {
             const qs_params& P = jobs[i].params;
             const int smax = u.jobs.empty() ? abs_slices(P) : u.smax;
-            const size_t b = cbed_unit_bytes(P, (int)u.jobs.size() + 1, smax);
-            if (!u.jobs.empty() && b > budget) {
+            const int kmax = std::max(u.jobs.empty() ? 0 : u.kmax, stored_slices(P));
+            if (!u.jobs.empty() && cbed_unit_bytes(P, (int)u.jobs.size() + 1, kmax, smax) > budget) {
                 units.push_back(u);
                 u = CbedUnit();
             }
-            if (u.jobs.empty()) u.smax = abs_slices(P);
+            if (u.jobs.empty()) {
+                u.smax = abs_slices(P);
+                u.kmax = 0;
+            }
             u.jobs.push_back(i);
-            u.bytes = cbed_unit_bytes(P, (int)u.jobs.size(), u.smax);
+            u.kmax = std::max(u.kmax, stored_slices(P));
+            u.bytes = cbed_unit_bytes(P, (int)u.jobs.size(), u.kmax, u.smax);
             if (u.bytes > budget) {
                 set_error("job " + std::to_string(i) + " needs " + std::to_string(u.bytes) +
                           " bytes of device memory, more than the " + std::to_string(budget) + " available");
@@ -1177,7 +1203,7 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
     }
     const int nstreams = (int)std::min<size_t>(4, units.size());
     std::vector<cudaStream_t> streams(nstreams, nullptr);
-    std::vector<cudaEvent_t> evs(nstreams + 1, nullptr);
+    std::vector<cudaEvent_t> evs(nstreams, nullptr);
     auto cleanup = [&]() {
         for (auto& e : evs) if (e) cudaEventDestroy(e);
         for (auto& t : streams) if (t) cudaStreamDestroy(t);
@@ -1190,10 +1216,6 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
             rc = QS_ERR_CUDA;
         }
     }
-    if (rc == QS_OK && cudaEventCreateWithFlags(&evs[nstreams], cudaEventDisableTiming) != cudaSuccess) {
-        set_error("event creation failed");
-        rc = QS_ERR_CUDA;
-    }
     size_t admitted = 0;
     for (size_t r = 0; r < rounds.size() && rc == QS_OK; r++) {
         rc = [&]() -> int {
@@ -1205,113 +1227,151 @@ int qs_cbed_batch_run(qs_ctx* c, const qs_cbed_job* jobs, int njobs, size_t max_
             struct Carved {
                 float2 *stacks, *probes, *waves;
                 float* dp;
-                float *kx2, *ky2;
+                float *kx2, *ky2, *k2max;
                 float2 *px, *py;
-                int *tiles, *zeros;
-                PropTables tb;
-                std::vector<int> tilesH;
-                int yA, yB;
+                int2 *band, *items;
+                int *steps, *zeros;
+                std::vector<int> itemStart;  // first work item of each wave (+ the total)
+                std::vector<int> S;          // steps of each wave
             };
             std::vector<Carved> cv(rounds[r].size());
-            // 1. slice stacks and probes on the context's stream
+            // host copies of the round's tables, alive until the round's
+            // closing synchronisation
+            std::vector<std::vector<unsigned char>> hostTabs(rounds[r].size());
+            // one event per unit, recorded once its stacks and probes are
+            // built: its scan starts then, while later units still build
+            std::vector<cudaEvent_t> built(rounds[r].size(), nullptr);
+            struct EvGuard {
+                std::vector<cudaEvent_t>& v;
+                ~EvGuard() { for (auto e : v) if (e) cudaEventDestroy(e); }
+            } guard{built};
+            for (auto& e : built) QS_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            // 1. slice stacks, probes and per-wave tables on the context's stream
             for (size_t k = 0; k < rounds[r].size(); k++) {
                 const CbedUnit& u = units[rounds[r][k]];
                 const qs_params& P0 = jobs[u.jobs[0]].params;
-                const int nb = (int)u.jobs.size();
-                const size_t N = (size_t)P0.nx * P0.ny, Pp = (size_t)P0.potNx * P0.potNy;
+                const int nb = (int)u.jobs.size(), nx = P0.nx, ny = P0.ny;
+                const size_t N = (size_t)nx * ny, Pp = (size_t)P0.potNx * P0.potNy;
+                const int Cw = col_tile_width(nx), tmax = (ny + Cw - 1) / Cw;
                 Carved& C = cv[k];
-                C.stacks = (float2*)take(sizeof(float2) * Pp * u.smax * nb);
+                C.stacks = (float2*)take(sizeof(float2) * Pp * u.kmax * nb);
                 C.probes = (float2*)take(sizeof(float2) * N * nb);
                 C.waves = (float2*)take(sizeof(float2) * N * nb);
                 C.dp = (float*)take(sizeof(float) * N * nb);
-                C.kx2 = (float*)take(sizeof(float) * (P0.nx + P0.ny));
-                C.ky2 = C.kx2 + P0.nx;
-                C.px = (float2*)take(sizeof(float2) * (P0.nx + P0.ny));
-                C.py = C.px + P0.nx;
-                C.tiles = (int*)take(sizeof(int) * (P0.ny + nb));
-                C.zeros = (int*)take(sizeof(int) * (P0.ny + nb));
+                C.kx2 = (float*)take(sizeof(float) * (size_t)nx * nb);
+                C.ky2 = (float*)take(sizeof(float) * (size_t)ny * nb);
+                C.px = (float2*)take(sizeof(float2) * (size_t)nx * nb);
+                C.py = (float2*)take(sizeof(float2) * (size_t)ny * nb);
+                C.k2max = (float*)take(sizeof(float) * nb);
+                C.band = (int2*)take(sizeof(int2) * nb);
+                C.items = (int2*)take(sizeof(int2) * (size_t)nb * tmax);
+                C.steps = (int*)take(sizeof(int) * (size_t)u.smax * nb);
+                C.zeros = (int*)take(sizeof(int) * nb);
+                // host side: tables, bands, work items (grouped by wave) and
+                // the step-to-slice table [step][wave]
+                std::vector<float> kx2(nx * (size_t)nb), ky2(ny * (size_t)nb), k2m(nb);
+                std::vector<float2> pxv(nx * (size_t)nb), pyv(ny * (size_t)nb);
+                std::vector<int2> band(nb), items;
+                std::vector<int> steps((size_t)u.smax * nb, 0), st;
+                C.S.resize(nb);
+                C.itemStart.assign(nb + 1, 0);
+                for (int w = 0; w < nb; w++) {
+                    const qs_params& P = jobs[u.jobs[w]].params;
+                    const PropTables tb = prop_tables(P);
+                    const Band bd = band_tiles(tb, ny, Cw);
+                    std::copy(tb.kx2.begin(), tb.kx2.end(), kx2.begin() + (size_t)w * nx);
+                    std::copy(tb.ky2.begin(), tb.ky2.end(), ky2.begin() + (size_t)w * ny);
+                    std::copy(tb.px.begin(), tb.px.end(), pxv.begin() + (size_t)w * nx);
+                    std::copy(tb.py.begin(), tb.py.end(), pyv.begin() + (size_t)w * ny);
+                    k2m[w] = tb.k2max;
+                    band[w] = make_int2(bd.yA, bd.yB);
+                    C.itemStart[w] = (int)items.size();
+                    for (int t0 : bd.tiles) items.push_back(make_int2(w, t0));
+                    step_slices(P, st);
+                    C.S[w] = (int)st.size();
+                    for (size_t a = 0; a < st.size(); a++) steps[a * nb + w] = st[a];
+                }
+                C.itemStart[nb] = (int)items.size();
+                // one host block per unit (kept in hostTabs), copied piece by piece
+                std::vector<unsigned char>& H = hostTabs[k];
+                struct Up { void* dst; size_t off, bytes; };
+                std::vector<Up> ups;
+                auto add = [&](void* dst, const void* src, size_t bytes) {
+                    if (!bytes) return;
+                    const size_t off = H.size();
+                    H.resize(off + bytes);
+                    std::memcpy(H.data() + off, src, bytes);
+                    ups.push_back({dst, off, bytes});
+                };
+                add(C.kx2, kx2.data(), sizeof(float) * kx2.size());
+                add(C.ky2, ky2.data(), sizeof(float) * ky2.size());
+                add(C.px, pxv.data(), sizeof(float2) * pxv.size());
+                add(C.py, pyv.data(), sizeof(float2) * pyv.size());
+                add(C.k2max, k2m.data(), sizeof(float) * k2m.size());
+                add(C.band, band.data(), sizeof(int2) * band.size());
+                add(C.items, items.data(), sizeof(int2) * items.size());
+                add(C.steps, steps.data(), sizeof(int) * steps.size());
+                for (const Up& up : ups)
+                    QS_CUDA_TRY(cudaMemcpyAsync(up.dst, H.data() + up.off, up.bytes, cudaMemcpyHostToDevice, s));
+                QS_CUDA_TRY(cudaMemsetAsync(C.zeros, 0, sizeof(int) * nb, s));
+                QS_CUDA_TRY(cudaMemsetAsync(C.dp, 0, sizeof(float) * N * nb, s));
                 for (int w = 0; w < nb; w++) {
                     const qs_cbed_job& J = jobs[u.jobs[w]];
-                    // the instance's stack in step order: block b = pc*R1 + r
-                    // of its stacking sequence holds slab pc % cellDiv; each
-                    // slab is built at its first block and copied to the
-                    // others (slab 0 everywhere for equal divisions, which
-                    // the reference reuses)
-                    const int D = std::max(1, J.params.cellDiv), Sj = J.params.slices;
-                    const int R1 = std::max(1, J.params.mulsRepeat1), R2 = std::max(1, J.params.mulsRepeat2);
-                    float2* st0 = C.stacks + (size_t)w * u.smax * Pp;
-                    const size_t blk = (size_t)Sj * Pp;
-                    for (int slab = 0; slab < D; slab++)
-                        if (slab == 0 || !J.params.equalDivs)
-                            QS_TRY(qs_slab_build(c, &J.params, J.atoms, J.natom, slab,
-                                                 (float*)(st0 + (size_t)slab * R1 * blk), 0));
-                    for (int pc = 0; pc < R2 * D; pc++)
-                        for (int r = 0; r < R1; r++) {
-                            const int k = J.params.equalDivs ? 0 : pc % D;
-                            if (pc == k && r == 0) continue;  // the block the slab was built in
-                            QS_CUDA_TRY(cudaMemcpyAsync(st0 + ((size_t)pc * R1 + r) * blk, st0 + (size_t)k * R1 * blk,
-                                                        sizeof(float2) * blk, cudaMemcpyDeviceToDevice, s));
-                        }
+                    // one stack per slab (slab 0's alone for equal divisions)
+                    float2* st0 = C.stacks + (size_t)w * u.kmax * Pp;
+                    const int nslab = stored_slices(J.params) / J.params.slices;
+                    for (int slab = 0; slab < nslab; slab++)
+                        QS_TRY(qs_slab_build(c, &J.params, J.atoms, J.natom, slab,
+                                             (float*)(st0 + (size_t)slab * J.params.slices * Pp), 0));
                     // doCBED's probe position (stem3/stem3.cpp:2096-2100)
                     const double dx = (double)(J.params.scanXStart - J.params.potOffsetX);
                     const double dy = (double)(J.params.scanYStart - J.params.potOffsetY);
                     QS_TRY(probe_into(c, J.params, dx, dy, C.probes + (size_t)w * N));
                 }
-                C.tb = prop_tables(P0);
-                const int ny = P0.ny;
-                const Band band = band_tiles(C.tb, ny, col_tile_width(P0.nx));
-                C.yA = band.yA;
-                C.yB = band.yB;
-                C.tilesH = band.tiles;
-                QS_CUDA_TRY(cudaMemcpyAsync(C.kx2, C.tb.kx2.data(), sizeof(float) * P0.nx, cudaMemcpyHostToDevice, s));
-                QS_CUDA_TRY(cudaMemcpyAsync(C.ky2, C.tb.ky2.data(), sizeof(float) * ny, cudaMemcpyHostToDevice, s));
-                QS_CUDA_TRY(cudaMemcpyAsync(C.px, C.tb.px.data(), sizeof(float2) * P0.nx, cudaMemcpyHostToDevice, s));
-                QS_CUDA_TRY(cudaMemcpyAsync(C.py, C.tb.py.data(), sizeof(float2) * ny, cudaMemcpyHostToDevice, s));
-                if (!C.tilesH.empty())
-                    QS_CUDA_TRY(cudaMemcpyAsync(C.tiles, C.tilesH.data(), sizeof(int) * C.tilesH.size(),
-                                                cudaMemcpyHostToDevice, s));
-                QS_CUDA_TRY(cudaMemsetAsync(C.zeros, 0, sizeof(int) * (P0.ny + nb), s));
-                QS_CUDA_TRY(cudaMemsetAsync(C.dp, 0, sizeof(float) * N * nb, s));
-                if (!twiddles(P0.nx, true) || !twiddles(P0.ny)) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
+                if (!twiddles(nx, true) || !twiddles(ny)) { set_error("twiddle table allocation failed"); return QS_ERR_NOMEM; }
+                QS_CUDA_TRY(cudaEventRecord(built[k], s));
             }
-            QS_CUDA_TRY(cudaEventRecord(evs[nstreams], s));
-            // 2. the units' scans, concurrently on the side streams
+            // 2. the units' scans, concurrently on the side streams, each
+            // after its own unit's build: per step
+            // one row pass over the waves still running and one column pass
+            // for those that go on (inverse) or end here (pattern)
             for (size_t k = 0; k < rounds[r].size(); k++) {
                 const CbedUnit& u = units[rounds[r][k]];
                 const Carved& C = cv[k];
                 cudaStream_t st = streams[k % nstreams];
-                QS_CUDA_TRY(cudaStreamWaitEvent(st, evs[nstreams], 0));
+                QS_CUDA_TRY(cudaStreamWaitEvent(st, built[k], 0));
                 const qs_params& P0 = jobs[u.jobs[0]].params;
                 const int nb = (int)u.jobs.size(), nx = P0.nx, ny = P0.ny;
                 const size_t N = (size_t)nx * ny, Pp = (size_t)P0.potNx * P0.potNy;
-                std::vector<int> S(nb);
-                for (int w = 0; w < nb; w++) S[w] = abs_slices(jobs[u.jobs[w]].params);
                 RowArgs ra{};
                 ra.nx = nx; ra.ny = ny; ra.potNx = P0.potNx; ra.potNy = P0.potNy;
-                ra.probe = C.probes; ra.probe_stride = N; ra.trans_stride = (size_t)u.smax * Pp;
+                ra.probe = C.probes; ra.probe_stride = N; ra.trans_stride = (size_t)u.kmax * Pp;
+                ra.trans_slice = C.stacks; ra.band = C.band;
                 ra.waves = C.waves; ra.posX = C.zeros; ra.posY = C.zeros; ra.tw = twiddles(ny);
-                ra.yA = C.yA; ra.yB = C.yB; ra.norm = (float)(1.0 / (double)N);
+                ra.norm = (float)(1.0 / (double)N);
                 ColArgs ca{};
                 ca.nx = nx; ca.ny = ny; ca.tw = twiddles(nx, true); ca.kx2 = C.kx2; ca.ky2 = C.ky2; ca.px = C.px;
-                ca.py = C.py; ca.k2max = C.tb.k2max; ca.tiles = C.tiles; ca.ntiles = (int)C.tilesH.size();
+                ca.py = C.py; ca.per_wave = 1; ca.k2max_w = C.k2max; ca.waves = C.waves; ca.ndet = 0;
                 ca.scaleDiff = 1.0 / std::sqrt((double)N);
                 for (int sl = 0; sl < u.smax; sl++) {
                     int active = 0, cont = 0;
                     for (int w = 0; w < nb; w++) {
-                        active += S[w] > sl;
-                        cont += S[w] > sl + 1;
+                        active += C.S[w] > sl;
+                        cont += C.S[w] > sl + 1;
                     }
                     ra.nwaves = active;
-                    ra.trans_slice = C.stacks + (size_t)sl * Pp;
+                    ra.step_slice = C.steps + (size_t)sl * nb;
                     QS_TRY(launch_rows(ra, sl == 0 ? ROW_FIRST : ROW_MID, st));
                     if (cont > 0) {
-                        ca.waves = C.waves; ca.nwaves = cont; ca.inverse = 1; ca.diffpat = nullptr; ca.ndet = 0;
+                        ca.nwaves = cont; ca.items = C.items; ca.nitems = C.itemStart[cont];
+                        ca.inverse = 1; ca.diffpat = nullptr;
                         QS_TRY(launch_cols(ca, st));
                     }
                     if (active > cont) {
-                        // waves whose last slice this is: the pattern, no inverse
-                        ca.waves = C.waves + (size_t)cont * N; ca.nwaves = active - cont; ca.inverse = 0;
-                        ca.diffpat = C.dp + (size_t)cont * N; ca.ndet = 0;
+                        // waves whose last step this is: the pattern, no inverse
+                        ca.nwaves = active; ca.items = C.items + C.itemStart[cont];
+                        ca.nitems = C.itemStart[active] - C.itemStart[cont];
+                        ca.inverse = 0; ca.diffpat = C.dp;
                         QS_TRY(launch_cols(ca, st));
                     }
                 }

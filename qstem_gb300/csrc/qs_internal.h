@@ -81,6 +81,10 @@ struct RowArgs {
     const float2* tw;            // twiddle table of the length-ny line transform
     int yA, yB;                  // ky index in band iff iy <= yA || iy >= yB
     float norm;                  // 1/(nx*ny)
+    // waves of different samplings in one launch (each may be null):
+    const int2* band;            // per-wave (yA, yB) in place of yA, yB
+    const int* step_slice;       // per-wave slice of its stack this step transmits
+                                 // (trans_slice then points at slice 0)
 };
 
 // Arguments of one column pass (transforms along x).
@@ -103,6 +107,11 @@ struct ColArgs {
     double* partial;             // [nwaves][ntiles][ndet]
     float* diffpat;              // [nwaves][nx][ny] or null
     double scaleDiff;
+    // waves of different samplings in one launch (no detectors):
+    const int2* items;           // (wave, first column) of each work item, or null
+    long nitems;                 // their number
+    int per_wave;                // kx2, ky2, px, py hold one table per wave (nx or ny apart)
+    const float* k2max_w;        // per-wave k2max, or null
 };
 
 int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s);

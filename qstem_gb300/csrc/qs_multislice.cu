@@ -85,6 +85,12 @@ __global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks
     const int b = (int)(line / a.nx);
     const int x = (int)(line - (long)b * a.nx);
     const SmemRow<Cfg::R0> sm{s_line};
+    int yA = a.yA, yB = a.yB;
+    if (a.band) {
+        const int2 v = __ldg(a.band + b);
+        yA = v.x;
+        yB = v.y;
+    }
     float2 reg[E];
     if constexpr (MODE == ROW_FIRST) {
         const float2* src = a.probe + b * a.probe_stride + (size_t)x * N;
@@ -95,7 +101,7 @@ __global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int y = t + T * e;
-            reg[e] = (y <= a.yA || y >= a.yB) ? src[y] : make_float2(0.f, 0.f);
+            reg[e] = (y <= yA || y >= yB) ? src[y] : make_float2(0.f, 0.f);
         }
         line_fft<Cfg, true>(reg, sm, s_tw, t);
 #pragma unroll
@@ -107,8 +113,9 @@ __global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks
         for (int e = 0; e < E; ++e) dst[t + T * e] = reg[e];
     } else {
         // transmit (stem3/stemlib.cpp:2867-2888): window at (posX, posY)
-        const float2* tr = a.trans_slice + b * a.trans_stride + (size_t)(x + __ldg(a.posX + b)) * a.potNy +
-                           __ldg(a.posY + b);
+        const float2* tr = a.trans_slice + b * a.trans_stride +
+                           (a.step_slice ? (size_t)__ldg(a.step_slice + b) * a.potNx * a.potNy : 0) +
+                           (size_t)(x + __ldg(a.posX + b)) * a.potNy + __ldg(a.posY + b);
 #pragma unroll
         for (int e = 0; e < E; ++e) reg[e] = cmul(reg[e], __ldg(tr + t + T * e));
         line_fft<Cfg, false>(reg, sm, s_tw, t);
@@ -116,7 +123,7 @@ __global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int y = t + T * e;
-            if (!always_out_of_band<N, T>(e) && (y <= a.yA || y >= a.yB)) dst[y] = reg[e];
+            if (!always_out_of_band<N, T>(e) && (y <= yA || y >= yB)) dst[y] = reg[e];
         }
     }
 }
@@ -167,10 +174,23 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_block
     const int c = threadIdx.x, t = threadIdx.y;
     for (int i = tid; i < Cfg::TW; i += NT) s_tw[i] = a.tw[i];
 
+    // work item -> wave b, first column ky0 of its tile, tile index
+    auto decode = [&](long item, int& b, int& ky0, int& tile) {
+        if (a.items) {
+            const int2 v = __ldg(a.items + item);
+            b = v.x;
+            ky0 = v.y;
+            tile = 0;
+        } else {
+            tile = (int)(item % a.ntiles);
+            b = (int)(item / a.ntiles);
+            ky0 = __ldg(a.tiles + tile);
+        }
+    };
     auto column = [&](long item) {
-        const int tile = (int)(item % a.ntiles);
-        const int b = (int)(item / a.ntiles);
-        return a.waves + (size_t)b * a.nx * a.ny + __ldg(a.tiles + tile) + c;
+        int b, ky0, tile;
+        decode(item, b, ky0, tile);
+        return a.waves + (size_t)b * a.nx * a.ny + ky0 + c;
     };
     auto prefetch = [&](long item, int stage) {
         if (item < nitems) {
@@ -201,18 +221,23 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_block
         const SmemCol<C> sm{stage, c};
         line_fft<Cfg, false, true>(reg, sm, s_tw, t);
 
-        const int tile = (int)(item % a.ntiles);
-        const int b = (int)(item / a.ntiles);
-        const int ky = __ldg(a.tiles + tile) + c;
+        int b, ky0, tile;
+        decode(item, b, ky0, tile);
+        const int ky = ky0 + c;
+        // the wave's propagator and k^2 tables
+        const size_t tb = a.per_wave ? (size_t)b : 0;
+        const float* kx2t = a.kx2 + tb * a.nx;
+        const float2* pxt = a.px + tb * a.nx;
+        const float k2max = a.k2max_w ? __ldg(a.k2max_w + b) : a.k2max;
         // propagate_slow (stem3/stemlib.cpp:2831-2849)
-        const float ky2 = __ldg(a.ky2 + ky);
-        const float2 pyv = __ldg(a.py + ky);
+        const float ky2 = __ldg(a.ky2 + tb * a.ny + ky);
+        const float2 pyv = __ldg(a.py + tb * a.ny + ky);
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int kx = t + T * e;
-            const float kx2 = __ldg(a.kx2 + kx);
-            if (!always_out_of_band<N, T>(e) && kx2 < a.k2max && (kx2 + ky2) < a.k2max)
-                reg[e] = cmul(cmul(reg[e], pyv), __ldg(a.px + kx));
+            const float kx2 = __ldg(kx2t + kx);
+            if (!always_out_of_band<N, T>(e) && kx2 < k2max && (kx2 + ky2) < k2max)
+                reg[e] = cmul(cmul(reg[e], pyv), __ldg(pxt + kx));
             else
                 reg[e] = make_float2(0.f, 0.f);
         }
@@ -229,7 +254,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_block
                 const float lo = a.k2in[d], hi = a.k2out[d];
 #pragma unroll
                 for (int e = 0; e < E; ++e) {
-                    const float k2 = __ldg(a.kx2 + t + T * e) + ky2;
+                    const float k2 = __ldg(kx2t + t + T * e) + ky2;
                     const float I = reg[e].x * reg[e].x + reg[e].y * reg[e].y;
                     if (k2 >= lo && k2 <= hi) acc += I;
                 }
@@ -383,7 +408,11 @@ static int cols_n3(const ColArgs& a, cudaStream_t s) {
         return QS_ERR_UNSUPPORTED;
     }
     dim3 block(col_tile<N>(), Cfg::T);
-    const long nitems = (long)a.nwaves * a.ntiles;
+    if (a.items && a.ndet > 0) {
+        set_error("column pass: per-wave work items carry no detector sums");
+        return QS_ERR_ARG;
+    }
+    const long nitems = a.items ? a.nitems : (long)a.nwaves * a.ntiles;
     if (nitems <= 0) return QS_OK;
     const long grid = std::min<long>(nitems, (long)sms * resident);
     ms_cols<N, DET, INV><<<(unsigned)grid, block, sm, s>>>(a, nitems);
