@@ -239,7 +239,9 @@ int qs_multislice_run(qs_ctx *ctx, const qs_params *p, const float *trans, const
  * (stem3/stem3.cpp:2795-2948): make3DSlices + initSTEMSlices from host
  * atoms into a context-owned device stack, then every position of `batch`
  * through qs_multislice_run.  Outputs are HOST buffers (as for QS_HOST_IO);
- * the transmission stack stays on the device. */
+ * the transmission stack stays on the device.  The slice loop runs on the
+ * context's own buffers with QS_GRAPH, so repeated configurations of the same
+ * scan replay it as one CUDA graph. */
 int qs_stem_run(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom,
                 const qs_batch *batch, float *det_images, float *diffpats);
 

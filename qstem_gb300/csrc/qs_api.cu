@@ -1051,8 +1051,10 @@ int qs_stem_run(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, 
         QS_TRY(ensure(c, B_OUT2, sizeof(float) * N * batch->npos, &d));
         ddp = (float*)d;
     }
+    // device buffers of the context throughout: repeated configurations of
+    // one scan replay the slice loop as a CUDA graph
     QS_TRY(qs_multislice_run(c, p, (const float*)dstack, nullptr, batch, ddet, ddp, nullptr,
-                             nslab > 1 ? QS_SLAB_STACKS : 0));
+                             (nslab > 1 ? QS_SLAB_STACKS : 0) | QS_GRAPH));
     if (ddet)
         QS_CUDA_TRY(cudaMemcpyAsync(det_images, ddet, sizeof(float) * (size_t)nT * P.detectorNum * npix,
                                     cudaMemcpyDeviceToHost, c->stream));

@@ -66,7 +66,9 @@ Band band_tiles(const PropTables& t, int ny, int colTile);
 // Arguments of one row pass (transforms along y, the contiguous index).
 enum RowMode { ROW_FIRST = 0, ROW_MID = 1, ROW_LAST = 2 };
 
-struct RowArgs {
+// (RowCore is what the single-sampling row kernels take: the same kernel
+// source given the larger RowArgs compiled to a 17 % slower 512^2 pass)
+struct RowCore {
     int nx, ny, potNx, potNy;
     int nwaves;
     const float2* trans_slice;   // potNx x potNy c64 of the slice applied here
@@ -81,7 +83,9 @@ struct RowArgs {
     const float2* tw;            // twiddle table of the length-ny line transform
     int yA, yB;                  // ky index in band iff iy <= yA || iy >= yB
     float norm;                  // 1/(nx*ny)
-    // waves of different samplings in one launch (each may be null):
+};
+struct RowArgs : RowCore {
+    // waves of different samplings in one launch (both set, or both null):
     const int2* band;            // per-wave (yA, yB) in place of yA, yB
     const int* step_slice;       // per-wave slice of its stack this step transmits
                                  // (trans_slice then points at slice 0)

@@ -68,9 +68,15 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // Shared memory of the row pass: the twiddle table (N float2) and one padded
 // exchange line per line transform.
-template <int N, int MODE>
+// PW: the waves come from instances of different samplings (per-wave bands
+// and step-to-slice table); a compile-time choice, so that the scan of one
+// sampling carries none of it (its kernels take the plain RowCore)
+template <bool PW> struct RowK { using type = RowArgs; };
+template <> struct RowK<false> { using type = RowCore; };
+
+template <int N, int MODE, bool PW>
 __global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks(N))
-    ms_rows(RowArgs a) {
+    ms_rows(typename RowK<PW>::type a) {
     using Cfg = typename Line<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E;
     extern __shared__ float2 dsm[];
@@ -86,7 +92,7 @@ __global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks
     const int x = (int)(line - (long)b * a.nx);
     const SmemRow<Cfg::R0> sm{s_line};
     int yA = a.yA, yB = a.yB;
-    if (a.band) {
+    if constexpr (PW) {
         const int2 v = __ldg(a.band + b);
         yA = v.x;
         yB = v.y;
@@ -113,9 +119,9 @@ __global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks
         for (int e = 0; e < E; ++e) dst[t + T * e] = reg[e];
     } else {
         // transmit (stem3/stemlib.cpp:2867-2888): window at (posX, posY)
-        const float2* tr = a.trans_slice + b * a.trans_stride +
-                           (a.step_slice ? (size_t)__ldg(a.step_slice + b) * a.potNx * a.potNy : 0) +
-                           (size_t)(x + __ldg(a.posX + b)) * a.potNy + __ldg(a.posY + b);
+        const float2* tr = a.trans_slice + b * a.trans_stride + (size_t)(x + __ldg(a.posX + b)) * a.potNy +
+                           __ldg(a.posY + b);
+        if constexpr (PW) tr += (size_t)__ldg(a.step_slice + b) * a.potNx * a.potNy;
 #pragma unroll
         for (int e = 0; e < E; ++e) reg[e] = cmul(reg[e], __ldg(tr + t + T * e));
         line_fft<Cfg, false>(reg, sm, s_tw, t);
@@ -157,7 +163,9 @@ constexpr int col_stages(int n) {
                        : 2;
 }
 
-template <int N, bool DET, bool INVERSE>
+// PW: per-wave work items and propagator/k^2 tables (waves of different
+// samplings; no detectors), compiled only into that variant
+template <int N, bool DET, bool INVERSE, bool PW>
 __global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_blocks(N))
     ms_cols(ColArgs a, long nitems) {
     using Cfg = typename LineCol<N>::cfg;
@@ -176,7 +184,7 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_block
 
     // work item -> wave b, first column ky0 of its tile, tile index
     auto decode = [&](long item, int& b, int& ky0, int& tile) {
-        if (a.items) {
+        if constexpr (PW) {
             const int2 v = __ldg(a.items + item);
             b = v.x;
             ky0 = v.y;
@@ -225,13 +233,19 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_block
         decode(item, b, ky0, tile);
         const int ky = ky0 + c;
         // the wave's propagator and k^2 tables
-        const size_t tb = a.per_wave ? (size_t)b : 0;
-        const float* kx2t = a.kx2 + tb * a.nx;
-        const float2* pxt = a.px + tb * a.nx;
-        const float k2max = a.k2max_w ? __ldg(a.k2max_w + b) : a.k2max;
+        const float *kx2t = a.kx2, *ky2t = a.ky2;
+        const float2 *pxt = a.px, *pyt = a.py;
+        float k2max = a.k2max;
+        if constexpr (PW) {
+            kx2t += (size_t)b * a.nx;
+            pxt += (size_t)b * a.nx;
+            ky2t += (size_t)b * a.ny;
+            pyt += (size_t)b * a.ny;
+            k2max = __ldg(a.k2max_w + b);
+        }
         // propagate_slow (stem3/stemlib.cpp:2831-2849)
-        const float ky2 = __ldg(a.ky2 + tb * a.ny + ky);
-        const float2 pyv = __ldg(a.py + tb * a.ny + ky);
+        const float ky2 = __ldg(ky2t + ky);
+        const float2 pyv = __ldg(pyt + ky);
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const int kx = t + T * e;
@@ -355,33 +369,34 @@ static size_t col_smem_plain() {
     return sizeof(float2) * (N + (size_t)N * col_tile<N>());
 }
 
-template <int N, int MODE>
+template <int N, int MODE, bool PW>
 static int rows_n(const RowArgs& a, cudaStream_t s) {
     using Cfg = typename Line<N>::cfg;
     const size_t sm = row_smem<N>();
-    QS_TRY(smem_attr((const void*)ms_rows<N, MODE>, sm));
+    QS_TRY(smem_attr((const void*)ms_rows<N, MODE, PW>, sm));
     const long lines = (long)a.nwaves * a.nx;
     if (lines % row_lines(N)) {
         set_error("row pass: nwaves*nx must be a multiple of " + std::to_string(row_lines(N)));
         return QS_ERR_ARG;
     }
     dim3 block(Cfg::T, row_lines(N));
-    ms_rows<N, MODE><<<(unsigned)(lines / row_lines(N)), block, sm, s>>>(a);
+    ms_rows<N, MODE, PW><<<(unsigned)(lines / row_lines(N)), block, sm, s>>>(
+        static_cast<const typename RowK<PW>::type&>(a));
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;
 }
 
-template <int MODE>
+template <int MODE, bool PW>
 static int rows_mode(const RowArgs& a, cudaStream_t s) {
     switch (a.ny) {
-        case 64: return rows_n<64, MODE>(a, s);
-        case 128: return rows_n<128, MODE>(a, s);
-        case 256: return rows_n<256, MODE>(a, s);
-        case 384: return rows_n<384, MODE>(a, s);
-        case 512: return rows_n<512, MODE>(a, s);
-        case 768: return rows_n<768, MODE>(a, s);
-        case 1024: return rows_n<1024, MODE>(a, s);
+        case 64: return rows_n<64, MODE, PW>(a, s);
+        case 128: return rows_n<128, MODE, PW>(a, s);
+        case 256: return rows_n<256, MODE, PW>(a, s);
+        case 384: return rows_n<384, MODE, PW>(a, s);
+        case 512: return rows_n<512, MODE, PW>(a, s);
+        case 768: return rows_n<768, MODE, PW>(a, s);
+        case 1024: return rows_n<1024, MODE, PW>(a, s);
     }
     set_error("row pass: unsupported ny");
     return QS_ERR_UNSUPPORTED;
@@ -392,30 +407,31 @@ int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s) {
         set_error("row pass given a null buffer");
         return QS_ERR_ARG;
     }
-    if (mode == ROW_FIRST) return rows_mode<ROW_FIRST>(a, s);
-    if (mode == ROW_MID) return rows_mode<ROW_MID>(a, s);
-    return rows_mode<ROW_LAST>(a, s);
+    const bool pw = a.band != nullptr;
+    if (pw != (a.step_slice != nullptr) || (pw && mode == ROW_LAST)) {
+        set_error("row pass: per-wave bands and step table go together, and not with exit waves");
+        return QS_ERR_ARG;
+    }
+    if (mode == ROW_FIRST) return pw ? rows_mode<ROW_FIRST, true>(a, s) : rows_mode<ROW_FIRST, false>(a, s);
+    if (mode == ROW_MID) return pw ? rows_mode<ROW_MID, true>(a, s) : rows_mode<ROW_MID, false>(a, s);
+    return rows_mode<ROW_LAST, false>(a, s);
 }
 
-template <int N, bool DET, bool INV>
+template <int N, bool DET, bool INV, bool PW>
 static int cols_n3(const ColArgs& a, cudaStream_t s) {
     using Cfg = typename LineCol<N>::cfg;
     const size_t sm = col_smem<N>();
     int resident = 0, sms = 0;  // CTAs per SM (occupancy calculator), SMs
-    QS_TRY(resident_ctas((const void*)ms_cols<N, DET, INV>, col_tile<N>() * Cfg::T, sm, &resident, &sms));
+    QS_TRY(resident_ctas((const void*)ms_cols<N, DET, INV, PW>, col_tile<N>() * Cfg::T, sm, &resident, &sms));
     if (resident < 1) {
         set_error("column pass does not fit on an SM");
         return QS_ERR_UNSUPPORTED;
     }
     dim3 block(col_tile<N>(), Cfg::T);
-    if (a.items && a.ndet > 0) {
-        set_error("column pass: per-wave work items carry no detector sums");
-        return QS_ERR_ARG;
-    }
-    const long nitems = a.items ? a.nitems : (long)a.nwaves * a.ntiles;
+    const long nitems = PW ? a.nitems : (long)a.nwaves * a.ntiles;
     if (nitems <= 0) return QS_OK;
     const long grid = std::min<long>(nitems, (long)sms * resident);
-    ms_cols<N, DET, INV><<<(unsigned)grid, block, sm, s>>>(a, nitems);
+    ms_cols<N, DET, INV, PW><<<(unsigned)grid, block, sm, s>>>(a, nitems);
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;
@@ -424,8 +440,18 @@ static int cols_n3(const ColArgs& a, cudaStream_t s) {
 template <int N>
 static int cols_n(const ColArgs& a, cudaStream_t s) {
     const bool det = a.ndet > 0 || a.diffpat != nullptr;
-    if (det) return a.inverse ? cols_n3<N, true, true>(a, s) : cols_n3<N, true, false>(a, s);
-    return a.inverse ? cols_n3<N, false, true>(a, s) : cols_n3<N, false, false>(a, s);
+    if (a.items) {
+        // per-wave work items and tables: no detector sums; the pattern of
+        // the waves that end here, or the inverse for those that go on
+        if (a.ndet > 0 || !a.per_wave || !a.k2max_w) {
+            set_error("column pass: per-wave work items need per-wave tables and carry no detector sums");
+            return QS_ERR_ARG;
+        }
+        if (a.inverse) return cols_n3<N, false, true, true>(a, s);
+        return cols_n3<N, true, false, true>(a, s);
+    }
+    if (det) return a.inverse ? cols_n3<N, true, true, false>(a, s) : cols_n3<N, true, false, false>(a, s);
+    return a.inverse ? cols_n3<N, false, true, false>(a, s) : cols_n3<N, false, false, false>(a, s);
 }
 
 int launch_cols(const ColArgs& a, cudaStream_t s) {
