@@ -125,6 +125,8 @@ int launch_det_finalize(const double* partial, int nwaves, int ntiles, int ndet,
                         const int* detPosX, const int* detPosY, int scanYN, int npix, float* det_out,
                         cudaStream_t s);
 
+// in-place line transforms of `nlines` contiguous lines of length n
+int line_fft_rows(float2* data, int n, long nlines, bool inverse, cudaStream_t s);
 // generic in-place 2-D transform of `howmany` n0 x n1 arrays
 int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t s);
 int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2, const float* ky2,

@@ -1,4 +1,6 @@
-// qs_multislice.cu -- the fused per-slice passes of the multislice loop.
+// qs_multislice.cu -- the fused per-slice passes of the multislice loop: the
+// column pass, the generic 2-D transforms and the band limit (the row pass
+// is in qs_rows.cu, compiled in parallel).
 //
 // The reference's slice step (runMulsSTEM, stem3/stemlib.cpp:2403-2486) is
 //   transmit -> FFT2 -> propagate_slow -> collectIntensity -> IFFT2 -> /N.
@@ -28,34 +30,6 @@
 
 namespace qs {
 
-// lines per CTA of the plain line-FFT kernels (fft_rows)
-constexpr int ROW_LINES = 8;
-
-// lines per CTA of the row pass, per line length (qs_tuned.h)
-constexpr int row_lines(int n) {
-    return n == 64     ? QS_ROW_LINES_64
-           : n == 128  ? QS_ROW_LINES_128
-           : n == 256  ? QS_ROW_LINES_256
-           : n == 384  ? QS_ROW_LINES_384
-           : n == 512  ? QS_ROW_LINES_512
-           : n == 768  ? QS_ROW_LINES_768
-           : n == 1024 ? QS_ROW_LINES_1024
-                       : 8;
-}
-
-// CTAs per SM the row pass is compiled for (register budget), per line
-// length, from the measured table in qs_tuned.h
-constexpr int row_min_blocks(int n) {
-    return n == 64     ? QS_ROW_MIN_BLOCKS_64
-           : n == 128  ? QS_ROW_MIN_BLOCKS_128
-           : n == 256  ? QS_ROW_MIN_BLOCKS_256
-           : n == 384  ? QS_ROW_MIN_BLOCKS_384
-           : n == 512  ? QS_ROW_MIN_BLOCKS_512
-           : n == 768  ? QS_ROW_MIN_BLOCKS_768
-           : n == 1024 ? QS_ROW_MIN_BLOCKS_1024
-                       : 1;
-}
-
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
@@ -64,74 +38,6 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int PENDING>
 __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
-}
-
-// Shared memory of the row pass: the twiddle table (N float2) and one padded
-// exchange line per line transform.
-// PW: the waves come from instances of different samplings (per-wave bands
-// and step-to-slice table); a compile-time choice, so that the scan of one
-// sampling carries none of it (its kernels take the plain RowCore)
-template <bool PW> struct RowK { using type = RowArgs; };
-template <> struct RowK<false> { using type = RowCore; };
-
-template <int N, int MODE, bool PW>
-__global__ void __launch_bounds__(line_threads(N) * row_lines(N), row_min_blocks(N))
-    ms_rows(typename RowK<PW>::type a) {
-    using Cfg = typename Line<N>::cfg;
-    constexpr int T = Cfg::T, E = Cfg::E;
-    extern __shared__ float2 dsm[];
-    float2* s_tw = dsm;
-    float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
-    const int tid = threadIdx.x + T * threadIdx.y;
-    for (int i = tid; i < Cfg::TW; i += T * row_lines(N)) s_tw[i] = a.tw[i];
-    __syncthreads();
-
-    const int t = threadIdx.x;
-    const long line = (long)blockIdx.x * row_lines(N) + threadIdx.y;
-    const int b = (int)(line / a.nx);
-    const int x = (int)(line - (long)b * a.nx);
-    const SmemRow<Cfg::R0> sm{s_line};
-    int yA = a.yA, yB = a.yB;
-    if constexpr (PW) {
-        const int2 v = __ldg(a.band + b);
-        yA = v.x;
-        yB = v.y;
-    }
-    float2 reg[E];
-    if constexpr (MODE == ROW_FIRST) {
-        const float2* src = a.probe + b * a.probe_stride + (size_t)x * N;
-#pragma unroll
-        for (int e = 0; e < E; ++e) reg[e] = __ldg(src + t + T * e);
-    } else {
-        const float2* src = a.waves + ((size_t)b * a.nx + x) * N;
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const int y = t + T * e;
-            reg[e] = (y <= yA || y >= yB) ? src[y] : make_float2(0.f, 0.f);
-        }
-        line_fft<Cfg, true>(reg, sm, s_tw, t);
-#pragma unroll
-        for (int e = 0; e < E; ++e) reg[e] = cscale(reg[e], a.norm);
-    }
-    if constexpr (MODE == ROW_LAST) {
-        float2* dst = a.exit_waves + ((size_t)b * a.nx + x) * N;
-#pragma unroll
-        for (int e = 0; e < E; ++e) dst[t + T * e] = reg[e];
-    } else {
-        // transmit (stem3/stemlib.cpp:2867-2888): window at (posX, posY)
-        const float2* tr = a.trans_slice + b * a.trans_stride + (size_t)(x + __ldg(a.posX + b)) * a.potNy +
-                           __ldg(a.posY + b);
-        if constexpr (PW) tr += (size_t)__ldg(a.step_slice + b) * a.potNx * a.potNy;
-#pragma unroll
-        for (int e = 0; e < E; ++e) reg[e] = cmul(reg[e], __ldg(tr + t + T * e));
-        line_fft<Cfg, false>(reg, sm, s_tw, t);
-        float2* dst = (a.waves_out ? a.waves_out : a.waves) + ((size_t)b * a.nx + x) * N;
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const int y = t + T * e;
-            if (!always_out_of_band<N, T>(e) && (y <= yA || y >= yB)) dst[y] = reg[e];
-        }
-    }
 }
 
 // Column pass, persistent: each CTA walks the (wave, column tile) work items
@@ -357,64 +263,12 @@ int resident_ctas(const void* func, int threads, size_t bytes, int* ctas, int* s
 }
 
 template <int N>
-static size_t row_smem(int lines = row_lines(N)) {
-    return sizeof(float2) * (N + (size_t)lines * Line<N>::cfg::SMEM);
-}
-template <int N>
 static size_t col_smem() {
     return sizeof(float2) * (N + (size_t)col_stages(N) * N * col_tile<N>());
 }
 template <int N>
 static size_t col_smem_plain() {
     return sizeof(float2) * (N + (size_t)N * col_tile<N>());
-}
-
-template <int N, int MODE, bool PW>
-static int rows_n(const RowArgs& a, cudaStream_t s) {
-    using Cfg = typename Line<N>::cfg;
-    const size_t sm = row_smem<N>();
-    QS_TRY(smem_attr((const void*)ms_rows<N, MODE, PW>, sm));
-    const long lines = (long)a.nwaves * a.nx;
-    if (lines % row_lines(N)) {
-        set_error("row pass: nwaves*nx must be a multiple of " + std::to_string(row_lines(N)));
-        return QS_ERR_ARG;
-    }
-    dim3 block(Cfg::T, row_lines(N));
-    ms_rows<N, MODE, PW><<<(unsigned)(lines / row_lines(N)), block, sm, s>>>(
-        static_cast<const typename RowK<PW>::type&>(a));
-    QS_CUDA_TRY(cudaGetLastError());
-    count_launch(1);
-    return QS_OK;
-}
-
-template <int MODE, bool PW>
-static int rows_mode(const RowArgs& a, cudaStream_t s) {
-    switch (a.ny) {
-        case 64: return rows_n<64, MODE, PW>(a, s);
-        case 128: return rows_n<128, MODE, PW>(a, s);
-        case 256: return rows_n<256, MODE, PW>(a, s);
-        case 384: return rows_n<384, MODE, PW>(a, s);
-        case 512: return rows_n<512, MODE, PW>(a, s);
-        case 768: return rows_n<768, MODE, PW>(a, s);
-        case 1024: return rows_n<1024, MODE, PW>(a, s);
-    }
-    set_error("row pass: unsupported ny");
-    return QS_ERR_UNSUPPORTED;
-}
-
-int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s) {
-    if ((mode == ROW_FIRST ? !a.probe : !a.waves) || (mode == ROW_LAST ? !a.exit_waves : !(a.waves_out || a.waves))) {
-        set_error("row pass given a null buffer");
-        return QS_ERR_ARG;
-    }
-    const bool pw = a.band != nullptr;
-    if (pw != (a.step_slice != nullptr) || (pw && mode == ROW_LAST)) {
-        set_error("row pass: per-wave bands and step table go together, and not with exit waves");
-        return QS_ERR_ARG;
-    }
-    if (mode == ROW_FIRST) return pw ? rows_mode<ROW_FIRST, true>(a, s) : rows_mode<ROW_FIRST, false>(a, s);
-    if (mode == ROW_MID) return pw ? rows_mode<ROW_MID, true>(a, s) : rows_mode<ROW_MID, false>(a, s);
-    return rows_mode<ROW_LAST, false>(a, s);
 }
 
 template <int N, bool DET, bool INV, bool PW>
@@ -499,30 +353,6 @@ int launch_det_finalize(const double* partial, int nwaves, int ntiles, int ndet,
 
 // ------------------------------------------------ generic 2-D transforms
 template <int N, bool INV>
-__global__ void __launch_bounds__(line_threads(N) * ROW_LINES) fft_rows(float2* data, long nlines, const float2* tw) {
-    using Cfg = typename Line<N>::cfg;
-    constexpr int T = Cfg::T, E = Cfg::E;
-    extern __shared__ float2 dsm[];
-    float2* s_tw = dsm;
-    float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
-    const int tid = threadIdx.x + T * threadIdx.y;
-    for (int i = tid; i < Cfg::TW; i += T * ROW_LINES) s_tw[i] = tw[i];
-    __syncthreads();
-    const long line = (long)blockIdx.x * ROW_LINES + threadIdx.y;
-    const bool ok = line < nlines;
-    float2* p = data + (ok ? line : 0) * N;
-    const int t = threadIdx.x;
-    float2 reg[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) reg[e] = ok ? p[t + T * e] : make_float2(0.f, 0.f);
-    line_fft<Cfg, INV>(reg, SmemRow<Cfg::R0>{s_line}, s_tw, t);
-    if (ok) {
-#pragma unroll
-        for (int e = 0; e < E; ++e) p[t + T * e] = reg[e];
-    }
-}
-
-template <int N, bool INV>
 __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
     fft_cols(float2* data, int ncols, const float2* tw) {
     // columns of length N, row stride ncols; blockIdx.y = array index
@@ -549,17 +379,6 @@ __global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
 }
 
 template <int N, bool INV>
-static int fft_rows_n(float2* data, long nlines, cudaStream_t s) {
-    const size_t sm = row_smem<N>(ROW_LINES);
-    QS_TRY(smem_attr((const void*)fft_rows<N, INV>, sm));
-    dim3 block(Line<N>::cfg::T, ROW_LINES);
-    fft_rows<N, INV><<<(unsigned)((nlines + ROW_LINES - 1) / ROW_LINES), block, sm, s>>>(data, nlines, twiddles(N));
-    QS_CUDA_TRY(cudaGetLastError());
-    count_launch(1);
-    return QS_OK;
-}
-
-template <int N, bool INV>
 static int fft_cols_n(float2* data, int ncols, int howmany, cudaStream_t s) {
     const size_t sm = col_smem_plain<N>();
     QS_TRY(smem_attr((const void*)fft_cols<N, INV>, sm));
@@ -570,21 +389,6 @@ static int fft_cols_n(float2* data, int ncols, int howmany, cudaStream_t s) {
     QS_CUDA_TRY(cudaGetLastError());
     count_launch(1);
     return QS_OK;
-}
-
-template <bool INV>
-static int fft_rows_any(float2* data, int n, long nlines, cudaStream_t s) {
-    switch (n) {
-        case 64: return fft_rows_n<64, INV>(data, nlines, s);
-        case 128: return fft_rows_n<128, INV>(data, nlines, s);
-        case 256: return fft_rows_n<256, INV>(data, nlines, s);
-        case 384: return fft_rows_n<384, INV>(data, nlines, s);
-        case 512: return fft_rows_n<512, INV>(data, nlines, s);
-        case 768: return fft_rows_n<768, INV>(data, nlines, s);
-        case 1024: return fft_rows_n<1024, INV>(data, nlines, s);
-    }
-    set_error("fft2d: unsupported row length " + std::to_string(n));
-    return QS_ERR_UNSUPPORTED;
 }
 
 template <bool INV>
@@ -609,10 +413,10 @@ int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t 
     }
     const long lines = (long)n0 * howmany;
     if (inverse) {
-        QS_TRY(fft_rows_any<true>(data, n1, lines, s));
+        QS_TRY(line_fft_rows(data, n1, lines, true, s));
         QS_TRY(fft_cols_any<true>(data, n0, n1, howmany, s));
     } else {
-        QS_TRY(fft_rows_any<false>(data, n1, lines, s));
+        QS_TRY(line_fft_rows(data, n1, lines, false, s));
         QS_TRY(fft_cols_any<false>(data, n0, n1, howmany, s));
     }
     return QS_OK;
@@ -636,7 +440,7 @@ int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2,
         set_error("twiddle table allocation failed");
         return QS_ERR_NOMEM;
     }
-    QS_TRY(fft_rows_any<false>(data, n1, (long)n0 * howmany, s));
+    QS_TRY(line_fft_rows(data, n1, (long)n0 * howmany, false, s));
     ColArgs ca{};
     ca.nx = n0;
     ca.ny = n1;
@@ -655,7 +459,7 @@ int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2,
     ca.ndet = 0;
     ca.diffpat = nullptr;
     QS_TRY(launch_cols(ca, s));
-    QS_TRY(fft_rows_any<true>(data, n1, (long)n0 * howmany, s));
+    QS_TRY(line_fft_rows(data, n1, (long)n0 * howmany, true, s));
     return QS_OK;
 }
 

@@ -13,7 +13,7 @@ column transform the one with the fastest column pass, independently.
 
 Phase 1, row and column passes: for each candidate budget k and row-pass
 shape L (line transforms per CTA, --lines) the slice-loop translation unit
-(qs_multislice.cu) is compiled with every QS_ROW_LINES_<N> = L and
+(qs_multislice.cu, qs_rows.cu) is compiled with every QS_ROW_LINES_<N> = L and
 QS_ROW_MIN_BLOCKS_<N> = QS_COL_MIN_BLOCKS_<N> = k and linked with the other
 objects of the normal build into a variant library in a temporary folder
 (the candidates compile in parallel).  Each variant times, in a fresh
@@ -45,19 +45,28 @@ RADIX_ALTS = {384: 5, 512: 2, 768: 5, 1024: 2}
 TILE16 = (64, 128, 256, 384, 512, 768)
 
 
-def _variant(tag, source, defs, tmp, extra_objs=()):
-    """Compile `source` with -D`defs` and link it with the normal build's
-    other objects (or `extra_objs` in their place) into a variant library."""
-    replaced = {os.path.basename(o).split("@")[0] for o in extra_objs} | {source}
+# the slice-loop translation units (row pass, column pass and transforms)
+SLICE_LOOP = ("qs_multislice.cu", "qs_rows.cu")
+
+
+def _variant(tag, sources, defs, tmp, extra_objs=()):
+    """Compile `sources` (one name or several) with -D`defs` and link them
+    with the normal build's other objects (or `extra_objs` in their place)
+    into a variant library.  Returns (library, [objects])."""
+    sources = [sources] if isinstance(sources, str) else list(sources)
+    replaced = {os.path.basename(o).split("@")[0] for o in extra_objs} | set(sources)
     objs = [os.path.join(_build.BUILD, s.replace(".cu", ".o")) for s in _build.SOURCES if s not in replaced]
-    obj = os.path.join(tmp, "%s@%s.o" % (source, tag))
-    cmd = ([_build.nvcc()] + _build.ARCH + _build.FLAGS + ["-D" + d for d in defs] +
-           ["-c", os.path.join(_build.SRC, source), "-o", obj])
-    subprocess.run(cmd, check=True, capture_output=True)
+    built = []
+    for source in sources:
+        obj = os.path.join(tmp, "%s@%s.o" % (source, tag))
+        cmd = ([_build.nvcc()] + _build.ARCH + _build.FLAGS + ["-D" + d for d in defs] +
+               ["-c", os.path.join(_build.SRC, source), "-o", obj])
+        subprocess.run(cmd, check=True, capture_output=True)
+        built.append(obj)
     lib = os.path.join(tmp, "libqstem_gpu_%s.so" % tag)
-    subprocess.run([_build.nvcc()] + _build.ARCH + ["-shared", "-o", lib, obj] + list(extra_objs) + objs +
+    subprocess.run([_build.nvcc()] + _build.ARCH + ["-shared", "-o", lib] + built + list(extra_objs) + objs +
                    ["-lcudart"], check=True, capture_output=True)
-    return lib, obj
+    return lib, built
 
 
 def measure(lib_path, sizes, reps=4):
@@ -166,7 +175,7 @@ def tune_factorisations(sizes, tmp):
         variants[v] = ["QS_COL_TILE_%d=%d" % (n, c if (st == 1 or c == 8 or n in TILE16) else 8) for n in sizes] + \
                       ["QS_COL_STAGES_%d=%d" % (n, st) for n in sizes]
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(variants)) as ex:
-        libs = dict(zip(variants, ex.map(lambda v: _variant(v, "qs_multislice.cu", variants[v], tmp)[0], variants)))
+        libs = dict(zip(variants, ex.map(lambda v: _variant(v, SLICE_LOOP, variants[v], tmp)[0], variants)))
     res = {v: _run_measure("--measure", sizes, libs[v]) for v in variants}
     best = {}
     print("factorisation k: row | column pass, us per position-slice")
@@ -220,7 +229,7 @@ def main(argv=None):
             ["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, k) for n in sizes for kind in ("ROW", "COL")] for L, k in combos}
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(combos)) as ex:
         libs = dict(zip(combos, ex.map(
-            lambda c: _variant("rc%d_%d" % c, "qs_multislice.cu", defs[c], tmp)[0], combos)))
+            lambda c: _variant("rc%d_%d" % c, SLICE_LOOP, defs[c], tmp)[0], combos)))
     res = {c: _run_measure("--measure", sizes, libs[c]) for c in combos}
     print("row pass, us per position-slice (lines per CTA x CTAs per SM)")
     print("N     " + "".join("%8s" % ("%dx%d" % c) for c in combos))
@@ -238,13 +247,13 @@ def main(argv=None):
     # phase 2: row adjoint, with the phase-1 winners
     fixed = (fdefs + ["QS_%s_MIN_BLOCKS_%d=%d" % (kind, n, best[(kind, n)]) for n in sizes for kind in ("ROW", "COL")] +
              ["QS_ROW_LINES_%d=%d" % (n, best[("LINES", n)]) for n in sizes])
-    _, ms_obj = _variant("fixed", "qs_multislice.cu", fixed, tmp)
+    _, ms_objs = _variant("fixed", SLICE_LOOP, fixed, tmp)
     # the adjoint's kernels share the factorisations and tiles (their twiddle
     # tables come from the slice-loop object)
     adefs = {k: fdefs + ["QS_ADJ_MIN_BLOCKS_%d=%d" % (n, k) for n in sizes] for k in cands}
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(cands)) as ex:
         alibs = dict(zip(cands, ex.map(
-            lambda k: _variant("adj%d" % k, "qs_adjoint.cu", adefs[k], tmp, extra_objs=[ms_obj])[0], cands)))
+            lambda k: _variant("adj%d" % k, "qs_adjoint.cu", adefs[k], tmp, extra_objs=ms_objs)[0], cands)))
     ares = {k: _run_measure("--measure-adjoint", sizes, alibs[k]) for k in cands}
     print("adjoint (every state kept, 8 slices), ms")
     print("N     " + "".join("%8d" % k for k in cands))
