@@ -146,13 +146,16 @@ def adjoint_measure(ctx, torch, reps=3, npix=32):
         return best, out
 
     t_fwd, _ = timed(lambda: ctx.multislice(p, T, probe, want_det=False, diffpats=dps, sync=False))
+    t_fwd_res, _ = timed(lambda: ctx.multislice(p, T, probe, want_det=False, diffpats=dps, sync=False,
+                                                resident=True))
     t_adj6, (loss, dV, _) = timed(lambda: ctx.adjoint(p, T, probe, target, ckpt=6))
     t_adj1, _ = timed(lambda: ctx.adjoint(p, T, probe, target, ckpt=1))
     t_adj0, _ = timed(lambda: ctx.adjoint(p, T, probe, target, ckpt=0))
     t_adjd, _ = timed(lambda: ctx.adjoint(p, T, probe, target, ckpt=6, deterministic=True))
     t_atoms, _ = timed(lambda: ctx.atoms_grad(p, atoms, dV))
     return {"workload": "4D-STEM SrTiO3 6x6x20, 256^2, 40 slices, 32x32 positions, 25 mrad, potential %dx%d"
-            % (p.potNx, p.potNy), "positions": npos, "forward_ms": t_fwd, "adjoint_ms": t_adj6,
+            % (p.potNx, p.potNy), "positions": npos, "forward_ms": t_fwd, "forward_resident_ms": t_fwd_res,
+            "adjoint_ms": t_adj6,
             "adjoint_over_forward": t_adj6 / t_fwd, "checkpoint_every": 6, "adjoint_ms_all_states": t_adj1,
             "adjoint_over_forward_all_states": t_adj1 / t_fwd, "adjoint_ms_auto": t_adj0,
             "adjoint_over_forward_auto": t_adj0 / t_fwd, "adjoint_ms_deterministic": t_adjd,
@@ -231,15 +234,15 @@ def stem256_measure(ctx, torch, cpu=True, reps=5):
     det = torch.zeros((p.thickness_count(), p.detectorNum, p.scanXN, p.scanYN), dtype=torch.float32, device="cuda")
     stream = torch.cuda.ExternalStream(ctx.stream_handle)
 
-    def scan_ms(graph):
+    def scan_ms(graph, resident=False):
         for _ in range(3):
-            ctx.multislice(p, T, probe, det=det, graph=graph)
+            ctx.multislice(p, T, probe, det=det, graph=graph, resident=resident)
         best = None
         for _ in range(reps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             e0.record(stream)
-            ctx.multislice(p, T, probe, det=det, graph=graph, sync=False)
+            ctx.multislice(p, T, probe, det=det, graph=graph, sync=False, resident=resident)
             e1.record(stream)
             torch.cuda.synchronize()
             t = e0.elapsed_time(e1)
@@ -247,9 +250,12 @@ def stem256_measure(ctx, torch, cpu=True, reps=5):
         return best
 
     launched, graphed = scan_ms(False), scan_ms(True)
+    # the wave-resident loop (QS_RESIDENT: one launch, waves on chip)
+    resident = scan_ms(True, resident=True)
     out = {"workload": "stem-haadf-256: SrTiO3 5x5x10, 256^2, 20 slices, 16x16 positions, HAADF 70-200 mrad, "
                        "no thermal displacement",
            "e2e_ms": best * 1e3, "positions_per_s": npos / best, "scan_ms": launched, "scan_graph_ms": graphed,
+           "scan_resident_ms": resident,
            "scan_positions_per_s": npos / (graphed * 1e-3), "haadf_mean": float(img.mean())}
     if cpu:
         from oracle import oracle

@@ -79,6 +79,11 @@ extern "C" {
                                    the same parameters, buffers and batch) */
 #define QS_DETERMINISTIC 64u    /* qs_adjoint_run: sum dL/dV over positions in a fixed order
                                    (bit-reproducible, slower) instead of with float atomics */
+#define QS_RESIDENT 128u        /* qs_multislice_run with 256 x 256 waves: the whole slice
+                                   loop in one launch, each wave held on chip by a cluster
+                                   of four CTAs for all of its slices, instead of a row and
+                                   a column pass per slice through HBM (measured slower:
+                                   the passes are issue-bound, not HBM-bound, at 256^2) */
 
 /* run modes, same numbering as libs/stemtypes_fftw3.h:35-42 */
 #define QS_MODE_STEM 1
@@ -230,6 +235,9 @@ int qs_probe(qs_ctx *ctx, const qs_params *p, double dx, double dy, float *wave,
  * diff_<t>.img of CBED runs (stem3/stemlib.cpp:2663-2676) and, for the slots
  * interimWave writes, its wave_<t>.img (stem3/stemlib.cpp:2538-2565); the
  * last slot is the final slice's.
+ * Each slice is a row pass and a column pass over the batch; with
+ * QS_RESIDENT, 256 x 256 waves (without QS_SERIES exit waves) run the whole
+ * loop in one launch with each wave resident on chip.
  * Buffers are device pointers, or host pointers with QS_HOST_IO. */
 int qs_multislice_run(qs_ctx *ctx, const qs_params *p, const float *trans, const float *probe,
                       const qs_batch *batch, float *det_images, float *diffpats,

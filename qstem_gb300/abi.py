@@ -21,6 +21,7 @@ QS_SLAB_STACKS = 8
 QS_SERIES = 16
 QS_GRAPH = 32
 QS_DETERMINISTIC = 64
+QS_RESIDENT = 128
 
 QS_MODE_STEM = 1
 QS_MODE_CBED = 2

@@ -83,7 +83,7 @@ static int ev_record(qs_ctx* c, size_t* idx) {
 
 enum Buf {
     B_WAVES, B_PROBE, B_PARTIAL, B_POS, B_TABLES, B_TILES, B_TRANS, B_OUT1, B_OUT2, B_OUT3, B_JOBS, B_LUTS,
-    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, B_BAND, B_VREAL, B_KNOTS, NBUF
+    B_LUTPTR, B_SUM, B_DIFF_IN, B_ADJ, B_TEM, B_CBED, B_DFT, B_BAND, B_VREAL, B_KNOTS, B_STEPS, NBUF
 };
 static_assert(NBUF <= kMaxBufs, "context buffer table too small");
 enum Pin { P_JOBS, P_LUTPTR, P_BAND, P_TABLES, P_KNOTS };
@@ -808,6 +808,20 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     // QS_SERIES: one pattern / exit wave per thickness slot
     const bool series = (flags & QS_SERIES) != 0;
     const size_t nS = series ? (size_t)nT : 1;
+    // QS_RESIDENT: the wave-resident loop (256 x 256, the band's columns
+    // within the cluster's, no real-space waves of intermediate slots)
+    int nbCols = 0;
+    for (int iy = 0; iy < ny; iy++) nbCols += (iy <= yA || iy >= yB) ? 1 : 0;
+    bool resident = (flags & QS_RESIDENT) && nx == 256 && ny == 256 && !(series && exit_waves) &&
+                    nbCols <= resident_band_columns();
+    if (resident) {
+        int clusters = 0;
+        QS_TRY(resident_clusters(&clusters));
+        resident = clusters > 0;
+    }
+    // detector partial sums per wave: one per column tile, or one per CTA of
+    // the resident loop's cluster
+    const int detParts = resident ? 4 : ntiles;
 
     // device buffers: tables | tiles | positions
     void* dtab = nullptr;
@@ -834,6 +848,15 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     QS_CUDA_TRY(cudaMemcpyAsync(d_py_pos, py.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
     QS_CUDA_TRY(cudaMemcpyAsync(d_dx_pos, dxp.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
     QS_CUDA_TRY(cudaMemcpyAsync(d_dy_pos, dyp.data(), sizeof(int) * npos, cudaMemcpyHostToDevice, s));
+    int* d_steps = nullptr;  // resident loop: [stack slice | slot] of every step
+    if (resident) {
+        std::vector<int> st(stepSlice);
+        st.insert(st.end(), slotOf.begin(), slotOf.end());
+        void* d = nullptr;
+        QS_TRY(ensure(c, B_STEPS, sizeof(int) * st.size(), &d));
+        d_steps = (int*)d;
+        QS_CUDA_TRY(cudaMemcpyAsync(d_steps, st.data(), sizeof(int) * st.size(), cudaMemcpyHostToDevice, s));
+    }
 
     // transmission and probe
     const size_t nTrans = (size_t)S * P.potNx * P.potNy * (slabStacks ? D : 1);
@@ -870,7 +893,7 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     // batch chunking by free device memory (admission control)
     size_t freeB = 0, totalB = 0;
     QS_CUDA_TRY(cudaMemGetInfo(&freeB, &totalB));
-    const size_t perWave = sizeof(float2) * N + (size_t)nT * ntiles * std::max(ndet, 1) * sizeof(double) +
+    const size_t perWave = sizeof(float2) * N + (size_t)nT * detParts * std::max(ndet, 1) * sizeof(double) +
                            (host && diffpats ? sizeof(float) * N * nS : 0) +
                            (host && exit_waves ? sizeof(float2) * N * nS : 0);
     const size_t have = c->cap[B_WAVES] / (sizeof(float2) * N);
@@ -883,7 +906,7 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
     QS_TRY(ensure(c, B_WAVES, sizeof(float2) * N * chunk, &dw));
     float2* waves = (float2*)dw;
     void* dpart = nullptr;
-    const size_t partPerT = chunk * ntiles * std::max(ndet, 1);
+    const size_t partPerT = chunk * detParts * std::max(ndet, 1);
     QS_TRY(ensure(c, B_PARTIAL, sizeof(double) * partPerT * nT, &dpart));
     float* dp_dev = nullptr;
     if (diffpats && host) {
@@ -958,6 +981,22 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
         if (dpOut)
             for (size_t k = 0; k < nS; k++)
                 QS_CUDA_TRY(cudaMemsetAsync(dpOut + k * slotStride, 0, sizeof(float) * N * nb, s));
+        if (resident) {
+            ResidentArgs r{};
+            r.potNx = P.potNx; r.potNy = P.potNy; r.nwaves = nb; r.nsteps = NS;
+            r.trans = transChunk; r.trans_stride = transStride;
+            r.probe = ra.probe; r.probe_stride = probeStride;
+            r.posX = ra.posX; r.posY = ra.posY;
+            r.step_slice = d_steps; r.step_slot = d_steps + NS;
+            r.tw = tw_y; r.yA = yA; r.yB = yB; r.nb = nbCols;
+            r.kx2 = d_kx2; r.ky2 = d_ky2; r.px = d_px; r.py = d_py; r.k2max = tb.k2max;
+            r.ndet = wantDet ? ndet : 0;
+            for (int d = 0; d < ndet; d++) { r.k2in[d] = ca.k2in[d]; r.k2out[d] = ca.k2out[d]; }
+            r.partial = (double*)dpart; r.partial_slot = partPerT;
+            r.diffpat = dpOut; r.dp_slot = slotStride; r.series = series ? 1 : 0;
+            r.exit_waves = ewOut; r.norm = ra.norm; r.scaleDiff = ca.scaleDiff;
+            QS_TRY(launch_resident(r, s));
+        } else {
         ra.trans_slice = sliceOf(0);
         QS_TRY(rows(ROW_FIRST));
         for (int a = 0; a < NS; a++) {
@@ -984,10 +1023,11 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
             ra.exit_waves = ewOut + (series ? (size_t)(nT - 1) * slotStride : 0);
             QS_TRY(launch_rows(ra, ROW_LAST, s));
         }
+        }
         if (wantDet)
             for (int t = 0; t < nT; t++) {
                 if (lastWriter[t] < 0) continue;
-                QS_TRY(launch_det_finalize((double*)dpart + (size_t)t * partPerT, nb, ntiles, ndet, scaleDet,
+                QS_TRY(launch_det_finalize((double*)dpart + (size_t)t * partPerT, nb, detParts, ndet, scaleDet,
                                            d_dx_pos + p0, d_dy_pos + p0, P.scanYN, npix,
                                            det_dev + (size_t)t * ndet * npix, s));
             }
@@ -999,7 +1039,7 @@ static int multislice_run_ex(qs_ctx* c, const qs_params* p, const float* trans_i
         if (graph)
             key.add(P).add(flags).add(trans_in).add(transStride).add(dprobe).add(probeStride).add(det_dev)
                 .add(diffpats).add(exit_waves).add(p0).add(nb).add(chunk).add(npos).add(waves).add(dpart).add(dtab)
-                .add(dtiles).add(dpos).add(tw_y).add(tw_x);
+                .add(dtiles).add(dpos).add(tw_y).add(tw_x).add(d_steps);
         QS_TRY(run_graphed(c, s, graph, key.b, work));
         for (size_t k = 0; k < nS; k++) {
             if (host && diffpats)

@@ -266,14 +266,37 @@ __device__ __forceinline__ void line_sync() {
     if constexpr (BLOCK) __syncthreads();
     else __syncwarp();
 }
+// the synchronisation between the passes of a line transform, as a type
+template <bool BLOCK>
+struct LineSync {
+    __device__ __forceinline__ static void sync() { line_sync<BLOCK>(); }
+};
+// named barrier ID over the first COUNT threads of the block (COUNT a
+// multiple of 32): lines spread over a subset of the block's warps
+template <int ID, int COUNT>
+struct NamedBarrier {
+    static_assert(COUNT % 32 == 0, "a named barrier counts whole warps");
+    __device__ __forceinline__ static void sync() { asm volatile("bar.sync %0, %1;" ::"n"(ID), "n"(COUNT) : "memory"); }
+};
 
 // Transform the E registers of thread t (elements t + T*e) in place.
 // sm: this line's shared scratch view; tw: the per-pass twiddle table of Cfg.
+// SYNC::sync() orders the exchanges between passes (every thread that takes
+// part in it must call).
+template <class Cfg, bool INV, class SYNC, class SM>
+__device__ __forceinline__ void line_fft_sync(float2 (&reg)[Cfg::E], const SM& sm, const float2* __restrict__ tw,
+                                              int t);
 // BLOCK selects __syncthreads (a line spread over several warps) instead of
 // __syncwarp; with BLOCK every thread of the block must call.
 template <class Cfg, bool INV, bool BLOCK = false, class SM>
 __device__ __forceinline__ void line_fft(float2 (&reg)[Cfg::E], const SM& sm, const float2* __restrict__ tw,
                                          int t) {
+    line_fft_sync<Cfg, INV, LineSync<BLOCK>>(reg, sm, tw, t);
+}
+
+template <class Cfg, bool INV, class SYNC, class SM>
+__device__ __forceinline__ void line_fft_sync(float2 (&reg)[Cfg::E], const SM& sm, const float2* __restrict__ tw,
+                                              int t) {
     constexpr int T = Cfg::T, E = Cfg::E;
     using RAD = typename Cfg::rad;
     sfor<0, Cfg::PASSES>([&](auto pi) {
@@ -309,10 +332,10 @@ __device__ __forceinline__ void line_fft(float2 (&reg)[Cfg::E], const SM& sm, co
             }
         }
         if constexpr (!last) {
-            line_sync<BLOCK>();
+            SYNC::sync();
 #pragma unroll
             for (int e = 0; e < E; ++e) reg[e] = sm(t + T * e);
-            line_sync<BLOCK>();
+            SYNC::sync();
         }
     });
 }

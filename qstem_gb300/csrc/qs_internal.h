@@ -118,6 +118,42 @@ struct ColArgs {
     const float* k2max_w;        // per-wave k2max, or null
 };
 
+// The whole slice loop of 256 x 256 waves in one launch, each wave held by a
+// cluster of four CTAs in distributed shared memory (qs_resident.cu).
+struct ResidentArgs {
+    int potNx, potNy, nwaves, nsteps;
+    const float2* trans;         // stack (slice a at a*potNx*potNy)
+    size_t trans_stride;         // elements between the stacks of consecutive waves (0: shared)
+    const float2* probe;         // incident waves, 256 x 256
+    size_t probe_stride;         // elements between consecutive waves' incident waves (0: shared)
+    const int* posX;             // nwaves window offsets
+    const int* posY;
+    const int* step_slice;       // nsteps: the stack slice each step transmits
+    const int* step_slot;        // nsteps: the thickness slot a step writes, or -1
+    const float2* tw;            // twiddles of the length-256 line transform
+    int yA, yB, nb;              // band (as RowCore) and its number of columns
+    const float* kx2;
+    const float* ky2;
+    const float2* px;
+    const float2* py;
+    float k2max;
+    int ndet;
+    float k2in[QS_MAX_DETECTORS], k2out[QS_MAX_DETECTORS];
+    double* partial;             // [slot][nwaves][4][ndet], partial_slot elements per slot
+    size_t partial_slot;
+    float* diffpat;              // patterns: per slot (series, dp_slot apart) or of the last step
+    size_t dp_slot;
+    int series;
+    float2* exit_waves;          // real-space waves after the last step, or null
+    float norm;                  // 1/(nx*ny)
+    double scaleDiff;
+};
+// clusters of the resident loop that fit on the current device at once
+int resident_clusters(int* out);
+// band columns the resident loop holds at most
+int resident_band_columns();
+int launch_resident(const ResidentArgs& a, cudaStream_t s);
+
 int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s);
 int launch_cols(const ColArgs& a, cudaStream_t s);
 int col_tile_width(int nx);

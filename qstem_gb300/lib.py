@@ -174,7 +174,7 @@ class Context:
     # -------------------------------------------------------- multislice
     def multislice(self, p, trans, probe=None, positions=None, det=None, diffpats=None, exit_waves=None,
                    want_det=True, want_diffpats=False, want_exit_waves=False, sync=True, slab_stacks=False,
-                   series=False, graph=False):
+                   series=False, graph=False, resident=False):
         """Run probe positions through the slice stack.
 
         positions: None (the full scan raster) or (iPosX, iPosY, detPosX, detPosY) int arrays.
@@ -182,7 +182,10 @@ class Context:
         series: diffraction patterns and exit waves of every thickness slot
         ([slot][position]...), not only the final slice's (QS_SERIES).
         graph: replay the slice loop as a CUDA graph on repeated calls with
-        the same parameters and device buffers (QS_GRAPH)."""
+        the same parameters and device buffers (QS_GRAPH).
+        resident: 256^2 waves through the wave-resident loop (one launch,
+        each wave on chip for all of its slices) instead of a row and a
+        column pass per slice (QS_RESIDENT)."""
         bx, keep = _batch(p, positions)
         npos = bx.npos
         host = not _is_torch(trans)
@@ -196,7 +199,7 @@ class Context:
             exit_waves = np.zeros(lead + (p.nx, p.ny, 2), np.float32) if host else None
         flags = (_io_flags(trans, probe, det, diffpats, exit_waves) | (abi.QS_SYNC if sync else 0) |
                  (abi.QS_SLAB_STACKS if slab_stacks else 0) | (abi.QS_SERIES if series else 0) |
-                 (abi.QS_GRAPH if graph else 0))
+                 (abi.QS_GRAPH if graph else 0) | (abi.QS_RESIDENT if resident else 0))
         _check(self.lib.qs_multislice_run(self.h, ctypes.byref(p), _ptr(trans), _ptr(probe), ctypes.byref(bx),
                                           _ptr(det), _ptr(diffpats), _ptr(exit_waves), flags))
         del keep
