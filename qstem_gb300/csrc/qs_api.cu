@@ -551,10 +551,10 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         // initSTEMSlices (stem3/stemlib.cpp:2280-2336)
         const double mm0 = (double)(1.0f + P.v0 / 511.0f);
         QS_TRY(launch_grating_from_real(Vr, trans, nTrans, mm0 * wavelength(P.v0), c->stream));
+        // line FFTs where they exist, DFT matrix products otherwise
+        const bool lines = line_supported(P.potNx) && line_supported(P.potNy);
         if (P.bandlimittrans) {
             const int nx = P.potNx, ny = P.potNy;
-            // line FFTs where they exist, DFT matrix products otherwise
-            const bool lines = line_supported(nx) && line_supported(ny);
             float2* scr = nullptr;
             int scrSlices = 0;
             if (!lines) {
@@ -582,8 +582,14 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
             k2max = k2max * k2max;
             void* dt = nullptr;
             if (lines) {
-                // fused: FFT_y, one column pass (FFT_x, mask and 1/N, IFFT_x), IFFT_y
-                const int Cw = col_tile_width(nx), ntl = ny / Cw;
+                // FFT_y storing the in-band columns, one column pass over
+                // their tiles (FFT_x, mask and 1/N, IFFT_x), IFFT_y
+                const int Cw = col_tile_width(nx);
+                PropTables bt;
+                bt.ky2 = ky2;
+                bt.k2max = k2max;
+                const Band band = band_tiles(bt, ny, Cw);
+                const int ntl = (int)band.tiles.size();
                 const size_t bytes = sizeof(float) * (nx + ny) + sizeof(float2) * (nx + ny) + sizeof(int) * ntl;
                 QS_TRY(ensure(c, B_BAND, bytes, &dt));
                 void* hbuf = nullptr;
@@ -596,12 +602,12 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
                 for (int i = 0; i < nx; i++) hp[i] = make_float2(sc, 0.f);
                 for (int i = 0; i < ny; i++) hp[nx + i] = make_float2(1.f, 0.f);
                 int* ht = (int*)(hp + nx + ny);
-                for (int k = 0; k < ntl; k++) ht[k] = k * Cw;
+                for (int k = 0; k < ntl; k++) ht[k] = band.tiles[k];
                 QS_TRY(stage_copy(c, P_BAND, dt, bytes));
                 const float* dk = (const float*)dt;
                 const float2* dp = (const float2*)(dk + nx + ny);
                 QS_TRY(bandlimit_lines(trans, nx, ny, P.slices, dk, dk + nx, dp, dp + nx, (const int*)(dp + nx + ny),
-                                       k2max, c->stream));
+                                       ntl, band.yA, band.yB, k2max, c->stream));
             } else {
                 QS_TRY(ensure(c, B_TABLES, sizeof(float) * (nx + ny), &dt));
                 std::vector<float> both(kx2);

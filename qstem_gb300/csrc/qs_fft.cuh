@@ -42,6 +42,18 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 
+// ------------------------------------------------ asynchronous copies
+// global -> shared copies that bypass the registers (cp.async, 8 bytes)
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+
 // --------------------------------------------------- compile-time twiddles
 // sin/cos evaluated by the compiler (argument in [-pi, pi], reduced to
 // [-pi/4, pi/4] by quadrant, then a Taylor series to double precision).

@@ -166,7 +166,11 @@ int line_fft_rows(float2* data, int n, long nlines, bool inverse, cudaStream_t s
 // generic in-place 2-D transform of `howmany` n0 x n1 arrays
 int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t s);
 int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2, const float* ky2,
-                    const float2* px, const float2* py, const int* tiles, float k2max, cudaStream_t s);
+                    const float2* px, const float2* py, const int* tiles, int ntiles, int yA, int yB, float k2max,
+                    cudaStream_t s);
+// the row passes of bandlimit_lines (qs_rows.cu): forward with only the
+// in-band columns stored (inverse false), or inverse from the in-band columns
+int bandlimit_rows(float2* data, int n, long nlines, int yA, int yB, bool inverse, cudaStream_t s);
 // in-place 2-D DFT of any size as batched complex matrix products (for
 // potential grids the line FFTs do not cover); scratch holds scratch_slices
 // n0 x n1 arrays

@@ -30,15 +30,6 @@
 
 namespace qs {
 
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int PENDING>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
-}
 
 // Column pass, persistent: each CTA walks the (wave, column tile) work items
 // blockIdx.x, blockIdx.x + gridDim.x, ...  While one tile is transformed, the
@@ -424,13 +415,16 @@ int fft2d(float2* data, int n0, int n1, int howmany, bool inverse, cudaStream_t 
 
 // The transmission band limit of initSTEMSlices (stem3/stemlib.cpp:2305-2336)
 // on every slice of `data` (howmany slices of n0 x n1) in three passes:
-// forward line FFTs along y, one column pass (FFT_x, the mask with its 1/N
-// scale as a separable "propagator" of (1/N, 0) x (1, 0) limited to
-// k^2 < k2max, IFFT_x; every column, so the out-of-band ones come out zero),
-// inverse line FFTs along y.  tab: device tables kx2[n0], ky2[n1],
-// px[n0] = (1/N, 0), py[n1] = (1, 0), tiles[n1 / column-tile width].
+// forward line FFTs along y that store only the in-band columns
+// (bl_rows_fwd); one column pass over the tiles holding them (FFT_x, the mask
+// with its 1/N scale as a separable "propagator" of (1/N, 0) x (1, 0) limited
+// to k^2 < k2max, IFFT_x); inverse line FFTs along y that read the other
+// columns as zeros (bl_rows_inv).  Columns ky are in band iff ky <= yA or
+// ky >= yB; tab: device tables kx2[n0], ky2[n1], px[n0] = (1/N, 0),
+// py[n1] = (1, 0), tiles[ntiles] (first columns of the in-band tiles).
 int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2, const float* ky2,
-                    const float2* px, const float2* py, const int* tiles, float k2max, cudaStream_t s) {
+                    const float2* px, const float2* py, const int* tiles, int ntiles, int yA, int yB, float k2max,
+                    cudaStream_t s) {
     if (!line_supported(n0) || !line_supported(n1)) {
         set_error("band limit: size " + std::to_string(n0) + "x" + std::to_string(n1) + " not supported");
         return QS_ERR_UNSUPPORTED;
@@ -440,7 +434,8 @@ int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2,
         set_error("twiddle table allocation failed");
         return QS_ERR_NOMEM;
     }
-    QS_TRY(line_fft_rows(data, n1, (long)n0 * howmany, false, s));
+    const long lines = (long)n0 * howmany;
+    QS_TRY(bandlimit_rows(data, n1, lines, yA, yB, false, s));
     ColArgs ca{};
     ca.nx = n0;
     ca.ny = n1;
@@ -454,12 +449,12 @@ int bandlimit_lines(float2* data, int n0, int n1, int howmany, const float* kx2,
     ca.py = py;
     ca.k2max = k2max;
     ca.tiles = tiles;
-    ca.ntiles = n1 / col_tile_width(n0);
+    ca.ntiles = ntiles;
     ca.inverse = 1;
     ca.ndet = 0;
     ca.diffpat = nullptr;
     QS_TRY(launch_cols(ca, s));
-    QS_TRY(line_fft_rows(data, n1, (long)n0 * howmany, true, s));
+    QS_TRY(bandlimit_rows(data, n1, lines, yA, yB, true, s));
     return QS_OK;
 }
 

@@ -309,10 +309,13 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
 // iOffsZ tests) and stages them in shared memory as (value, slope) pairs
 // L[ir], L[ir+1] - L[ir], the charge-dependent table already added in with
 // the atom's charge (the interpolation is linear in both), so that a slice
-// costs one shared load, one FMA and one reduction per pixel.  The box pixel
-// advances by fixed quotient/remainder steps instead of a division.  The sums
-// go to a real array (unit stride: a warp's reductions cover half the
-// sectors of the complex stack's real parts); the phase grating expands it.
+// costs one shared load, one FMA and one reduction per pixel.  The pixels are
+// walked row by row (scatter_rows): a warp takes a box row, computes its x
+// offset, wrapped index and the columns that can reach the table once, and
+// its lanes take 32 consecutive columns at a time; the box corners beyond
+// the table's radius are never visited, and the slice loop is unrolled for
+// the atom's run length.  The sums go to a real array (unit stride: a warp's
+// reductions cover consecutive words); the phase grating expands it.
 void scatter_knots(double dr, int Nr, std::vector<double>& T) {
     // T[k] = min{s >= 0 : floor(fl(fl(sqrt(s)) / dr)) >= k}; non-negative
     // doubles order like their bit patterns, so bisect over those
@@ -338,6 +341,89 @@ void scatter_knots(double dr, int Nr, std::vector<double>& T) {
 __device__ __forceinline__ int lut_row(int iOffsZ, int Nr, int limLo, int limHi) {
     if (iOffsZ < 0) return iOffsZ > limLo ? -iOffsZ + Nr : -1;
     return iOffsZ < limHi ? iOffsZ : -1;
+}
+
+// The reference's radial interval of a pixel at (ddx, ddy) from the atom
+// (make3DSlices, stem3/stemlib.cpp:935-990): ir and the interpolation weight
+// ddr; false when the pixel lies beyond the table (ir >= Nr - 1).
+__device__ __forceinline__ bool lut_interval(float ddx, float ddy, float inv_dr, int Nr,
+                                             const double* __restrict__ knots, int& ir, float& ddr) {
+    const float r2 = fmaf(ddx, ddx, ddy * ddy);
+    const float rr = r2 > 0.f ? r2 * rsqrtf(r2) * inv_dr : 0.f;
+    ir = (int)rr;
+    ddr = rr - (float)ir;
+    if (ddr < 2e-4f || ddr > 1.f - 2e-4f) {
+        // the knot k nearest to rr: the interval is k - 1 or k
+        const int k = (int)(rr + 0.5f);
+        if (k > 0 && k <= Nr) {
+            const double s2 = fma((double)ddx, (double)ddx, (double)ddy * (double)ddy);
+            ir = s2 < __ldg(knots + k) ? k - 1 : k;
+        } else {
+            ir = k;
+        }
+        ddr = fminf(fmaxf(rr - (float)ir, 0.f), 1.f);
+    }
+    return ir < Nr - 1;
+}
+
+// One pixel's contributions to the NR slices of its run (NR = 0: nr of them,
+// a loop), from the staged (value, slope) rows.
+template <int NR>
+__device__ __forceinline__ void add_slices(float* dst, size_t step, const float2* pr, int prs, float ddr, int nr) {
+    if constexpr (NR > 0) {
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            const float2 ls = pr[r * prs];
+            atomicAdd(dst + r * step, fmaf(ddr, ls.y, ls.x));
+        }
+    } else {
+#pragma unroll 4
+        for (int r = 0; r < nr; r++, dst += step, pr += prs) {
+            const float2 ls = *pr;
+            atomicAdd(dst, fmaf(ddr, ls.y, ls.x));
+        }
+    }
+}
+
+// The staged scatter's pixel walk: warp w takes the box rows qx = w,
+// w + 8, ...; in a row only the columns within Nr*dr of the atom (plus one
+// pixel each side: the exact interval test still decides every pixel) are
+// visited, 32 consecutive columns at a time, so that a row's x offset, its
+// wrapped index and the cut-off are computed once per row and a warp's
+// reductions cover consecutive words.
+template <int NR>
+__device__ __forceinline__ void scatter_rows(const AtomJob& J, float* base, size_t sliceStep, const float2* s_pair,
+                                             int Nr, int nr, float dx, float dy, const double* __restrict__ knots,
+                                             float inv_dr, int potNx, int potNy, int periodic) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int nxBox = J.iax1 - J.iax0 + 1;
+    const bool wideY = periodic && (J.iay1 - J.iay0 + 1 > potNy);
+    const float rcut = (float)Nr / inv_dr;
+    const float rc2 = rcut * rcut;
+    for (int qx = warp; qx < nxBox; qx += nwarps) {
+        const int iax = J.iax0 + qx;
+        // x2 = iax*dx - atomX in float as the reference forms it
+        // (stem3/stemlib.cpp:935-938), rounded step by step (no FMA)
+        const float ddx = __fsub_rn(__fmul_rn((float)iax, dx), J.atomX);
+        const float rem = rc2 - ddx * ddx;
+        if (rem < 0.f) continue;
+        const float half = sqrtf(rem);
+        const int y0 = max(J.iay0, (int)floorf((J.atomY - half) / dy) - 1);
+        const int y1 = min(J.iay1, (int)floorf((J.atomY + half) / dy) + 2);
+        const int cx = periodic ? ((iax % potNx) + potNx) % potNx : iax;
+        const int cy0 = periodic ? ((y0 % potNy) + potNy) % potNy : y0;
+        float* const row = base + (size_t)cx * potNy;
+        for (int iay = y0 + lane, cy = cy0 + lane; iay <= y1; iay += 32, cy += 32) {
+            const float ddy = __fsub_rn(__fmul_rn((float)iay, dy), J.atomY);
+            int ir;
+            float ddr;
+            if (!lut_interval(ddx, ddy, inv_dr, Nr, knots, ir, ddr)) continue;
+            int c = cy;
+            if (wideY) c %= potNy;
+            else if (periodic) c -= c >= potNy ? potNy : 0;
+            add_slices<NR>(row + c, sliceStep, s_pair + ir, Nr - 1, ddr, nr);
+        }
+    }
 }
 
 // CTAs per SM the scatter is compiled for (its register budget): 4 measured
@@ -392,11 +478,33 @@ __global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(cons
         }
         __syncthreads();
     }
+    float* const base = V + (size_t)(J.iAtomZ + J.iaz0 + r0) * sliceStep;
+    if constexpr (STAGED) {
+        switch (nr) {
+            case 1: scatter_rows<1>(J, base, sliceStep, s_pair, Nr, nr, dx, dy, knots, inv_dr, potNx, potNy, periodic); break;
+            case 2: scatter_rows<2>(J, base, sliceStep, s_pair, Nr, nr, dx, dy, knots, inv_dr, potNx, potNy, periodic); break;
+            case 3: scatter_rows<3>(J, base, sliceStep, s_pair, Nr, nr, dx, dy, knots, inv_dr, potNx, potNy, periodic); break;
+            case 4: scatter_rows<4>(J, base, sliceStep, s_pair, Nr, nr, dx, dy, knots, inv_dr, potNx, potNy, periodic); break;
+            case 5: scatter_rows<5>(J, base, sliceStep, s_pair, Nr, nr, dx, dy, knots, inv_dr, potNx, potNy, periodic); break;
+            case 6: scatter_rows<6>(J, base, sliceStep, s_pair, Nr, nr, dx, dy, knots, inv_dr, potNx, potNy, periodic); break;
+            case 7: scatter_rows<7>(J, base, sliceStep, s_pair, Nr, nr, dx, dy, knots, inv_dr, potNx, potNy, periodic); break;
+            case 8: scatter_rows<8>(J, base, sliceStep, s_pair, Nr, nr, dx, dy, knots, inv_dr, potNx, potNy, periodic); break;
+            default: scatter_rows<0>(J, base, sliceStep, s_pair, Nr, nr, dx, dy, knots, inv_dr, potNx, potNy, periodic);
+        }
+        return;
+    }
     const int sx = blockDim.x / w, sy = blockDim.x - sx * w;
     int qx = threadIdx.x / w, qy = threadIdx.x - qx * w;
-    float* const base = V + (size_t)(J.iAtomZ + J.iaz0 + r0) * sliceStep;
+    // periodic wrap: the box's first row and column are wrapped into the
+    // cell once; while the box is no wider than the cell, a pixel's wrapped
+    // index is then that offset plus its place in the box, less one period
+    // at most (no integer division per pixel)
+    const int wx0 = periodic ? ((J.iax0 % potNx) + potNx) % potNx : J.iax0;
+    const int wy0 = periodic ? ((J.iay0 % potNy) + potNy) % potNy : J.iay0;
+    const bool wide = periodic && (J.iax1 - J.iax0 + 1 > potNx || w > potNy);
     for (int k = threadIdx.x; k < npx; k += blockDim.x) {
         const int iax = J.iax0 + qx, iay = J.iay0 + qy;
+        int cx = wx0 + qx, cy = wy0 + qy;
         qx += sx;
         qy += sy;
         if (qy >= w) {
@@ -407,40 +515,24 @@ __global__ void __launch_bounds__(256, QS_SCATTER_MIN_BLOCKS) scatter_atoms(cons
         // (stem3/stemlib.cpp:935-938), rounded step by step (no FMA)
         const float ddx = __fsub_rn(__fmul_rn((float)iax, dx), J.atomX);
         const float ddy = __fsub_rn(__fmul_rn((float)iay, dy), J.atomY);
-        const float r2 = fmaf(ddx, ddx, ddy * ddy);
-        const float rr = r2 > 0.f ? r2 * rsqrtf(r2) * inv_dr : 0.f;
-        int ir = (int)rr;
-        float ddr = rr - (float)ir;
-        if (ddr < 2e-4f || ddr > 1.f - 2e-4f) {
-            // the knot k nearest to rr: the interval is k - 1 or k
-            const int k = (int)(rr + 0.5f);
-            if (k > 0 && k <= Nr) {
-                const double s2 = fma((double)ddx, (double)ddx, (double)ddy * (double)ddy);
-                ir = s2 < __ldg(knots + k) ? k - 1 : k;
-            } else {
-                ir = k;
-            }
-            ddr = fminf(fmaxf(rr - (float)ir, 0.f), 1.f);
+        int ir;
+        float ddr;
+        if (!lut_interval(ddx, ddy, inv_dr, Nr, knots, ir, ddr)) continue;
+        if (wide) {
+            cx = ((iax % potNx) + potNx) % potNx;
+            cy = ((iay % potNy) + potNy) % potNy;
+        } else if (periodic) {
+            cx -= cx >= potNx ? potNx : 0;
+            cy -= cy >= potNy ? potNy : 0;
         }
-        if (ir >= Nr - 1) continue;
-        const int cx = periodic ? ((iax % potNx) + potNx) % potNx : iax;
-        const int cy = periodic ? ((iay % potNy) + potNy) % potNy : iay;
+        // LUT rows from global memory (tables too large to stage)
         float* dst = base + (size_t)cx * potNy + cy;
-        if constexpr (STAGED) {
-            const float2* pr = s_pair + ir;
-#pragma unroll 4
-            for (int r = 0; r < nr; r++, dst += sliceStep, pr += Nr - 1) {
-                const float2 ls = *pr;
-                atomicAdd(dst, fmaf(ddr, ls.y, ls.x));
-            }
-        } else {
-            const float w0 = 1.f - ddr;
-            for (int r = 0; r < nr; r++, dst += sliceStep) {
-                const int row = lut_row(iOffsZ0 + (r0 + r) * step, Nr, limLo, limHi);
-                float v = w0 * __ldg(lut + row + ir) + ddr * __ldg(lut + row + ir + 1);
-                if (lutq) v += q * (w0 * __ldg(lutq + row + ir) + ddr * __ldg(lutq + row + ir + 1));
-                atomicAdd(dst, v);
-            }
+        const float w0 = 1.f - ddr;
+        for (int r = 0; r < nr; r++, dst += sliceStep) {
+            const int row = lut_row(iOffsZ0 + (r0 + r) * step, Nr, limLo, limHi);
+            float v = w0 * __ldg(lut + row + ir) + ddr * __ldg(lut + row + ir + 1);
+            if (lutq) v += q * (w0 * __ldg(lutq + row + ir) + ddr * __ldg(lutq + row + ir + 1));
+            atomicAdd(dst, v);
         }
     }
 }

@@ -26,6 +26,12 @@ __global__ void probe_kspace(ProbeK P, float2* __restrict__ wave) {
     const double ky = (iy > P.ny / 2) ? (double)(iy - P.ny) : (double)iy;
     const double kx = (ix > P.nx / 2) ? (double)(ix - P.nx) : (double)ix;
     const double k2 = kx * kx * P.rx2 + ky * ky * P.ry2;
+    // outside the aperture and its smoothed edge the probe is zero: skip
+    // the FP64 aberration phase there (most of k-space for small apertures)
+    if (k2 > P.k2max && !(P.ismoth != 0 && fabs(k2 - P.k2max) <= P.pixel)) {
+        wave[i] = make_float2(0.f, 0.f);
+        return;
+    }
     double kt2 = k2 * (P.wavlen * P.wavlen);
     const double kt = sqrt(kt2);
     const double phi = atan2(P.ry * ky, P.rx * kx);

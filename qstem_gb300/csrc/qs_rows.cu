@@ -159,6 +159,108 @@ int launch_rows(const RowArgs& a, RowMode mode, cudaStream_t s) {
     return rows_mode<ROW_LAST, false>(a, s);
 }
 
+// Row passes of the transmission band limit (initSTEMSlices,
+// stem3/stemlib.cpp:2305-2336), which bracket one column pass:
+//   bl_rows_fwd  FFT_y of the transmission function, and only the in-band
+//                ky (iy <= yA or iy >= yB) stored: the mask zeroes every
+//                other column
+//   bl_rows_inv  the in-band ky (the others read as the zeros the mask
+//                gives them), IFFT_y, the whole line stored
+// The values are those of the unpruned 2-D transform, mask and inverse; the
+// out-of-band columns are never written or read in between.  (The phase
+// grating stays a kernel of its own: its sincosf, fused into the transform,
+// made the pass issue-bound at twice the time of the two kernels.)
+template <int N>
+__global__ void __launch_bounds__(line_threads(N) * ROW_LINES)
+    bl_rows_fwd(float2* __restrict__ data, long nlines, int yA, int yB, const float2* tw) {
+    using Cfg = typename Line<N>::cfg;
+    constexpr int T = Cfg::T, E = Cfg::E;
+    extern __shared__ float2 dsm[];
+    float2* s_tw = dsm;
+    float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
+    const int tid = threadIdx.x + T * threadIdx.y;
+    for (int i = tid; i < Cfg::TW; i += T * ROW_LINES) s_tw[i] = tw[i];
+    __syncthreads();
+    const long line = (long)blockIdx.x * ROW_LINES + threadIdx.y;
+    const bool ok = line < nlines;
+    float2* p = data + (size_t)(ok ? line : 0) * N;
+    const int t = threadIdx.x;
+    float2 reg[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) reg[e] = ok ? p[t + T * e] : make_float2(0.f, 0.f);
+    line_fft<Cfg, false>(reg, SmemRow<Cfg::R0>{s_line}, s_tw, t);
+    if (ok) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int y = t + T * e;
+            if (y <= yA || y >= yB) p[y] = reg[e];
+        }
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(line_threads(N) * ROW_LINES)
+    bl_rows_inv(float2* __restrict__ data, long nlines, int yA, int yB, const float2* tw) {
+    using Cfg = typename Line<N>::cfg;
+    constexpr int T = Cfg::T, E = Cfg::E;
+    extern __shared__ float2 dsm[];
+    float2* s_tw = dsm;
+    float2* s_line = dsm + N + threadIdx.y * Cfg::SMEM;
+    const int tid = threadIdx.x + T * threadIdx.y;
+    for (int i = tid; i < Cfg::TW; i += T * ROW_LINES) s_tw[i] = tw[i];
+    __syncthreads();
+    const long line = (long)blockIdx.x * ROW_LINES + threadIdx.y;
+    const bool ok = line < nlines;
+    float2* p = data + (size_t)(ok ? line : 0) * N;
+    const int t = threadIdx.x;
+    float2 reg[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int y = t + T * e;
+        reg[e] = (ok && (y <= yA || y >= yB)) ? p[y] : make_float2(0.f, 0.f);
+    }
+    line_fft<Cfg, true>(reg, SmemRow<Cfg::R0>{s_line}, s_tw, t);
+    if (ok) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) p[t + T * e] = reg[e];
+    }
+}
+
+template <int N>
+static int bl_rows_n(float2* data, long nlines, int yA, int yB, bool inverse, cudaStream_t s) {
+    const size_t sm = row_smem<N>(ROW_LINES);
+    dim3 block(Line<N>::cfg::T, ROW_LINES);
+    const unsigned grid = (unsigned)((nlines + ROW_LINES - 1) / ROW_LINES);
+    if (inverse) {
+        QS_TRY(smem_attr((const void*)bl_rows_inv<N>, sm));
+        bl_rows_inv<N><<<grid, block, sm, s>>>(data, nlines, yA, yB, twiddles(N));
+    } else {
+        QS_TRY(smem_attr((const void*)bl_rows_fwd<N>, sm));
+        bl_rows_fwd<N><<<grid, block, sm, s>>>(data, nlines, yA, yB, twiddles(N));
+    }
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
+int bandlimit_rows(float2* data, int n, long nlines, int yA, int yB, bool inverse, cudaStream_t s) {
+    if (!twiddles(n)) {
+        set_error("twiddle table allocation failed");
+        return QS_ERR_NOMEM;
+    }
+    switch (n) {
+        case 64: return bl_rows_n<64>(data, nlines, yA, yB, inverse, s);
+        case 128: return bl_rows_n<128>(data, nlines, yA, yB, inverse, s);
+        case 256: return bl_rows_n<256>(data, nlines, yA, yB, inverse, s);
+        case 384: return bl_rows_n<384>(data, nlines, yA, yB, inverse, s);
+        case 512: return bl_rows_n<512>(data, nlines, yA, yB, inverse, s);
+        case 768: return bl_rows_n<768>(data, nlines, yA, yB, inverse, s);
+        case 1024: return bl_rows_n<1024>(data, nlines, yA, yB, inverse, s);
+    }
+    set_error("band limit: unsupported row length " + std::to_string(n));
+    return QS_ERR_UNSUPPORTED;
+}
+
 template <int N, bool INV>
 __global__ void __launch_bounds__(line_threads(N) * ROW_LINES) fft_rows(float2* data, long nlines, const float2* tw) {
     using Cfg = typename Line<N>::cfg;

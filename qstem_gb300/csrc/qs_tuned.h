@@ -179,3 +179,4 @@
 #ifndef QS_RADIX_COL_1024
 #define QS_RADIX_COL_1024 0
 #endif
+
