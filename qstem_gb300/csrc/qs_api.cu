@@ -61,6 +61,9 @@ struct qs_ctx {
     // the scatter's knot thresholds in B_KNOTS were made for this (dr, Nr)
     double knots_dr = -1.0;
     int knots_Nr = 0;
+    // knot thresholds computed so far (host), keyed by (dr, Nr): instances
+    // of different samplings in turn reuse them
+    std::map<std::pair<double, int>, std::vector<double>> knots_host;
 };
 
 namespace qs {
@@ -533,8 +536,8 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         QS_TRY(ensure(c, B_KNOTS, sizeof(double) * (Nr + 1), &dk));
         const double dr = (double)(P.resolutionX / 2);  // make3DSlices' dr (stem3/stemlib.cpp:576)
         if (c->knots_dr != dr || c->knots_Nr != Nr) {
-            std::vector<double> knots;
-            scatter_knots(dr, Nr, knots);
+            std::vector<double>& knots = c->knots_host[{dr, Nr}];
+            if (knots.empty()) scatter_knots(dr, Nr, knots);
             QS_TRY(upload(c, P_KNOTS, dk, knots.data(), sizeof(double) * knots.size()));
             c->knots_dr = dr;
             c->knots_Nr = Nr;
