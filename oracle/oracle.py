@@ -48,6 +48,8 @@ def lib():
         L.qso_lut.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, fp,
                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                               ctypes.POINTER(ctypes.c_int)]
+        L.qso_lut2d.argtypes = [P, ctypes.c_int, ctypes.c_double, fp, ctypes.POINTER(ctypes.c_int),
+                                ctypes.POINTER(ctypes.c_int)]
         L.qso_potential.argtypes = [P, fp, ctypes.c_int, fp]
         L.qso_potential_slab.argtypes = [P, fp, ctypes.c_int, ctypes.c_int, fp]
         L.qso_stem_slabs.argtypes = [P, fp, ctypes.c_int, fp, ctypes.c_int, ctypes.c_int, fp, fp, fp, ctypes.c_int]
@@ -75,6 +77,18 @@ def lut(p, Z, B=0.0, charged=False):
     rc = L.qso_lut(ctypes.byref(p), Z, B, int(charged), _ptr(out), None, None, None)
     assert rc == 0, rc
     return out, ns.value
+
+
+def lut2d(p, Z, B=0.0):
+    """getAtomPotential2D: the (nx, ny, 2) complex table."""
+    L = lib()
+    nx, ny = ctypes.c_int(), ctypes.c_int()
+    rc = L.qso_lut2d(ctypes.byref(p), Z, B, None, ctypes.byref(nx), ctypes.byref(ny))
+    assert rc == 0, rc
+    out = np.zeros((nx.value, ny.value, 2), np.float32)
+    rc = L.qso_lut2d(ctypes.byref(p), Z, B, _ptr(out), None, None)
+    assert rc == 0, rc
+    return out
 
 
 def potential(p, atoms, slab=0):

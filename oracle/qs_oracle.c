@@ -192,6 +192,50 @@ int qso_lut(const qs_params *p, int Z, double B, int charged, float *out, int *N
     return QS_OK;
 }
 
+/* getAtomPotential2D (stem3/stemlib.cpp:1750-1857): the oversampled 2-D
+ * projected-potential table of element Z, nx x ny complex floats
+ * (nx = 2*OVERSAMP_X*ceil(R/dx)), f(k) e^{i phase} on the k-grid (the
+ * scattering-factor tail truncated at kmax as the reference truncates its
+ * global table on the first call), inverse 2-D FFT, real part scaled by
+ * dkx*dky*OVERSAMP_X^2 (the imaginary part left unscaled, as the reference
+ * leaves it).  out may be NULL to query the size. */
+int qso_lut2d(const qs_params *p, int Z, double B, float *out, int *nxO, int *nyO) {
+    if (Z < 1 || Z >= QS_REZ_NELEM) return QS_ERR_ARG;
+    const float rx = p->resolutionX, ry = p->resolutionY, R = p->atomRadius;
+    const int nx = 2 * OVERSAMP_X * (int)ceilf(R / rx);
+    const int ny = 2 * OVERSAMP_X * (int)ceilf(R / ry);
+    if (nxO) *nxO = nx;
+    if (nyO) *nyO = ny;
+    if (!out) return QS_OK;
+    const double dkx = 0.5 * OVERSAMP_X / (double)((float)nx * rx);
+    const double dky = 0.5 * OVERSAMP_X / (double)((float)ny * ry);
+    double kmax2 = 0.5 * nx * dkx / (double)OVERSAMP_X;
+    double fg[NSF], fr[NSF], sb[NSF], sc[NSF], sd[NSF];
+    memcpy(fg, QS_REZ_F[0], sizeof fg);
+    memcpy(fr, QS_REZ_F[Z], sizeof fr);
+    truncate_tail(fg, fr, kmax2);
+    kmax2 *= kmax2;
+    qso_splinh(fg, fr, sb, sc, sd, NSF);
+    memset(out, 0, sizeof(float) * 2 * (size_t)nx * ny);
+    for (int ix = 0; ix < nx; ix++) {
+        const double kx = dkx * (ix < nx / 2 ? ix : nx - ix);
+        for (int iy = 0; iy < ny; iy++) {
+            const double ky = dky * (iy < ny / 2 ? iy : ny - iy);
+            const double s2 = kx * kx + ky * ky;
+            if (s2 < kmax2) {
+                const double f = qso_seval(fg, fr, sb, sc, sd, NSF, sqrt(s2)) * exp(-s2 * B * 0.25);
+                const double phase = REF_PI * (kx * (double)rx * nx + ky * (double)ry * ny);
+                out[2 * (iy + (size_t)ix * ny)] = (float)(f * cos(phase));
+                out[2 * (iy + (size_t)ix * ny) + 1] = (float)(f * sin(phase));
+            }
+        }
+    }
+    qs_fft2d_c64(nx, ny, out, +1);
+    const double scale = dkx * dky * (OVERSAMP_X * OVERSAMP_X);
+    for (size_t i = 0; i < (size_t)nx * ny; i++) out[2 * i] = (float)((double)out[2 * i] * scale);
+    return QS_OK;
+}
+
 /* ------------------------------------------------------------- potential */
 static int cmp_z(const void *a, const void *b) {
     /* atomCompare, stem3/stemutil.cpp:1524-1531: by z only */
@@ -249,8 +293,16 @@ int qso_potential(const qs_params *p, const qs_atom *atoms_in, int natom, float 
 /* make3DSlices' call for slab `slab` of a cellDiv-divided cell: the atoms are
  * offset by -slab * c, c = slices * sliceThickness (stem3/stemlib.cpp:456-465,
  * :572, :709-713; divCount counts the slabs down from cellDiv - 1). */
+static int potential2d_periodic(const qs_params *p, const qs_atom *atoms_in, int natom, int slab, float *trans);
+
 int qso_potential_slab(const qs_params *p, const qs_atom *atoms_in, int natom, int slab, float *trans) {
-    if (!p->fftpotential || !p->potential3D || slab < 0 || slab >= p->cellDiv) return QS_ERR_UNSUPPORTED;
+    if (!p->fftpotential || slab < 0 || slab >= p->cellDiv) return QS_ERR_UNSUPPORTED;
+    if (!p->potential3D) {
+        /* only the periodic 2-D branch: the non-periodic one reads its table
+         * outside the array for atoms near the edges */
+        if (p->nonPeriod) return QS_ERR_UNSUPPORTED;
+        return potential2d_periodic(p, atoms_in, natom, slab, trans);
+    }
     const int potNx = p->potNx, potNy = p->potNy, slices = p->slices;
     const size_t sliceStep = 2 * (size_t)potNx * potNy; /* floats */
     memset(trans, 0, sizeof(float) * sliceStep * slices);
@@ -339,6 +391,86 @@ int qso_potential_slab(const qs_params *p, const qs_atom *atoms_in, int natom, i
         }
     }
     for (int z = 0; z < QS_REZ_NELEM; z++) { free(cache.lut[z]); free(cache.lutq[z]); }
+    free(atoms);
+    return QS_OK;
+}
+
+/* make3DSlices' periodic 2-D branch (stem3/stemlib.cpp:709-731 for the atom
+ * z, :1215-1262): each atom adds the bilinear interpolation of its element's
+ * 2-D table (getAtomPotential2D; B of the element's first atom in z order)
+ * into the one slice floor(atomZ/dz) it lies in, over a 2 iRadX x 2 iRadY box
+ * wrapped into the array; the interpolation weights are the reference's,
+ * whose names are swapped against the corners they multiply.  Atoms whose
+ * slice falls outside the stack are skipped (the reference writes outside its
+ * array there). */
+static int potential2d_periodic(const qs_params *p, const qs_atom *atoms_in, int natom, int slab, float *trans) {
+    const int potNx = p->potNx, potNy = p->potNy, slices = p->slices;
+    const size_t sliceStep = 2 * (size_t)potNx * potNy; /* floats */
+    memset(trans, 0, sizeof(float) * sliceStep * slices);
+    if (natom < 1) return QS_OK;
+    qs_atom *atoms = (qs_atom *)malloc(sizeof(qs_atom) * (size_t)natom);
+    memcpy(atoms, atoms_in, sizeof(qs_atom) * (size_t)natom);
+    qsort(atoms, natom, sizeof(qs_atom), cmp_z);
+    const float c = p->sliceThickness * (float)slices;
+    const float dx = p->resolutionX, dy = p->resolutionY, dzs = p->sliceThickness;
+    const int iRadX = (int)ceilf(p->atomRadius / dx);
+    const int iRadY = (int)ceilf(p->atomRadius / dy);
+    const int nyAtBox = 2 * OVERSAMP_X * (int)ceilf(p->atomRadius / dy), nyAtBox2 = 2 * nyAtBox;
+    float *tab[QS_REZ_NELEM];
+    memset(tab, 0, sizeof tab);
+    int nx2 = 0, ny2 = 0;
+    qso_lut2d(p, 1, 0.0, NULL, &nx2, &ny2);
+    for (int iatom = 0; iatom < natom; iatom++) {
+        while (iatom < natom && atoms[iatom].Znum == 0) iatom++;
+        if (iatom >= natom) break;
+        float atomZ = (float)((double)(atoms[iatom].z - c * (float)slab + p->czOffset) -
+                              0.5 * p->sliceThickness * (1 - p->centerSlices));
+        atomZ = (float)((double)atomZ + 0.5 * p->sliceThickness);
+        if (p->nonPeriodZ) {
+            if (atomZ > c) break;
+            do {
+                if (atomZ >= 0) break;
+                ++iatom;
+                atomZ = (float)((double)(atoms[iatom].z - c * (float)slab + p->czOffset) -
+                                0.5 * p->sliceThickness * (1 - p->centerSlices));
+                atomZ = (float)((double)atomZ + 0.5 * p->sliceThickness);
+            } while (iatom < natom - 1);
+        }
+        const float atomX = atoms[iatom].x - p->potOffsetX;
+        const float atomY = atoms[iatom].y - p->potOffsetY;
+        const int iAtomX = (int)floorf(atomX / dx);
+        const int iAtomY = (int)floorf(atomY / dy);
+        const int iAtomZ = (int)floor(atomZ / dzs);
+        const int Z = atoms[iatom].Znum;
+        if (Z < 1 || Z >= QS_REZ_NELEM) continue;
+        if (iAtomZ < 0 || iAtomZ >= slices) continue;
+        if (!tab[Z]) {
+            tab[Z] = (float *)malloc(sizeof(float) * 2 * (size_t)nx2 * ny2);
+            qso_lut2d(p, Z, p->tds ? 0.0 : atoms[iatom].dw, tab[Z], NULL, NULL);
+        }
+        const float *L = tab[Z];
+        const int iax0 = iAtomX - iRadX + 2 * potNx, iax1 = iAtomX + iRadX + 2 * potNx;
+        const int iay0 = iAtomY - iRadY + 2 * potNy, iay1 = iAtomY + iRadY + 2 * potNy;
+        double ddx = (-(double)iax0 + (atomX / dx - (double)(iRadX - 2 * potNx))) * (double)OVERSAMP_X;
+        double ddy = (-(double)iay0 + (atomY / dy - (double)(iRadY - 2 * potNy))) * (double)OVERSAMP_X;
+        const int iOffsX = (int)floor(ddx), iOffsY = (int)floor(ddy);
+        ddx -= (double)iOffsX;
+        ddy -= (double)iOffsY;
+        const double s22 = (1 - ddx) * (1 - ddy), s21 = (1 - ddx) * ddy, s12 = ddx * (1 - ddy), s11 = ddx * ddy;
+        float *slice = trans + (size_t)iAtomZ * sliceStep;
+        for (int iax = iax0; iax < iax1; iax++) {
+            const int atPosX = OVERSAMP_X * (iax - iax0) - iOffsX;
+            if (atPosX < 0 || atPosX >= nyAtBox - 1) continue;
+            for (int iay = iay0; iay < iay1; iay++) {
+                const int atPosY = (iay - iay0) * OVERSAMP_X - iOffsY;
+                if (atPosY >= nyAtBox - 1 || atPosY < 0) continue;
+                const float *ptr = L + 2 * ((size_t)atPosX * nyAtBox + atPosY);
+                float *t = slice + 2 * ((size_t)(iax % potNx) * potNy + (iay % potNy));
+                *t = (float)((double)*t + (s11 * ptr[0] + s12 * ptr[2] + s21 * ptr[nyAtBox2] + s22 * ptr[nyAtBox2 + 2]));
+            }
+        }
+    }
+    for (int z = 0; z < QS_REZ_NELEM; z++) free(tab[z]);
     free(atoms);
     return QS_OK;
 }

@@ -26,6 +26,7 @@
  */
 #include <cstdio>
 #include <cstdlib>
+#include <cmath>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -98,6 +99,23 @@ int main(int argc, char **argv) {
         FILE *f = fopen((g_out + "/lut_dims.txt").c_str(), k ? "a" : "w");
         fprintf(f, "%d %d %d %d\n", Z, Nz, Nr, nzSub);
         fclose(f);
+    }
+
+    if (!muls.potential3D) {
+        /* the 2-D tables make3DSlices used (cached by Z after their first
+         * call, stem3/stemlib.cpp:1750-1857) */
+        const int nx2 = 2 * 2 * (int)ceil(muls.atomRadius / muls.resolutionX);
+        const int ny2 = 2 * 2 * (int)ceil(muls.atomRadius / muls.resolutionY);
+        for (int k = 0; k < muls.atomKinds; k++) {
+            int Z = muls.Znums[k];
+            fftwf_complex *l2 = getAtomPotential2D(Z, &muls, 0.0);
+            char nm[64];
+            snprintf(nm, sizeof nm, "lut2d_%d.bin", Z);
+            dump(nm, l2, sizeof(fftwf_complex) * (size_t)nx2 * ny2);
+            FILE *f = fopen((g_out + "/lut2d_dims.txt").c_str(), k ? "a" : "w");
+            fprintf(f, "%d %d %d\n", Z, nx2, ny2);
+            fclose(f);
+        }
     }
 
     initSTEMSlices(&muls, muls.slices);

@@ -325,7 +325,7 @@ def make_params(*, mode=abi.QS_MODE_STEM, nx, ny=None, resolutionX, resolutionY=
                 astig_nm=0.0, astig_deg=0.0, outputInterval=None, czOffset=0.0,
                 centerSlices=False, periodicXY=False, periodicZ=False, bandlimit=False,
                 atomRadius=5.0, smooth=True, gaussian=None, aAIS=0.0, beamCurrent=1.0,
-                dwellTime=1.6021773e-4, tds=False, cellDiv=1, nCellZ=None):
+                dwellTime=1.6021773e-4, tds=False, cellDiv=1, nCellZ=None, potential3D=True):
     """qs_params as stem3's readFile would fill them from the corresponding
     .qsc keys (units as in the .qsc: mm, nm, mrad, deg).
     scan = (x_start, x_stop, x_pixels, y_start, y_stop, y_pixels) in A.
@@ -354,7 +354,7 @@ def make_params(*, mode=abi.QS_MODE_STEM, nx, ny=None, resolutionX, resolutionY=
     p.nonPeriodZ = 0 if periodicZ else 1
     p.bandlimittrans = int(bool(bandlimit))
     p.fftpotential = 1
-    p.potential3D = 1
+    p.potential3D = int(bool(potential3D))
     p.tds = int(bool(tds))
     p.atomRadius = F32(atomRadius)
     # scan window and potential array (stem3/stem3.cpp:1054-1068, :1436-1455)
@@ -442,7 +442,7 @@ def write_qsc(path, *, cfg_file, ncell, nx, resolutionX, v0, slices, sliceThickn
               detectors=(), alpha=20.0, Cs_mm=0.0, C5_mm=0.0, defocus_nm=0.0, outputInterval=None,
               mode="STEM", bandlimit=False, periodicXY=False, periodicZ=False, folder="out",
               saveLevel=0, smooth=True, czOffset=0.0, atomRadius=5.0, centerSlices=False, cellDiv=1,
-              sequence=(1, 1)):
+              sequence=(1, 1), potential3D=True):
     """A stem3 input file for the same run make_params describes
     (sequence: the stacking sequence m1 m2)."""
     yn = lambda b: "yes" if b else "no"
@@ -471,7 +471,7 @@ def write_qsc(path, *, cfg_file, ncell, nx, resolutionX, v0, slices, sliceThickn
     L += ["nx: %d" % nx, "ny: %d" % nx, "Cs: %r" % float(Cs_mm), "C5: %r" % float(C5_mm),
           "Cc: 0", "alpha: %r" % float(alpha), "defocus: %r" % float(defocus_nm),
           "beam current: 1", "dwell time: 1.6021773e-4", "smooth: %s" % yn(smooth),
-          "gaussian: no", "potential3D: yes", "atom radius: %r" % float(atomRadius),
+          "gaussian: no", "potential3D: %s" % yn(potential3D), "atom radius: %r" % float(atomRadius),
           "bandlimit f_trans: %s" % yn(bandlimit), "one time integration: yes",
           'Folder: "%s"' % folder, "Runs for averaging: 1", "Structure Factors: WK",
           "sequence: %d %d" % tuple(sequence)]

@@ -306,6 +306,72 @@ static void plan_atoms(const qs_params& P, const qs_atom* atoms, int natom, std:
 
 }
 
+// The atoms of make3DSlices' periodic 2-D branch (stem3/stemlib.cpp:709-731
+// for the atom z, :1215-1262): z-sorted, vacancies skipped, the 2-D z offset
+// (+ dz/2 where the 3-D branch takes - dz), one slice floor(atomZ/dz) per
+// atom (atoms whose slice lies outside the stack are left out: the
+// reference writes outside its array there), the box, table offsets and
+// bilinear weights formed as the reference forms them.  keys: (Z, B) of
+// every element's table, B that of its first atom in z order.
+static void plan_atoms_2d(const qs_params& P, const qs_atom* atoms, int natom, std::vector<Atom2DJob>& jobs,
+                          std::vector<std::pair<int, double>>& keys, int slab = 0) {
+    std::vector<int> order(natom);
+    for (int i = 0; i < natom; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return atoms[a].z < atoms[b].z; });
+    const float cz = P.sliceThickness * (float)P.slices;
+    const float dx = P.resolutionX, dy = P.resolutionY, dzs = P.sliceThickness;
+    const int iRadX = (int)ceilf(P.atomRadius / dx), iRadY = (int)ceilf(P.atomRadius / dy);
+    jobs.clear();
+    keys.clear();
+    std::map<int, int> index;
+    auto atomz = [&](int i) {
+        float z = (float)((double)(atoms[order[i]].z - cz * (float)slab + P.czOffset) -
+                          0.5 * P.sliceThickness * (1 - P.centerSlices));
+        return (float)((double)z + 0.5 * P.sliceThickness);
+    };
+    for (int ia = 0; ia < natom; ia++) {
+        while (ia < natom && atoms[order[ia]].Znum == 0) ia++;
+        if (ia >= natom) break;
+        float atomZ = atomz(ia);
+        if (P.nonPeriodZ) {
+            if (atomZ > cz) break;
+            do {
+                if (atomZ >= 0) break;
+                ++ia;
+                atomZ = atomz(ia);
+            } while (ia < natom - 1);
+        }
+        const qs_atom& A = atoms[order[ia]];
+        const float atomX = A.x - P.potOffsetX, atomY = A.y - P.potOffsetY;
+        const int iAtomX = (int)floorf(atomX / dx), iAtomY = (int)floorf(atomY / dy);
+        const int iAtomZ = (int)floor(atomZ / dzs);
+        const int Z = A.Znum;
+        if (Z < 1 || Z >= 93 || iAtomZ < 0 || iAtomZ >= P.slices) continue;
+        if (!index.count(Z)) {
+            index[Z] = (int)keys.size();
+            keys.push_back({Z, P.tds ? 0.0 : A.dw});
+        }
+        Atom2DJob J;
+        J.lut = index[Z];
+        J.iAtomZ = iAtomZ;
+        J.iax0 = iAtomX - iRadX;
+        J.iay0 = iAtomY - iRadY;
+        // (-iax0' + (atomX/dx - (iRadX - 2 potNx))) * OVERSAMP with the
+        // reference's iax0' = iax0 + 2 potNx, the quotient in float
+        double ddx = (-(double)(J.iax0 + 2 * P.potNx) + (atomX / dx - (double)(iRadX - 2 * P.potNx))) * 2.0;
+        double ddy = (-(double)(J.iay0 + 2 * P.potNy) + (atomY / dy - (double)(iRadY - 2 * P.potNy))) * 2.0;
+        J.iOffsX = (int)floor(ddx);
+        J.iOffsY = (int)floor(ddy);
+        ddx -= (double)J.iOffsX;
+        ddy -= (double)J.iOffsY;
+        J.s22 = (1 - ddx) * (1 - ddy);
+        J.s21 = (1 - ddx) * ddy;
+        J.s12 = ddx * (1 - ddy);
+        J.s11 = ddx * ddy;
+        jobs.push_back(J);
+    }
+}
+
 // Device LUT pointers for lutKeys, built on first use and kept by the context.
 static int prepare_luts(qs_ctx* c, const qs_params& P, const std::vector<std::pair<int, double>>& lutKeys,
                         const float* const** d_ptrs, int* Nz, int* Nr, int* nzSub) {
@@ -501,9 +567,22 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         set_error("slab " + std::to_string(slab) + " outside 0.." + std::to_string(p->cellDiv - 1));
         return QS_ERR_ARG;
     }
-    if (!p->fftpotential || !p->potential3D) {
-        set_error("only the 3-D FFT-integrated potential (one time integration, potential3D) is supported");
+    if (!p->fftpotential) {
+        set_error("only the FFT-integrated potential (one time integration) is supported");
         return QS_ERR_UNSUPPORTED;
+    }
+    if (!p->potential3D) {
+        // the 2-D potential: its periodic branch only (the non-periodic one
+        // reads its table outside the array for atoms near the edges), and
+        // tables at least as wide in x as in y (the reference bounds x by the
+        // y width and reads past a narrower table)
+        const int nx2 = 2 * 2 * (int)ceilf(p->atomRadius / p->resolutionX);
+        const int ny2 = 2 * 2 * (int)ceilf(p->atomRadius / p->resolutionY);
+        if (p->nonPeriod || nx2 < ny2) {
+            set_error(p->nonPeriod ? "the 2-D potential needs a periodic potential array (periodicXY)"
+                                   : "the 2-D potential needs ceil(atomRadius/dx) >= ceil(atomRadius/dy)");
+            return QS_ERR_UNSUPPORTED;
+        }
     }
     QS_CUDA_TRY(cudaSetDevice(c->device));
     const qs_params& P = *p;
@@ -523,7 +602,52 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
 
     std::vector<AtomJob> jobs;
     std::vector<std::pair<int, double>> lutKeys;
-    plan_atoms(P, atoms, natom, jobs, lutKeys, slab);
+    if (!P.potential3D) {
+        // make3DSlices' periodic 2-D branch
+        std::vector<Atom2DJob> jobs2;
+        plan_atoms_2d(P, atoms, natom, jobs2, lutKeys, slab);
+        if (!jobs2.empty()) {
+            int nx2 = 0, ny2 = 0;
+            QS_TRY(build_lut2d(P, 1, 0.0, nullptr, &nx2, &ny2, c->stream));
+            void* dp = nullptr;
+            QS_TRY(ensure(c, B_LUTPTR, sizeof(float*) * lutKeys.size(), &dp));
+            std::vector<const float*> ptrs(lutKeys.size());
+            for (size_t k = 0; k < lutKeys.size(); k++) {
+                // cached with the 3-D tables (charge flag 2 marks a 2-D table)
+                const qs_ctx::LutKey key{lutKeys[k].first, 2, lutKeys[k].second, P.resolutionX, P.resolutionY,
+                                         0.f, P.atomRadius};
+                auto it = c->luts.find(key);
+                if (it == c->luts.end()) {
+                    float* d = nullptr;
+                    cudaError_t e = cudaMalloc(&d, sizeof(float) * (size_t)nx2 * ny2);
+                    if (e != cudaSuccess) {
+                        cudaGetLastError();
+                        set_error(std::string("2-D table allocation failed: ") + cudaGetErrorString(e));
+                        return QS_ERR_NOMEM;
+                    }
+                    const int rc = build_lut2d(P, key.Z, key.B, d, nullptr, nullptr, c->stream);
+                    if (rc != QS_OK) {
+                        cudaStreamSynchronize(c->stream);
+                        cudaFree(d);
+                        return rc;
+                    }
+                    it = c->luts.emplace(key, d).first;
+                    // the builder's host tables must outlive their copies
+                    QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+                }
+                ptrs[k] = it->second;
+            }
+            QS_TRY(upload(c, P_LUTPTR, dp, ptrs.data(), sizeof(float*) * ptrs.size()));
+            void* dj = nullptr;
+            QS_TRY(ensure(c, B_JOBS, sizeof(Atom2DJob) * jobs2.size(), &dj));
+            QS_TRY(upload(c, P_JOBS, dj, jobs2.data(), sizeof(Atom2DJob) * jobs2.size()));
+            const int iRadX = (int)ceilf(P.atomRadius / P.resolutionX), iRadY = (int)ceilf(P.atomRadius / P.resolutionY);
+            QS_TRY(launch_scatter2d((const Atom2DJob*)dj, (int)jobs2.size(), (const float* const*)dp, ny2, 2 * iRadX,
+                                    2 * iRadY, P, Vr, c->stream));
+        }
+    } else {
+        plan_atoms(P, atoms, natom, jobs, lutKeys, slab);
+    }
 
     if (!jobs.empty()) {
         int Nz = 0, Nr = 0, ns = 0;

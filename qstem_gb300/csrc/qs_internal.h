@@ -200,6 +200,17 @@ struct AtomJob {
     int iAtomZ;
     int lut, lutq;               // LUT indices (-1: none)
 };
+// One atom of the periodic 2-D potential (make3DSlices' 2-D branch): its
+// slice, the unwrapped first pixel of its 2 iRadX x 2 iRadY box, the table
+// offsets and the bilinear weights, as the reference forms them.
+struct Atom2DJob {
+    double s11, s12, s21, s22;
+    int lut, iAtomZ, iax0, iay0, iOffsX, iOffsY;
+};
+// getAtomPotential2D: nx x ny real parts (float) into d_out (null: sizes only)
+int build_lut2d(const qs_params& p, int Z, double B, float* d_out, int* nx, int* ny, cudaStream_t s);
+int launch_scatter2d(const Atom2DJob* d_jobs, int njobs, const float* const* d_luts, int nyAtBox, int boxX, int boxY,
+                     const qs_params& p, float* V, cudaStream_t s);
 // the scatter-sum into V[slices][potNx][potNy] (float, zeroed by the caller);
 // charged: some job has a charge LUT (lutq >= 0)
 int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* const* d_luts, int Nz, int Nr,

@@ -288,6 +288,180 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
     return rc;
 }
 
+// --------------------------------------------------------- 2-D tables
+// getAtomPotential2D (stem3/stemlib.cpp:1750-1857): f(k) e^{i phase} on the
+// oversampled nx x ny k-grid (stored as float, as the reference stores it),
+// the inverse 2-D DFT in FP64, the real part rounded to float and scaled by
+// dkx*dky*OVERSAMP^2.
+__global__ void lut2d_fgrid(const double* __restrict__ tab, int nx, int ny, double dkx, double dky, double kmax2,
+                            double B, double sx, double sy, float2* __restrict__ temp) {
+    const int iy = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ix = blockIdx.y;
+    if (iy >= ny) return;
+    const double* g = tab;
+    const double* r = tab + NSF;
+    const double* sb = tab + 2 * NSF;
+    const double* sc = tab + 3 * NSF;
+    const double* sd = tab + 4 * NSF;
+    const double kx = dkx * (ix < nx / 2 ? ix : nx - ix);
+    const double ky = dky * (iy < ny / 2 ? iy : ny - iy);
+    const double s2 = kx * kx + ky * ky;
+    float2 out = make_float2(0.f, 0.f);
+    if (s2 < kmax2) {
+        const double f = spline_eval(g, r, sb, sc, sd, sqrt(s2)) * exp(-s2 * B * 0.25);
+        // the reference's PI (stem3/stemlib.cpp:75) times (kx dx nx + ky dy ny)
+        const double phase = 3.14159265358979 * (kx * sx + ky * sy);
+        double sn, cs;
+        sincos(phase, &sn, &cs);
+        out = make_float2((float)(f * cs), (float)(f * sn));
+    }
+    temp[(size_t)ix * ny + iy] = out;
+}
+
+// inverse DFT of every row (length n, all n outputs, FP64)
+__global__ void lut2d_dft_rows(const float2* __restrict__ in, const double2* __restrict__ W, int n,
+                               double2* __restrict__ out) {
+    extern __shared__ double2 lsm[];
+    double2* w = lsm;
+    double2* row = lsm + n;
+    const int ix = blockIdx.y;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        w[i] = W[i];
+        const float2 v = in[(size_t)ix * n + i];
+        row[i] = make_double2(v.x, v.y);
+    }
+    __syncthreads();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double re = 0, im = 0;
+    int m = 0;  // (iy * k) mod n
+    for (int iy = 0; iy < n; iy++) {
+        const double2 v = row[iy], t = w[m];
+        re += v.x * t.x - v.y * t.y;
+        im += v.x * t.y + v.y * t.x;
+        m += k;
+        if (m >= n) m -= n;
+    }
+    out[(size_t)ix * n + k] = make_double2(re, im);
+}
+
+// inverse DFT along x of the row transforms; the real part, rounded to float,
+// times scale (rounded to float again)
+__global__ void lut2d_dft_cols(const double2* __restrict__ G, const double2* __restrict__ W, int nx, int ny,
+                               double scale, float* __restrict__ out) {
+    extern __shared__ double2 lsm[];
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) lsm[i] = W[i];
+    __syncthreads();
+    const int ky = blockIdx.x * blockDim.x + threadIdx.x;
+    const int kx = blockIdx.y;
+    if (ky >= ny) return;
+    double re = 0;
+    int m = 0;  // (ix * kx) mod nx
+    for (int ix = 0; ix < nx; ix++) {
+        const double2 v = G[(size_t)ix * ny + ky], t = lsm[m];
+        re += v.x * t.x - v.y * t.y;
+        m += kx;
+        if (m >= nx) m -= nx;
+    }
+    out[(size_t)kx * ny + ky] = (float)((double)(float)re * scale);
+}
+
+int build_lut2d(const qs_params& p, int Z, double B, float* d_out, int* nxO, int* nyO, cudaStream_t s) {
+    if (Z < 1 || Z >= QS_REZ_NELEM) {
+        set_error("2-D potential table: atomic number out of range");
+        return QS_ERR_ARG;
+    }
+    const float rx = p.resolutionX, ry = p.resolutionY, R = p.atomRadius;
+    const int nx = 2 * OVERSAMP * (int)ceilf(R / rx);
+    const int ny = 2 * OVERSAMP * (int)ceilf(R / ry);
+    if (nxO) *nxO = nx;
+    if (nyO) *nyO = ny;
+    if (!d_out) return QS_OK;
+    const double dkx = 0.5 * OVERSAMP / (double)((float)nx * rx);
+    const double dky = 0.5 * OVERSAMP / (double)((float)ny * ry);
+    const double kmax = 0.5 * nx * dkx / (double)OVERSAMP;
+    std::vector<double> tab(5 * NSF);
+    double *g = tab.data(), *r = g + NSF, *sb = g + 2 * NSF, *sc = g + 3 * NSF, *sd = g + 4 * NSF;
+    std::memcpy(g, QS_REZ_F[0], sizeof(double) * NSF);
+    std::memcpy(r, QS_REZ_F[Z], sizeof(double) * NSF);
+    truncate_tail(g, r, kmax);
+    akima(g, r, sb, sc, sd, NSF);
+    double* d_tab = nullptr;
+    float2* d_temp = nullptr;
+    double2 *d_W = nullptr, *d_G = nullptr;
+    int rc = QS_OK;
+    auto fail = [&](cudaError_t e, const char* what) {
+        set_error(std::string("2-D potential table: ") + what + ": " + cudaGetErrorString(e));
+        rc = QS_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaMallocAsync(&d_tab, sizeof(double) * 5 * NSF, s)) != cudaSuccess) { fail(e, "alloc"); return rc; }
+    if ((e = cudaMallocAsync(&d_temp, sizeof(float2) * (size_t)nx * ny, s)) != cudaSuccess) fail(e, "alloc");
+    if (!rc && (e = cudaMallocAsync(&d_W, sizeof(double2) * (size_t)(nx + ny), s)) != cudaSuccess) fail(e, "alloc");
+    if (!rc && (e = cudaMallocAsync(&d_G, sizeof(double2) * (size_t)nx * ny, s)) != cudaSuccess) fail(e, "alloc");
+    const size_t smr = sizeof(double2) * 2 * (size_t)ny, smc = sizeof(double2) * (size_t)nx;
+    if (!rc) rc = smem_attr((const void*)lut2d_dft_rows, smr);
+    if (!rc) rc = smem_attr((const void*)lut2d_dft_cols, smc);
+    if (!rc) {
+        cudaMemcpyAsync(d_tab, tab.data(), sizeof(double) * 5 * NSF, cudaMemcpyHostToDevice, s);
+        lut2d_fgrid<<<dim3((ny + 127) / 128, nx), 128, 0, s>>>(d_tab, nx, ny, dkx, dky, kmax * kmax, B,
+                                                               (double)rx * nx, (double)ry * ny, d_temp);
+        lut_twiddles<<<(ny + 127) / 128, 128, 0, s>>>(ny, d_W);
+        lut_twiddles<<<(nx + 127) / 128, 128, 0, s>>>(nx, d_W + ny);
+        lut2d_dft_rows<<<dim3((ny + 127) / 128, nx), 128, smr, s>>>(d_temp, d_W, ny, d_G);
+        lut2d_dft_cols<<<dim3((ny + 127) / 128, nx), 128, smc, s>>>(d_G, d_W + ny, nx, ny,
+                                                                   dkx * dky * (OVERSAMP * OVERSAMP), d_out);
+        if ((e = cudaGetLastError()) != cudaSuccess) fail(e, "launch");
+        else count_launch(5);
+    }
+    cudaFreeAsync(d_G, s);
+    cudaFreeAsync(d_W, s);
+    cudaFreeAsync(d_temp, s);
+    cudaFreeAsync(d_tab, s);
+    return rc;
+}
+
+// make3DSlices' periodic 2-D branch (stem3/stemlib.cpp:1215-1262): one CTA
+// per atom; warp w takes box rows w, w + 8, ...; every pixel whose table
+// position lies inside the table adds the bilinear interpolation of its
+// element's 2-D table (the reference's weights, named against other corners
+// than the ones they multiply) to the atom's slice, wrapped into the array.
+// The interpolation is FP64 as in the reference; the sum a float reduction.
+__global__ void __launch_bounds__(256) scatter2d(const Atom2DJob* __restrict__ jobs, const float* const* __restrict__ luts,
+                                                 int nyAtBox, int boxX, int boxY, int potNx, int potNy,
+                                                 float* __restrict__ V) {
+    const Atom2DJob J = jobs[blockIdx.x];
+    const float* L = luts[J.lut];
+    float* const slice = V + (size_t)J.iAtomZ * potNx * potNy;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int qx = warp; qx < boxX; qx += nwarps) {
+        const int atPosX = OVERSAMP * qx - J.iOffsX;
+        if (atPosX < 0 || atPosX >= nyAtBox - 1) continue;
+        const int iax = J.iax0 + qx;
+        const int cx = ((iax % potNx) + potNx) % potNx;
+        const float* row0 = L + (size_t)atPosX * nyAtBox;
+        const float* row1 = row0 + nyAtBox;
+        float* const dst = slice + (size_t)cx * potNy;
+        for (int qy = lane; qy < boxY; qy += 32) {
+            const int atPosY = OVERSAMP * qy - J.iOffsY;
+            if (atPosY >= nyAtBox - 1 || atPosY < 0) continue;
+            const double v = J.s11 * (double)__ldg(row0 + atPosY) + J.s12 * (double)__ldg(row0 + atPosY + 1) +
+                             J.s21 * (double)__ldg(row1 + atPosY) + J.s22 * (double)__ldg(row1 + atPosY + 1);
+            const int iay = J.iay0 + qy;
+            atomicAdd(dst + ((iay % potNy) + potNy) % potNy, (float)v);
+        }
+    }
+}
+
+int launch_scatter2d(const Atom2DJob* d_jobs, int njobs, const float* const* d_luts, int nyAtBox, int boxX, int boxY,
+                     const qs_params& p, float* V, cudaStream_t s) {
+    if (njobs <= 0) return QS_OK;
+    scatter2d<<<njobs, 256, 0, s>>>(d_jobs, d_luts, nyAtBox, boxX, boxY, p.potNx, p.potNy, V);
+    QS_CUDA_TRY(cudaGetLastError());
+    count_launch(1);
+    return QS_OK;
+}
+
 // --------------------------------------------------------- scatter-sum
 // One block per atom job; threads stride over the atom's pixel box.  The
 // interpolation follows stem3/stemlib.cpp:935-1028 (radial linear

@@ -21,9 +21,10 @@ generator in the reference's order (qstem_gb300.thermal).
 
 Inputs that need parts of the reference outside this library, or that the
 reference cannot run, are refused with NotImplementedError: the 2-D
-potential (potential3D: no), more than one stacking-sequence line, a
-phonon file with a "Cube:" box (the reference exits there) and modes other
-than STEM, CBED and TEM.
+potential (potential3D: no) on a non-periodic potential array (the
+reference reads its table outside the array there), more than one
+stacking-sequence line, a phonon file with a "Cube:" box (the reference
+exits there) and modes other than STEM, CBED and TEM.
 """
 import math
 import os
@@ -489,8 +490,9 @@ def read_qsc(path, seed=20261203, rng="numpy", clock=0):
                 "one time integration:"):
         ans(g(key))
     pot3d = ans(g("potential3D:"))
-    if pot3d is not None and not _yes(pot3d, True):
-        unsupported.append("potential3D: no (the 2-D potential)")
+    potential3D = pot3d is None or _yes(pot3d, True)
+    if not potential3D and not periodicXY:
+        unsupported.append("potential3D: no (the 2-D potential) without periodicXY")
     avg_runs = int(_num(g("Runs for averaging:"), 10))
     ans(g("Store TDS diffr. patt. series:"))
     if not tds:  # stem3/stem3.cpp:1023
@@ -591,7 +593,8 @@ def read_qsc(path, seed=20261203, rng="numpy", clock=0):
                            astig_deg=astig_deg, outputInterval=outputInterval, czOffset=czOffset,
                            centerSlices=centerSlices, periodicXY=periodicXY, periodicZ=periodicZ,
                            bandlimit=bandlimit, atomRadius=atomRadius, smooth=smooth, gaussian=gaussian, aAIS=aAIS,
-                           beamCurrent=beam, dwellTime=dwell, tds=tds, cellDiv=cellDiv, nCellZ=ncz)
+                           beamCurrent=beam, dwellTime=dwell, tds=tds, cellDiv=cellDiv, nCellZ=ncz,
+                           potential3D=potential3D)
     p.mulsRepeat1, p.mulsRepeat2 = m1, m2
     if df is not None and df_w[:1].lower() == "o":  # "optimum" defocus, stem3/stem3.cpp:1160-1163
         p.df0 = F32(-float(F32(math.sqrt(float(p.Cs) * config.wavelength(float(p.v0))))))

@@ -60,7 +60,7 @@ class Golden:
         return self.z.files
 
 
-GOLDEN_CASES = ["sto64", "sto64q", "sto64bl", "sto64d2", "sto64d2u", "si64cbed", "si64tem"]
+GOLDEN_CASES = ["sto64", "sto64q", "sto64bl", "sto64d2", "sto64d2u", "si64cbed", "si64tem", "sto64p2d"]
 
 
 @pytest.fixture(params=GOLDEN_CASES)

@@ -71,6 +71,12 @@ CASES = {
     "si64cbed": dict(cell="si", ncell=(4, 3, 3), nx=64, resolutionX=0.06788, v0=300.0, slices=5, sliceThickness=2.0,
                      scan=None, detectors=[], alpha=10.0, Cs_mm=1.2, defocus_nm=-60.0, bandlimit=True,
                      mode="CBED", run=True, saveLevel=1),
+    # the 2-D potential (potential3D: no) on a periodic potential array: the
+    # periodic 2-D branch of make3DSlices and getAtomPotential2D's tables
+    "sto64p2d": dict(cell="sto", ncell=(3, 3, 4), nx=64, resolutionX=0.0915, v0=200.0, slices=8,
+                     sliceThickness=1.9525, scan=(3.905, 7.81, 3, 3.905, 7.81, 3),
+                     detectors=[(0.0, 20.0, "BF"), (40.0, 90.0, "HAADF")], alpha=20.0, periodicXY=True,
+                     potential3D=False, mode="STEM", run=True),
     # TEM: plane wave through a band-limited Si [110] slab (doTEM's exit wave)
     "si64tem": dict(cell="si", ncell=(4, 3, 4), nx=64, resolutionX=0.06, v0=300.0, slices=7, sliceThickness=2.0,
                     scan=None, detectors=[], alpha=0.0, bandlimit=True, mode="TEM", run=True),
@@ -101,7 +107,8 @@ def params_for(case):
                            outputInterval=case.get("outputInterval"), czOffset=case.get("czOffset", 0.0),
                            centerSlices=case.get("centerSlices", False),
                            periodicXY=case.get("periodicXY", False), bandlimit=case.get("bandlimit", False),
-                           cellDiv=case.get("cellDiv", 1), nCellZ=case["ncell"][2])
+                           cellDiv=case.get("cellDiv", 1), nCellZ=case["ncell"][2],
+                           potential3D=case.get("potential3D", True))
     return cell, atoms, p
 
 
@@ -117,7 +124,8 @@ def run_case(name, case, workdir):
                      outputInterval=case.get("outputInterval"), mode=case["mode"],
                      bandlimit=case.get("bandlimit", False), periodicXY=case.get("periodicXY", False),
                      folder="out", saveLevel=case.get("saveLevel", 2 if case["run"] else 0), czOffset=case.get("czOffset", 0.0),
-                     centerSlices=case.get("centerSlices", False), cellDiv=case.get("cellDiv", 1))
+                     centerSlices=case.get("centerSlices", False), cellDiv=case.get("cellDiv", 1),
+                     potential3D=case.get("potential3D", True))
     dump = os.path.join(workdir, "dump")
     oracle.run_reference(qsc, dump, run=case["run"])
     meta = dict(l.split(" = ", 1) for l in open(os.path.join(dump, "meta.txt")).read().strip().split("\n"))
@@ -141,6 +149,11 @@ def run_case(name, case, workdir):
         if os.path.exists(qf):
             out["lutq_%d" % Z] = np.fromfile(qf, np.float32).reshape(Nz, Nr, 2)[..., 0]
         out["nzsub"] = np.int32(ns)
+    l2d = os.path.join(dump, "lut2d_dims.txt")
+    if os.path.exists(l2d):
+        for line in open(l2d):
+            Z, nx2, ny2 = map(int, line.split())
+            out["lut2d_%d" % Z] = np.fromfile(os.path.join(dump, "lut2d_%d.bin" % Z), np.float32).reshape(nx2, ny2, 2)
     if case["run"] and case["mode"] == "STEM":
         nt = p.thickness_count()
         det = np.zeros((nt, p.detectorNum, p.scanXN, p.scanYN), np.float32)

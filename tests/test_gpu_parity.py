@@ -105,6 +105,28 @@ def test_slabs_from_atoms(ctx, name):
     assert rel_l2(det, g["det"]) <= TOL_MS
 
 
+def test_2d_potential_from_atoms(ctx):
+    """The periodic 2-D potential (potential3D: no; make3DSlices' 2-D branch
+    with getAtomPotential2D's tables): qs_stem_run from atoms against the
+    reference's detector images, and a 256^2 stack of 1,000 atoms against the
+    oracle's; the non-periodic 2-D branch is refused."""
+    g = Golden("sto64p2d")
+    p = g.params
+    det = ctx.stem_run(p, g["atoms"])
+    assert rel_l2(det, g["det"]) <= TOL_MS
+    cell = config.srtio3_cell()
+    atoms, ax, by, c = config.replicate(cell, 5, 5, 10)
+    q = config.make_params(nx=256, resolutionX=0.0763, v0=200, slices=20, sliceThickness=1.9525, ax=ax, by=by, c=c,
+                           scan=(7.81, 11.715, 2, 7.81, 11.715, 2), detectors=[(70, 200, "HAADF")], alpha=20,
+                           periodicXY=True, potential3D=False)
+    V = ctx.slices(q, atoms, potential_only=True)
+    Vo = oracle.potential(q, atoms)
+    assert rel_l2(V, Vo) <= TOL_BUILD
+    q.nonPeriod = 1
+    with pytest.raises(lib.QsError):
+        ctx.slices(q, atoms, potential_only=True)
+
+
 def test_end_to_end_from_atoms(ctx):
     """atoms -> slices -> probe -> scan entirely on the GPU vs the oracle chain."""
     g = Golden("sto64")

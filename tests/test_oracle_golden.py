@@ -43,6 +43,19 @@ def test_lut(golden):
         assert np.abs(mine - ref).max() <= TOL * np.abs(ref).max(), k
 
 
+def test_lut2d(golden):
+    """getAtomPotential2D's tables (the 2-D potential, potential3D: no)."""
+    keys = [k for k in golden.keys() if k.startswith("lut2d_")]
+    if not keys:
+        pytest.skip("not a 2-D potential case")
+    for k in keys:
+        Z = int(k.split("_")[1])
+        mine = oracle.lut2d(golden.params, Z, lut_B(golden, Z, False))
+        ref = golden[k]
+        assert mine.shape == ref.shape
+        assert np.abs(mine - ref).max() <= TOL * np.abs(ref).max(), k
+
+
 def test_potential(golden):
     V = oracle.potential(golden.params, golden["atoms"])
     ref = golden["V"]

@@ -79,7 +79,7 @@ def test_fixture_inputs_read_back(name):
                      outputInterval=case.get("outputInterval"), mode=case["mode"],
                      bandlimit=case.get("bandlimit", False), periodicXY=case.get("periodicXY", False),
                      czOffset=case.get("czOffset", 0.0), centerSlices=case.get("centerSlices", False),
-                     cellDiv=case.get("cellDiv", 1))
+                     cellDiv=case.get("cellDiv", 1), potential3D=case.get("potential3D", True))
     run = qsc.read_qsc(os.path.join(d, "run.qsc"))
     for f, _ in abi.QsParams._fields_:
         # equalDivs means nothing for an undivided cell (and older fixtures
@@ -99,7 +99,8 @@ def test_refused_inputs():
     for extra in ("potential3D: no", "mode: NBED", "sequence: 0 1", "sequence: 1 1\nsequence: 2 1"):
         text = base.replace("print level: 1", extra + "\nprint level: 1")
         if extra.startswith("potential3D"):
-            text = base.replace("potential3D: yes", extra)
+            # the 2-D potential on a non-periodic array (the periodic one runs)
+            text = base.replace("potential3D: yes", extra).replace("periodicXY: yes", "periodicXY: no")
         if extra.startswith("mode"):
             text = base.replace("mode: STEM", extra)
         if extra.startswith("sequence"):
