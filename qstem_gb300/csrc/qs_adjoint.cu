@@ -29,7 +29,11 @@
 
 namespace qs {
 
-constexpr int ADJ_ROW_LINES = 8;
+// lines per CTA of the row adjoint
+#ifndef QS_ADJ_ROW_LINES
+#define QS_ADJ_ROW_LINES 8
+#endif
+constexpr int ADJ_ROW_LINES = QS_ADJ_ROW_LINES;
 // the row adjoint's register budget (qs_tuned.h)
 constexpr int adj_min_blocks(int n) {
     return n == 64     ? QS_ADJ_MIN_BLOCKS_64

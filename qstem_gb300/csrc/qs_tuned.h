@@ -15,6 +15,10 @@
 // row-pass shapes and the budgets of both passes, phase 2 the row adjoint's
 // budget (it prints the whole sweep).  For the column pass a stated 1 (the
 // compiler may use up to 255 registers) differs from leaving the bound open.
+// The column pass's tiles, stages and budgets at 256, 384, 512 and 768 were
+// measured again after its tile copies became 16-byte copies of column pairs
+// (profiles/slice_loop_autotune.md): 256 8 columns x 2 stages at 4 CTAs per
+// SM, 384 16 x 2 at 2, 512 16 x 1 at 2, 768 8 x 2 at 2.
 #pragma once
 
 #ifndef QS_ROW_MIN_BLOCKS_64
@@ -45,16 +49,16 @@
 #define QS_COL_MIN_BLOCKS_128 1
 #endif
 #ifndef QS_COL_MIN_BLOCKS_256
-#define QS_COL_MIN_BLOCKS_256 2
+#define QS_COL_MIN_BLOCKS_256 4
 #endif
 #ifndef QS_COL_MIN_BLOCKS_384
-#define QS_COL_MIN_BLOCKS_384 4
+#define QS_COL_MIN_BLOCKS_384 2
 #endif
 #ifndef QS_COL_MIN_BLOCKS_512
 #define QS_COL_MIN_BLOCKS_512 2
 #endif
 #ifndef QS_COL_MIN_BLOCKS_768
-#define QS_COL_MIN_BLOCKS_768 1
+#define QS_COL_MIN_BLOCKS_768 2
 #endif
 #ifndef QS_COL_MIN_BLOCKS_1024
 #define QS_COL_MIN_BLOCKS_1024 2
@@ -111,16 +115,16 @@
 #define QS_COL_TILE_128 16
 #endif
 #ifndef QS_COL_TILE_256
-#define QS_COL_TILE_256 16
+#define QS_COL_TILE_256 8
 #endif
 #ifndef QS_COL_TILE_384
-#define QS_COL_TILE_384 8
+#define QS_COL_TILE_384 16
 #endif
 #ifndef QS_COL_TILE_512
 #define QS_COL_TILE_512 16
 #endif
 #ifndef QS_COL_TILE_768
-#define QS_COL_TILE_768 16
+#define QS_COL_TILE_768 8
 #endif
 #ifndef QS_COL_TILE_1024
 #define QS_COL_TILE_1024 8
@@ -139,13 +143,13 @@
 #define QS_COL_STAGES_256 2
 #endif
 #ifndef QS_COL_STAGES_384
-#define QS_COL_STAGES_384 1
+#define QS_COL_STAGES_384 2
 #endif
 #ifndef QS_COL_STAGES_512
-#define QS_COL_STAGES_512 2
+#define QS_COL_STAGES_512 1
 #endif
 #ifndef QS_COL_STAGES_768
-#define QS_COL_STAGES_768 1
+#define QS_COL_STAGES_768 2
 #endif
 #ifndef QS_COL_STAGES_1024
 #define QS_COL_STAGES_1024 1

@@ -195,6 +195,27 @@ def tune_factorisations(sizes, tmp):
     return best, defs
 
 
+def compare(specs, sizes, tmp):
+    """Time slice-loop builds with -D overrides side by side (best of two
+    measurements of each): specs "tag:DEF1,DEF2" ("tag:" for the defaults)."""
+    variants = {}
+    for spec in specs:
+        tag, _, defs = spec.partition(":")
+        variants[tag] = [d for d in defs.split(",") if d]
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(variants)) as ex:
+        libs = dict(zip(variants, ex.map(lambda v: _variant(v, SLICE_LOOP, variants[v], tmp)[0], variants)))
+    res = {}
+    for _ in range(2):
+        for v in variants:
+            r = _run_measure("--measure", sizes, libs[v])
+            res[v] = r if v not in res else {n: tuple(min(x, y) for x, y in zip(res[v][n], r[n])) for n in sizes}
+    print("row | column pass, us per position-slice")
+    print("N     " + "".join("%18s" % v for v in variants))
+    for n in sizes:
+        print("%-6d" % n + "".join("%9.3f%9.3f" % tuple(res[v][n]) for v in variants))
+    return 0
+
+
 def _run_measure(mode, sizes, path):
     r = subprocess.run([sys.executable, "-m", "qstem_gb300.tune", "--sizes", ",".join(map(str, sizes)), mode, path],
                        capture_output=True, text=True, check=True, cwd=os.path.dirname(_build.HERE))
@@ -207,6 +228,9 @@ def main(argv=None):
     ap.add_argument("--sizes", default=",".join(map(str, SIZES)))
     ap.add_argument("--lines", default="4,8")
     ap.add_argument("--write", action="store_true")
+    ap.add_argument("--compare", nargs="+", metavar="TAG:DEF,DEF",
+                    help="time the row and column passes of slice-loop builds with the given -D overrides "
+                         "(e.g. base: t8:QS_COL_TILE_256=8,QS_COL_MIN_BLOCKS_256=4) side by side and stop")
     ap.add_argument("--measure", help=argparse.SUPPRESS)          # internal: time one library
     ap.add_argument("--measure-adjoint", help=argparse.SUPPRESS)  # internal
     a = ap.parse_args(argv)
@@ -218,8 +242,10 @@ def main(argv=None):
         print(json.dumps(measure_adjoint(a.measure_adjoint, sizes)))
         return 0
     _build.build()
-    cands = [int(k) for k in a.candidates.split(",")]
     tmp = tempfile.mkdtemp(prefix="qs_tune_")
+    if a.compare:
+        return compare(a.compare, sizes, tmp)
+    cands = [int(k) for k in a.candidates.split(",")]
     # phase 0: factorisations and column tiles
     best, fdefs = tune_factorisations(sizes, tmp)
     # phase 1: row and column passes
