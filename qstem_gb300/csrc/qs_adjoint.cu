@@ -138,28 +138,36 @@ __global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES, adj_min_block
     const int b = (int)(line / a.nx);
     const int x = (int)(line - (long)b * a.nx);
     const SmemRow<Cfg::R0> sm{s_line};
-    // g_phi = IFFT_y(g_A)
+    // g_phi = IFFT_y(g_A), and psi of this slice: the probe, or
+    // IFFT_y(h)/N of the stored state.  With up to 16 elements a thread both
+    // lines' loads are issued before either transform, so that their
+    // latencies overlap (longer lines keep them apart: registers)
+    constexpr bool EARLY = E <= 16;
     float2* grow = a.grad + ((size_t)b * a.nx + x) * N;
-    float2 g[E];
+    float2 g[E], psi[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const int y = t + T * e;
         g[e] = (y <= a.yA || y >= a.yB) ? grow[y] : make_float2(0.f, 0.f);
     }
-    line_fft<Cfg, true>(g, sm, s_tw, t);
-    // psi of this slice: the probe, or IFFT_y(h)/N of the stored state
-    float2 psi[E];
-    if constexpr (FIRST) {
-        const float2* src = a.probe + (size_t)x * N;
+    auto load_psi = [&]() {
+        if constexpr (FIRST) {
+            const float2* src = a.probe + (size_t)x * N;
 #pragma unroll
-        for (int e = 0; e < E; ++e) psi[e] = __ldg(src + t + T * e);
-    } else {
-        const float2* src = a.state + ((size_t)b * a.nx + x) * N;
+            for (int e = 0; e < E; ++e) psi[e] = __ldg(src + t + T * e);
+        } else {
+            const float2* src = a.state + ((size_t)b * a.nx + x) * N;
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const int y = t + T * e;
-            psi[e] = (y <= a.yA || y >= a.yB) ? src[y] : make_float2(0.f, 0.f);
+            for (int e = 0; e < E; ++e) {
+                const int y = t + T * e;
+                psi[e] = (y <= a.yA || y >= a.yB) ? src[y] : make_float2(0.f, 0.f);
+            }
         }
+    };
+    if constexpr (EARLY) load_psi();
+    line_fft<Cfg, true>(g, sm, s_tw, t);
+    if constexpr (!EARLY) load_psi();
+    if constexpr (!FIRST) {
         line_fft<Cfg, true>(psi, sm, s_tw, t);
 #pragma unroll
         for (int e = 0; e < E; ++e) psi[e] = cscale(psi[e], a.norm);
