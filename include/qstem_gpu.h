@@ -10,6 +10,9 @@
  *   qs_slices_build     make3DSlices + initSTEMSlices (qs_slab_build: one slab
  *                       of a cell divided along z)
  *                       (stem3/stemlib.h:45, :39; stem3/stemlib.cpp:383, :2199)
+ *   qs_slices_build_custom  make3DSlicesFT + initSTEMSlices: custom
+ *                       scattering factors (stem3/customslice.h:28;
+ *                       stem3/customslice.cpp:56)
  *   qs_probe            probe (stem3/stemlib.h:36; stem3/stemlib.cpp:1952)
  *   qs_multislice_run   the position loop of doSTEM/doCBED around runMulsSTEM,
  *                       which fuses transmit, the 2-D FFT pair, propagate_slow,
@@ -209,6 +212,21 @@ int qs_slices_build(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int n
  * :709-713).  qs_slices_build is slab 0. */
 int qs_slab_build(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom, int slab,
                   float *trans, unsigned flags);
+
+/* The same from custom scattering factors ("Structure Factors: custom"):
+ * make3DSlicesFT (stem3/customslice.cpp:56-317), the path doCBED and doNBED
+ * take for them (stem3/stem3.cpp:2177-2197), followed by initSTEMSlices.
+ * k[nk] (1/A) and f[kind][nk] (A) are the table readSFactLUT reads
+ * (stem3/stem3.cpp:555-600: "Nk:", "k:", one line per element), for the
+ * elements Z[kind]; every atom's element must be among them.  The potential
+ * of each element is the inverse 2-D FFT of f on a 40 A (z, r) box, cut off
+ * where it first turns negative, interpolated bicubically for every atom,
+ * pixel and slice within the cut-off (a brute force, as in the reference).
+ * potential3D and cellDiv do not change it (the reference builds slab 0's
+ * stack on every call); slices must be at least 2 (the reference adds no
+ * atom to a single slice).  Flags as for qs_slices_build. */
+int qs_slices_build_custom(qs_ctx *ctx, const qs_params *p, const qs_atom *atoms, int natom, const double *k,
+                           int nk, const int *Z, const double *f, int nkinds, float *trans, unsigned flags);
 
 /* ----------------------------------------------------------------- probe */
 /* nx x ny c64 real-space probe centred at (dx, dy) A. */

@@ -50,6 +50,7 @@ def lib():
                               ctypes.POINTER(ctypes.c_int)]
         L.qso_lut2d.argtypes = [P, ctypes.c_int, ctypes.c_double, fp, ctypes.POINTER(ctypes.c_int),
                                 ctypes.POINTER(ctypes.c_int)]
+        L.qso_potential_ft.argtypes = [P, fp, ctypes.c_int, fp, ctypes.c_int, fp, fp, ctypes.c_int, fp]
         L.qso_potential.argtypes = [P, fp, ctypes.c_int, fp]
         L.qso_potential_slab.argtypes = [P, fp, ctypes.c_int, ctypes.c_int, fp]
         L.qso_stem_slabs.argtypes = [P, fp, ctypes.c_int, fp, ctypes.c_int, ctypes.c_int, fp, fp, fp, ctypes.c_int]
@@ -87,6 +88,19 @@ def lut2d(p, Z, B=0.0):
     assert rc == 0, rc
     out = np.zeros((nx.value, ny.value, 2), np.float32)
     rc = L.qso_lut2d(ctypes.byref(p), Z, B, _ptr(out), None, None)
+    assert rc == 0, rc
+    return out
+
+
+def potential_ft(p, atoms, k, Zs, f):
+    """make3DSlicesFT with the custom table k[nk], f[kind][nk] of elements Zs."""
+    out = np.zeros((p.slices, p.potNx, p.potNy, 2), np.float32)
+    a = abi.atoms_to_numpy(atoms)
+    k = np.ascontiguousarray(k, np.float64)
+    Z = np.ascontiguousarray(Zs, np.int32)
+    f = np.ascontiguousarray(f, np.float64)
+    rc = lib().qso_potential_ft(ctypes.byref(p), _ptr(a), len(a), _ptr(k), len(k), _ptr(Z), _ptr(f), len(Z),
+                                _ptr(out))
     assert rc == 0, rc
     return out
 

@@ -475,6 +475,195 @@ static int potential2d_periodic(const qs_params *p, const qs_atom *atoms_in, int
     return QS_OK;
 }
 
+/* ------------------------------------------ custom scattering factors */
+/* make3DSlicesFT (stem3/customslice.cpp:56-317) with the custom table of
+ * readSFactLUT (stem3/stem3.cpp:555-600): k[nk] and f[kind][nk] as read,
+ * extended by k = 2 k[nk-1] with f = 0; sfLUT (stem3/stemutil.cpp:1427-1467)
+ * evaluates them with the Akima spline, 0 above the last k and where
+ * negative. */
+typedef struct {
+    int n;
+    double *k, *f, *b, *c, *d;
+} ft_sf;
+
+static double ft_sfeval(const ft_sf *t, double s) {
+    if (s > t->k[t->n - 1]) return 0.0;
+    const double v = qso_seval(t->k, t->f, t->b, t->c, t->d, t->n, s);
+    return v < 0 ? 0.0 : v;
+}
+
+/* reduceAndExpand (stem3/customslice.cpp:359-401) on a flat nz x nx array:
+ * the real part summed over the z oversampling into rows 1..Nzm, columns
+ * 1..Nxm (the last column landing on the next row's first element, as the
+ * reference's row-major array places it), then row 0 and column 0
+ * extrapolated. */
+static double *ft_reduce(const double *fc, int Nz, int Nx, int zOversample, int *fNz, int *fNx) {
+    const int Nxm = Nx / 2, Nzm = Nz / 2, nx = Nxm, nz = Nzm + 2;
+    double *ff = (double *)calloc((size_t)nz * nx, sizeof(double));
+    *fNx = nx;
+    *fNz = nz;
+    const int Ninteg = (zOversample - 1) / 2;
+    for (int iz = 0; iz < Nzm; iz++)
+        for (int ix = 0; ix < Nxm; ix++)
+            for (int j = -Ninteg; j <= Ninteg; j++)
+                if ((iz + j + Nzm >= 0) && (iz + j < Nzm))
+                    ff[(size_t)(iz + 1) * nx + ix + 1] += fc[2 * ((size_t)(iz + Nzm + j) * Nx + ix + Nxm)];
+    for (int iz = 1; iz <= Nzm; iz++)
+        ff[(size_t)iz * nx] = ff[(size_t)iz * nx + 1] + (ff[(size_t)iz * nx + 1] - ff[(size_t)iz * nx + 2]);
+    for (int ix = 0; ix <= Nxm; ix++) ff[ix] = ff[nx + ix] + (ff[nx + ix] - ff[2 * (size_t)nx + ix]);
+    return ff;
+}
+
+/* bicubic (stem3/stemutil.cpp:1470-1520) on the flat table */
+static double ft_bicubic(const double *ff, int Nz, int Nx, double z, double x) {
+    const int xi = (int)x, zi = (int)z;
+    x = x - (double)xi;
+    z = z - (double)zi;
+    const double x0 = ((2.0 - x) * x - 1.0) * x;
+    const double x1 = (3.0 * x - 5.0) * x * x + 2.0;
+    const double x2 = ((4.0 - 3.0 * x) * x + 1.0) * x;
+    x = (x - 1.0) * x * x;
+#define FTX(r) (ff[(size_t)(r) * Nx + xi - 1] * x0 + ff[(size_t)(r) * Nx + xi] * x1 + \
+                ff[(size_t)(r) * Nx + xi + 1] * x2 + ff[(size_t)(r) * Nx + xi + 2] * x)
+    double f;
+    if (Nz > 2) {
+        if ((zi > Nz - 3) || (xi > Nx - 3)) return 0.0;
+        if ((zi < 1) && (xi < 1)) return ff[0];
+        if (zi < 1) return ff[xi];
+        if (xi < 1) return ff[(size_t)zi * Nx];
+        f = FTX(zi - 1) * (((2.0 - z) * z - 1) * z);
+        f += FTX(zi) * ((3.0 * z - 5.0) * z * z + 2.0);
+        f += FTX(zi + 1) * (((4.0 - 3.0 * z) * z + 1.0) * z);
+        f += FTX(zi + 2) * ((z - 1.0) * z * z);
+        f *= 0.25;
+    } else {
+        f = 0.5 * FTX(0);
+    }
+#undef FTX
+    return f;
+}
+
+int qso_potential_ft(const qs_params *p, const qs_atom *atoms_in, int natom, const double *k, int nk,
+                     const int *Zs, const double *sf, int nkinds, float *trans) {
+    const int Nxp = p->potNx, Nyp = p->potNy, Nzp = p->slices;
+    if (Nzp < 2 || nk < 4 || nkinds < 1) return QS_ERR_UNSUPPORTED;
+    const size_t sliceStep = 2 * (size_t)Nxp * Nyp;
+    memset(trans, 0, sizeof(float) * sliceStep * Nzp);
+    /* box geometry (stem3/customslice.cpp:114-160) */
+    const float czp = p->c / (float)p->cellDiv;
+    const float axp = p->potSizeX, byp = p->potSizeY;
+    const float dXp = (float)(axp / (double)Nxp), dYp = (float)(byp / (double)Nyp), dZp = (float)(czp / (double)Nzp);
+    float ax = 40.0f, cz = 40.0f;
+    double dZ = dZp;
+    int zOversample = 1;
+    while (dZ > 0.4) zOversample += 2, dZ = dZp / (double)(zOversample);
+    int Nz = (int)(cz / dZ + 0.5);
+    if (Nz / 2 < 0.5 * (double)Nz) Nz++;
+    cz = (float)((double)Nz * dZ);
+    double dX = (dXp < dYp ? dXp : dYp);
+    int xOversample = 1;
+    while (dX > 0.1) dX = dXp / (double)(++xOversample);
+    int Nx = (int)(ax / dX);
+    if (Nx / 2 < 0.5 * (double)Nx) Nx++;
+    ax = (float)((double)Nx * dX);
+    const int Nxm = Nx / 2;
+    const double dsX = 1.0 / ax, dsZ = 1.0 / cz;
+    double sx2max = 10.8 * (Nxm * dsX);
+    sx2max = 1.0 / (sx2max * sx2max);
+    int Nzm;
+    double sz2max;
+    if (Nz > 1) Nzm = Nz / 2, sz2max = 1.0 / ((10.8 * (Nzm * dsZ)) * (10.8 * (Nzm * dsZ)));
+    else Nzm = 1, sz2max = 1.0;
+    const double twopi = 6.28318530717959;
+    double **lut = (double **)calloc(nkinds, sizeof(double *));
+    double *rc = (double *)calloc(nkinds, sizeof(double));
+    int Nzl = 0, Nxl = 0;
+    double *pot = (double *)malloc(sizeof(double) * 2 * (size_t)Nz * Nx);
+    ft_sf t;
+    t.n = nk + 1;
+    t.k = (double *)malloc(sizeof(double) * t.n);
+    t.f = (double *)malloc(sizeof(double) * t.n);
+    t.b = (double *)malloc(sizeof(double) * t.n);
+    t.c = (double *)malloc(sizeof(double) * t.n);
+    t.d = (double *)malloc(sizeof(double) * t.n);
+    memcpy(t.k, k, sizeof(double) * nk);
+    t.k[nk] = 2.0 * k[nk - 1];
+    for (int kind = 0; kind < nkinds; kind++) {
+        memcpy(t.f, sf + (size_t)kind * nk, sizeof(double) * nk);
+        t.f[nk] = 0.0;
+        qso_splinh(t.k, t.f, t.b, t.c, t.d, t.n);
+        memset(pot, 0, sizeof(double) * 2 * (size_t)Nz * Nx);
+        for (int iz = 0; iz < Nz; iz++) {
+            const double sz = (iz < Nzm ? iz : iz - Nz) * dsZ, sz2 = sz * sz, sz2r = sz2max * sz2;
+            if ((Nz < 2) || (sz2r <= 1.0)) {
+                for (int ix = 0; ix < Nx; ix++) {
+                    const double sx = (ix < Nxm ? ix : ix - Nx) * dsX, sx2 = sx * sx;
+                    if (sz2r + sx2max * sx2 <= 1.0) {
+                        const double s = sqrt(sz2 + sx2);
+                        const double arg = twopi * (sx * (0.5 * ax) + sz * (0.5 * cz));
+                        const double ffr = cos(arg), ffi = sin(arg);
+                        pot[2 * ((size_t)iz * Nx + ix)] = ft_sfeval(&t, 0.5 * s) * ffr;
+                        pot[2 * ((size_t)iz * Nx + ix) + 1] = ft_sfeval(&t, 0.5 * s) * ffi;
+                    }
+                }
+            }
+        }
+        const int dims[2] = {Nz, Nx};
+        qs_fftnd_c128(2, dims, 1, 0, pot, +1);
+        const double scale = 2 * 47.87658 / (sqrt((double)(Nx * Nz) * ax * cz));
+        double rcut = 50;
+        for (int iz = 0; iz < Nz; iz++)
+            for (int ix = 0; ix < Nx; ix++) {
+                double *v = pot + 2 * ((size_t)iz * Nx + ix);
+                const double r = sqrt((dZ * (iz - Nzm)) * (dZ * (iz - Nzm)) + (dX * (ix - Nxm)) * (dX * (ix - Nxm)));
+                if (r > rcut) v[0] = 0.0, v[1] = 0.0;
+                else if (v[0] < 0) rcut = r, v[0] = 0.0, v[1] = 0.0;
+                else v[0] *= scale, v[1] *= scale;
+            }
+        for (int iz = 0; iz < Nz; iz++)
+            for (int ix = 0; ix < Nx; ix++) {
+                const double r = sqrt((dZ * (iz - Nzm)) * (dZ * (iz - Nzm)) + (dX * (ix - Nxm)) * (dX * (ix - Nxm)));
+                if (r > rcut) pot[2 * ((size_t)iz * Nx + ix)] = 0.0, pot[2 * ((size_t)iz * Nx + ix) + 1] = 0.0;
+            }
+        rc[kind] = rcut;
+        lut[kind] = ft_reduce(pot, Nz, Nx, zOversample, &Nzl, &Nxl);
+    }
+    /* the atoms, sorted by z (atomCompare), each added to every pixel of
+     * every slice within the cut-off (stem3/customslice.cpp:260-290); divCount
+     * is a local of the reference's function, so the z origin is czOffset */
+    qs_atom *atoms = (qs_atom *)malloc(sizeof(qs_atom) * (size_t)(natom > 0 ? natom : 1));
+    if (natom > 0) memcpy(atoms, atoms_in, sizeof(qs_atom) * (size_t)natom);
+    qsort(atoms, natom, sizeof(qs_atom), cmp_z);
+    const double zStart = p->czOffset;
+    int rc_ok = QS_OK;
+    for (int j = 0; j < natom && rc_ok == QS_OK; j++) {
+        int kind = 0;
+        while (kind < nkinds && Zs[kind] != atoms[j].Znum) kind++;
+        if (kind == nkinds) { rc_ok = QS_ERR_ARG; break; }
+        for (int iz = 0; iz < Nzp; iz++) {
+            const double z = fabs((iz + 0.5) * dZp - (atoms[j].z - zStart) + 0 * czp);
+            if (z <= rc[kind] + dZp) {
+                for (int ix = 0; ix < Nxp; ix++) {
+                    const double x = ((ix + 0.5) * dXp - atoms[j].x + 0 * axp) + p->potOffsetX;
+                    for (int iy = 0; iy < Nyp; iy++) {
+                        const double y = ((iy + 0.5) * dYp - atoms[j].y + 0 * byp) + p->potOffsetY;
+                        const double rxy2 = x * x + y * y;
+                        const double r = sqrt(rxy2 + z * z);
+                        if (r <= rc[kind] + dZp + dXp) {
+                            float *tp = trans + (size_t)iz * sliceStep + 2 * ((size_t)ix * Nyp + iy);
+                            *tp = (float)((double)*tp + ft_bicubic(lut[kind], Nzl, Nxl, z / dZ + 1.0, sqrt(rxy2) / dX + 1.0));
+                        }
+                    }
+                }
+            }
+        }
+    }
+    for (int kind = 0; kind < nkinds; kind++) free(lut[kind]);
+    free(lut); free(rc); free(pot); free(atoms);
+    free(t.k); free(t.f); free(t.b); free(t.c); free(t.d);
+    return rc_ok;
+}
+
 /* ---------------------------------------------------------- transmission */
 int qso_transmission(const qs_params *p, float *trans) {
     /* stem3/stemlib.cpp:2199-2357 */

@@ -39,6 +39,10 @@ int qso_lut(const qs_params *p, int Znum, double B, int charged, float *out, int
  * trans: slices*potNx*potNy c64, overwritten with V in .re and 0 in .im.
  * atoms is not modified (a sorted copy is used). */
 int qso_potential(const qs_params *p, const qs_atom *atoms, int natom, float *trans);
+/* make3DSlicesFT with a custom scattering-factor table: k[nk], f[kind][nk]
+ * for the elements Zs[kind] */
+int qso_potential_ft(const qs_params *p, const qs_atom *atoms, int natom, const double *k, int nk,
+                     const int *Zs, const double *sf, int nkinds, float *trans);
 /* getAtomPotential2D: nx x ny complex floats (out NULL: sizes only) */
 int qso_lut2d(const qs_params *p, int Znum, double B, float *out, int *nx, int *ny);
 /* the same for slab `slab` of a cell divided into cellDiv slabs along z */

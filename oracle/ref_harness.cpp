@@ -35,6 +35,7 @@
 #include "readparams.h"
 #include "stemlib.h"
 #include "stemutil.h"
+#include "customslice.h"
 
 extern MULS muls;
 void readFile();
@@ -73,12 +74,26 @@ int main(int argc, char **argv) {
 
     dump("atoms.bin", muls.atoms, sizeof(atom) * (size_t)muls.natom);
 
+    /* make3DSlicesFT clears trans with sizeof(fftw_complex) (16 bytes) per
+     * element of its fftwf_complex (8-byte) array, writing past the end of
+     * the array readFile allocated (stem3/customslice.cpp:251, against
+     * stem3/stem3.cpp:1532).  For custom scattering factors the harness
+     * hands it a stack of twice the slices, so that the clearing stays in
+     * memory it owns; the slices it fills are the first half, unchanged.
+     * (The potential-array FFT plans stay on readFile's array: the band
+     * limit that uses them is off in these runs.) */
+    if (muls.scatFactor == CUSTOM)
+        muls.trans = complex3Df(2 * muls.slices, muls.potNx, muls.potNy, "trans");
+
     /* The reference builds the slices and phase gratings once per run inside
      * doSTEM; here the same calls are made once beforehand so that their
      * outputs can be captured (they are repeated identically inside the run). */
     int saveAvg = muls.avgCount;
     muls.avgCount = 0;
-    make3DSlices(&muls, muls.slices, muls.atomPosFile, NULL);
+    if (muls.scatFactor == CUSTOM) /* doCBED's custom scattering factors (stem3/stem3.cpp:2177) */
+        make3DSlicesFT(&muls);
+    else
+        make3DSlices(&muls, muls.slices, muls.atomPosFile, NULL);
     dump("atoms_sorted.bin", muls.atoms, sizeof(atom) * (size_t)muls.natom);
     size_t ntrans = (size_t)muls.slices * muls.potNx * muls.potNy;
     dump("potential.bin", muls.trans[0][0], ntrans * sizeof(fftwf_complex));

@@ -17,7 +17,7 @@ LIB = os.path.join(LIBDIR, "libqstem_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-I" + os.path.join(HERE, "..", "include")]
-SOURCES = ["qs_multislice.cu", "qs_rows.cu", "qs_potential.cu", "qs_probe.cu", "qs_api.cu", "qs_noalloc.cu", "qs_adjoint.cu", "qs_tem.cu", "qs_dft.cu", "qs_resident.cu"]
+SOURCES = ["qs_multislice.cu", "qs_rows.cu", "qs_potential.cu", "qs_probe.cu", "qs_api.cu", "qs_noalloc.cu", "qs_adjoint.cu", "qs_tem.cu", "qs_dft.cu", "qs_resident.cu", "qs_custom.cu"]
 
 
 def nvcc():

@@ -442,9 +442,11 @@ def write_qsc(path, *, cfg_file, ncell, nx, resolutionX, v0, slices, sliceThickn
               detectors=(), alpha=20.0, Cs_mm=0.0, C5_mm=0.0, defocus_nm=0.0, outputInterval=None,
               mode="STEM", bandlimit=False, periodicXY=False, periodicZ=False, folder="out",
               saveLevel=0, smooth=True, czOffset=0.0, atomRadius=5.0, centerSlices=False, cellDiv=1,
-              sequence=(1, 1), potential3D=True):
+              sequence=(1, 1), potential3D=True, custom_sf=None):
     """A stem3 input file for the same run make_params describes
-    (sequence: the stacking sequence m1 m2)."""
+    (sequence: the stacking sequence m1 m2; custom_sf: (k values, {Z: f
+    values}) for "Structure Factors: custom", the table readSFactLUT reads,
+    stem3/stem3.cpp:555-600)."""
     yn = lambda b: "yes" if b else "no"
     L = ["mode: %s" % mode, "print level: 1", "save level: %d" % saveLevel,
          "filename: %s" % cfg_file, "resolutionX: %r" % float(resolutionX),
@@ -473,7 +475,14 @@ def write_qsc(path, *, cfg_file, ncell, nx, resolutionX, v0, slices, sliceThickn
           "beam current: 1", "dwell time: 1.6021773e-4", "smooth: %s" % yn(smooth),
           "gaussian: no", "potential3D: %s" % yn(potential3D), "atom radius: %r" % float(atomRadius),
           "bandlimit f_trans: %s" % yn(bandlimit), "one time integration: yes",
-          'Folder: "%s"' % folder, "Runs for averaging: 1", "Structure Factors: WK",
-          "sequence: %d %d" % tuple(sequence)]
+          'Folder: "%s"' % folder, "Runs for averaging: 1"]
+    if custom_sf is None:
+        L.append("Structure Factors: WK")
+    else:
+        kv, table = custom_sf
+        L += ["Structure Factors: custom", "Nk: %d" % len(kv), "k: " + " ".join("%.6g" % v for v in kv)]
+        for Z, f in table.items():
+            L.append("%s: " % SYMBOL[Z] + " ".join("%.6g" % v for v in f))
+    L.append("sequence: %d %d" % tuple(sequence))
     with open(path, "w") as f:
         f.write("\n".join(L) + "\n")

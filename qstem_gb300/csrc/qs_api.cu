@@ -559,19 +559,34 @@ int qs_slices_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int nat
     return qs_slab_build(c, p, atoms, natom, 0, trans_out, flags);
 }
 
-int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, int slab, float* trans_out,
-                  unsigned flags) {
+}  // extern "C"
+
+namespace {
+// a custom scattering-factor table (readSFactLUT, stem3/stem3.cpp:555-600)
+struct CustomSF {
+    const double* k;
+    int nk;
+    const int* Z;
+    const double* f;
+    int nkinds;
+};
+}  // namespace
+
+// qs_slab_build, and with a custom table make3DSlicesFT in place of
+// make3DSlices
+static int slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, int slab, float* trans_out,
+                      unsigned flags, const CustomSF* cs) {
     if (!c || !trans_out || (natom > 0 && !atoms)) { set_error("null argument"); return QS_ERR_ARG; }
     QS_TRY(check_params(p));
     if (slab < 0 || slab >= p->cellDiv) {
         set_error("slab " + std::to_string(slab) + " outside 0.." + std::to_string(p->cellDiv - 1));
         return QS_ERR_ARG;
     }
-    if (!p->fftpotential) {
+    if (!cs && !p->fftpotential) {
         set_error("only the FFT-integrated potential (one time integration) is supported");
         return QS_ERR_UNSUPPORTED;
     }
-    if (!p->potential3D) {
+    if (!cs && !p->potential3D) {
         // the 2-D potential: its periodic branch only (the non-periodic one
         // reads its table outside the array for atoms near the edges), and
         // tables at least as wide in x as in y (the reference bounds x by the
@@ -602,7 +617,11 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
 
     std::vector<AtomJob> jobs;
     std::vector<std::pair<int, double>> lutKeys;
-    if (!P.potential3D) {
+    if (cs) {
+        // make3DSlicesFT: every slab's stack is slab 0's (the reference's
+        // slab counter is a local of the function, restarted at 0)
+        QS_TRY(build_custom_potential(P, atoms, natom, cs->k, cs->nk, cs->Z, cs->f, cs->nkinds, Vr, c->stream));
+    } else if (!P.potential3D) {
         // make3DSlices' periodic 2-D branch
         std::vector<Atom2DJob> jobs2;
         plan_atoms_2d(P, atoms, natom, jobs2, lutKeys, slab);
@@ -754,6 +773,23 @@ int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom
         QS_CUDA_TRY(cudaStreamSynchronize(c->stream));
     }
     return QS_OK;
+}
+
+extern "C" {
+
+int qs_slab_build(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, int slab, float* trans_out,
+                  unsigned flags) {
+    return slab_build(c, p, atoms, natom, slab, trans_out, flags, nullptr);
+}
+
+int qs_slices_build_custom(qs_ctx* c, const qs_params* p, const qs_atom* atoms, int natom, const double* k, int nk,
+                           const int* Z, const double* f, int nkinds, float* trans_out, unsigned flags) {
+    if (!k || !Z || !f || nk < 4 || nkinds < 1) {
+        set_error("custom scattering factors: k, Z and f tables needed (nk >= 4, nkinds >= 1)");
+        return QS_ERR_ARG;
+    }
+    const CustomSF cs{k, nk, Z, f, nkinds};
+    return slab_build(c, p, atoms, natom, 0, trans_out, flags, &cs);
 }
 
 static int probe_into(qs_ctx* c, const qs_params& P, double dx, double dy, float2* w) {

@@ -215,6 +215,14 @@ int launch_scatter2d(const Atom2DJob* d_jobs, int njobs, const float* const* d_l
 // charged: some job has a charge LUT (lutq >= 0)
 int launch_scatter(const AtomJob* d_jobs, int njobs, bool charged, const float* const* d_luts, int Nz, int Nr,
                    int nzSub, const qs_params& p, const double* d_knots, float* V, cudaStream_t s);
+// Akima's local cubic spline coefficients of (x, y), n >= 4 knots
+// (stem3/stemutil.cpp:975-1041)
+void akima_spline(const double* x, const double* y, double* b, double* c, double* d, int n);
+// make3DSlicesFT's potential (custom scattering factors k[nk], f[kind][nk]
+// of the elements Zs[kind]) into the real array V[slices][potNx][potNy]
+// (qs_custom.cu); synchronises the stream
+int build_custom_potential(const qs_params& P, const qs_atom* atoms, int natom, const double* k, int nk,
+                           const int* Zs, const double* sf, int nkinds, float* V, cudaStream_t s);
 // knots[k], k = 0..Nr: the smallest s = x^2 + y^2 (double) whose radial
 // interval floor(fl(fl(sqrt(s)) / dr)) in make3DSlices is at least k
 void scatter_knots(double dr, int Nr, std::vector<double>& knots);

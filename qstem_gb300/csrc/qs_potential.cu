@@ -22,7 +22,7 @@ constexpr int NSF = QS_REZ_NSF;
 constexpr int OVERSAMP = 2;
 
 // --------------------------------------------------------------- spline
-static void akima(const double* x, const double* y, double* b, double* c, double* d, int n) {
+void akima_spline(const double* x, const double* y, double* b, double* c, double* d, int n) {
     // Akima local cubic with linearly extrapolated end secants
     // (same construction as stem3/stemutil.cpp:975-1041)
     const double tiny = 1.0e-25;
@@ -239,7 +239,7 @@ int build_lut(const qs_params& p, int Z, double B, int charged, float* d_out, in
         std::memcpy(g1, g2, sizeof(double) * NSF);
         std::memcpy(r1, r2, sizeof(double) * NSF);
     }
-    akima(g1, r1, sb, sc, sd, NSF);
+    akima_spline(g1, r1, sb, sc, sd, NSF);
     // the charged table's qy sum evaluates the neutral table with the charged
     // spline coefficients and the y step dky (stem3/stemlib.cpp:1668-1675)
     const double dqy = charged ? g.dky : g.dkx;
@@ -385,7 +385,7 @@ int build_lut2d(const qs_params& p, int Z, double B, float* d_out, int* nxO, int
     std::memcpy(g, QS_REZ_F[0], sizeof(double) * NSF);
     std::memcpy(r, QS_REZ_F[Z], sizeof(double) * NSF);
     truncate_tail(g, r, kmax);
-    akima(g, r, sb, sc, sd, NSF);
+    akima_spline(g, r, sb, sc, sd, NSF);
     double* d_tab = nullptr;
     float2* d_temp = nullptr;
     double2 *d_W = nullptr, *d_G = nullptr;

@@ -23,7 +23,7 @@ EXPORTS = ["qs_ctx_create", "qs_ctx_destroy", "qs_last_error", "qs_abi_version",
            "qs_params_finalize", "qs_thickness_count", "qs_lut_build", "qs_slices_build", "qs_probe",
            "qs_multislice_run", "qs_collect", "qs_stem_run", "qs_ctx_profile", "qs_ctx_stats",
            "qs_multislice_run_noalloc", "qs_phase_grating", "qs_adjoint_run", "qs_atoms_grad", "qs_tem_run",
-           "qs_cbed_batch_run", "qs_slab_build", "qs_tem_run_tilted"]
+           "qs_cbed_batch_run", "qs_slab_build", "qs_tem_run_tilted", "qs_slices_build_custom"]
 
 _lib = None
 
@@ -57,6 +57,8 @@ def load(path=LIB_PATH):
                                ctypes.POINTER(ctypes.c_int), ctypes.c_uint]
     L.qs_slices_build.argtypes = [vp, P, vp, ctypes.c_int, vp, ctypes.c_uint]
     L.qs_slab_build.argtypes = [vp, P, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_uint]
+    L.qs_slices_build_custom.argtypes = [vp, P, vp, ctypes.c_int, vp, ctypes.c_int, vp, vp, ctypes.c_int, vp,
+                                         ctypes.c_uint]
     L.qs_probe.argtypes = [vp, P, ctypes.c_double, ctypes.c_double, vp, ctypes.c_uint]
     L.qs_multislice_run.argtypes = [vp, P, vp, vp, ctypes.POINTER(abi.QsBatch), vp, vp, vp, ctypes.c_uint]
     L.qs_collect.argtypes = [vp, P, vp, vp, vp, ctypes.c_uint]
@@ -157,6 +159,22 @@ class Context:
         flags = _io_flags(out) | (abi.QS_OUT_POTENTIAL if potential_only else 0) | (abi.QS_SYNC if sync else 0)
         _check(self.lib.qs_slab_build(self.h, ctypes.byref(p), a.ctypes.data_as(ctypes.c_void_p), len(a),
                                       int(slab), _ptr(out), flags))
+        return out
+
+    def slices_custom(self, p, atoms, k, Zs, f, out=None, potential_only=False, sync=True):
+        """make3DSlicesFT + initSTEMSlices with the custom scattering-factor
+        table k[nk] (1/A), f[kind][nk] (A) of the elements Zs[kind]."""
+        a = abi.atoms_to_numpy(atoms)
+        k = np.ascontiguousarray(k, np.float64)
+        Z = np.ascontiguousarray(Zs, np.int32)
+        f = np.ascontiguousarray(f, np.float64)
+        if f.shape != (len(Z), len(k)):
+            raise ValueError("f must be [len(Zs)][len(k)]")
+        if out is None:
+            out = np.zeros((p.slices, p.potNx, p.potNy, 2), np.float32)
+        flags = _io_flags(out) | (abi.QS_OUT_POTENTIAL if potential_only else 0) | (abi.QS_SYNC if sync else 0)
+        _check(self.lib.qs_slices_build_custom(self.h, ctypes.byref(p), a.ctypes.data_as(ctypes.c_void_p), len(a),
+                                               _ptr(k), len(k), _ptr(Z), _ptr(f), len(Z), _ptr(out), flags))
         return out
 
     # ------------------------------------------------------------- probe

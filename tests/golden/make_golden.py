@@ -77,6 +77,11 @@ CASES = {
                      sliceThickness=1.9525, scan=(3.905, 7.81, 3, 3.905, 7.81, 3),
                      detectors=[(0.0, 20.0, "BF"), (40.0, 90.0, "HAADF")], alpha=20.0, periodicXY=True,
                      potential3D=False, mode="STEM", run=True),
+    # custom scattering factors ("Structure Factors: custom"): doCBED builds
+    # its slices with make3DSlicesFT (stem3/customslice.cpp:56-317)
+    "sto64ft": dict(cell="sto", ncell=(3, 3, 2), nx=64, resolutionX=0.18, v0=200.0, slices=4,
+                    sliceThickness=1.9525, scan=None, detectors=[], alpha=10.0, mode="CBED", run=True,
+                    saveLevel=1, custom_sf="sto"),
     # TEM: plane wave through a band-limited Si [110] slab (doTEM's exit wave)
     "si64tem": dict(cell="si", ncell=(4, 3, 4), nx=64, resolutionX=0.06, v0=300.0, slices=7, sliceThickness=2.0,
                     scan=None, detectors=[], alpha=0.0, bandlimit=True, mode="TEM", run=True),
@@ -94,6 +99,20 @@ def cell_of(name):
     if name == "si":
         return config.si110_cell()
     raise KeyError(name)
+
+
+def custom_table(name):
+    """A synthetic custom scattering-factor table (k in 1/A, f in A): f_Z(k)
+    = A_Z / (1 + (k / 0.6)^2)^2, A_Z = 0.28 Z^0.7, written with 6 significant
+    digits; returns (k, {Z: f}) as the reference parses them back."""
+    if name != "sto":
+        raise KeyError(name)
+    k = [float("%.6g" % (0.25 * i)) for i in range(25)]
+    table = {}
+    for Z in (38, 22, 8):
+        A = 0.28 * Z ** 0.7
+        table[Z] = [float("%.6g" % (A / (1.0 + (kk / 0.6) ** 2) ** 2)) for kk in k]
+    return k, table
 
 
 def params_for(case):
@@ -125,7 +144,8 @@ def run_case(name, case, workdir):
                      bandlimit=case.get("bandlimit", False), periodicXY=case.get("periodicXY", False),
                      folder="out", saveLevel=case.get("saveLevel", 2 if case["run"] else 0), czOffset=case.get("czOffset", 0.0),
                      centerSlices=case.get("centerSlices", False), cellDiv=case.get("cellDiv", 1),
-                     potential3D=case.get("potential3D", True))
+                     potential3D=case.get("potential3D", True),
+                     custom_sf=custom_table(case["custom_sf"]) if "custom_sf" in case else None)
     dump = os.path.join(workdir, "dump")
     oracle.run_reference(qsc, dump, run=case["run"])
     meta = dict(l.split(" = ", 1) for l in open(os.path.join(dump, "meta.txt")).read().strip().split("\n"))
@@ -179,6 +199,11 @@ def run_case(name, case, workdir):
         # diff.img it never wrote (stem3/stem3.cpp:2494-2517, 2545-2547)
         ww = imageio.read_img(os.path.join(folder, "wave.img"))
         out["exit_wave"] = np.stack([ww.data.real, ww.data.imag], -1).astype(np.float32)
+    if "custom_sf" in case:
+        kv, table = custom_table(case["custom_sf"])
+        out["sf_k"] = np.array(kv, np.float64)
+        out["sf_Z"] = np.array(list(table), np.int32)
+        out["sf_f"] = np.array([table[Z] for Z in table], np.float64)
     out["params_json"] = np.array(json.dumps(p.as_dict()))
     out["meta_json"] = np.array(json.dumps(meta))
     out["case_json"] = np.array(json.dumps({k: v for k, v in case.items()}))

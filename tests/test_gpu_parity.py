@@ -127,6 +127,28 @@ def test_2d_potential_from_atoms(ctx):
         ctx.slices(q, atoms, potential_only=True)
 
 
+def test_custom_scattering_factors(ctx):
+    """make3DSlicesFT (custom scattering factors; qs_slices_build_custom)
+    against the reference's own doCBED run of it: potential, transmission, and
+    the CBED pattern through the GPU's stack; an element without a table is
+    refused."""
+    g = Golden("sto64ft")
+    p = g.params
+    args = (g["atoms"], g["sf_k"], g["sf_Z"], g["sf_f"])
+    V = ctx.slices_custom(p, *args, potential_only=True)
+    assert rel_l2(V, g["V"]) <= TOL_BUILD
+    T = ctx.slices_custom(p, *args)
+    assert rel_l2(T, g["T"]) <= TOL_BUILD
+    dx = float(np.float32(p.scanXStart) - np.float32(p.potOffsetX))
+    dy = float(np.float32(p.scanYStart) - np.float32(p.potOffsetY))
+    pr = ctx.probe(p, dx, dy)
+    z = np.zeros(1, np.int32)
+    _, dps, _ = ctx.multislice(p, T, pr, positions=(z, z, z, z), want_det=False, want_diffpats=True)
+    assert rel_l2(dps[0], g["cbed_diffpat"]) <= TOL_MS
+    with pytest.raises(lib.QsError):
+        ctx.slices_custom(p, g["atoms"], g["sf_k"], g["sf_Z"][:2], g["sf_f"][:2])
+
+
 def test_end_to_end_from_atoms(ctx):
     """atoms -> slices -> probe -> scan entirely on the GPU vs the oracle chain."""
     g = Golden("sto64")

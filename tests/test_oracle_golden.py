@@ -5,7 +5,7 @@ machine's libm (cos/sin/exp of the host the tests run on)."""
 import numpy as np
 import pytest
 
-from conftest import rel_l2, scan_stack
+from conftest import Golden, rel_l2, scan_stack
 from oracle import oracle
 from qstem_gb300 import abi
 
@@ -162,3 +162,20 @@ def test_tem_exit_wave(golden):
     plane[..., 0] = 1.0
     w, _, _ = oracle.run_position(p, golden["T"], 0, 0, plane)
     assert rel_l2(w, golden["exit_wave"]) <= TOL
+
+
+def test_custom_scattering_factors():
+    """make3DSlicesFT with a custom table ("Structure Factors: custom"; the
+    fixture is doCBED's run of it): the restatement's potential and
+    transmission against the reference's (bit-exact here), and the CBED
+    pattern through the restated stack."""
+    g = Golden("sto64ft")
+    p = g.params
+    V = oracle.potential_ft(p, g["atoms"], g["sf_k"], g["sf_Z"], g["sf_f"])
+    assert np.abs(V - g["V"]).max() <= TOL * np.abs(g["V"]).max()
+    assert np.all(V[..., 1] == 0)
+    T = oracle.transmission(p, V)
+    assert np.abs(T - g["T"]).max() <= TOL
+    pr = oracle.probe(p, *cbed_probe_offset(p))
+    _, _, dp = oracle.run_position(p, T, 0, 0, pr)
+    assert rel_l2(dp, g["cbed_diffpat"]) <= TOL
