@@ -19,15 +19,22 @@ Thermal displacements (tds) follow the Einstein model or a phonon file
 numpy's generator or, on request, from the reference's own clock-seeded
 generator in the reference's order (qstem_gb300.thermal).
 
+"Structure Factors: custom" tables (Nk, k and one array per element) are
+read as readSFactLUT reads them; CBED runs build their slices from them
+(qs_slices_build_custom), STEM and TEM runs keep the parameterised
+potential, as doSTEM and doTEM do.
+
 Inputs that need parts of the reference outside this library, or that the
 reference cannot run, are refused with NotImplementedError: the 2-D
 potential (potential3D: no) on a non-periodic potential array (the
 reference reads its table outside the array there), more than one
 stacking-sequence line, a phonon file with a "Cube:" box (the reference
-exits there) and modes other than STEM, CBED and TEM.
+exits there), custom scattering factors on a divided cell or with fewer
+than four k values in CBED mode, and modes other than STEM, CBED and TEM.
 """
 import math
 import os
+import re
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -75,6 +82,22 @@ class ParamFile:
             self.pos = n
         return None
 
+    def array(self, title, n):
+        """readArray (stem3/stem3.cpp:531-549): n numbers that start after
+        `title` and run on over the following lines (comments cut, blank
+        lines skipped), each read as atof reads it; None when the title is
+        missing, ValueError when the file ends first."""
+        v = self.get(title)
+        if v is None:
+            return None
+        toks = v.split()
+        while len(toks) < n:
+            if self.pos >= len(self.lines):
+                raise ValueError("incomplete reading of the %s array (%d of %d values)" % (title, len(toks), n))
+            toks += self._line(self.pos).split()
+            self.pos += 1
+        return np.array([_atof(t) for t in toks[:n]], np.float64)
+
     def all(self, title):
         """Every line containing `title`, in file order (readparam with
         wrapFlag 0 from the start, as the detector loop reads them)."""
@@ -101,6 +124,15 @@ def _num(v, default):
         return float(t[0])
     except ValueError:
         return default
+
+
+_ATOF = re.compile(r"[+-]?(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?")
+
+
+def _atof(t):
+    """atof: the longest leading decimal number, 0 without one."""
+    m = _ATOF.match(t)
+    return float(m.group(0)) if m else 0.0
 
 
 def _yes(v, default=False):
@@ -269,6 +301,7 @@ class QscRun:
     cube: tuple = None                          # "Cube:" box size (None: NCELL mode)
     tilt_back: bool = True                      # "Tilt back:" (TEM: wave.img tilted back)
     spread: tuple = (0.0, 0.0, 0.0)             # dE/E, dI/I, dV/V as read (CBED/TEM use them as such)
+    custom_sf: tuple = None                     # (k[nk], Z[kinds], f[kinds][nk]): "Structure Factors: custom"
 
     def einstein_sigma(self):
         """Per-atom, per-axis rms displacement of the Einstein model with
@@ -553,6 +586,35 @@ def read_qsc(path, seed=20261203, rng="numpy", clock=0):
         names.append(t[2])
     pf.pos = 0
     atomRadius = _num(g("atom radius:"), 5.0)
+    # "Structure Factors: custom": the k table and one f table per element
+    # kind, in the order the unit cell names the kinds (readSFactLUT,
+    # stem3/stem3.cpp:555-600, 1402-1419).  doCBED builds its slices from
+    # them (make3DSlicesFT); doSTEM and doTEM read them and keep the
+    # parameterised potential.
+    custom_sf = None
+    if _word(g("Structure Factors:"))[:1].lower() == "c":
+        nk_v = g("Nk:")
+        if nk_v is None:
+            raise ValueError("%s: custom scattering factors without Nk" % path)
+        nk = int(_atof(nk_v.strip()))
+        kv = pf.array("k:", nk)
+        if kv is None:
+            raise ValueError("%s: custom scattering factors without the k: array" % path)
+        kinds = []
+        for t in cell.atoms:
+            if int(t[0]) > 0 and int(t[0]) not in kinds:
+                kinds.append(int(t[0]))
+        tables = []
+        for Z in kinds:
+            fz = pf.array(_SYMBOLS[Z] + ":", nk)
+            if fz is None:
+                raise ValueError("%s: custom scattering factors without the %s: array" % (path, _SYMBOLS[Z]))
+            tables.append(fz)
+        custom_sf = (kv, np.array(kinds, np.int32), np.array(tables, np.float64))
+        if mode == "CBED" and cellDiv > 1:
+            unsupported.append("custom scattering factors with a divided cell")
+        if mode == "CBED" and nk < 4:
+            unsupported.append("custom scattering factors with Nk < 4")
     # the stacking sequence (doSTEM/doTEM/doCBED's "sequence: m1 m2" loop,
     # stem3/stem3.cpp:2761-2790): m1 repeats each slab's stack inside
     # runMulsSTEM, m2 the slab loop (m2 < 1 reads as 1).  One line is
@@ -607,7 +669,7 @@ def read_qsc(path, seed=20261203, rng="numpy", clock=0):
                   scan_step=scan_step, save_level=save_level, spread=(dE_E, dI_I, dV_V),
                   beam_tilt=tuple(beam_tilt), tilt_back=tilt_back, tilt=tuple(tilt), offset=(xoff, yoff),
                   source_radius=source_radius, replicator=replicator,
-                  cube=tuple(cube) if cube is not None else None)
+                  cube=tuple(cube) if cube is not None else None, custom_sf=custom_sf)
 
 
 def _isnum(t):
@@ -954,8 +1016,14 @@ def _run_cbed(ctx, run, where, seed):
             from . import thermal
             off = thermal.source_offset(seed, j, run.source_radius)
         probe = probe_at(off)
-        atoms = _run_atoms(run, j, seed)
-        T, slabs = _stacks(ctx, p, atoms)
+        if run.custom_sf is not None:
+            # make3DSlicesFT builds from readFile's atoms every run (it draws
+            # no new configuration, stem3/customslice.cpp:115): one stack
+            if j == 0:
+                T, slabs = ctx.slices_custom(p, run.atoms, *run.custom_sf), False
+        else:
+            atoms = _run_atoms(run, j, seed)
+            T, slabs = _stacks(ctx, p, atoms)
         # the pattern each slot's file ends the run with and its thickness,
         # interimWave's files, the final wave
         slot_pat, slot_t = [None] * nT, [0.0] * nT

@@ -89,3 +89,33 @@ def has_gpu():
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+def custom_qsc(tmp_path, split=False):
+    """The sto64ft case (doCBED with "Structure Factors: custom") as a .qsc;
+    split: every table broken over several lines with comments and blank
+    lines between them, as readArray reads on."""
+    from tests.golden import make_golden
+    from qstem_gb300 import config
+    case = Golden("sto64ft").case
+    cell, _, _ = make_golden.params_for(case)
+    config.write_cfg(cell, str(tmp_path / "cell.cfg"))
+    path = str(tmp_path / "run.qsc")
+    config.write_qsc(path, cfg_file="cell.cfg", ncell=case["ncell"], nx=case["nx"],
+                     resolutionX=case["resolutionX"], v0=case["v0"], slices=case["slices"],
+                     sliceThickness=case["sliceThickness"], scan=case["scan"], detectors=case["detectors"],
+                     alpha=case["alpha"], mode="CBED", folder="out", saveLevel=case["saveLevel"],
+                     custom_sf=make_golden.custom_table("sto"))
+    if split:
+        lines = []
+        for line in open(path).read().split("\n"):
+            head, _, vals = line.partition(": ")
+            if head in ("k", "Sr", "Ti", "O"):
+                v = vals.split()
+                lines += [head + ": " + " ".join(v[:7]) + "   % first values",
+                          "", "  " + " ".join(v[7:20]), "% a comment line", " ".join(v[20:])]
+            else:
+                lines.append(line)
+        open(path, "w").write("\n".join(lines))
+    return path, str(tmp_path / "out")
+

@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY: it lets the CPU suite check the host-side logic
 of qstem_gb300.qsc.run_qsc (which files a run writes, their headers, the
 averaging over runs) without a GPU.  It implements the calls run_qsc makes
--- slices, probe, stem_run, multislice (with thickness series) -- through
+-- slices, slices_custom, probe, stem_run, multislice (with thickness series) -- through
 the oracle's C restatement of the reference (oracle/qs_oracle.c).  It
 records every multislice result in `log` so that tests can rebuild the
 averages they expect.
@@ -23,6 +23,9 @@ class OracleContext:
 
     def slices(self, p, atoms, slab=0):
         return oracle.transmission(p, oracle.potential(p, atoms, slab=slab))
+
+    def slices_custom(self, p, atoms, k, Zs, f):
+        return oracle.transmission(p, oracle.potential_ft(p, atoms, k, Zs, f))
 
     def probe(self, p, dx=None, dy=None):
         return oracle.probe(p, dx, dy)

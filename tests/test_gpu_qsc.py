@@ -105,3 +105,14 @@ def test_tilted_and_boxed_crystals_end_to_end(name):
     ref = z["det"]
     assert out["adf"].shape == ref[:, 0].shape
     assert rel_l2(out["adf"], ref[:, 0]) <= 1e-4
+
+
+def test_custom_scattering_factors_end_to_end(tmp_path):
+    """A doCBED input with "Structure Factors: custom" (the table spread
+    over lines with comments): the slices built from it on the GPU
+    (qs_slices_build_custom) and the final pattern against the reference's
+    own run."""
+    from conftest import Golden, custom_qsc
+    path, out = custom_qsc(tmp_path, split=True)
+    res = qsc.run_qsc(path, folder=out)
+    assert rel_l2(res["diffpat"], Golden("sto64ft")["cbed_diffpat"]) <= 1e-4

@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, rel_l2
+from conftest import GOLDEN, custom_qsc, rel_l2
 from oracle import oracle
 from oracle_ctx import OracleContext
 from qstem_gb300 import imageio, qsc
@@ -186,3 +186,37 @@ def test_step_helpers_reduce_to_the_plain_slot_rule():
     # second repeat of the second pass: index 5 + 2i against (5 + i) * 2
     s = [st for st in steps if st[4] == 5 + 3][1]
     assert (s[2], s[3]) == (5 + 3 * 2, (5 + 3) * 2)
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_custom_scattering_factors_read_and_run(tmp_path, split):
+    """A "Structure Factors: custom" table read as readSFactLUT reads it (k,
+    then one array per element kind in the cell's order, running on over
+    lines), and a CBED run built from it (make3DSlicesFT through the
+    stand-in): the final pattern against the reference's doCBED run."""
+    from conftest import Golden
+    g = Golden("sto64ft")
+    path, out = custom_qsc(tmp_path, split)
+    run = qsc.read_qsc(path)
+    k, Z, f = run.custom_sf
+    np.testing.assert_array_equal(k, g["sf_k"])
+    np.testing.assert_array_equal(Z, g["sf_Z"])
+    np.testing.assert_array_equal(f, g["sf_f"])
+    res = qsc.run_qsc(path, ctx=OracleContext(), folder=out)
+    assert rel_l2(res["diffpat"], g["cbed_diffpat"]) <= 1e-5
+
+
+def test_custom_scattering_factors_refused_or_missing(tmp_path):
+    path, _ = custom_qsc(tmp_path)
+    text = open(path).read()
+    # an element kind without its table: the reference exits
+    open(path, "w").write("\n".join(l for l in text.split("\n") if not l.startswith("Ti:")))
+    with pytest.raises(ValueError):
+        qsc.read_qsc(path)
+    # a divided cell in CBED mode
+    open(path, "w").write(text.replace("NCELLZ: 2", "NCELLZ: 2/2"))
+    with pytest.raises(NotImplementedError):
+        qsc.read_qsc(path)
+    # STEM and TEM read the table and keep the parameterised potential
+    open(path, "w").write(text.replace("mode: CBED", "mode: TEM"))
+    assert qsc.read_qsc(path).custom_sf is not None
