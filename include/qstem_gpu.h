@@ -427,6 +427,9 @@ int qs_ctx_stats(qs_ctx *ctx, qs_stats *out); /* synchronises the stream */
  *     a message giving the bytes needed.  Split the scan into such batches.
  *   - The first call on each device looks up the scratch address with
  *     cudaGetSymbolAddress; make that first call before any stream capture.
+ *     Later calls can be captured into a CUDA graph: they copy nothing from
+ *     host memory (tables and positions travel as kernel arguments), so a
+ *     replay reads the buffers' current contents.
  *   - All calls share the one scratch area, which keeps the previous call's
  *     contents (the call clears what must start at zero): calls whose GPU work
  *     overlaps race on it and must be serialised by the caller. */

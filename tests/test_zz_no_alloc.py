@@ -90,3 +90,48 @@ def test_noalloc_512_and_limit():
                                      ctypes.c_void_p(det.data_ptr()), None, None)
     assert rc == abi.QS_ERR_ARG
     assert b"bytes of scratch" in L.qs_last_error()
+
+
+def test_noalloc_captured_in_a_graph_and_replayed():
+    """After its first call, the entry point can be captured into a CUDA
+    graph: it copies nothing from host memory (the tables and positions
+    travel as kernel arguments), so each replay reads the slice stack's and
+    the probe's current contents and rewrites the outputs."""
+    import torch
+    g = Golden("sto64")
+    p = g.params
+    T = torch.from_numpy(np.ascontiguousarray(g["T"])).cuda()
+    probe = torch.from_numpy(np.ascontiguousarray(g["probe"])).cuda()
+    px, py, dx, dy = config.scan_offsets(p)
+    ref, _ = _run_both(p, T, probe, (px, py, dx, dy))  # includes the first, uncaptured calls
+    L = lib.load()
+    arrs = [np.ascontiguousarray(a, dtype=np.int32) for a in (px, py, dx, dy)]
+    b = abi.QsBatch(len(px), *[a.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) for a in arrs])
+    det = torch.zeros(ref[0].shape, device="cuda")
+    dp = torch.zeros(ref[1].shape, device="cuda")
+    ew = torch.zeros(ref[2].shape, device="cuda")
+    graph = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.graph(graph, stream=s):
+        rc = L.qs_multislice_run_noalloc(ctypes.c_void_p(s.cuda_stream), ctypes.byref(p),
+                                         ctypes.c_void_p(T.data_ptr()), ctypes.c_void_p(probe.data_ptr()),
+                                         ctypes.byref(b), ctypes.c_void_p(det.data_ptr()),
+                                         ctypes.c_void_p(dp.data_ptr()), ctypes.c_void_p(ew.data_ptr()))
+    assert rc == 0, L.qs_last_error().decode()
+    del arrs  # the replay needs none of the host arrays
+    for _ in range(2):
+        det.fill_(7.0)
+        dp.fill_(7.0)
+        graph.replay()
+        torch.cuda.synchronize()
+        assert rel_l2(det.cpu().numpy(), ref[0]) <= TOL
+        assert rel_l2(dp.cpu().numpy(), ref[1]) <= TOL
+        assert rel_l2(ew.cpu().numpy(), ref[2]) <= TOL
+    # the replay reads the stack's current contents: a vacuum stack (T = 1)
+    # leaves the probe's own intensity in the bright field
+    T[..., 0] = 1.0
+    T[..., 1] = 0.0
+    graph.replay()
+    torch.cuda.synchronize()
+    assert rel_l2(det.cpu().numpy(), ref[0]) > 1e-3
