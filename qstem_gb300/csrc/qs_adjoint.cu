@@ -51,7 +51,7 @@ constexpr int adj_min_blocks(int n) {
 // and propagator of the last slice, loss terms, g_B' = 2 (I - T) c B',
 // g_A = IFFT_x(conj(P) g_B').
 template <int N>
-__global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
+__global__ void __launch_bounds__(col_tile<N>() * col_line_threads(N))
     adj_last_cols(AdjLastArgs a) {
     using Cfg = typename LineCol<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();

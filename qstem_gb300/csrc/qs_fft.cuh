@@ -228,7 +228,12 @@ struct radices {
 
 // threads per line for a supported length (usable in __launch_bounds__)
 constexpr int line_threads(int n) {
-    return n <= 128 ? 8 : (n <= 512 ? 16 : 32);
+    return n == 384 ? QS_LINE_T_384 : n == 768 ? QS_LINE_T_768 : (n <= 128 ? 8 : (n <= 512 ? 16 : 32));
+}
+// threads per column line (the column transforms may hold more elements a
+// thread than the row transforms of the same length)
+constexpr int col_line_threads(int n) {
+    return n == 384 ? QS_COL_LINE_T_384 : n == 768 ? QS_COL_LINE_T_768 : line_threads(n);
 }
 
 // Line configuration: N points, T threads per line.
@@ -382,30 +387,32 @@ struct pick<0, A, Rest...> { using type = A; };
 template <int I, class A, class... Rest>
 struct pick<I, A, Rest...> { using type = typename pick<I - 1, Rest...>::type; };
 template <int I>
-using Rad384 = typename pick<I, rad_t<8, 6, 8>, rad_t<6, 8, 8>, rad_t<8, 8, 6>, rad_t<12, 4, 8>, rad_t<24, 4, 4>>::type;
+using Rad384 = typename pick<I, rad_t<8, 6, 8>, rad_t<6, 8, 8>, rad_t<8, 8, 6>, rad_t<12, 4, 8>, rad_t<24, 4, 4>,
+                             rad_t<8, 48>, rad_t<48, 8>>::type;
 template <int I>
 using Rad512 = typename pick<I, rad_t<32, 16>, rad_t<16, 32>>::type;
 template <int I>
-using Rad768 = typename pick<I, rad_t<8, 12, 8>, rad_t<12, 8, 8>, rad_t<8, 8, 12>, rad_t<24, 4, 8>, rad_t<24, 8, 4>>::type;
+using Rad768 = typename pick<I, rad_t<8, 12, 8>, rad_t<12, 8, 8>, rad_t<8, 8, 12>, rad_t<24, 4, 8>, rad_t<24, 8, 4>,
+                             rad_t<16, 48>, rad_t<48, 16>>::type;
 template <int I>
 using Rad1024 = typename pick<I, rad_t<32, 32>, rad_t<8, 16, 8>>::type;
 
-// (the product kernels size __launch_bounds__ with line_threads(N))
+// (the product kernels size __launch_bounds__ with line_threads(N) and col_line_threads(N))
 template <int N>
 struct Line;
 template <> struct Line<64> { using cfg = LineCfg<64, 8, radices<8, 8>>; };
 template <> struct Line<128> { using cfg = LineCfg<128, 8, radices<16, 8>>; };
 template <> struct Line<256> { using cfg = LineCfg<256, 16, radices<16, 16>>; };
-template <> struct Line<384> { using cfg = LineCfg<384, 16, Rad384<QS_RADIX_ROW_384>>; };
+template <> struct Line<384> { using cfg = LineCfg<384, QS_LINE_T_384, Rad384<QS_RADIX_ROW_384>>; };
 template <> struct Line<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_ROW_512>>; };
-template <> struct Line<768> { using cfg = LineCfg<768, 32, Rad768<QS_RADIX_ROW_768>>; };
+template <> struct Line<768> { using cfg = LineCfg<768, QS_LINE_T_768, Rad768<QS_RADIX_ROW_768>>; };
 template <> struct Line<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_ROW_1024>>; };
 // column transforms
 template <int N>
 struct LineCol { using cfg = typename Line<N>::cfg; };
-template <> struct LineCol<384> { using cfg = LineCfg<384, 16, Rad384<QS_RADIX_COL_384>>; };
+template <> struct LineCol<384> { using cfg = LineCfg<384, QS_COL_LINE_T_384, Rad384<QS_RADIX_COL_384>>; };
 template <> struct LineCol<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_COL_512>>; };
-template <> struct LineCol<768> { using cfg = LineCfg<768, 32, Rad768<QS_RADIX_COL_768>>; };
+template <> struct LineCol<768> { using cfg = LineCfg<768, QS_COL_LINE_T_768, Rad768<QS_RADIX_COL_768>>; };
 template <> struct LineCol<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_COL_1024>>; };
 
 // columns per column-pass tile (qs_tuned.h: 16 = 128-byte row segments)
@@ -423,12 +430,12 @@ constexpr int col_tile() {
 
 template <int N>
 constexpr bool line_threads_match() {
-    return Line<N>::cfg::T == line_threads(N);
+    return Line<N>::cfg::T == line_threads(N) && LineCol<N>::cfg::T == col_line_threads(N);
 }
 static_assert(line_threads_match<64>() && line_threads_match<128>() && line_threads_match<256>() &&
                   line_threads_match<384>() && line_threads_match<512>() && line_threads_match<768>() &&
                   line_threads_match<1024>(),
-              "line_threads() must match the Line<N> configurations");
+              "line_threads() and col_line_threads() must match the Line<N> / LineCol<N> configurations");
 
 inline bool line_supported(int n) {
     return n == 64 || n == 128 || n == 256 || n == 384 || n == 512 || n == 768 || n == 1024;

@@ -65,7 +65,7 @@ constexpr int col_stages(int n) {
 // PW: per-wave work items and propagator/k^2 tables (waves of different
 // samplings; no detectors), compiled only into that variant
 template <int N, bool DET, bool INVERSE, bool PW>
-__global__ void __launch_bounds__(col_tile<N>() * line_threads(N), col_min_blocks(N))
+__global__ void __launch_bounds__(col_tile<N>() * col_line_threads(N), col_min_blocks(N))
     ms_cols(ColArgs a, long nitems) {
     using Cfg = typename LineCol<N>::cfg;
     constexpr int T = Cfg::T, E = Cfg::E, C = col_tile<N>();
@@ -352,7 +352,7 @@ int launch_det_finalize(const double* partial, int nwaves, int ntiles, int ndet,
 
 // ------------------------------------------------ generic 2-D transforms
 template <int N, bool INV>
-__global__ void __launch_bounds__(col_tile<N>() * line_threads(N))
+__global__ void __launch_bounds__(col_tile<N>() * col_line_threads(N))
     fft_cols(float2* data, int ncols, const float2* tw) {
     // columns of length N, row stride ncols; blockIdx.y = array index
     using Cfg = typename LineCol<N>::cfg;

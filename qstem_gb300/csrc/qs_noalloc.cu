@@ -147,10 +147,15 @@ extern "C" int qs_multislice_run_noalloc(void* stream_handle, const qs_params* p
     QS_TRY(check_raster(P, *batch, wantDet));
     cudaStream_t s = (cudaStream_t)stream_handle;
     {
-        // the scratch address handed to the kernels is the current device's
+        // the scratch address handed to the kernels is the current device's;
+        // the stream's device cannot be queried while the stream captures
+        // (the capture's launches then fail if the two differ)
         int cur = 0, sdev = 0;
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
         QS_CUDA_TRY(cudaGetDevice(&cur));
-        QS_CUDA_TRY(cudaStreamGetDevice(s, &sdev));
+        QS_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+        if (cap == cudaStreamCaptureStatusNone) QS_CUDA_TRY(cudaStreamGetDevice(s, &sdev));
+        else sdev = cur;
         if (sdev != cur) {
             set_error(std::string(fn) + "the stream belongs to device " + std::to_string(sdev) +
                       ", the current device is " + std::to_string(cur));

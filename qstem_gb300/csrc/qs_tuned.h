@@ -18,7 +18,11 @@
 // The column pass's tiles, stages and budgets at 256, 384, 512 and 768 were
 // measured again after its tile copies became 16-byte copies of column pairs
 // (profiles/slice_loop_autotune.md): 256 8 columns x 2 stages at 4 CTAs per
-// SM, 384 16 x 2 at 2, 512 16 x 1 at 2, 768 8 x 2 at 2.
+// SM, 384 16 x 2 at 2, 512 16 x 1 at 2, 768 8 x 2 at 2.  The 768-point
+// lines then moved to two passes (16 threads x 48 elements, radices 48 x 16;
+// rows 8 lines a CTA at 2 CTAs per SM) and the 384-point column lines to 8
+// threads x 48 elements (48 x 8): 768 rows 2.49 -> 2.37 us and columns
+// 1.90 -> 1.81 us per position-slice, 384 columns 0.414 -> 0.386.
 #pragma once
 
 #ifndef QS_ROW_MIN_BLOCKS_64
@@ -37,7 +41,7 @@
 #define QS_ROW_MIN_BLOCKS_512 3
 #endif
 #ifndef QS_ROW_MIN_BLOCKS_768
-#define QS_ROW_MIN_BLOCKS_768 4
+#define QS_ROW_MIN_BLOCKS_768 2
 #endif
 #ifndef QS_ROW_MIN_BLOCKS_1024
 #define QS_ROW_MIN_BLOCKS_1024 4
@@ -100,7 +104,7 @@
 #define QS_ROW_LINES_512 8
 #endif
 #ifndef QS_ROW_LINES_768
-#define QS_ROW_LINES_768 4
+#define QS_ROW_LINES_768 8
 #endif
 #ifndef QS_ROW_LINES_1024
 #define QS_ROW_LINES_1024 4
@@ -155,6 +159,24 @@
 #define QS_COL_STAGES_1024 1
 #endif
 
+// QS_LINE_T_384, QS_LINE_T_768: threads per row line of the 384- and
+// 768-point transforms: 16 and 32 hold 24 elements a
+// thread (three radix passes), 8 and 16 hold 48 (the two-pass
+// factorisations 8x48 / 48x8 and 16x48 / 48x16, lists entries 5 and 6).
+#ifndef QS_LINE_T_384
+#define QS_LINE_T_384 16
+#endif
+#ifndef QS_LINE_T_768
+#define QS_LINE_T_768 16
+#endif
+// QS_COL_LINE_T_<N>: the same for the column lines (default: the rows')
+#ifndef QS_COL_LINE_T_384
+#define QS_COL_LINE_T_384 8
+#endif
+#ifndef QS_COL_LINE_T_768
+#define QS_COL_LINE_T_768 QS_LINE_T_768
+#endif
+
 // QS_RADIX_ROW_<N>, QS_RADIX_COL_<N>: which factorisation of the row and of
 // the column line transform (the lists of Line / LineCol in qs_fft.cuh;
 // 0 = the first).  Every translation unit must be compiled with the same
@@ -166,19 +188,19 @@
 #define QS_RADIX_ROW_512 0
 #endif
 #ifndef QS_RADIX_ROW_768
-#define QS_RADIX_ROW_768 3
+#define QS_RADIX_ROW_768 6
 #endif
 #ifndef QS_RADIX_ROW_1024
 #define QS_RADIX_ROW_1024 0
 #endif
 #ifndef QS_RADIX_COL_384
-#define QS_RADIX_COL_384 0
+#define QS_RADIX_COL_384 6
 #endif
 #ifndef QS_RADIX_COL_512
 #define QS_RADIX_COL_512 0
 #endif
 #ifndef QS_RADIX_COL_768
-#define QS_RADIX_COL_768 0
+#define QS_RADIX_COL_768 6
 #endif
 #ifndef QS_RADIX_COL_1024
 #define QS_RADIX_COL_1024 0

@@ -6,7 +6,8 @@ and the register budgets (CTAs per SM).
 
 Phase 0, factorisations and tiles: variant k compiles every line length
 with its k-th factorisation (QS_RADIX_ROW_<N> = QS_RADIX_COL_<N> = k, where
-that length has a k-th one; qs_fft.cuh lists them), plus one variant with
+that length has a k-th one that fits the thread layout of its row or column
+lines; qs_fft.cuh lists them), plus one variant with
 16-column tiles wherever the double-buffered tile fits (QS_COL_TILE_<N>);
 the row transform keeps the factorisation with the fastest row pass, the
 column transform the one with the fastest column pass, independently.
@@ -40,7 +41,27 @@ from . import build as _build
 SIZES = (256, 384, 512, 768, 1024)
 WAVES = {64: 2048, 128: 2048, 256: 1024, 384: 512, 512: 512, 768: 192, 1024: 128}
 # factorisations per line length (the lists of qs_fft.cuh's Line / LineCol)
-RADIX_ALTS = {384: 5, 512: 2, 768: 5, 1024: 2}
+RADIX_LISTS = {384: [(8, 6, 8), (6, 8, 8), (8, 8, 6), (12, 4, 8), (24, 4, 4), (8, 48), (48, 8)],
+               512: [(32, 16), (16, 32)],
+               768: [(8, 12, 8), (12, 8, 8), (8, 8, 12), (24, 4, 8), (24, 8, 4), (16, 48), (48, 16)],
+               1024: [(32, 32), (8, 16, 8)]}
+RADIX_ALTS = {n: len(v) for n, v in RADIX_LISTS.items()}
+# threads per row / column line of the lengths whose layout qs_tuned.h sets
+# (QS_LINE_T_<N>, QS_COL_LINE_T_<N>); the others: qs_fft.cuh's line_threads
+ROW_T = {384: 16, 768: 16}
+COL_T = {384: 8, 768: 16}
+
+
+def _line_threads(n, col=False):
+    t = (COL_T if col else ROW_T).get(n)
+    return t if t else (8 if n <= 128 else 16 if n <= 512 else 32)
+
+
+def radix_ok(n, k, col=False):
+    """Factorisation k of length n fits its thread layout (every radix
+    divides the elements a thread holds)."""
+    e = n // _line_threads(n, col)
+    return k < RADIX_ALTS.get(n, 1) and all(e % r == 0 for r in RADIX_LISTS[n][k])
 # lengths whose double-buffered 16-column tile fits in shared memory
 TILE16 = (64, 128, 256, 384, 512, 768)
 
@@ -166,8 +187,9 @@ def write_table(best):
 def tune_factorisations(sizes, tmp):
     """Phase 0: {("RROW"|"RCOL"|"TILE"|"STAGES", N): choice} and the defines fixing them."""
     nalt = max([RADIX_ALTS.get(n, 1) for n in sizes])
-    variants = {"r%d" % k: ["QS_RADIX_ROW_%d=%d" % (n, k) for n in sizes if k < RADIX_ALTS.get(n, 1)] +
-                ["QS_RADIX_COL_%d=%d" % (n, k) for n in sizes if k < RADIX_ALTS.get(n, 1)] for k in range(nalt)}
+    variants = {"r%d" % k: ["QS_RADIX_ROW_%d=%d" % (n, k) for n in sizes if n in RADIX_LISTS and radix_ok(n, k)] +
+                ["QS_RADIX_COL_%d=%d" % (n, k) for n in sizes if n in RADIX_LISTS and radix_ok(n, k, True)]
+                for k in range(nalt)}
     # column tiles: (columns, stages); a double-buffered 16-column tile only
     # where it fits
     tiles = {"t8s2": (8, 2), "t16s2": (16, 2), "t8s1": (8, 1), "t16s1": (16, 1)}
@@ -182,10 +204,11 @@ def tune_factorisations(sizes, tmp):
     print("N     " + "".join("%16s" % v for v in variants))
     for n in sizes:
         print("%-6d" % n + "".join("%8.3f%8.3f" % tuple(res[v][n]) for v in variants))
-        ks = range(RADIX_ALTS.get(n, 1))
         if n in RADIX_ALTS:
-            best[("RROW", n)] = min(ks, key=lambda k: res["r%d" % k][n][0])
-            best[("RCOL", n)] = min(ks, key=lambda k: res["r%d" % k][n][1])
+            best[("RROW", n)] = min([k for k in range(RADIX_ALTS[n]) if radix_ok(n, k)],
+                                    key=lambda k: res["r%d" % k][n][0])
+            best[("RCOL", n)] = min([k for k in range(RADIX_ALTS[n]) if radix_ok(n, k, True)],
+                                    key=lambda k: res["r%d" % k][n][1])
         cand = [v for v in tiles if v != "t16s2" or n in TILE16]
         tv = min(cand, key=lambda v: res[v][n][1])
         best[("TILE", n)], best[("STAGES", n)] = tiles[tv]
