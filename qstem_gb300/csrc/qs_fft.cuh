@@ -33,6 +33,32 @@ namespace qs {
 // ---------------------------------------------------------------- complex
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// the same with one packed two-lane instruction (add/sub.rn.f32x2, sm_100
+// family; each lane rounds as the scalar operation does)
+__device__ __forceinline__ float2 cadd_x2(float2 a, float2 b) {
+    float2 r;
+    asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+        " add.rn.f32x2 rd, ra, rb;\n mov.b64 {%0, %1}, rd;\n}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 csub_x2(float2 a, float2 b) {
+    float2 r;
+    asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+        " sub.rn.f32x2 rd, ra, rb;\n mov.b64 {%0, %1}, rd;\n}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+template <bool PK>
+__device__ __forceinline__ float2 cadd_p(float2 a, float2 b) {
+    if constexpr (PK) return cadd_x2(a, b);
+    else return cadd(a, b);
+}
+template <bool PK>
+__device__ __forceinline__ float2 csub_p(float2 a, float2 b) {
+    if constexpr (PK) return csub_x2(a, b);
+    else return csub(a, b);
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -159,38 +185,39 @@ struct first_radix {
     static constexpr int value = (N % 4 == 0 && N != 8) ? 4 : (N % 2 == 0 ? 2 : (N % 3 == 0 ? 3 : N));
 };
 
-template <int N, bool INV, int STRIDE, int OFF, int L>
+// PK: additions as packed two-lane instructions
+template <int N, bool INV, int STRIDE, int OFF, bool PK = false, int L>
 __device__ __forceinline__ void dft_reg(float2 (&x)[L]) {
     if constexpr (N == 1) {
         return;
     } else if constexpr (N == 2) {
         float2 a = x[OFF], b = x[OFF + STRIDE];
-        x[OFF] = cadd(a, b);
-        x[OFF + STRIDE] = csub(a, b);
+        x[OFF] = cadd_p<PK>(a, b);
+        x[OFF + STRIDE] = csub_p<PK>(a, b);
     } else if constexpr (N == 3) {
         constexpr float h = 0.86602540378443864676f;
         float2 a = x[OFF], b = x[OFF + STRIDE], c = x[OFF + 2 * STRIDE];
-        float2 t1 = cadd(b, c), t2 = csub(b, c);
+        float2 t1 = cadd_p<PK>(b, c), t2 = csub_p<PK>(b, c);
         float2 m = make_float2(a.x - 0.5f * t1.x, a.y - 0.5f * t1.y);
         // n = (s*h) * i * t2, s = -1 forward
         float2 n = INV ? make_float2(-h * t2.y, h * t2.x) : make_float2(h * t2.y, -h * t2.x);
-        x[OFF] = cadd(a, t1);
-        x[OFF + STRIDE] = cadd(m, n);
-        x[OFF + 2 * STRIDE] = csub(m, n);
+        x[OFF] = cadd_p<PK>(a, t1);
+        x[OFF + STRIDE] = cadd_p<PK>(m, n);
+        x[OFF + 2 * STRIDE] = csub_p<PK>(m, n);
     } else if constexpr (N == 4) {
         float2 a = x[OFF], b = x[OFF + STRIDE], c = x[OFF + 2 * STRIDE], d = x[OFF + 3 * STRIDE];
-        float2 t0 = cadd(a, c), t1 = csub(a, c), t2 = cadd(b, d), dd = csub(b, d);
+        float2 t0 = cadd_p<PK>(a, c), t1 = csub_p<PK>(a, c), t2 = cadd_p<PK>(b, d), dd = csub_p<PK>(b, d);
         float2 t3 = INV ? make_float2(-dd.y, dd.x) : make_float2(dd.y, -dd.x);
-        x[OFF] = cadd(t0, t2);
-        x[OFF + STRIDE] = cadd(t1, t3);
-        x[OFF + 2 * STRIDE] = csub(t0, t2);
-        x[OFF + 3 * STRIDE] = csub(t1, t3);
+        x[OFF] = cadd_p<PK>(t0, t2);
+        x[OFF + STRIDE] = cadd_p<PK>(t1, t3);
+        x[OFF + 2 * STRIDE] = csub_p<PK>(t0, t2);
+        x[OFF + 3 * STRIDE] = csub_p<PK>(t1, t3);
     } else {
         constexpr int R = first_radix<N>::value;
         constexpr int M = N / R;
         static_assert(R * M == N, "unsupported radix");
         // sub-DFTs of the decimated sequences x[OFF + STRIDE*(r + R*m)]
-        sfor<0, R>([&](auto r) { dft_reg<M, INV, STRIDE * R, OFF + STRIDE * decltype(r)::value>(x); });
+        sfor<0, R>([&](auto r) { dft_reg<M, INV, STRIDE * R, OFF + STRIDE * decltype(r)::value, PK>(x); });
         // combine: y[m + M*k] = sum_r W_N^{r m} X_r[m] W_R^{r k}
         float2 y[N];
         sfor<0, M>([&](auto mi) {
@@ -200,7 +227,7 @@ __device__ __forceinline__ void dft_reg(float2 (&x)[L]) {
                 constexpr int r = decltype(ri)::value;
                 v[r] = ctw<r * m, N, INV>(x[OFF + STRIDE * (r + R * m)]);
             });
-            dft_reg<R, INV, 1, 0>(v);
+            dft_reg<R, INV, 1, 0, PK>(v);
             sfor<0, R>([&](auto ki) {
                 constexpr int k = decltype(ki)::value;
                 y[m + M * k] = v[k];
@@ -245,10 +272,11 @@ constexpr int col_line_threads(int n) {
 // earlier radices) multiplies input r of butterfly j by
 // exp(-+2 pi i r (j mod Ns)/(Ns R)); the table stores them per pass as
 // [r-1][j mod Ns] so that consecutive lanes read consecutive words.
-template <int N_, int T_, class RAD>
+template <int N_, int T_, class RAD, bool PK_ = false>
 struct LineCfg {
     static constexpr int N = N_;
     static constexpr int T = T_;
+    static constexpr bool PK = PK_;  // butterflies' additions packed (cadd_x2)
     static constexpr int E = N / T;
     static constexpr int PASSES = RAD::count;
     static constexpr int R0 = RAD::at(0);
@@ -342,7 +370,7 @@ __device__ __forceinline__ void line_fft_sync(float2 (&reg)[Cfg::E], const SM& s
                     v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
                 }
             }
-            dft_reg<R, INV, 1, 0>(v);
+            dft_reg<R, INV, 1, 0, Cfg::PK>(v);
             if constexpr (last) {
 #pragma unroll
                 for (int r = 0; r < R; ++r) reg[q + r * Q] = v[r];
@@ -403,17 +431,17 @@ struct Line;
 template <> struct Line<64> { using cfg = LineCfg<64, 8, radices<8, 8>>; };
 template <> struct Line<128> { using cfg = LineCfg<128, 8, radices<16, 8>>; };
 template <> struct Line<256> { using cfg = LineCfg<256, 16, radices<16, 16>>; };
-template <> struct Line<384> { using cfg = LineCfg<384, QS_LINE_T_384, Rad384<QS_RADIX_ROW_384>>; };
-template <> struct Line<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_ROW_512>>; };
-template <> struct Line<768> { using cfg = LineCfg<768, QS_LINE_T_768, Rad768<QS_RADIX_ROW_768>>; };
-template <> struct Line<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_ROW_1024>>; };
+template <> struct Line<384> { using cfg = LineCfg<384, QS_LINE_T_384, Rad384<QS_RADIX_ROW_384>, QS_PACKED_ROWS>; };
+template <> struct Line<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_ROW_512>, QS_PACKED_ROWS>; };
+template <> struct Line<768> { using cfg = LineCfg<768, QS_LINE_T_768, Rad768<QS_RADIX_ROW_768>, QS_PACKED_ROWS>; };
+template <> struct Line<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_ROW_1024>, QS_PACKED_ROWS>; };
 // column transforms
 template <int N>
 struct LineCol { using cfg = typename Line<N>::cfg; };
-template <> struct LineCol<384> { using cfg = LineCfg<384, QS_COL_LINE_T_384, Rad384<QS_RADIX_COL_384>>; };
-template <> struct LineCol<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_COL_512>>; };
-template <> struct LineCol<768> { using cfg = LineCfg<768, QS_COL_LINE_T_768, Rad768<QS_RADIX_COL_768>>; };
-template <> struct LineCol<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_COL_1024>>; };
+template <> struct LineCol<384> { using cfg = LineCfg<384, QS_COL_LINE_T_384, Rad384<QS_RADIX_COL_384>, QS_PACKED_COLS>; };
+template <> struct LineCol<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_COL_512>, QS_PACKED_COLS>; };
+template <> struct LineCol<768> { using cfg = LineCfg<768, QS_COL_LINE_T_768, Rad768<QS_RADIX_COL_768>, QS_PACKED_COLS>; };
+template <> struct LineCol<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_COL_1024>, QS_PACKED_COLS>; };
 
 // columns per column-pass tile (qs_tuned.h: 16 = 128-byte row segments)
 template <int N>

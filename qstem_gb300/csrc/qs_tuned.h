@@ -206,3 +206,14 @@
 #define QS_RADIX_COL_1024 0
 #endif
 
+// QS_PACKED_ROWS, QS_PACKED_COLS: the butterflies' complex additions of the
+// 384- to 1024-point row / column transforms as packed two-lane float
+// instructions (add/sub.rn.f32x2; results bit-identical).  Measured: rows
+// 14.5 % faster at 512 points, 12 % at 1024, 5 % at 768 and 4 % at 384;
+// columns 2-4 % slower.
+#ifndef QS_PACKED_ROWS
+#define QS_PACKED_ROWS 1
+#endif
+#ifndef QS_PACKED_COLS
+#define QS_PACKED_COLS 0
+#endif
