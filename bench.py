@@ -504,7 +504,11 @@ def run_ours(args, rank, world):
     traffic = None
     tf = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tf):
-        traffic = json.load(open(tf)).get(kern)
+        # ncu DRAM bytes of one launch over `waves` waves, scaled to this
+        # launch's waves (traffic grows with the number of waves)
+        tj = json.load(open(tf))
+        if tj.get(kern):
+            traffic = tj[kern] * (p.scanXN * p.scanYN) / float(tj.get("waves", 4096))
 
     # CPU baseline on this host (bounded sample) and the plain GPU path
     cpu = None
