@@ -22,7 +22,9 @@
 // lines then moved to two passes (16 threads x 48 elements, radices 48 x 16;
 // rows 8 lines a CTA at 2 CTAs per SM) and the 384-point column lines to 8
 // threads x 48 elements (48 x 8): 768 rows 2.49 -> 2.37 us and columns
-// 1.90 -> 1.81 us per position-slice, 384 columns 0.414 -> 0.386.
+// 1.90 -> 1.81 us per position-slice, 384 columns 0.414 -> 0.386.  With the
+// packed row additions the 768 row pass runs best at 3 CTAs per SM (2.25 ->
+// 1.92 us); budgets 4 and 5 at 384/512/1024 and 3 at 1024 measured slower.
 #pragma once
 
 #ifndef QS_ROW_MIN_BLOCKS_64
@@ -41,7 +43,7 @@
 #define QS_ROW_MIN_BLOCKS_512 3
 #endif
 #ifndef QS_ROW_MIN_BLOCKS_768
-#define QS_ROW_MIN_BLOCKS_768 2
+#define QS_ROW_MIN_BLOCKS_768 3
 #endif
 #ifndef QS_ROW_MIN_BLOCKS_1024
 #define QS_ROW_MIN_BLOCKS_1024 4
