@@ -14,6 +14,7 @@
 
 #include "qs_fft.cuh"
 #include "qs_internal.h"
+#include "qs_zorder.h"
 
 constexpr int kMaxBufs = 32;
 
@@ -230,9 +231,8 @@ static int thickness_count(const qs_params& p) { return (p.slices * p.cellDiv) /
 // reference's per-element LUT cache keeps it (:1417).
 static void plan_atoms(const qs_params& P, const qs_atom* atoms, int natom, std::vector<AtomJob>& jobs,
                        std::vector<std::pair<int, double>>& lutKeys, int slab = 0) {
-    std::vector<int> order(natom);
-    for (int i = 0; i < natom; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return atoms[a].z < atoms[b].z; });
+    std::vector<int> order;
+    z_order(natom, [&](int i) { return atoms[i].z; }, order);
     std::vector<qs_atom> at(natom);
     for (int i = 0; i < natom; i++) at[i] = atoms[order[i]];
     const float cz = P.sliceThickness * (float)P.slices;
@@ -315,9 +315,8 @@ static void plan_atoms(const qs_params& P, const qs_atom* atoms, int natom, std:
 // every element's table, B that of its first atom in z order.
 static void plan_atoms_2d(const qs_params& P, const qs_atom* atoms, int natom, std::vector<Atom2DJob>& jobs,
                           std::vector<std::pair<int, double>>& keys, int slab = 0) {
-    std::vector<int> order(natom);
-    for (int i = 0; i < natom; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return atoms[a].z < atoms[b].z; });
+    std::vector<int> order;
+    z_order(natom, [&](int i) { return atoms[i].z; }, order);
     const float cz = P.sliceThickness * (float)P.slices;
     const float dx = P.resolutionX, dy = P.resolutionY, dzs = P.sliceThickness;
     const int iRadX = (int)ceilf(P.atomRadius / dx), iRadY = (int)ceilf(P.atomRadius / dy);

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "qs_internal.h"
+#include "qs_zorder.h"
 
 namespace qs {
 
@@ -296,8 +297,10 @@ int build_custom_potential(const qs_params& P, const qs_atom* atoms_in, int nato
     // ties in input order, as a stable sort does), each with its element's
     // table index; per slice the run of atoms whose z can reach it (the
     // per-atom test z <= rc + dZp still decides)
-    std::vector<qs_atom> at(atoms_in, atoms_in + natom);
-    std::stable_sort(at.begin(), at.end(), [](const qs_atom& a, const qs_atom& b) { return a.z < b.z; });
+    std::vector<int> zo;
+    z_order(natom, [&](int i) { return atoms_in[i].z; }, zo);
+    std::vector<qs_atom> at(natom);
+    for (int i = 0; i < natom; i++) at[i] = atoms_in[zo[i]];
     std::vector<FtAtom> fa(std::max(natom, 1));
     for (int j = 0; j < natom; j++) {
         int kind = 0;
