@@ -14,6 +14,11 @@
 #include <cstring>
 #include <vector>
 
+// below this many atoms the comparison sort is as fast
+#ifndef QS_ZORDER_RADIX_MIN
+#define QS_ZORDER_RADIX_MIN 2048
+#endif
+
 namespace qs {
 
 inline uint32_t z_key(float z) {
@@ -28,7 +33,7 @@ template <class ZOf>
 void z_order(int n, ZOf zof, std::vector<int>& order) {
     order.resize(n > 0 ? n : 0);
     for (int i = 0; i < n; i++) order[i] = i;
-    if (n < 2048) {
+    if (n < QS_ZORDER_RADIX_MIN) {
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return zof(a) < zof(b); });
         return;
     }
