@@ -272,11 +272,12 @@ constexpr int col_line_threads(int n) {
 // earlier radices) multiplies input r of butterfly j by
 // exp(-+2 pi i r (j mod Ns)/(Ns R)); the table stores them per pass as
 // [r-1][j mod Ns] so that consecutive lanes read consecutive words.
-template <int N_, int T_, class RAD, bool PK_ = false>
+template <int N_, int T_, class RAD, int PK_ = 0>
 struct LineCfg {
     static constexpr int N = N_;
     static constexpr int T = T_;
-    static constexpr bool PK = PK_;  // butterflies' additions packed (cadd_x2)
+    // butterflies' additions packed (cadd_x2): bit 0 forward, bit 1 inverse
+    static constexpr int PK = PK_;
     static constexpr int E = N / T;
     static constexpr int PASSES = RAD::count;
     static constexpr int R0 = RAD::at(0);
@@ -370,7 +371,7 @@ __device__ __forceinline__ void line_fft_sync(float2 (&reg)[Cfg::E], const SM& s
                     v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
                 }
             }
-            dft_reg<R, INV, 1, 0, Cfg::PK>(v);
+            dft_reg<R, INV, 1, 0, ((Cfg::PK >> (INV ? 1 : 0)) & 1) != 0>(v);
             if constexpr (last) {
 #pragma unroll
                 for (int r = 0; r < R; ++r) reg[q + r * Q] = v[r];
@@ -438,10 +439,10 @@ template <> struct Line<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_R
 // column transforms
 template <int N>
 struct LineCol { using cfg = typename Line<N>::cfg; };
-template <> struct LineCol<384> { using cfg = LineCfg<384, QS_COL_LINE_T_384, Rad384<QS_RADIX_COL_384>, QS_PACKED_COLS>; };
-template <> struct LineCol<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_COL_512>, QS_PACKED_COLS>; };
-template <> struct LineCol<768> { using cfg = LineCfg<768, QS_COL_LINE_T_768, Rad768<QS_RADIX_COL_768>, QS_PACKED_COLS>; };
-template <> struct LineCol<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_COL_1024>, QS_PACKED_COLS>; };
+template <> struct LineCol<384> { using cfg = LineCfg<384, QS_COL_LINE_T_384, Rad384<QS_RADIX_COL_384>, QS_PACKED_COLS_384>; };
+template <> struct LineCol<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_COL_512>, QS_PACKED_COLS_512>; };
+template <> struct LineCol<768> { using cfg = LineCfg<768, QS_COL_LINE_T_768, Rad768<QS_RADIX_COL_768>, QS_PACKED_COLS_768>; };
+template <> struct LineCol<1024> { using cfg = LineCfg<1024, 32, Rad1024<QS_RADIX_COL_1024>, QS_PACKED_COLS_1024>; };
 
 // columns per column-pass tile (qs_tuned.h: 16 = 128-byte row segments)
 template <int N>
