@@ -431,7 +431,7 @@ template <int N>
 struct Line;
 template <> struct Line<64> { using cfg = LineCfg<64, 8, radices<8, 8>>; };
 template <> struct Line<128> { using cfg = LineCfg<128, 8, radices<16, 8>>; };
-template <> struct Line<256> { using cfg = LineCfg<256, 16, radices<16, 16>>; };
+template <> struct Line<256> { using cfg = LineCfg<256, 16, radices<16, 16>, QS_PACKED_256>; };
 template <> struct Line<384> { using cfg = LineCfg<384, QS_LINE_T_384, Rad384<QS_RADIX_ROW_384>, QS_PACKED_ROWS>; };
 template <> struct Line<512> { using cfg = LineCfg<512, 16, Rad512<QS_RADIX_ROW_512>, QS_PACKED_ROWS>; };
 template <> struct Line<768> { using cfg = LineCfg<768, QS_LINE_T_768, Rad768<QS_RADIX_ROW_768>, QS_PACKED_ROWS>; };

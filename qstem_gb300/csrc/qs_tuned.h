@@ -230,3 +230,8 @@
 #ifndef QS_PACKED_COLS_1024
 #define QS_PACKED_COLS_1024 1
 #endif
+// the 256-point lines (rows and columns share one configuration; forward,
+// inverse or both packed measured within 1 % of scalar additions)
+#ifndef QS_PACKED_256
+#define QS_PACKED_256 0
+#endif
