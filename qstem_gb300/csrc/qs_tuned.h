@@ -25,6 +25,8 @@
 // 1.90 -> 1.81 us per position-slice, 384 columns 0.414 -> 0.386.  With the
 // packed row additions the 768 row pass runs best at 3 CTAs per SM (2.25 ->
 // 1.92 us); budgets 4 and 5 at 384/512/1024 and 3 at 1024 measured slower.
+// The 384-point rows then also moved to 8 threads x 48 elements (48 x 8, 16
+// lines a CTA at 3 CTAs per SM): 0.578 -> 0.554 us.
 #pragma once
 
 #ifndef QS_ROW_MIN_BLOCKS_64
@@ -100,7 +102,7 @@
 #define QS_ROW_LINES_256 8
 #endif
 #ifndef QS_ROW_LINES_384
-#define QS_ROW_LINES_384 8
+#define QS_ROW_LINES_384 16
 #endif
 #ifndef QS_ROW_LINES_512
 #define QS_ROW_LINES_512 8
@@ -166,14 +168,14 @@
 // thread (three radix passes), 8 and 16 hold 48 (the two-pass
 // factorisations 8x48 / 48x8 and 16x48 / 48x16, lists entries 5 and 6).
 #ifndef QS_LINE_T_384
-#define QS_LINE_T_384 16
+#define QS_LINE_T_384 8
 #endif
 #ifndef QS_LINE_T_768
 #define QS_LINE_T_768 16
 #endif
 // QS_COL_LINE_T_<N>: the same for the column lines (default: the rows')
 #ifndef QS_COL_LINE_T_384
-#define QS_COL_LINE_T_384 8
+#define QS_COL_LINE_T_384 QS_LINE_T_384
 #endif
 #ifndef QS_COL_LINE_T_768
 #define QS_COL_LINE_T_768 QS_LINE_T_768
@@ -184,7 +186,7 @@
 // 0 = the first).  Every translation unit must be compiled with the same
 // choice (the twiddle tables follow it).
 #ifndef QS_RADIX_ROW_384
-#define QS_RADIX_ROW_384 4
+#define QS_RADIX_ROW_384 6
 #endif
 #ifndef QS_RADIX_ROW_512
 #define QS_RADIX_ROW_512 0

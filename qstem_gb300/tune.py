@@ -48,7 +48,7 @@ RADIX_LISTS = {384: [(8, 6, 8), (6, 8, 8), (8, 8, 6), (12, 4, 8), (24, 4, 4), (8
 RADIX_ALTS = {n: len(v) for n, v in RADIX_LISTS.items()}
 # threads per row / column line of the lengths whose layout qs_tuned.h sets
 # (QS_LINE_T_<N>, QS_COL_LINE_T_<N>); the others: qs_fft.cuh's line_threads
-ROW_T = {384: 16, 768: 16}
+ROW_T = {384: 8, 768: 16}
 COL_T = {384: 8, 768: 16}
 
 
