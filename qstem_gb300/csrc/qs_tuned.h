@@ -26,7 +26,9 @@
 // packed row additions the 768 row pass runs best at 3 CTAs per SM (2.25 ->
 // 1.92 us); budgets 4 and 5 at 384/512/1024 and 3 at 1024 measured slower.
 // The 384-point rows then also moved to 8 threads x 48 elements (48 x 8, 16
-// lines a CTA at 3 CTAs per SM): 0.578 -> 0.554 us.
+// lines a CTA at 3 CTAs per SM): 0.578 -> 0.554 us.  With the 48-element
+// column lines, one-stage 16-column tiles measured fastest at 768 (two CTAs
+// per SM; 1.667 -> 1.502 us) and at 384 (three CTAs per SM; 0.370 -> 0.356).
 #pragma once
 
 #ifndef QS_ROW_MIN_BLOCKS_64
@@ -60,7 +62,7 @@
 #define QS_COL_MIN_BLOCKS_256 4
 #endif
 #ifndef QS_COL_MIN_BLOCKS_384
-#define QS_COL_MIN_BLOCKS_384 2
+#define QS_COL_MIN_BLOCKS_384 3
 #endif
 #ifndef QS_COL_MIN_BLOCKS_512
 #define QS_COL_MIN_BLOCKS_512 2
@@ -132,7 +134,7 @@
 #define QS_COL_TILE_512 16
 #endif
 #ifndef QS_COL_TILE_768
-#define QS_COL_TILE_768 8
+#define QS_COL_TILE_768 16
 #endif
 #ifndef QS_COL_TILE_1024
 #define QS_COL_TILE_1024 8
@@ -151,13 +153,13 @@
 #define QS_COL_STAGES_256 2
 #endif
 #ifndef QS_COL_STAGES_384
-#define QS_COL_STAGES_384 2
+#define QS_COL_STAGES_384 1
 #endif
 #ifndef QS_COL_STAGES_512
 #define QS_COL_STAGES_512 1
 #endif
 #ifndef QS_COL_STAGES_768
-#define QS_COL_STAGES_768 2
+#define QS_COL_STAGES_768 1
 #endif
 #ifndef QS_COL_STAGES_1024
 #define QS_COL_STAGES_1024 1
