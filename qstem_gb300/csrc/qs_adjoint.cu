@@ -122,10 +122,23 @@ __global__ void __launch_bounds__(col_tile<N>() * col_line_threads(N))
 // SUM: add g_t = conj(psi) g_phi into the slice's window sum a.gsum with
 // float atomics (vector reductions into an L2-resident potNx x potNy array)
 // instead of storing every position's g_t for the two-kernel gather.
+// QS_PACKED_ADJ: packed-addition bits of the row adjoint's transforms at
+// 256 points and below (-1: those of the forward row transforms).  The
+// inverse transform packed (2) measured fastest on the 256^2 4D-STEM
+// adjoint: 42.50 -> 42.01 ms at 6-slice checkpoints (both: 42.07, forward
+// only: 42.71), the forward row pass unchanged.
+#ifndef QS_PACKED_ADJ
+#define QS_PACKED_ADJ 2
+#endif
+template <int N>
+using AdjRowCfg = typename std::conditional<(N <= 256 && QS_PACKED_ADJ >= 0),
+                                            typename with_packing<typename Line<N>::cfg,
+                                                                  (QS_PACKED_ADJ < 0 ? 0 : QS_PACKED_ADJ)>::type,
+                                            typename Line<N>::cfg>::type;
 template <int N, bool FIRST, bool SUM>
 __global__ void __launch_bounds__(line_threads(N) * ADJ_ROW_LINES, adj_min_blocks(N))
     adj_rows(AdjRowArgs a) {
-    using Cfg = typename Line<N>::cfg;
+    using Cfg = AdjRowCfg<N>;
     constexpr int T = Cfg::T, E = Cfg::E;
     extern __shared__ float2 dsm[];
     float2* s_tw = dsm;

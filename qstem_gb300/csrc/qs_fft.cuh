@@ -295,6 +295,15 @@ struct LineCfg {
     static_assert(TW <= N, "twiddle table must fit in N entries");
 };
 
+// The same line configuration with other packed-addition bits (the
+// transforms, twiddle tables and shared-memory layout are unchanged).
+template <class Cfg, int PK>
+struct with_packing;
+template <int N_, int T_, class RAD, int P_, int PK>
+struct with_packing<LineCfg<N_, T_, RAD, P_>, PK> {
+    using type = LineCfg<N_, T_, RAD, PK>;
+};
+
 // Shared-memory views of a line's exchange scratch.
 // Row lines: one padded line of Cfg::SMEM float2 per line.
 template <int R0>
