@@ -8,27 +8,31 @@
 // 8 slices, 128-1024 waves) and writes the fastest here.  Any value can be
 // overridden with -D at build time.
 //
-// The tables below are the output of
+// The tables below began as the output of
 //   python -m qstem_gb300.tune --write
 // (candidates 1,2,3,4,6,8, row shapes of 4 and 8 lines, sizes 256-1024) on
 // GB300: phase 0 picked the factorisations and column tiles, phase 1 the
 // row-pass shapes and the budgets of both passes, phase 2 the row adjoint's
 // budget (it prints the whole sweep).  For the column pass a stated 1 (the
 // compiler may use up to 255 registers) differs from leaving the bound open.
-// The column pass's tiles, stages and budgets at 256, 384, 512 and 768 were
-// measured again after its tile copies became 16-byte copies of column pairs
-// (profiles/slice_loop_autotune.md): 256 8 columns x 2 stages at 4 CTAs per
-// SM, 384 16 x 2 at 2, 512 16 x 1 at 2, 768 8 x 2 at 2.  The 768-point
-// lines then moved to two passes (16 threads x 48 elements, radices 48 x 16;
-// rows 8 lines a CTA at 2 CTAs per SM) and the 384-point column lines to 8
-// threads x 48 elements (48 x 8): 768 rows 2.49 -> 2.37 us and columns
-// 1.90 -> 1.81 us per position-slice, 384 columns 0.414 -> 0.386.  With the
-// packed row additions the 768 row pass runs best at 3 CTAs per SM (2.25 ->
-// 1.92 us); budgets 4 and 5 at 384/512/1024 and 3 at 1024 measured slower.
-// The 384-point rows then also moved to 8 threads x 48 elements (48 x 8, 16
-// lines a CTA at 3 CTAs per SM): 0.578 -> 0.554 us.  With the 48-element
-// column lines, one-stage 16-column tiles measured fastest at 768 (two CTAs
-// per SM; 1.667 -> 1.502 us) and at 384 (three CTAs per SM; 0.370 -> 0.356).
+// Later changes were each timed side by side against the tables of the day
+// (python -m qstem_gb300.tune --compare ...), in this order:
+//  - after the column tiles became 16-byte copies of column pairs: tiles,
+//    stages and budgets 256 8 columns x 2 stages at 4 CTAs per SM, 512 16 x 1
+//    at 2;
+//  - 768-point lines as 16 threads x 48 elements (radices 48 x 16, two
+//    passes): rows 2.49 -> 2.37 us, columns 1.90 -> 1.81 us per
+//    position-slice; 384-point column lines as 8 x 48 (48 x 8): 0.414 ->
+//    0.386;
+//  - packed two-lane additions (QS_PACKED_*, below);
+//  - then the 768 row pass at 3 CTAs per SM (2.25 -> 1.92 us; budgets 4 and 5
+//    at 384/512/1024 and 3 at 1024 measured slower), 384-point rows as
+//    8 x 48 with 16 lines a CTA at 3 CTAs per SM (0.578 -> 0.554 us), and
+//    one-stage 16-column tiles at 768 (2 CTAs per SM; 1.667 -> 1.502 us) and
+//    384 (3 CTAs per SM; 0.370 -> 0.356).
+// The tuner sweeps budgets, row shapes, factorisations and tiles; the thread
+// layouts (QS_LINE_T_*, QS_COL_LINE_T_*) and the packing bits are set here
+// from the side-by-side timings.
 #pragma once
 
 #ifndef QS_ROW_MIN_BLOCKS_64
@@ -166,9 +170,9 @@
 #endif
 
 // QS_LINE_T_384, QS_LINE_T_768: threads per row line of the 384- and
-// 768-point transforms: 16 and 32 hold 24 elements a
-// thread (three radix passes), 8 and 16 hold 48 (the two-pass
-// factorisations 8x48 / 48x8 and 16x48 / 48x16, lists entries 5 and 6).
+// 768-point transforms: 16 and 32 hold 24 elements a thread (three radix
+// passes), 8 and 16 hold 48 (the two-pass factorisations 8x48 / 48x8 and
+// 16x48 / 48x16, entries 5 and 6 of the lists).
 #ifndef QS_LINE_T_384
 #define QS_LINE_T_384 8
 #endif
