@@ -558,7 +558,10 @@ def run_ours(args, rank, world):
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
                          "both_passes_achieved": both, "both_passes_frac": both / peak,
-                         "bytes_model": "40 B per pixel per slice-step (row pass 24, column pass 16)",
+                         "bytes_model": "40 B per pixel per slice-step (row pass 24, column pass 16); the "
+                                        "passes skip the out-of-band columns and read the transmission "
+                                        "window from L2, so frac can exceed 1 and traffic_frac is the "
+                                        "share of DRAM bandwidth really drawn",
                          # the same kernel on the DRAM bytes it really moves (ncu traffic per launch / the
                          # live per-launch time): the 2/3 band limit skips a third of the columns and the
                          # transmission window stays in L2, so this is the bandwidth the pass draws
