@@ -176,3 +176,19 @@ def test_tilted_and_boxed_crystals_match_the_references_readfile(name):
             assert got == int(v), k
         else:
             assert F32(got) == F32(float(v)), (k, got, v)
+
+
+def test_param_file_arrays_read_as_readarray():
+    """readArray (stem3/stem3.cpp:531-549): numbers after the title, running
+    on over following lines (comments cut, blank lines skipped), each read as
+    atof reads it; a missing title gives None, a file that ends first an
+    error."""
+    d = _write({"a.qsc": "x: 1\nk: 1 2.5e-1   % three of five\n\n% note\n  -3 4x .5\nO: 7\n"})
+    pf = qsc.ParamFile(os.path.join(d, "a.qsc"))
+    np.testing.assert_array_equal(pf.array("k:", 5), [1.0, 0.25, -3.0, 4.0, 0.5])
+    np.testing.assert_array_equal(pf.array("O:", 1), [7.0])
+    assert pf.array("Sr:", 3) is None
+    pf.pos = 0
+    with pytest.raises(ValueError):
+        pf.array("k:", 9)
+    assert qsc._atof("1e3x") == 1000.0 and qsc._atof("abc") == 0.0 and qsc._atof("-.5e-1") == -0.05
